@@ -1,0 +1,560 @@
+"""FP64 NumPy oracle for the neural-eigenfluid hot path.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker that the CUDA product is
+compared against; the product (``neb_gb300``) never imports, links or calls it.
+Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
+``--impl reference`` legs of ``bench.py`` may use it.
+
+It restates, in plain FP64 NumPy, the algorithm of the reference
+(baiming-zhang/NEB) for the path "jet MLP -> fields -> weighted Grams ->
+generalized eigenproblem -> spectral objective -> hand-written reverse pass ->
+Adam", specialised to the shared tanh network of the benchmark configurations:
+
+* jet algebra (value / gradient / Laplacian in 2D, value / gradient / Hessian in
+  3D) follows the reference's chain rule ``unary2``
+  (experiments/2d/_backend/periodic_core/vortex_merger/src/eigenfluid/gen/
+  vortex_merger2d/hardcoded_backend.py:252-271) and its transpose
+  ``unary_backward_jet2`` (same file :1147-1173), and the 3D compact Jet2 of
+  experiments/metaball/_backend/flow/cases/metaball/velocity_trace_jet2.py:31-55;
+* the linear layer and its transpose follow ``linear_forward_batch_jet2`` /
+  ``linear_backward_batch_jet2`` (hardcoded_backend.py:1005-1035, :1115-1144):
+  one weight matrix for every jet channel, bias on the value channel only;
+* periodic Fourier features follow ``encoding_jet2`` ``periodic_sincos_xy``
+  (hardcoded_backend.py:576-588): for axis in (x, y), for n, (sin, cos);
+* fields follow u = (d_y psi, -d_x psi), omega = -lap psi in 2D and
+  u = curl A, omega = curl curl A in 3D (velocity_trace_jet2.py:93-98);
+* Grams follow M = sum_p w u_i.u_j, S = sum_p w omega_i.omega_j
+  (experiments/periodic/paper_rollout.py:171-179,
+  experiments/metaball/_backend/flow/cases/metaball/velocity/core.py:40-46);
+* the generalized eigenproblem follows ``scipy.linalg.eigh(S, M)``
+  (paper_rollout.py:187) and the trace objective's adjoints follow
+  ``trace_objective`` (velocity_trace_jet2.py:107-117);
+* Adam follows ``Model.adam`` (experiments/metaball/_backend/flow/cases/
+  metaball/native_cupy_core.py:156-171).
+
+Array convention: a jet is one array ``[C, N, F]`` with the channel first.
+2D channels (C=4): value, d/dx, d/dy, Laplacian.  3D channels (C=10): value,
+d/dx, d/dy, d/dz, then the Hessian entries in the order
+(xx, xy, xz, yy, yz, zz) of velocity_trace_jet2.py:9.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.linalg as sla
+
+PAIRS = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+_HI = {p: i for i, p in enumerate(PAIRS)}
+
+
+def hid(a: int, b: int) -> int:
+    """Hessian slot of the unordered pair (a, b) (velocity_trace_jet2.py:9-11)."""
+    return _HI[tuple(sorted((a, b)))]
+
+
+def channels(dim: int) -> int:
+    return 4 if dim == 2 else 10
+
+
+# --------------------------------------------------------------------------
+# activations: value and first three derivatives
+# --------------------------------------------------------------------------
+def tanh_derivs(z):
+    t = np.tanh(z)
+    s1 = 1.0 - t * t
+    s2 = -2.0 * t * s1
+    s3 = -2.0 * s1 * (s1 - 2.0 * t * t)
+    return t, s1, s2, s3
+
+
+def sin_derivs(z):
+    s, c = np.sin(z), np.cos(z)
+    return s, c, -s, -c
+
+
+ACTIVATIONS = {"tanh": tanh_derivs, "sin": sin_derivs}
+
+
+# --------------------------------------------------------------------------
+# jet chain rule and its transpose
+# --------------------------------------------------------------------------
+def act_forward(Z, dim, act="tanh"):
+    """y = s(z); grad y = s' grad z; 2D: lap y = s' lap z + s'' |grad z|^2;
+    3D: H y = s' H z + s'' grad z grad z^T  (hardcoded_backend.py:252-271)."""
+    t, s1, s2, _ = ACTIVATIONS[act](Z[0])
+    Y = np.empty_like(Z)
+    Y[0] = t
+    for a in range(dim):
+        Y[1 + a] = s1 * Z[1 + a]
+    if dim == 2:
+        Y[3] = s1 * Z[3] + s2 * (Z[1] ** 2 + Z[2] ** 2)
+    else:
+        for k, (i, j) in enumerate(PAIRS):
+            Y[4 + k] = s1 * Z[4 + k] + s2 * Z[1 + i] * Z[1 + j]
+    return Y
+
+
+def act_backward(Z, Ybar, dim, act="tanh"):
+    """Transpose of :func:`act_forward` (hardcoded_backend.py:1147-1173,
+    velocity_trace_jet2.py:35-41, with the tanh derivatives)."""
+    t, s1, s2, s3 = ACTIVATIONS[act](Z[0])
+    Zb = np.empty_like(Z)
+    zb = Ybar[0] * s1
+    for a in range(dim):
+        zb = zb + Ybar[1 + a] * Z[1 + a] * s2
+        Zb[1 + a] = s1 * Ybar[1 + a]
+    if dim == 2:
+        g2 = Z[1] ** 2 + Z[2] ** 2
+        zb = zb + Ybar[3] * (s2 * Z[3] + s3 * g2)
+        Zb[1] += 2.0 * s2 * Ybar[3] * Z[1]
+        Zb[2] += 2.0 * s2 * Ybar[3] * Z[2]
+        Zb[3] = s1 * Ybar[3]
+    else:
+        for k, (i, j) in enumerate(PAIRS):
+            hb = Ybar[4 + k]
+            zb = zb + hb * (s2 * Z[4 + k] + s3 * Z[1 + i] * Z[1 + j])
+            Zb[1 + i] += s2 * hb * Z[1 + j]
+            Zb[1 + j] += s2 * hb * Z[1 + i]
+            Zb[4 + k] = s1 * hb
+    Zb[0] = zb
+    return Zb
+
+
+def linear_forward(X, W, b):
+    """z_c = W x_c for every channel c, + b on the value channel
+    (hardcoded_backend.py:1005-1035)."""
+    Z = X @ W.T
+    Z[0] += b
+    return Z
+
+
+def linear_backward(X, Zbar, W):
+    """Transpose (hardcoded_backend.py:1115-1144): Xbar_c = Zbar_c W,
+    gW = sum_c Zbar_c^T X_c, gb = sum_points Zbar_value."""
+    Xbar = Zbar @ W
+    gW = np.einsum("cno,cni->oi", Zbar, X)
+    gb = Zbar[0].sum(axis=0)
+    return Xbar, gW, gb
+
+
+# --------------------------------------------------------------------------
+# input features with jets
+# --------------------------------------------------------------------------
+def features_periodic(points, frequencies=16, period=2 * math.pi):
+    """Fourier features sin/cos(n s), s in (x, y), n = 1..F with value,
+    gradient and Laplacian channels (hardcoded_backend.py:576-588 with
+    xmin=0, xmax=period, so phase = 2 pi n s / period)."""
+    points = np.asarray(points, dtype=np.float64)
+    n_pts = len(points)
+    out = np.zeros((4, n_pts, 4 * frequencies))
+    col = 0
+    for axis in range(2):
+        s = points[:, axis]
+        for n in range(1, frequencies + 1):
+            k = 2.0 * math.pi * n / period
+            sn, cs = np.sin(k * s), np.cos(k * s)
+            out[0, :, col] = sn
+            out[1 + axis, :, col] = k * cs
+            out[3, :, col] = -k * k * sn
+            col += 1
+            out[0, :, col] = cs
+            out[1 + axis, :, col] = -k * sn
+            out[3, :, col] = -k * k * cs
+            col += 1
+    return out
+
+
+MULTIHOLE_CENTRES = np.array([[0.3, 0.3], [0.7, 0.4], [0.45, 0.75]])
+MULTIHOLE_RADII = np.array([0.10, 0.08, 0.09])
+
+
+def features_multihole(points, centres=MULTIHOLE_CENTRES):
+    """Raw (x, y) plus one atan2 angle about each hole centre.  The angle is
+    harmonic, so its Laplacian channel is zero."""
+    p = np.asarray(points, dtype=np.float64)
+    n_pts = len(p)
+    out = np.zeros((4, n_pts, 2 + len(centres)))
+    out[0, :, 0], out[1, :, 0] = p[:, 0], 1.0
+    out[0, :, 1], out[2, :, 1] = p[:, 1], 1.0
+    for h, (cx, cy) in enumerate(centres):
+        dx, dy = p[:, 0] - cx, p[:, 1] - cy
+        r2 = dx * dx + dy * dy
+        out[0, :, 2 + h] = np.arctan2(dy, dx)
+        out[1, :, 2 + h] = -dy / r2
+        out[2, :, 2 + h] = dx / r2
+    return out
+
+
+def features_raw3d(points):
+    p = np.asarray(points, dtype=np.float64)
+    out = np.zeros((10, len(p), 3))
+    for a in range(3):
+        out[0, :, a] = p[:, a]
+        out[1 + a, :, a] = 1.0
+    return out
+
+
+# --------------------------------------------------------------------------
+# network
+# --------------------------------------------------------------------------
+def glorot_init(widths, seed):
+    """Glorot-normal weights, std sqrt(2/(fan_in+fan_out)), zero biases, drawn
+    layer by layer from numpy.random.default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    params = []
+    for fan_in, fan_out in zip(widths[:-1], widths[1:]):
+        std = math.sqrt(2.0 / (fan_in + fan_out))
+        params.append((rng.normal(0.0, std, (fan_out, fan_in)), np.zeros(fan_out)))
+    return params
+
+
+def mlp_forward(params, X0, dim, act="tanh"):
+    """Hidden layers with the jet activation, then the linear output layer.
+    Returns (inputs of every layer, pre-activations of hidden layers, output
+    jet).  Matches ``forward`` of velocity_trace_jet2.py:65-76 without the
+    envelope (identity envelope of the periodic and benchmark cases)."""
+    X = X0
+    xs, zs = [], []
+    for W, b in params[:-1]:
+        xs.append(X)
+        Z = linear_forward(X, W, b)
+        zs.append(Z)
+        X = act_forward(Z, dim, act)
+    xs.append(X)
+    W, b = params[-1]
+    return xs, zs, linear_forward(X, W, b)
+
+
+def mlp_backward(params, xs, zs, Psibar, dim, act="tanh"):
+    """Hand-written reverse of :func:`mlp_forward`
+    (velocity_trace_jet2.py:77-82)."""
+    grads = [None] * len(params)
+    Xbar, gW, gb = linear_backward(xs[-1], Psibar, params[-1][0])
+    grads[-1] = (gW, gb)
+    for layer in range(len(params) - 2, -1, -1):
+        Zbar = act_backward(zs[layer], Xbar, dim, act)
+        Xbar, gW, gb = linear_backward(xs[layer], Zbar, params[layer][0])
+        grads[layer] = (gW, gb)
+    return grads
+
+
+# --------------------------------------------------------------------------
+# fields and Grams
+# --------------------------------------------------------------------------
+def fields_2d(Psi):
+    """u = (d_y psi, -d_x psi), omega = -lap psi; U stacked [2, N, K]."""
+    U = np.stack([Psi[2], -Psi[1]])
+    Om = -Psi[3][None]
+    return U, Om
+
+
+def fields_3d(Psi):
+    """A_k = (psi_{3k}, psi_{3k+1}, psi_{3k+2}); u = curl A, omega = curl u
+    = grad div A - lap A (velocity_trace_jet2.py:93-98).  Returns [3, N, K]."""
+    K = Psi.shape[2] // 3
+
+    def g(comp, axis):  # d_axis A_comp  -> [N, K]
+        return Psi[1 + axis][:, comp::3]
+
+    def h(comp, a, b):
+        return Psi[4 + hid(a, b)][:, comp::3]
+
+    U = np.stack([g(2, 1) - g(1, 2), g(0, 2) - g(2, 0), g(1, 0) - g(0, 1)])
+    Om = np.stack([sum(h(b, a, b) - h(a, b, b) for b in range(3)) for a in range(3)])
+    assert U.shape[2] == K
+    return U, Om
+
+
+def fields(Psi, dim):
+    return fields_2d(Psi) if dim == 2 else fields_3d(Psi)
+
+
+def grams(U, Om, w):
+    """M = sum_p w_p u_i.u_j, S = sum_p w_p omega_i.omega_j
+    (paper_rollout.py:178-179)."""
+    w = np.broadcast_to(np.asarray(w, dtype=np.float64), U.shape[1:2])
+    M = sum((U[a] * w[:, None]).T @ U[a] for a in range(U.shape[0]))
+    S = sum((Om[a] * w[:, None]).T @ Om[a] for a in range(Om.shape[0]))
+    return 0.5 * (M + M.T), 0.5 * (S + S.T)
+
+
+# --------------------------------------------------------------------------
+# finite part of the pencil (S, M) and the spectral objectives
+# --------------------------------------------------------------------------
+def finite_pencil(S, M, rank_rtol=1e-10):
+    """Finite generalized eigenpairs S v = lam M v, v^T M v = 1, ascending.
+
+    When M has full rank this is ``scipy.linalg.eigh(S, M)`` (the recipe of
+    paper_rollout.py:187).  When the K fields span fewer than K dimensions
+    (a shared network whose last hidden width is below K), S and M share that
+    null space; the finite eigenvalues are those of the pencil restricted to
+    range(M), computed through M = Q diag(e) Q^T with the eigenvalues above
+    ``rank_rtol * max(e)``.  The reference's rank gate
+    (paper_rollout.py:180-186) uses the same eigenvalue-ratio test.
+    """
+    e, Q = np.linalg.eigh(M)
+    keep = e > rank_rtol * e[-1]
+    r = int(keep.sum())
+    if r == len(M):
+        lam, V = sla.eigh(S, M)
+        return lam, V, r
+    Qr = Q[:, keep] / np.sqrt(e[keep])
+    C = Qr.T @ S @ Qr
+    lam, Y = np.linalg.eigh(0.5 * (C + C.T))
+    return lam, Qr @ Y, r
+
+
+def objective_weights(kind, r):
+    """c_k: 'trace' -> 1 (L = tr(M^-1 S) = sum lam), 'ordering' -> 1/k."""
+    if kind == "trace":
+        return np.ones(r)
+    if kind == "ordering":
+        return 1.0 / np.arange(1, r + 1)
+    raise ValueError(kind)
+
+
+def spectral_objective(M, S, kind, rank_rtol=1e-10):
+    """L = sum_k c_k lam_k over the finite eigenvalues, and its matrix
+    adjoints dL/dS = V diag(c) V^T, dL/dM = -V diag(c lam) V^T.  For
+    kind='trace' these are M^-1 and -M^-1 S M^-1 (velocity_trace_jet2.py:
+    114-116 up to its 1/k normalisation)."""
+    lam, V, r = finite_pencil(S, M, rank_rtol)
+    c = objective_weights(kind, r)
+    GS = (V * c) @ V.T
+    GM = -(V * (c * lam)) @ V.T
+    return dict(loss=float(c @ lam), lam=lam, V=V, rank=r, GS=GS, GM=GM)
+
+
+# --------------------------------------------------------------------------
+# field adjoints (transpose of ``fields``)
+# --------------------------------------------------------------------------
+def fields_adjoint(Ubar, Ombar, dim, n_out):
+    """Psi-bar from U-bar, Omega-bar (velocity_trace_jet2.py:102-106 and
+    core.py:32-38 for 3D)."""
+    C = channels(dim)
+    n = Ubar.shape[1]
+    Pb = np.zeros((C, n, n_out))
+    if dim == 2:
+        Pb[2] += Ubar[0]
+        Pb[1] -= Ubar[1]
+        Pb[3] -= Ombar[0]
+        return Pb
+
+    def addg(comp, axis, val):
+        Pb[1 + axis][:, comp::3] += val
+
+    def addh(comp, a, b, val):
+        Pb[4 + hid(a, b)][:, comp::3] += val
+
+    addg(2, 1, Ubar[0]); addg(1, 2, -Ubar[0])
+    addg(0, 2, Ubar[1]); addg(2, 0, -Ubar[1])
+    addg(1, 0, Ubar[2]); addg(0, 1, -Ubar[2])
+    for a in range(3):
+        for b in range(3):
+            addh(b, a, b, Ombar[a])
+            addh(a, b, b, -Ombar[a])
+    return Pb
+
+
+# --------------------------------------------------------------------------
+# one objective + gradient step
+# --------------------------------------------------------------------------
+@dataclass
+class StepResult:
+    loss: float
+    lam: np.ndarray
+    M: np.ndarray
+    S: np.ndarray
+    rank: int
+    grads: list = field(default_factory=list)
+
+
+def objective_and_grad(params, X0, w, dim, kind, act="tanh", want_grad=True,
+                       rank_rtol=1e-10):
+    """Direct route: full output layer, U and Omega, K x K Grams, the finite
+    pencil, the objective and its parameter gradient."""
+    xs, zs, Psi = mlp_forward(params, X0, dim, act)
+    U, Om = fields(Psi, dim)
+    M, S = grams(U, Om, w)
+    obj = spectral_objective(M, S, kind, rank_rtol)
+    res = StepResult(obj["loss"], obj["lam"], M, S, obj["rank"])
+    if want_grad:
+        wv = np.broadcast_to(np.asarray(w, dtype=np.float64), (U.shape[1],))[:, None]
+        Ubar = np.stack([2.0 * wv * (U[a] @ obj["GM"]) for a in range(U.shape[0])])
+        Obar = np.stack([2.0 * wv * (Om[a] @ obj["GS"]) for a in range(Om.shape[0])])
+        Psibar = fields_adjoint(Ubar, Obar, dim, Psi.shape[2])
+        res.grads = mlp_backward(params, xs, zs, Psibar, dim, act)
+    return res
+
+
+def hidden_grams_2d(H, w):
+    """Grams of the last hidden layer's field channels, 2D scalar potential:
+    A_M = sum_p w (h_x h_x^T + h_y h_y^T), A_S = sum_p w h_lap h_lap^T.
+    With psi = W_out h + b:  M = W_out A_M W_out^T, S = W_out A_S W_out^T."""
+    wv = np.broadcast_to(np.asarray(w, dtype=np.float64), (H.shape[1],))[:, None]
+    AM = (H[1] * wv).T @ H[1] + (H[2] * wv).T @ H[2]
+    AS = (H[3] * wv).T @ H[3]
+    return 0.5 * (AM + AM.T), 0.5 * (AS + AS.T)
+
+
+def objective_and_grad_factored(params, X0, w, kind, act="tanh", want_grad=True):
+    """Factored route for the 2D scalar potential: Grams in the span of the
+    last hidden layer.  When K >= H the finite eigenvalues of (S, M) are those
+    of (A_S, A_M) (W_out of full column rank) and dL/dW_out = 0; otherwise the
+    K x K pencil W A W^T is solved.  Identical results to
+    :func:`objective_and_grad` (checked by the tests)."""
+    dim = 2
+    xs, zs, _ = mlp_forward(params, X0, dim, act)
+    H = xs[-1]
+    W_out = params[-1][0]
+    K, Hn = W_out.shape
+    AM, AS = hidden_grams_2d(H, w)
+    if K >= Hn:
+        obj = spectral_objective(AM, AS, kind)
+        GMh, GSh = obj["GM"], obj["GS"]
+        M = W_out @ AM @ W_out.T
+        S = W_out @ AS @ W_out.T
+        gWout = np.zeros_like(W_out)
+    else:
+        M = W_out @ AM @ W_out.T
+        S = W_out @ AS @ W_out.T
+        obj = spectral_objective(M, S, kind)
+        GMh = W_out.T @ obj["GM"] @ W_out
+        GSh = W_out.T @ obj["GS"] @ W_out
+        gWout = 2.0 * (obj["GM"] @ W_out @ AM + obj["GS"] @ W_out @ AS)
+    res = StepResult(obj["loss"], obj["lam"], 0.5 * (M + M.T), 0.5 * (S + S.T), obj["rank"])
+    if want_grad:
+        wv = np.broadcast_to(np.asarray(w, dtype=np.float64), (H.shape[1],))[:, None]
+        Hbar = np.zeros_like(H)
+        Hbar[1] = 2.0 * wv * (H[1] @ GMh)
+        Hbar[2] = 2.0 * wv * (H[2] @ GMh)
+        Hbar[3] = 2.0 * wv * (H[3] @ GSh)
+        grads = [None] * len(params)
+        grads[-1] = (gWout, np.zeros(K))
+        Xbar = Hbar
+        for layer in range(len(params) - 2, -1, -1):
+            Zbar = act_backward(zs[layer], Xbar, dim, act)
+            Xbar, gW, gb = linear_backward(xs[layer], Zbar, params[layer][0])
+            grads[layer] = (gW, gb)
+        res.grads = grads
+    return res
+
+
+# --------------------------------------------------------------------------
+# Adam (native_cupy_core.py:156-171, one shared network: one global norm)
+# --------------------------------------------------------------------------
+def adam_step(params, moments, grads, step, lr, clip=8.0, beta1=0.9, beta2=0.999,
+              eps=1e-8):
+    """One Adam transaction.  Raises FloatingPointError and changes nothing
+    when the global gradient norm is not finite and positive."""
+    flat = [g for pair in grads for g in pair]
+    norm = math.sqrt(sum(float(np.sum(np.asarray(g, dtype=np.float64) ** 2)) for g in flat))
+    if not (math.isfinite(norm) and norm > 0):
+        raise FloatingPointError("Invalid parameter gradients; no optimizer update")
+    scale = min(1.0, clip / max(norm, 1e-30))
+    t = step + 1
+    new_params, new_moments = [], []
+    for (W, b), (gW, gb), ((mW, vW), (mb, vb)) in zip(params, grads, moments):
+        out = []
+        for p, g, m, v in ((W, gW, mW, vW), (b, gb, mb, vb)):
+            g = g * scale
+            m = beta1 * m + (1 - beta1) * g
+            v = beta2 * v + (1 - beta2) * g * g
+            p = p - lr * (m / (1 - beta1 ** t)) / (np.sqrt(v / (1 - beta2 ** t)) + eps)
+            out.append((p, m, v))
+        new_params.append((out[0][0], out[1][0]))
+        new_moments.append(((out[0][1], out[0][2]), (out[1][1], out[1][2])))
+    return new_params, new_moments, norm
+
+
+def zero_moments(params):
+    return [((np.zeros_like(W), np.zeros_like(W)), (np.zeros_like(b), np.zeros_like(b)))
+            for W, b in params]
+
+
+# --------------------------------------------------------------------------
+# quadrature points
+# --------------------------------------------------------------------------
+def periodic_grid(n, period=2 * math.pi):
+    g = np.arange(n) * (period / n)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    return np.stack([X.ravel(), Y.ravel()], axis=1), (period / n) ** 2
+
+
+def periodic_minibatch(count, seed, step, period=2 * math.pi):
+    """Points ~ U[0, period)^2 from default_rng((seed, step)); equal weights."""
+    rng = np.random.default_rng([seed, step])
+    return rng.uniform(0.0, period, (count, 2)), period * period / count
+
+
+def multihole_points(count, seed, centres=MULTIHOLE_CENTRES, radii=MULTIHOLE_RADII):
+    """Seeded rejection sampling of the unit square minus the disks; equal
+    weights area / N."""
+    rng = np.random.default_rng(seed)
+    pieces, remain = [], count
+    while remain:
+        cand = rng.random((max(2 * remain, 256), 2))
+        ok = np.ones(len(cand), bool)
+        for (cx, cy), r in zip(centres, radii):
+            ok &= (cand[:, 0] - cx) ** 2 + (cand[:, 1] - cy) ** 2 > r * r
+        acc = cand[ok][:remain]
+        pieces.append(acc)
+        remain -= len(acc)
+    area = 1.0 - math.pi * float(np.sum(np.asarray(radii) ** 2))
+    return np.concatenate(pieces), area / count
+
+
+def metaball_points(count, seed, n_centres=8, sigma=0.08, level=0.5, chunk=1 << 20):
+    """Seeded rejection sampling of {x in [0,1]^3 : sum_i exp(-|x-c_i|^2 /
+    (2 sigma^2)) < level}, centres ~ U[0.2, 0.8]^3 drawn first from the same
+    generator; equal weights 1/N."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.2, 0.8, (n_centres, 3))
+    pieces, remain = [], count
+    while remain:
+        cand = rng.random((min(max(2 * remain, 256), chunk), 3))
+        d2 = ((cand[:, None, :] - centres[None]) ** 2).sum(-1)
+        ok = np.exp(-d2 / (2 * sigma * sigma)).sum(1) < level
+        acc = cand[ok][:remain]
+        pieces.append(acc)
+        remain -= len(acc)
+    return np.concatenate(pieces), 1.0 / count, centres
+
+
+# --------------------------------------------------------------------------
+# benchmark configurations
+# --------------------------------------------------------------------------
+CONFIGS = {
+    "c1": dict(dim=2, features="periodic", frequencies=16, widths=[64, 128, 128, 128, 64],
+               kind="trace"),
+    "c2": dict(dim=2, features="periodic", frequencies=16,
+               widths=[64, 512, 512, 512, 512, 1024], kind="ordering"),
+    "c3": dict(dim=2, features="periodic", frequencies=16,
+               widths=[64, 512, 512, 512, 512, 1024], kind="ordering"),
+    "c4": dict(dim=2, features="multihole", widths=[5, 256, 256, 256, 256, 1024],
+               kind="ordering"),
+    "c5": dict(dim=3, features="raw3d", widths=[3, 512, 512, 512, 512, 1536],
+               kind="ordering"),
+}
+
+
+def features(kind, points, frequencies=16):
+    if kind == "periodic":
+        return features_periodic(points, frequencies)
+    if kind == "multihole":
+        return features_multihole(points)
+    if kind == "raw3d":
+        return features_raw3d(points)
+    raise ValueError(kind)
+
+
+def scaled_widths(widths, hidden=None, outputs=None):
+    """Shrink a configuration's hidden width / output count for small tests."""
+    w = list(widths)
+    if hidden is not None:
+        w = [w[0]] + [hidden] * (len(w) - 2) + [w[-1]]
+    if outputs is not None:
+        w[-1] = outputs
+    return w

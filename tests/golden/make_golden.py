@@ -1,0 +1,199 @@
+"""Generate the golden fixtures that pin the oracle to the reference.
+
+Runs the reference's own (CuPy) functions on the CPU by installing a NumPy
+stand-in for ``cupy`` / ``cupyx`` (the pattern of the reference's
+tests/test_finite_gauge.py:10-16) and records small seeded input/output
+vectors in ``tests/golden/reference_vectors.npz``.  It needs the reference
+checkout (default ``/root/reference``, or ``$NEB_REFERENCE``), which exists only
+where the fixtures are made; the tests read the committed ``.npz`` alone.
+
+Reference functions exercised (paths relative to the reference project):
+
+* experiments/2d/_backend/periodic_core/vortex_merger/src/eigenfluid/gen/
+  vortex_merger2d/hardcoded_backend.py: ``unary2`` (:252), ``xy_jets2`` (:496),
+  ``encoding_jet2`` periodic branch (:576), ``linear_forward_batch_jet2``
+  (:1005), ``linear_backward_batch_jet2`` (:1115), ``unary_backward_jet2`` (:1147);
+* experiments/metaball/_backend/flow/cases/metaball/velocity_trace_jet2.py:
+  ``sine`` (:31), ``sine_reverse`` (:35), ``velocity`` (:93), ``vorticity`` (:96),
+  ``lift_reverse`` (:102), ``trace_objective`` (:107);
+* experiments/metaball/_backend/flow/cases/metaball/velocity/core.py: ``grams`` (:40);
+* experiments/metaball/_backend/flow/cases/metaball/native_cupy_core.py:
+  ``Model`` forward / backward / adam (:111-171);
+* experiments/periodic/paper_rollout.py:178-187 recipe (Grams, then
+  ``scipy.linalg.eigh(S, M)``).
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import importlib.util
+import math
+import os
+import sys
+import types
+from pathlib import Path
+from types import SimpleNamespace
+
+import numpy as np
+import scipy.linalg as sla
+
+REF = Path(os.environ.get("NEB_REFERENCE", "/root/reference"))
+OUT = Path(__file__).resolve().parent / "reference_vectors.npz"
+
+
+class _NumpyCupy(types.ModuleType):
+    """Module that answers every ``cupy`` attribute from NumPy."""
+
+    def __init__(self):
+        super().__init__("cupy")
+        self.cuda = SimpleNamespace(
+            Stream=SimpleNamespace(null=SimpleNamespace(synchronize=lambda: None)))
+        self.linalg = np.linalg
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+    @staticmethod
+    def asnumpy(a):
+        return np.asarray(a)
+
+    @staticmethod
+    def get_default_memory_pool():
+        return SimpleNamespace(free_all_blocks=lambda: None, set_limit=lambda **k: None)
+
+
+def install_shim():
+    cp = _NumpyCupy()
+    sys.modules["cupy"] = cp
+    cupyx = types.ModuleType("cupyx")
+    cupyx_scipy = types.ModuleType("cupyx.scipy")
+    cupyx_linalg = types.ModuleType("cupyx.scipy.linalg")
+    cupyx_linalg.solve_triangular = sla.solve_triangular
+    cupyx.scipy = cupyx_scipy
+    cupyx_scipy.linalg = cupyx_linalg
+    sys.modules["cupyx"] = cupyx
+    sys.modules["cupyx.scipy"] = cupyx_scipy
+    sys.modules["cupyx.scipy.linalg"] = cupyx_linalg
+    return cp
+
+
+def load(path, name):
+    spec = importlib.util.spec_from_file_location(name, path)
+    module = importlib.util.module_from_spec(spec)
+    sys.modules[name] = module
+    spec.loader.exec_module(module)
+    return module
+
+
+def main():
+    install_shim()
+    hb_src = REF / "experiments/2d/_backend/periodic_core/vortex_merger/src"
+    sys.path.insert(0, str(hb_src))
+    from eigenfluid.gen.vortex_merger2d import hardcoded_backend as HB
+    HB.F32 = np.float64  # run the reference's FP32-typed GEMMs in FP64
+    vendor = REF / "experiments/metaball/_backend"
+    metaball = vendor / "flow/cases/metaball"
+    sys.path[:0] = [str(vendor), str(metaball)]
+    ncc = load(metaball / "native_cupy_core.py", "native_cupy_core")
+    ncc.old.F32 = np.float64  # the analytic_jets transposes NCC calls
+    vtj2 = load(metaball / "velocity_trace_jet2.py", "velocity_trace_jet2")
+    vcore = load(metaball / "velocity/core.py", "velocity_core")
+
+    rng = np.random.default_rng(20261203)
+    g = {}
+
+    # --- 2D tanh jet chain rule and its transpose (unary2 / unary_backward_jet2)
+    n, f = 9, 6
+    z = rng.normal(size=(n, f))
+    grad = rng.normal(size=(n, f, 2))
+    hess = rng.normal(size=(n, f, 3))
+    t = np.tanh(z); s1 = 1 - t * t; s2 = -2 * t * s1; s3 = -2 * s1 * (s1 - 2 * t * t)
+    y = HB.unary2(HB.Jet2(z, grad, hess), t, s1, s2)
+    g.update(act2d_z=z, act2d_grad=grad, act2d_hess=hess,
+             act2d_y=y.value, act2d_ygrad=y.grad, act2d_yhess=y.hess)
+    av, ag, al = rng.normal(size=(n, f)), rng.normal(size=(n, f, 2)), rng.normal(size=(n, f))
+    adj = HB.Jet2(av, ag, np.stack([al, np.zeros_like(al), al], -1))
+    back = HB.unary_backward_jet2(HB.Jet2(z, grad, hess), adj, s1, s2, s3)
+    g.update(act2d_av=av, act2d_ag=ag, act2d_al=al,
+             act2d_zb=back.value, act2d_gb=back.grad, act2d_hb=back.hess)
+
+    # --- 2D linear jet layer and its transpose (shared source, one mode)
+    n, fi, fo = 7, 5, 4
+    src = HB.Jet2(rng.normal(size=(n, fi)), rng.normal(size=(n, fi, 2)), rng.normal(size=(n, fi, 3)))
+    W = rng.normal(size=(1, fo, fi)); b = rng.normal(size=(1, fo))
+    out = HB.linear_forward_batch_jet2(src, W, b, np.float64)
+    ad = HB.Jet2(rng.normal(size=(1, n, fo)), rng.normal(size=(1, n, fo, 2)), rng.normal(size=(1, n, fo, 3)))
+    xb, gW, gb = HB.linear_backward_batch_jet2(src, ad, W)
+    g.update(lin_x=src.value, lin_xg=src.grad, lin_xh=src.hess, lin_W=W[0], lin_b=b[0],
+             lin_z=out.value[0], lin_zg=out.grad[0], lin_zh=out.hess[0],
+             lin_av=ad.value[0], lin_ag=ad.grad[0], lin_ah=ad.hess[0],
+             lin_xbv=xb.value[0], lin_xbg=xb.grad[0], lin_xbh=xb.hess[0], lin_gW=gW[0], lin_gb=gb[0])
+
+    # --- periodic Fourier encoding with second-order jets
+    cfg = SimpleNamespace(input_encoding="periodic_sincos_xy", xmin=0.0, xmax=2 * math.pi,
+                          ymin=0.0, ymax=2 * math.pi, frequencies=5)
+    pts = rng.uniform(0, 2 * math.pi, size=(11, 2))
+    x, yj = HB.xy_jets2(pts, np.float64)
+    enc = HB.encoding_jet2(cfg, x, yj, 0.0, 0.0)
+    g.update(enc_points=pts, enc_value=enc.value, enc_grad=enc.grad, enc_hess=enc.hess,
+             enc_frequencies=np.asarray(5))
+
+    # --- 3D compact Jet2 sine chain rule and transpose
+    n, f = 6, 4
+    z3 = rng.normal(size=(n, f)); g3 = rng.normal(size=(n, f, 3)); h3 = rng.normal(size=(n, f, 6))
+    y3 = vtj2.sine(vtj2.J2(z3, g3, h3))
+    a3 = vtj2.J2(rng.normal(size=(n, f)), rng.normal(size=(n, f, 3)), rng.normal(size=(n, f, 6)))
+    b3 = vtj2.sine_reverse(vtj2.J2(z3, g3, h3), a3)
+    g.update(act3d_z=z3, act3d_grad=g3, act3d_hess=h3, act3d_y=y3.value, act3d_ygrad=y3.grad,
+             act3d_yhess=y3.hess, act3d_av=a3.value, act3d_ag=a3.grad, act3d_ah=a3.hess,
+             act3d_zb=b3.value, act3d_gb=b3.grad, act3d_hb=b3.hess)
+
+    # --- 3D fields (curl, curl curl) and their transpose
+    k, n = 3, 5
+    fj = vtj2.J2(rng.normal(size=(k, n, 3)), rng.normal(size=(k, n, 3, 3)), rng.normal(size=(k, n, 3, 6)))
+    gu, gw = rng.normal(size=(k, n, 3)), rng.normal(size=(k, n, 3))
+    lifted = vtj2.lift_reverse(gu, gw)
+    g.update(f3_value=fj.value, f3_grad=fj.grad, f3_hess=fj.hess, f3_u=vtj2.velocity(fj),
+             f3_w=vtj2.vorticity(fj), f3_gu=gu, f3_gw=gw, f3_lift_grad=lifted.grad,
+             f3_lift_hess=lifted.hess)
+
+    # --- Grams (core.py:40-46) and the eigen recipe (paper_rollout.py:178-187)
+    n, k = 40, 6
+    U = rng.normal(size=(3 * n, k)); D = rng.normal(size=(3 * n, k))
+    M, S = vcore.grams(U, D)
+    lam, V = sla.eigh(S, M)
+    g.update(gram_U=U, gram_D=D, gram_M=M, gram_S=S, eig_lam=lam, eig_V=V)
+
+    # --- trace objective with adjoints (velocity_trace_jet2.py:107-117)
+    tr = vtj2.trace_objective(U, D, adjoints=True)
+    g.update(trace_loss=np.asarray(float(tr["loss"])), trace_GU=tr["GU"], trace_GO=tr["GO"])
+
+    # --- the reference's own network-backend Model: forward, reverse, Adam
+    c = SimpleNamespace(hidden=8, hidden_layers=2, siren_first_omega0=2.3, siren_hidden_omega0=1.7)
+    model = ncc.Model(c, K=1, seed=31)
+    n = 5
+    feat = rng.normal(size=(n, 15)); fgrad = rng.normal(size=(n, 15, 3))
+    env = ncc.Jet1(np.ones((n, 1)), np.zeros((n, 1, 3)))
+    data = SimpleNamespace(features=ncc.Jet1(feat, fgrad), envelope=env)
+    W0 = [w.copy() for w in model.W]; b0 = [bb.copy() for bb in model.b]
+    val, tape = model.forward(data, 0, 1, True)
+    av = rng.normal(size=val.value.shape); agr = rng.normal(size=val.grad.shape)
+    gw, gbias = model.backward(data, 0, 1, tape, ncc.Jet1(av, agr))
+    model.adam(gw, gbias, 1e-3, clip=0.5)
+    model.adam([2 * x for x in gw], [-x for x in gbias], 1e-3, clip=0.5)
+    for j in range(len(W0)):
+        g[f"ncc_W{j}"] = W0[j][0]; g[f"ncc_b{j}"] = b0[j][0]
+        g[f"ncc_gW{j}"] = gw[j][0]; g[f"ncc_gb{j}"] = gbias[j][0]
+        g[f"ncc_W{j}_after"] = model.W[j][0]; g[f"ncc_b{j}_after"] = model.b[j][0]
+        g[f"ncc_mW{j}"] = model.mW[j][0]; g[f"ncc_vW{j}"] = model.vW[j][0]
+    g.update(ncc_feat=feat, ncc_fgrad=fgrad, ncc_value=val.value[0], ncc_grad=val.grad[0],
+             ncc_av=av[0], ncc_ag=agr[0], ncc_omega=np.asarray([2.3, 1.7]),
+             ncc_layers=np.asarray(len(W0)))
+    g = {key: np.asarray(v, dtype=np.float64) if np.asarray(v).dtype.kind == "f" else np.asarray(v)
+         for key, v in g.items()}
+    np.savez_compressed(OUT, **g)
+    print(f"wrote {OUT} ({len(g)} arrays)")
+
+
+if __name__ == "__main__":
+    main()
