@@ -1,0 +1,192 @@
+/*
+ * neb_gb300 — C ABI of the GB300 (sm_103a) neural-eigenfluid hot path.
+ *
+ * Every entry point takes device pointers, explicit sizes and a CUDA stream,
+ * returns an int status (NEB_OK or a negative NEB_ERR_* code, with a message
+ * in neb_last_error()), allocates no device memory on the hot path (the caller
+ * owns every buffer, including the workspace and the activation tape), and
+ * never synchronises the host except where noted.
+ *
+ * Device layout of a jet array: [n_points][C][width] row-major, C = 4 in 2D
+ * (value, d/dx, d/dy, Laplacian) and C = 10 in 3D (value, d/dx, d/dy, d/dz,
+ * Hessian xx, xy, xz, yy, yz, zz).  Parameters: W_l is [width_out][width_in]
+ * row-major, b_l is [width_out]; "master" type is float for NEB_PREC_FP32 and
+ * NEB_PREC_BF16X3 and double for NEB_PREC_FP64.
+ *
+ * The reference (baiming-zhang/NEB) is Python/CuPy and has no C interface;
+ * each entry names the reference function whose role it takes over.  Paths
+ * are relative to the reference project:
+ *   HB  = experiments/2d/_backend/periodic_core/vortex_merger/src/eigenfluid/
+ *         gen/vortex_merger2d/hardcoded_backend.py
+ *   NCC = experiments/metaball/_backend/flow/cases/metaball/native_cupy_core.py
+ *   VTJ2= experiments/metaball/_backend/flow/cases/metaball/velocity_trace_jet2.py
+ *   VC  = experiments/metaball/_backend/flow/cases/metaball/velocity/core.py
+ *   ROLL= experiments/periodic/paper_rollout.py
+ */
+#ifndef NEB_GB300_H
+#define NEB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* neb_stream_t; /* a cudaStream_t; NULL = legacy stream */
+
+enum {
+  NEB_OK = 0,
+  NEB_ERR_ARG = -1,          /* bad shape / pointer / option (ValueError)          */
+  NEB_ERR_CUDA = -2,         /* CUDA runtime or library failure                     */
+  NEB_ERR_WORKSPACE = -3,    /* workspace smaller than neb_*_workspace_bytes        */
+  NEB_ERR_NOT_PD = -4,       /* mass matrix not positive definite (rank gate)       */
+  NEB_ERR_NONFINITE = -5,    /* non-finite value detected (FloatingPointError)      */
+  NEB_ERR_SOLVER = -6,       /* eigensolver did not converge                        */
+  NEB_ERR_UNSUPPORTED = -7,  /* configuration not built for this device / options  */
+  NEB_ERR_TIMEOUT = -8       /* a bounded device-side wait gave up                  */
+};
+
+enum { NEB_PREC_FP32 = 0, NEB_PREC_FP64 = 1, NEB_PREC_BF16X3 = 2 };
+enum { NEB_FEAT_PERIODIC = 0, NEB_FEAT_MULTIHOLE = 1, NEB_FEAT_RAW3D = 2 };
+
+#define NEB_MAX_HIDDEN 8
+
+/* Shape of the shared tanh MLP: widths[0] input features, widths[1..n_hidden]
+ * hidden widths, widths[n_hidden + 1] outputs (K in 2D, 3K in 3D). */
+typedef struct neb_net {
+  int32_t dim;        /* 2 or 3 */
+  int32_t n_hidden;   /* 1..NEB_MAX_HIDDEN */
+  int32_t widths[NEB_MAX_HIDDEN + 2];
+  int32_t precision;  /* NEB_PREC_* */
+} neb_net;
+
+/* Thread-local message of the last failing call. */
+const char* neb_last_error(void);
+
+/* Bytes of the activation tape (inputs and pre-activations of every layer,
+ * in the precision's storage format) for n_points; and of the scratch
+ * workspace every neb_* call below needs for n_points. */
+size_t neb_tape_bytes(const neb_net* net, int64_t n_points);
+size_t neb_workspace_bytes(const neb_net* net, int64_t n_points);
+
+/* Input features with their spatial jets, written as a [n][C][widths[0]]
+ * master-type array.  kind = NEB_FEAT_PERIODIC: sin/cos(2 pi k s / period),
+ * s in (x, y), k = 1..n_freq (params[0] = period; HB:576-588 encoding_jet2,
+ * periodic_sincos_xy).  NEB_FEAT_MULTIHOLE: (x, y, atan2 about each centre),
+ * params = centres (2 per hole, at most 32 holes).  NEB_FEAT_RAW3D: (x, y, z).
+ * params is a HOST array; points: [n][dim] double, device. */
+int neb_features(const neb_net* net, int kind, int n_freq, const double* params,
+                 int n_params, const double* points, int64_t n_points, void* features,
+                 neb_stream_t stream);
+
+/* Hidden layers of the jet MLP: for l = 1..n_hidden, z_l = W_l x_{l-1} (+ b_l
+ * on the value channel), x_l = tanh-jet(z_l); inputs and pre-activations are
+ * kept in the tape for the reverse pass.  Replaces HB:1716-1880
+ * forward_stream_jet1/2 with HB:1005-1070 linear_forward_batch_jet2 +
+ * sine_forward_jet2 per layer, NCC:130-140 Model.forward, VTJ2:65-76 forward.
+ * W, b: host arrays of n_hidden + 1 device pointers (the output layer's are
+ * not read here). */
+int neb_forward(const neb_net* net, const void* const* W, const void* const* b,
+                const void* features, int64_t n_points, void* tape, void* workspace,
+                size_t workspace_bytes, neb_stream_t stream);
+
+/* Output-layer jets psi = W_out x_L + b_out for output rows [start, stop):
+ * psi is [n][C][stop - start], master type.  Role of the output linear of
+ * NCC:138-139 / VTJ2:71-73. */
+int neb_output(const neb_net* net, const void* W_out, const void* b_out, int start,
+               int stop, int64_t n_points, const void* tape, void* psi,
+               neb_stream_t stream);
+
+/* 2D scalar potential: weighted Grams of the last hidden layer's field
+ * channels, A_M = sum_p w_p (h_x h_x^T + h_y h_y^T), A_S = sum_p w_p h_lap
+ * h_lap^T (FP64, [H][H]); per-CTA partial sums, FP64 cross-CTA reduction.
+ * With psi = W_out h + b: M = W_out A_M W_out^T, S = W_out A_S W_out^T, i.e.
+ * the Grams of ROLL:178-179 and VC:40-46.  qw: [n] quadrature weights,
+ * master type. */
+int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n_points,
+                    const void* tape, double* A_M, double* A_S, void* workspace,
+                    size_t workspace_bytes, neb_stream_t stream);
+
+/* FP64 K x K Grams of the fields of output rows [0, widths[L+1]) assembled
+ * from the output jets without storing them: 2D u = (psi_y, -psi_x),
+ * omega = -lap psi; 3D u = curl A, omega = curl curl A (VTJ2:93-98).
+ * M = sum_p w u_i.u_j, S = sum_p w omega_i.omega_j (ROLL:178-179, VC:40-46).
+ * accumulate != 0 adds into M and S (point chunks). */
+int neb_fields_gram(const neb_net* net, const void* W_out, const void* qw,
+                    int64_t n_points, const void* tape, double* M, double* S, int accumulate,
+                    void* workspace, size_t workspace_bytes, neb_stream_t stream);
+
+/* FP64 spectral stage on an m x m pencil (S, M), M positive definite:
+ * Cholesky of M, generalized symmetric eigensolve S v = lam M v with
+ * V^T M V = I (ascending lam), loss = sum_k c_k lam_k and its adjoints
+ * G_S = dL/dS = V diag(c) V^T, G_M = dL/dM = -V diag(c lam) V^T.
+ * Replaces ROLL:180-187 (rank gate + scipy eigh(S, M)), VTJ2:107-117
+ * trace_objective (c = 1) and VC:48-69 coefficient_peel's FP64 Cholesky.
+ * Outputs lam[m], V[m][m], G_M, G_S [m][m], loss[1] (all device, FP64);
+ * info[1] (device int) receives the solver status without a host
+ * synchronisation: 0 = success, > m = M not positive definite (rank gate),
+ * other > 0 = no convergence, -1 = non-finite loss. */
+size_t neb_spectral_workspace_bytes(int m);
+int neb_spectral(int m, const double* M, const double* S, const double* c, double* lam,
+                 double* V, double* G_M, double* G_S, double* loss, int* info,
+                 void* workspace, size_t workspace_bytes, neb_stream_t stream);
+
+/* K x H output weights between the hidden pencil and the K x K pencil
+ * (FP64): M = W A_M W^T, S = W A_S W^T; and back: G_Mh = W^T G_M W,
+ * G_Sh = W^T G_S W, gW = 2 (G_M W A_M + G_S W A_S). */
+size_t neb_pencil_workspace_bytes(int K, int H);
+int neb_pencil_project(int K, int H, const double* W_out, const double* A_M,
+                       const double* A_S, double* M, double* S, void* workspace,
+                       size_t workspace_bytes, neb_stream_t stream);
+int neb_pencil_pullback(int K, int H, const double* W_out, const double* A_M,
+                        const double* A_S, const double* G_M, const double* G_S,
+                        double* G_Mh, double* G_Sh, double* gW_out, void* workspace,
+                        size_t workspace_bytes, neb_stream_t stream);
+
+/* Reverse pass from the hidden-Gram adjoints (2D scalar potential):
+ * h_bar_x,y = 2 w h_x,y G_Mh, h_bar_lap = 2 w h_lap G_Sh, then through every
+ * hidden layer (tanh-jet transpose, data and weight gradients).  gW, gb:
+ * host arrays of n_hidden device pointers, overwritten.  Replaces
+ * HB:2034-2138 backward_gradients_block_jet1/2 with HB:1115-1173 and
+ * VTJ2:77-82 backward, VC:88-103. */
+int neb_backward_hidden(const neb_net* net, const void* const* W, const double* G_Mh,
+                        const double* G_Sh, const void* qw, int64_t n_points,
+                        const void* tape, void* const* gW, void* const* gb,
+                        void* workspace, size_t workspace_bytes, neb_stream_t stream);
+
+/* Reverse pass from adjoint output jets psibar ([n][C][stop - start]) of
+ * output rows [start, stop): gradients of every layer (output layer: rows
+ * [start, stop) of gW[n_hidden], gb[n_hidden]).  NCC:142-154 Model.backward.
+ * accumulate != 0 adds into gW / gb (point chunks of one objective). */
+int neb_backward_output(const neb_net* net, const void* const* W, int start, int stop,
+                        const void* psibar, int64_t n_points, const void* tape,
+                        void* const* gW, void* const* gb, int accumulate, void* workspace,
+                        size_t workspace_bytes, neb_stream_t stream);
+
+/* Reverse pass from the K x K Gram adjoints G_M, G_S of neb_fields_gram:
+ * field adjoints 2 w u G_M, 2 w omega G_S, their transpose onto the output
+ * jets, and then every layer.  gW, gb: n_hidden + 1 device pointers. */
+int neb_backward_fields(const neb_net* net, const void* const* W, const double* G_M,
+                        const double* G_S, const void* qw, int64_t n_points,
+                        const void* tape, void* const* gW, void* const* gb, int accumulate,
+                        void* workspace, size_t workspace_bytes, neb_stream_t stream);
+
+/* One Adam transaction over n_tensors parameter tensors (float when dtype
+ * is 0, double when 1): global gradient norm, clip scale min(1, clip/norm),
+ * commit only when every gradient is finite and the norm positive (device
+ * flag; nothing changes otherwise), bias-corrected moments with step + 1.
+ * Replaces NCC:156-171 Model.adam and HB:2184-2277 adam_step_jet1_device.
+ * norm_out, committed_out: device pointers (double, int). */
+size_t neb_adam_workspace_bytes(void);
+int neb_adam(int dtype, int n_tensors, void* const* params, void* const* exp_avg,
+             void* const* exp_avg_sq, const void* const* grads, const int64_t* sizes,
+             int step, double lr, double clip, double beta1, double beta2, double eps,
+             double* norm_out, int* committed_out, void* workspace,
+             size_t workspace_bytes, neb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NEB_GB300_H */

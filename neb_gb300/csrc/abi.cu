@@ -1,0 +1,560 @@
+// extern "C" entry points of the jet MLP, the Grams and the reverse pass.
+// Precision dispatch: NEB_PREC_FP32 / NEB_PREC_FP64 run the SIMT kernels;
+// NEB_PREC_BF16X3 runs the tcgen05 kernels of tc_path.cu.
+#include <cstdarg>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "simt_kernels.cuh"
+#include "elementwise.cuh"
+#include "tc_path.cuh"
+
+namespace neb {
+
+thread_local std::string g_last_error;
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+namespace {
+
+size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int net_channels(const neb_net* net) { return net->dim == 2 ? 4 : 10; }
+
+int check_net(const neb_net* net) {
+  NEB_REQUIRE(net != nullptr, "null neb_net");
+  NEB_REQUIRE(net->dim == 2 || net->dim == 3, "neb_net.dim must be 2 or 3 (got %d)", net->dim);
+  NEB_REQUIRE(net->n_hidden >= 1 && net->n_hidden <= NEB_MAX_HIDDEN,
+              "neb_net.n_hidden must be in [1, %d] (got %d)", NEB_MAX_HIDDEN, net->n_hidden);
+  for (int l = 0; l <= net->n_hidden + 1; ++l)
+    NEB_REQUIRE(net->widths[l] > 0 && net->widths[l] <= 65536, "neb_net.widths[%d] = %d invalid", l,
+                net->widths[l]);
+  NEB_REQUIRE(net->precision == NEB_PREC_FP32 || net->precision == NEB_PREC_FP64 ||
+                  net->precision == NEB_PREC_BF16X3,
+              "unknown precision %d", net->precision);
+  if (net->dim == 3) NEB_REQUIRE(net->widths[net->n_hidden + 1] % 3 == 0,
+                                 "3D output width must be 3 K");
+  return NEB_OK;
+}
+
+size_t master_size(const neb_net* net) { return net->precision == NEB_PREC_FP64 ? 8 : 4; }
+
+// Tape: X_0 | Z_1 | X_1 | ... | Z_L | X_L, each [n][C][w] in storage format.
+// X_l storage: FP32 -> float, FP64 -> double, BF16X3 -> hi and lo bf16 planes.
+// Z_l storage: master type.
+struct TapeLayout {
+  size_t x_off[NEB_MAX_HIDDEN + 1];
+  size_t z_off[NEB_MAX_HIDDEN + 1];
+  size_t total;
+};
+
+TapeLayout tape_layout(const neb_net* net, int64_t n) {
+  TapeLayout t{};
+  const int C = net_channels(net);
+  const size_t es = master_size(net);
+  size_t off = 0;
+  for (int l = 0; l <= net->n_hidden; ++l) {
+    size_t elems = (size_t)n * C * net->widths[l];
+    if (l > 0) {
+      t.z_off[l] = off;
+      off += a256(elems * es);
+    }
+    t.x_off[l] = off;
+    off += a256(elems * es);  // bf16 hi + lo planes = 4 bytes per element
+  }
+  t.total = off;
+  return t;
+}
+
+int64_t chunk_points(int64_t n) {
+  int64_t c = ceil_div(n, 32);
+  if (c < 256) c = 256;
+  return c;
+}
+
+int max_width(const neb_net* net) {
+  int m = 0;
+  for (int l = 0; l <= net->n_hidden + 1; ++l) m = m > net->widths[l] ? m : net->widths[l];
+  return m;
+}
+
+// Workspace: [Zbar ping][Zbar pong][partials][bias partials][G casts][tc scratch]
+struct WsLayout {
+  size_t zb0, zb1, part, partb, gcast, tc, total;
+};
+
+WsLayout ws_layout(const neb_net* net, int64_t n) {
+  WsLayout w{};
+  const int C = net_channels(net);
+  const size_t es = master_size(net);
+  const int mw = max_width(net);
+  const int64_t chunks = ceil_div(n, chunk_points(n));
+  size_t zb = a256((size_t)n * C * mw * es);
+  size_t part = a256((size_t)chunks * mw * mw * sizeof(double));
+  size_t partb = a256((size_t)chunks * mw * sizeof(double));
+  size_t gcast = a256((size_t)2 * mw * mw * es);
+  size_t tc = net->precision == NEB_PREC_BF16X3 ? a256(tc_workspace_bytes(net, n)) : 0;
+  w.zb0 = 0;
+  w.zb1 = zb;
+  w.part = 2 * zb;
+  w.partb = w.part + part;
+  w.gcast = w.partb + partb;
+  w.tc = w.gcast + gcast;
+  w.total = w.tc + tc;
+  return w;
+}
+
+template <typename T, int C>
+int launch_fwd(const T* X, const T* W, const T* b, T* Z, T* Y, int64_t n, int K, int N, int ldo,
+               cudaStream_t s) {
+  using Tl = simt::Tile<C>;
+  dim3 grid((unsigned)ceil_div(N, simt::kBN), (unsigned)ceil_div(n * C, Tl::BM));
+  if (Y)
+    simt::jet_gemm_fwd<T, C, true><<<grid, simt::kThreads, 0, s>>>(X, W, b, Z, Y, n, K, N, ldo);
+  else
+    simt::jet_gemm_fwd<T, C, false><<<grid, simt::kThreads, 0, s>>>(X, W, b, Z, Y, n, K, N, ldo);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+template <typename T, int C, int MAP>
+int launch_bwd(const T* A, const T* B0, const T* B1, const T* rowscale, T scale, const T* Zprev,
+               T* Out, int64_t n, int K, int N, cudaStream_t s) {
+  using Tl = simt::Tile<C>;
+  dim3 grid((unsigned)ceil_div(N, simt::kBN), (unsigned)ceil_div(n * C, Tl::BM));
+  if (Zprev)
+    simt::jet_gemm_bwd<T, C, MAP, true>
+        <<<grid, simt::kThreads, 0, s>>>(A, B0, B1, rowscale, scale, Zprev, Out, n, K, N);
+  else
+    simt::jet_gemm_bwd<T, C, MAP, false>
+        <<<grid, simt::kThreads, 0, s>>>(A, B0, B1, rowscale, scale, Zprev, Out, n, K, N);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+// Out[m][n] = scale * sum_{p, c in chans} w_p P[r][m] Q[r][n] -> OutT
+template <typename T, int C, typename OutT>
+int launch_rowsum(const T* P, int ldp, const T* Q, int ldq, const T* w, simt::ChanSet chans,
+                  int64_t n, int M, int N, bool sym, double scale, double* part, OutT* out,
+                  cudaStream_t s, int accumulate = 0) {
+  const int64_t cp = chunk_points(n);
+  const int chunks = (int)ceil_div(n, cp);
+  const int mt = (int)ceil_div(M, 128), nt = (int)ceil_div(N, simt::kBN);
+  const int tiles = sym ? nt * (nt + 1) / 2 : mt * nt;
+  if (sym) NEB_REQUIRE(M == N, "symmetric rowsum needs M == N");
+  dim3 grid(tiles, chunks);
+  simt::rowsum_gemm<T, C><<<grid, simt::kThreads, 0, s>>>(P, ldp, Q, ldq, w, chans, n, cp, M, N,
+                                                          sym ? 1 : 0, part);
+  NEB_LAUNCH_CHECK();
+  int64_t total = (int64_t)M * N;
+  int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 4096);
+  simt::reduce_chunks<OutT><<<blocks, 256, 0, s>>>(part, chunks, M, N, sym ? 1 : 0, scale,
+                                                    accumulate, out);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+template <typename T, int C, typename OutT>
+int launch_bias(const T* Zb, int64_t n, int N, double* partb, OutT* out, cudaStream_t s,
+                int accumulate = 0) {
+  const int64_t cp = chunk_points(n);
+  const int chunks = (int)ceil_div(n, cp);
+  dim3 grid((unsigned)ceil_div(N, 128), chunks);
+  simt::bias_partial<T, C><<<grid, 128, 0, s>>>(Zb, n, cp, N, partb);
+  NEB_LAUNCH_CHECK();
+  int blocks = (int)ceil_div(N, 256);
+  simt::reduce_chunks<OutT><<<blocks, 256, 0, s>>>(partb, chunks, 1, N, 0, 1.0, accumulate, out);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+// ---------------------------------------------------------------- forward
+template <typename T, int C>
+int forward_simt(const neb_net* net, const void* const* W, const void* const* b,
+                 const void* feats, int64_t n, void* tape, cudaStream_t s) {
+  TapeLayout tl = tape_layout(net, n);
+  char* tp = (char*)tape;
+  NEB_CUDA_CHECK(cudaMemcpyAsync(tp + tl.x_off[0], feats,
+                                 (size_t)n * C * net->widths[0] * sizeof(T),
+                                 cudaMemcpyDeviceToDevice, s));
+  for (int l = 1; l <= net->n_hidden; ++l) {
+    const T* X = (const T*)(tp + tl.x_off[l - 1]);
+    T* Z = (T*)(tp + tl.z_off[l]);
+    T* Y = (T*)(tp + tl.x_off[l]);
+    int st = launch_fwd<T, C>(X, (const T*)W[l - 1], (const T*)b[l - 1], Z, Y, n,
+                              net->widths[l - 1], net->widths[l], net->widths[l], s);
+    if (st) return st;
+  }
+  return NEB_OK;
+}
+
+// ------------------------------------------------------- hidden backward
+// Zbar of layer `l` is in `zb`; walk down to layer 1, writing gW/gb.
+template <typename T, int C>
+int backward_layers(const neb_net* net, const void* const* W, int top, T* zb, T* zb_other,
+                    const char* tp, const TapeLayout& tl, void* const* gW, void* const* gb,
+                    double* part, double* partb, int64_t n, cudaStream_t s, int accumulate = 0) {
+  simt::ChanSet all{C, {0, 1, 2, 3, 4, 5, 6, 7, 8, 9}};
+  for (int l = top; l >= 1; --l) {
+    const int in = net->widths[l - 1], out = net->widths[l];
+    const T* X = (const T*)(tp + tl.x_off[l - 1]);
+    // gW_l[o][i] = sum_r zb[r][o] X[r][i];  gb_l[o] = sum_p zb[p, value][o]
+    int st = launch_rowsum<T, C, T>(zb, out, X, in, nullptr, all, n, out, in, false, 1.0, part,
+                                    (T*)gW[l - 1], s, accumulate);
+    if (st) return st;
+    st = launch_bias<T, C, T>(zb, n, out, partb, (T*)gb[l - 1], s, accumulate);
+    if (st) return st;
+    if (l > 1) {
+      const T* Zp = (const T*)(tp + tl.z_off[l - 1]);
+      st = launch_bwd<T, C, 0>(zb, (const T*)W[l - 1], nullptr, nullptr, T(1), Zp, zb_other, n, out,
+                               in, s);
+      if (st) return st;
+      T* t = zb;
+      zb = zb_other;
+      zb_other = t;
+    }
+  }
+  return NEB_OK;
+}
+
+template <typename T, int C>
+int backward_hidden_simt(const neb_net* net, const void* const* W, const double* GMh,
+                         const double* GSh, const void* qw, int64_t n, const void* tape,
+                         void* const* gW, void* const* gb, void* ws, cudaStream_t s) {
+  const int L = net->n_hidden, H = net->widths[L];
+  TapeLayout tl = tape_layout(net, n);
+  WsLayout wl = ws_layout(net, n);
+  char* w = (char*)ws;
+  const char* tp = (const char*)tape;
+  T* zb0 = (T*)(w + wl.zb0);
+  T* zb1 = (T*)(w + wl.zb1);
+  T* gM = (T*)(w + wl.gcast);
+  T* gS = gM + (size_t)H * H;
+  int64_t hh = (int64_t)H * H;
+  int blocks = (int)std::min<int64_t>(ceil_div(hh, 256), 4096);
+  convert_kernel<double, T><<<blocks, 256, 0, s>>>(GMh, gM, hh);
+  convert_kernel<double, T><<<blocks, 256, 0, s>>>(GSh, gS, hh);
+  NEB_LAUNCH_CHECK();
+  // hbar = 2 w (h G) per channel, then the tanh-jet transpose of layer L
+  const T* HL = (const T*)(tp + tl.x_off[L]);
+  const T* ZL = (const T*)(tp + tl.z_off[L]);
+  int st = launch_bwd<T, C, 1>(HL, gM, gS, (const T*)qw, T(2), ZL, zb0, n, H, H, s);
+  if (st) return st;
+  return backward_layers<T, C>(net, W, L, zb0, zb1, tp, tl, gW, gb, (double*)(w + wl.part),
+                               (double*)(w + wl.partb), n, s);
+}
+
+template <typename T, int C>
+int backward_output_simt(const neb_net* net, const void* const* W, int start, int stop,
+                         const void* psibar, int64_t n, const void* tape, void* const* gW,
+                         void* const* gb, void* ws, cudaStream_t s, int accumulate) {
+  const int L = net->n_hidden, H = net->widths[L], Ko = stop - start;
+  TapeLayout tl = tape_layout(net, n);
+  WsLayout wl = ws_layout(net, n);
+  char* w = (char*)ws;
+  const char* tp = (const char*)tape;
+  T* zb0 = (T*)(w + wl.zb0);
+  T* zb1 = (T*)(w + wl.zb1);
+  double* part = (double*)(w + wl.part);
+  double* partb = (double*)(w + wl.partb);
+  simt::ChanSet all{C, {0, 1, 2, 3, 4, 5, 6, 7, 8, 9}};
+  const T* PB = (const T*)psibar;
+  const T* HL = (const T*)(tp + tl.x_off[L]);
+  const T* Wout = (const T*)W[L] + (size_t)start * H;
+  // output layer gradients for rows [start, stop)
+  int st = launch_rowsum<T, C, T>(PB, Ko, HL, H, nullptr, all, n, Ko, H, false, 1.0, part,
+                                  (T*)gW[L] + (size_t)start * H, s, accumulate);
+  if (st) return st;
+  st = launch_bias<T, C, T>(PB, n, Ko, partb, (T*)gb[L] + start, s, accumulate);
+  if (st) return st;
+  // hbar = psibar W_out[start:stop], then tanh-jet transpose of layer L
+  const T* ZL = (const T*)(tp + tl.z_off[L]);
+  st = launch_bwd<T, C, 0>(PB, Wout, nullptr, nullptr, T(1), ZL, zb0, n, Ko, H, s);
+  if (st) return st;
+  return backward_layers<T, C>(net, W, L, zb0, zb1, tp, tl, gW, gb, part, partb, n, s,
+                               accumulate);
+}
+
+template <typename T, int C>
+int hidden_gram_simt(const neb_net* net, const void* qw, int64_t n, const void* tape, double* AM,
+                     double* AS, void* ws, cudaStream_t s) {
+  const int L = net->n_hidden, H = net->widths[L];
+  TapeLayout tl = tape_layout(net, n);
+  WsLayout wl = ws_layout(net, n);
+  const T* HL = (const T*)((const char*)tape + tl.x_off[L]);
+  double* part = (double*)((char*)ws + wl.part);
+  simt::ChanSet grad{2, {1, 2}};
+  simt::ChanSet lap{1, {3}};
+  int st = launch_rowsum<T, C, double>(HL, H, HL, H, (const T*)qw, grad, n, H, H, true, 1.0, part,
+                                       AM, s);
+  if (st) return st;
+  return launch_rowsum<T, C, double>(HL, H, HL, H, (const T*)qw, lap, n, H, H, true, 1.0, part, AS,
+                                     s);
+}
+
+}  // namespace
+}  // namespace neb
+
+using namespace neb;
+
+#define NEB_DISPATCH(net, FN, ...)                                                 \
+  ((net)->precision == NEB_PREC_FP64                                               \
+       ? ((net)->dim == 2 ? FN<double, 4>(__VA_ARGS__) : FN<double, 10>(__VA_ARGS__)) \
+       : ((net)->dim == 2 ? FN<float, 4>(__VA_ARGS__) : FN<float, 10>(__VA_ARGS__)))
+
+extern "C" const char* neb_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" size_t neb_tape_bytes(const neb_net* net, int64_t n) {
+  if (check_net(net) != NEB_OK || n <= 0) return 0;
+  return tape_layout(net, n).total;
+}
+
+extern "C" size_t neb_workspace_bytes(const neb_net* net, int64_t n) {
+  if (check_net(net) != NEB_OK || n <= 0) return 0;
+  return ws_layout(net, n).total;
+}
+
+extern "C" int neb_features(const neb_net* net, int kind, int n_freq, const double* params,
+                            int n_params, const double* points, int64_t n, void* feats,
+                            neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  NEB_REQUIRE(n > 0 && points && feats, "neb_features: bad arguments");
+  const int F = net->widths[0];
+  double period = 0.0;
+  if (kind == NEB_FEAT_PERIODIC) {
+    NEB_REQUIRE(net->dim == 2 && n_freq > 0 && F == 4 * n_freq && n_params >= 1 && params,
+                "periodic features need dim 2, widths[0] == 4 n_freq and params[0] = period");
+    // the period is read on the host: params is a host array here
+    period = params[0];
+    NEB_REQUIRE(period > 0, "period must be positive");
+  } else if (kind == NEB_FEAT_MULTIHOLE) {
+    NEB_REQUIRE(net->dim == 2 && n_params % 2 == 0 && F == 2 + n_params / 2,
+                "multihole features need widths[0] == 2 + holes and 2 params per hole");
+  } else if (kind == NEB_FEAT_RAW3D) {
+    NEB_REQUIRE(net->dim == 3 && F == 3, "raw 3D features need dim 3 and widths[0] == 3");
+  } else {
+    NEB_REQUIRE(false, "unknown feature kind %d", kind);
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  // hole centres (host array) travel to the kernel by value
+  FeatureParams dprm{};
+  if (kind == NEB_FEAT_MULTIHOLE) {
+    NEB_REQUIRE(n_params <= 64, "at most 32 holes");
+    dprm.n = n_params;
+    for (int i = 0; i < n_params; ++i) dprm.v[i] = params[i];
+  }
+  int64_t total = n * F;
+  int blocks = (int)ceil_div(total, 256);
+  if (net->precision == NEB_PREC_FP64) {
+    if (net->dim == 2)
+      features_kernel<double, 4><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
+                                                        (double*)feats);
+    else
+      features_kernel<double, 10><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
+                                                         (double*)feats);
+  } else {
+    if (net->dim == 2)
+      features_kernel<float, 4><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
+                                                       (float*)feats);
+    else
+      features_kernel<float, 10><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
+                                                        (float*)feats);
+  }
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+extern "C" int neb_forward(const neb_net* net, const void* const* W, const void* const* b,
+                           const void* feats, int64_t n, void* tape, void* ws, size_t ws_bytes,
+                           neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  NEB_REQUIRE(n > 0 && W && b && feats && tape, "neb_forward: bad arguments");
+  for (int l = 0; l < net->n_hidden; ++l) NEB_REQUIRE(W[l] && b[l], "neb_forward: null W/b[%d]", l);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (net->precision == NEB_PREC_BF16X3) {
+    if (ws_bytes < ws_layout(net, n).total || !ws) {
+      set_error("neb_forward: workspace too small");
+      return NEB_ERR_WORKSPACE;
+    }
+    WsLayout wl = ws_layout(net, n);
+    TapeLayout tl = tape_layout(net, n);
+    TcTape tt;
+    for (int l = 0; l <= net->n_hidden; ++l) {
+      tt.x[l] = (char*)tape + tl.x_off[l];
+      tt.z[l] = (char*)tape + tl.z_off[l];
+    }
+    return tc_forward(net, (const float* const*)W, (const float* const*)b, (const float*)feats, n,
+                      tt, (char*)ws + wl.tc, s);
+  }
+  return NEB_DISPATCH(net, forward_simt, net, W, b, feats, n, tape, s);
+}
+
+template <typename T, int C>
+static int output_simt(const neb_net* net, const void* Wout, const void* bout, int start, int stop,
+                       int64_t n, const void* tape, void* psi, cudaStream_t s) {
+  const int L = net->n_hidden, H = net->widths[L];
+  TapeLayout tl = tape_layout(net, n);
+  const T* HL = (const T*)((const char*)tape + tl.x_off[L]);
+  return launch_fwd<T, C>(HL, (const T*)Wout + (size_t)start * H,
+                          bout ? (const T*)bout + start : nullptr, (T*)psi, nullptr, n, H,
+                          stop - start, stop - start, s);
+}
+
+extern "C" int neb_output(const neb_net* net, const void* Wout, const void* bout, int start,
+                          int stop, int64_t n, const void* tape, void* psi, neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  const int K = net->widths[net->n_hidden + 1];
+  NEB_REQUIRE(n > 0 && Wout && tape && psi && 0 <= start && start < stop && stop <= K,
+              "neb_output: bad arguments");
+  if (net->precision == NEB_PREC_BF16X3)
+    return tc_output(net, (const float*)Wout, (const float*)bout, start, stop, n, tape, psi,
+                     (cudaStream_t)stream);
+  return NEB_DISPATCH(net, output_simt, net, Wout, bout, start, stop, n, tape, psi,
+                      (cudaStream_t)stream);
+}
+
+extern "C" int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n, const void* tape,
+                               double* AM, double* AS, void* ws, size_t ws_bytes,
+                               neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  NEB_REQUIRE(net->dim == 2, "neb_hidden_gram: 2D scalar potential only");
+  NEB_REQUIRE(n > 0 && qw && tape && AM && AS, "neb_hidden_gram: bad arguments");
+  if (ws_bytes < ws_layout(net, n).total || !ws) {
+    set_error("neb_hidden_gram: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (net->precision == NEB_PREC_BF16X3) {
+    TapeLayout tl = tape_layout(net, n);
+    WsLayout wl = ws_layout(net, n);
+    return tc_hidden_gram(net, (const float*)qw, n, (const char*)tape + tl.x_off[net->n_hidden],
+                          AM, AS, (char*)ws + wl.part, (char*)ws + wl.tc, s);
+  }
+  if (net->precision == NEB_PREC_FP64) return hidden_gram_simt<double, 4>(net, qw, n, tape, AM, AS, ws, s);
+  return hidden_gram_simt<float, 4>(net, qw, n, tape, AM, AS, ws, s);
+}
+
+extern "C" int neb_backward_hidden(const neb_net* net, const void* const* W, const double* GMh,
+                                   const double* GSh, const void* qw, int64_t n, const void* tape,
+                                   void* const* gW, void* const* gb, void* ws, size_t ws_bytes,
+                                   neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  NEB_REQUIRE(net->dim == 2, "neb_backward_hidden: 2D scalar potential only");
+  NEB_REQUIRE(n > 0 && W && GMh && GSh && qw && tape && gW && gb, "neb_backward_hidden: bad arguments");
+  for (int l = 0; l < net->n_hidden; ++l)
+    NEB_REQUIRE(W[l] && gW[l] && gb[l], "neb_backward_hidden: null pointer at layer %d", l);
+  if (ws_bytes < ws_layout(net, n).total || !ws) {
+    set_error("neb_backward_hidden: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (net->precision == NEB_PREC_BF16X3) {
+    TapeLayout tl = tape_layout(net, n);
+    WsLayout wl = ws_layout(net, n);
+    TcTape tt;
+    for (int l = 0; l <= net->n_hidden; ++l) {
+      tt.x[l] = (char*)tape + tl.x_off[l];
+      tt.z[l] = (char*)tape + tl.z_off[l];
+    }
+    return tc_backward_hidden(net, (const float* const*)W, GMh, GSh, (const float*)qw, n, tt,
+                              (float* const*)gW, (float* const*)gb, (char*)ws, wl.zb1,
+                              (char*)ws + wl.part, (char*)ws + wl.partb, (char*)ws + wl.tc, s);
+  }
+  if (net->precision == NEB_PREC_FP64)
+    return backward_hidden_simt<double, 4>(net, W, GMh, GSh, qw, n, tape, gW, gb, ws, s);
+  return backward_hidden_simt<float, 4>(net, W, GMh, GSh, qw, n, tape, gW, gb, ws, s);
+}
+
+extern "C" int neb_backward_output(const neb_net* net, const void* const* W, int start, int stop,
+                                   const void* psibar, int64_t n, const void* tape,
+                                   void* const* gW, void* const* gb, int accumulate, void* ws,
+                                   size_t ws_bytes, neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  const int K = net->widths[net->n_hidden + 1];
+  NEB_REQUIRE(n > 0 && W && psibar && tape && gW && gb && 0 <= start && start < stop && stop <= K,
+              "neb_backward_output: bad arguments");
+  for (int l = 0; l <= net->n_hidden; ++l)
+    NEB_REQUIRE(W[l] && gW[l] && gb[l], "neb_backward_output: null pointer at layer %d", l);
+  if (ws_bytes < ws_layout(net, n).total || !ws) {
+    set_error("neb_backward_output: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  NEB_REQUIRE(net->precision != NEB_PREC_BF16X3,
+              "neb_backward_output: use NEB_PREC_FP32 or NEB_PREC_FP64 for output-jet adjoints");
+  return NEB_DISPATCH(net, backward_output_simt, net, W, start, stop, psibar, n, tape, gW, gb, ws,
+                      (cudaStream_t)stream, accumulate);
+}
+
+extern "C" int neb_fields_gram(const neb_net* net, const void* Wout, const void* qw, int64_t n,
+                               const void* tape, double* M, double* S, int accumulate, void* ws,
+                               size_t ws_bytes, neb_stream_t stream) {
+  set_error("neb_fields_gram: direct-route Grams are not built yet");
+  return NEB_ERR_UNSUPPORTED;
+}
+
+extern "C" int neb_backward_fields(const neb_net* net, const void* const* W, const double* GM,
+                                   const double* GS, const void* qw, int64_t n, const void* tape,
+                                   void* const* gW, void* const* gb, int accumulate, void* ws,
+                                   size_t ws_bytes, neb_stream_t stream) {
+  set_error("neb_backward_fields: direct-route reverse pass is not built yet");
+  return NEB_ERR_UNSUPPORTED;
+}
+
+extern "C" size_t neb_adam_workspace_bytes(void) { return 256; }
+
+extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* const* m,
+                        void* const* v, const void* const* grads, const int64_t* sizes, int step,
+                        double lr, double clip, double beta1, double beta2, double eps,
+                        double* norm_out, int* committed_out, void* ws, size_t ws_bytes,
+                        neb_stream_t stream) {
+  NEB_REQUIRE(dtype == 0 || dtype == 1, "neb_adam: dtype must be 0 (float) or 1 (double)");
+  NEB_REQUIRE(n_tensors > 0 && n_tensors <= kMaxAdamTensors, "neb_adam: 1..%d tensors",
+              kMaxAdamTensors);
+  NEB_REQUIRE(params && m && v && grads && sizes && step >= 0, "neb_adam: bad arguments");
+  if (ws_bytes < neb_adam_workspace_bytes() || !ws) {
+    set_error("neb_adam: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  AdamTable t{};
+  t.n = n_tensors;
+  t.off[0] = 0;
+  for (int i = 0; i < n_tensors; ++i) {
+    NEB_REQUIRE(params[i] && m[i] && v[i] && grads[i] && sizes[i] >= 0,
+                "neb_adam: bad tensor %d", i);
+    t.p[i] = params[i];
+    t.m[i] = m[i];
+    t.v[i] = v[i];
+    t.g[i] = grads[i];
+    t.off[i + 1] = t.off[i] + sizes[i];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  double* acc = (double*)ws;
+  int* flag = (int*)((char*)ws + 64);
+  NEB_CUDA_CHECK(cudaMemsetAsync(ws, 0, 128, s));
+  int64_t total = t.off[n_tensors];
+  int blocks = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(total, 256), 1), 1184);
+  if (dtype == 0) {
+    adam_norm<float><<<blocks, 256, 0, s>>>(t, acc, flag);
+    adam_update<float><<<blocks, 256, 0, s>>>(t, acc, flag, (double)step + 1, lr, clip, beta1,
+                                              beta2, eps, norm_out, committed_out);
+  } else {
+    adam_norm<double><<<blocks, 256, 0, s>>>(t, acc, flag);
+    adam_update<double><<<blocks, 256, 0, s>>>(t, acc, flag, (double)step + 1, lr, clip, beta1,
+                                               beta2, eps, norm_out, committed_out);
+  }
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}

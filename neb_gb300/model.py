@@ -1,0 +1,371 @@
+"""Host side of the hot path: the network-backend API over the C ABI.
+
+``Model`` keeps the method names and meaning of the reference's native
+network backend (experiments/metaball/_backend/flow/cases/metaball/
+native_cupy_core.py:111-185): ``W``/``b`` parameter lists, Adam moments
+``mW, vW, mb, vb``, ``epoch``, ``forward(data, start, stop, cache)``,
+``backward(data, start, stop, tape, adj)``, ``adam(gW, gb, lr, clip)``,
+``save``/``load`` with the keys ``W_j, b_j, mW_j, vW_j, mb_j, vb_j, epoch``.
+It differs in the network: one shared tanh MLP whose K outputs are the
+modes, instead of K per-mode SIREN networks.
+
+``spectral_step`` is the new entry of the hot path: features -> jet MLP ->
+weighted Grams -> FP64 generalized eigensolve -> objective -> hand-written
+reverse pass, with ``SpectralObjective`` as its ``torch.autograd.Function``.
+
+All device memory comes from PyTorch; kernels run on the current CUDA stream.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .configs import NebConfig, glorot_params, objective_weights
+from .jets import Jet, pack, unpack
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+class _Buffers:
+    """Grow-only device byte buffers keyed by role."""
+
+    def __init__(self, device):
+        self.device = device
+        self.bufs: dict[str, torch.Tensor] = {}
+
+    def get(self, key: str, nbytes: int) -> torch.Tensor:
+        nbytes = max(int(nbytes), 256)
+        b = self.bufs.get(key)
+        if b is None or b.numel() < nbytes:
+            b = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self.bufs[key] = b
+        return b
+
+
+@dataclass
+class Tape:
+    """Activation tape of one forward pass (inputs and pre-activations of
+    every hidden layer, in the library's storage format)."""
+    buffer: torch.Tensor
+    n_points: int
+    features: torch.Tensor
+
+
+class Model:
+    """Shared tanh MLP with analytic spatial jets (reference backend API)."""
+
+    def __init__(self, cfg: NebConfig, K: int | None = None, seed: int = 0,
+                 precision: str = "bf16x3", device: str | torch.device = "cuda"):
+        if precision not in N.PREC:
+            raise ValueError(f"precision must be one of {tuple(N.PREC)}")
+        if K is not None:
+            cfg = cfg.scaled(outputs=K * (3 if cfg.dim == 3 else 1))
+        self.c = cfg
+        self.K = cfg.K
+        self.precision = precision
+        self.device = torch.device(device)
+        self.dtype = torch.float64 if precision == "fp64" else torch.float32
+        self.epoch = 0
+        self.W, self.b = [], []
+        for W, b in glorot_params(cfg.widths, seed):
+            self.W.append(torch.tensor(W, dtype=self.dtype, device=self.device))
+            self.b.append(torch.tensor(b, dtype=self.dtype, device=self.device))
+        self.mW = [torch.zeros_like(w) for w in self.W]
+        self.vW = [torch.zeros_like(w) for w in self.W]
+        self.mb = [torch.zeros_like(b) for b in self.b]
+        self.vb = [torch.zeros_like(b) for b in self.b]
+        self.net = N.NebNet.make(cfg.dim, cfg.widths, precision)
+        self._buf = _Buffers(self.device)
+        N.load()
+
+    # ------------------------------------------------------------ helpers
+    @property
+    def channels(self) -> int:
+        return 4 if self.c.dim == 2 else 10
+
+    @property
+    def n_hidden(self) -> int:
+        return len(self.c.widths) - 2
+
+    def parameters(self):
+        return [*self.W, *self.b]
+
+    def set_parameters(self, params) -> None:
+        """Load (W, b) pairs (float64 arrays or tensors) into the masters."""
+        for j, (W, b) in enumerate(params):
+            self.W[j].copy_(torch.as_tensor(np.asarray(W), dtype=self.dtype))
+            self.b[j].copy_(torch.as_tensor(np.asarray(b), dtype=self.dtype))
+
+    def _ws(self, n: int) -> torch.Tensor:
+        return self._buf.get("ws", N.load().neb_workspace_bytes(ctypes.byref(self.net), n))
+
+    def features(self, points) -> torch.Tensor:
+        """Input feature jets [n, C, F] (device, master dtype) of points [n, dim]."""
+        pts = torch.as_tensor(points, dtype=torch.float64, device=self.device).contiguous()
+        if pts.ndim != 2 or pts.shape[1] != self.c.dim:
+            raise ValueError(f"points must be [n, {self.c.dim}]")
+        n = pts.shape[0]
+        out = torch.empty((n, self.channels, self.c.widths[0]), dtype=self.dtype, device=self.device)
+        prm = self.c.feature_params()
+        arr = (ctypes.c_double * max(len(prm), 1))(*prm)
+        N.call("neb_features", ctypes.byref(self.net), N.FEAT[self.c.features], self.c.n_freq, arr,
+               len(prm), pts.data_ptr(), n, out.data_ptr(), _stream())
+        return out
+
+    def run_forward(self, feats: torch.Tensor) -> Tape:
+        """Hidden layers over packed feature jets; returns the tape."""
+        feats = feats.to(self.dtype).contiguous()
+        n = feats.shape[0]
+        tape = self._buf.get("tape", N.load().neb_tape_bytes(ctypes.byref(self.net), n))
+        ws = self._ws(n)
+        N.call("neb_forward", ctypes.byref(self.net), N.ptr_array(self.W), N.ptr_array(self.b),
+               feats.data_ptr(), n, tape.data_ptr(), ws.data_ptr(), ws.numel(), _stream())
+        return Tape(tape, n, feats)
+
+    def output(self, tape: Tape, start: int = 0, stop: int | None = None) -> torch.Tensor:
+        stop = self.c.widths[-1] if stop is None else stop
+        psi = torch.empty((tape.n_points, self.channels, stop - start), dtype=self.dtype,
+                          device=self.device)
+        N.call("neb_output", ctypes.byref(self.net), self.W[-1].data_ptr(), self.b[-1].data_ptr(),
+               start, stop, tape.n_points, tape.buffer.data_ptr(), psi.data_ptr(), _stream())
+        return psi
+
+    # ------------------------------------------------- reference backend API
+    def forward(self, data, start: int = 0, stop: int | None = None, cache: bool = False):
+        """Output jets of outputs [start, stop) at ``data.features``.
+
+        ``data.features``: a :class:`Jet` or a packed [n, C, F] tensor.  An
+        ``envelope`` other than the identity is not supported.  Returns
+        ``(field_jet, tape)``; the tape is None unless ``cache``."""
+        _check_identity_envelope(data)
+        feats = data.features
+        feats = pack(feats, self.c.dim).to(self.device, self.dtype) if isinstance(feats, Jet) else feats
+        tape = self.run_forward(feats)
+        if cache:  # keep this tape: later calls must not overwrite it
+            tape = Tape(tape.buffer.clone(), tape.n_points, tape.features)
+        psi = self.output(tape, start, stop)
+        return unpack(psi, self.c.dim), (tape if cache else None)
+
+    def backward(self, data, start: int, stop: int | None, tape: Tape, adj):
+        """Parameter gradients of <adj, forward(data, start, stop)> (lists of
+        tensors shaped like ``W`` and ``b``; output rows outside [start, stop)
+        are zero)."""
+        stop = self.c.widths[-1] if stop is None else stop
+        pb = pack(adj, self.c.dim).to(self.device, self.dtype).contiguous() \
+            if isinstance(adj, Jet) else adj.to(self.dtype).contiguous()
+        if pb.shape != (tape.n_points, self.channels, stop - start):
+            raise ValueError(f"adjoint shape {tuple(pb.shape)} does not match the outputs")
+        gW = [torch.zeros_like(w) for w in self.W]
+        gb = [torch.zeros_like(b) for b in self.b]
+        ws = self._ws(tape.n_points)
+        N.call("neb_backward_output", ctypes.byref(self.net), N.ptr_array(self.W), start, stop,
+               pb.data_ptr(), tape.n_points, tape.buffer.data_ptr(), N.ptr_array(gW),
+               N.ptr_array(gb), 0, ws.data_ptr(), ws.numel(), _stream())
+        return gW, gb
+
+    def adam(self, gW, gb, lr: float, clip: float = 8.0, beta1: float = 0.9,
+             beta2: float = 0.999, eps: float = 1e-8) -> float:
+        """One Adam transaction with global-norm clipping.  Raises
+        FloatingPointError, with nothing changed, when a gradient is not
+        finite or the norm is zero."""
+        norm, committed = self.adam_async(gW, gb, lr, clip, beta1, beta2, eps)
+        if not bool(committed.item()):
+            raise FloatingPointError("Invalid parameter gradients; no optimizer update")
+        return float(norm.item())
+
+    def adam_async(self, gW, gb, lr, clip=8.0, beta1=0.9, beta2=0.999, eps=1e-8):
+        """Adam without a host synchronisation: returns device (norm,
+        committed) tensors; the epoch advances (the caller checks commit)."""
+        params = [*self.W, *self.b]
+        grads = [g.to(self.dtype).contiguous() for g in [*gW, *gb]]
+        for p, g in zip(params, grads):
+            if p.shape != g.shape:
+                raise ValueError(f"gradient shape {tuple(g.shape)} != parameter {tuple(p.shape)}")
+        sizes = (ctypes.c_int64 * len(params))(*[p.numel() for p in params])
+        norm = torch.empty((), dtype=torch.float64, device=self.device)
+        committed = torch.empty((), dtype=torch.int32, device=self.device)
+        ws = self._buf.get("adam", N.load().neb_adam_workspace_bytes())
+        N.call("neb_adam", 1 if self.dtype == torch.float64 else 0, len(params),
+               N.ptr_array(params), N.ptr_array([*self.mW, *self.mb]),
+               N.ptr_array([*self.vW, *self.vb]), N.ptr_array(grads), sizes, self.epoch, lr, clip,
+               beta1, beta2, eps, norm.data_ptr(), committed.data_ptr(), ws.data_ptr(), ws.numel(),
+               _stream())
+        self.epoch += 1
+        return norm, committed
+
+    def save(self, path, configuration=None) -> None:
+        arrays = {f"{name}_{j}": a.detach().cpu().numpy()
+                  for name in ("W", "b", "mW", "vW", "mb", "vb")
+                  for j, a in enumerate(getattr(self, name))}
+        arrays["epoch"] = np.asarray(self.epoch)
+        path = Path(path)
+        tmp = path.with_suffix(".tmp.npz")
+        np.savez(tmp, **arrays)
+        tmp.replace(path)
+
+    def load(self, path, configuration=None) -> None:
+        with np.load(path) as z:
+            self.epoch = int(z["epoch"])
+            for name in ("W", "b", "mW", "vW", "mb", "vb"):
+                for j, a in enumerate(getattr(self, name)):
+                    a.copy_(torch.as_tensor(z[f"{name}_{j}"], dtype=self.dtype))
+
+
+def _check_identity_envelope(data) -> None:
+    env = getattr(data, "envelope", None)
+    if env is None:
+        return
+    v = env.value if isinstance(env, Jet) else torch.as_tensor(env)
+    g = env.grad if isinstance(env, Jet) else None
+    ok = bool(torch.all(torch.as_tensor(v) == 1)) and (g is None or bool(torch.all(torch.as_tensor(g) == 0)))
+    if not ok:
+        raise ValueError("only the identity envelope (periodic / free domains) is supported")
+
+
+# ----------------------------------------------------------------- spectral
+@dataclass
+class SpectralResult:
+    loss: torch.Tensor            # device scalar (FP64)
+    eigenvalues: torch.Tensor     # [m] FP64, ascending
+    eigenvectors: torch.Tensor    # [m][m] FP64, row k = eigenvector k (pencil coordinates)
+    rank: int                     # m: dimension of the span of the K fields
+    info: torch.Tensor            # device int: solver status
+    grads: tuple | None = None    # (gW list, gb list) when training
+    M: torch.Tensor | None = None
+    S: torch.Tensor | None = None
+    A_M: torch.Tensor | None = None
+    A_S: torch.Tensor | None = None
+
+
+class SpectralState:
+    """Per-model FP64 buffers of the spectral stage."""
+
+    def __init__(self, model: Model):
+        self.model = model
+        self.buf = _Buffers(model.device)
+
+
+def _f64(shape, device):
+    return torch.empty(shape, dtype=torch.float64, device=device)
+
+
+def spectral_step(model: Model, points=None, weights=None, training: bool = True,
+                  objective: str | None = None, return_grams: bool = False,
+                  features: torch.Tensor | None = None, check: bool = True) -> SpectralResult:
+    """One objective (+ gradient) evaluation of the eigenfluid basis.
+
+    points [n, dim] and weights [n] (host arrays or device tensors), or
+    ``features`` (packed jets) with ``weights``.  2D scalar potentials use
+    the hidden-layer pencil: A_M, A_S (H x H) from the last hidden layer,
+    and M = W_out A_M W_out^T, S = W_out A_S W_out^T.  When K >= H the finite
+    eigenvalues of (S, M) are those of (A_S, A_M) (the K fields span the H
+    hidden fields); otherwise the K x K pencil is solved.  ``check`` reads
+    the solver status back (one 4-byte D2H) and raises FloatingPointError.
+    """
+    cfg = model.c
+    if cfg.dim != 2:
+        raise NotImplementedError("spectral_step: the 3D curl path uses the direct Grams")
+    kind = objective or cfg.objective
+    dev = model.device
+    feats = model.features(points) if features is None else features
+    qw = torch.as_tensor(weights, device=dev).to(model.dtype).contiguous()
+    n = feats.shape[0]
+    if qw.shape != (n,):
+        raise ValueError("weights must be [n]")
+    lib = N.load()
+    st = getattr(model, "_spectral", None) or SpectralState(model)
+    model._spectral = st
+    s = _stream()
+    tape = model.run_forward(feats)
+    H, K = cfg.hidden, cfg.widths[-1]
+    AM, AS = _f64((H, H), dev), _f64((H, H), dev)
+    ws = model._ws(n)
+    N.call("neb_hidden_gram", ctypes.byref(model.net), qw.data_ptr(), n, tape.buffer.data_ptr(),
+           AM.data_ptr(), AS.data_ptr(), ws.data_ptr(), ws.numel(), s)
+    Wout = model.W[-1].to(torch.float64).contiguous()
+    pws = st.buf.get("pencil", lib.neb_pencil_workspace_bytes(K, H))
+    M = S = None
+    if K < H or return_grams:
+        M, S = _f64((K, K), dev), _f64((K, K), dev)
+        N.call("neb_pencil_project", K, H, Wout.data_ptr(), AM.data_ptr(), AS.data_ptr(),
+               M.data_ptr(), S.data_ptr(), pws.data_ptr(), pws.numel(), s)
+    if K >= H:
+        m, PM, PS = H, AM, AS
+    else:
+        m, PM, PS = K, M, S
+    c = torch.as_tensor(objective_weights(kind, m), dtype=torch.float64, device=dev)
+    lam, V, GM, GS = _f64((m,), dev), _f64((m, m), dev), _f64((m, m), dev), _f64((m, m), dev)
+    loss = _f64((), dev)
+    info = torch.zeros((), dtype=torch.int32, device=dev)
+    sws = st.buf.get("spectral", lib.neb_spectral_workspace_bytes(m))
+    N.call("neb_spectral", m, PM.data_ptr(), PS.data_ptr(), c.data_ptr(), lam.data_ptr(),
+           V.data_ptr(), GM.data_ptr(), GS.data_ptr(), loss.data_ptr(), info.data_ptr(),
+           sws.data_ptr(), sws.numel(), s)
+    res = SpectralResult(loss, lam, V, m, info, M=M, S=S, A_M=AM, A_S=AS)
+    if training:
+        L = model.n_hidden
+        gW = [torch.empty_like(w) for w in model.W]
+        gb = [torch.empty_like(b) for b in model.b]
+        if K >= H:
+            GMh, GSh = GM, GS
+            gW[L].zero_()
+        else:
+            GMh, GSh = _f64((H, H), dev), _f64((H, H), dev)
+            gWo = _f64((K, H), dev)
+            N.call("neb_pencil_pullback", K, H, Wout.data_ptr(), AM.data_ptr(), AS.data_ptr(),
+                   GM.data_ptr(), GS.data_ptr(), GMh.data_ptr(), GSh.data_ptr(), gWo.data_ptr(),
+                   pws.data_ptr(), pws.numel(), s)
+            gW[L].copy_(gWo)
+        gb[L].zero_()
+        N.call("neb_backward_hidden", ctypes.byref(model.net), N.ptr_array(model.W),
+               GMh.data_ptr(), GSh.data_ptr(), qw.data_ptr(), n, tape.buffer.data_ptr(),
+               N.ptr_array(gW[:L]), N.ptr_array(gb[:L]), ws.data_ptr(), ws.numel(), s)
+        res.grads = (gW, gb)
+    if check:
+        code = int(info.item())
+        if code != 0:
+            raise FloatingPointError(
+                f"spectral stage failed (info={code}): the mass matrix is not positive definite "
+                "or the eigensolver did not converge; no update")
+    return res
+
+
+def train_step(model: Model, points, weights, lr: float | None = None,
+               clip: float | None = None, check: bool = True) -> SpectralResult:
+    """spectral_step + Adam (one optimizer update)."""
+    res = spectral_step(model, points, weights, training=True, check=check)
+    gW, gb = res.grads
+    lr = model.c.lr if lr is None else lr
+    clip = model.c.clip if clip is None else clip
+    if check:
+        model.adam(gW, gb, lr, clip)
+    else:
+        model.adam_async(gW, gb, lr, clip)
+    return res
+
+
+class SpectralObjective(torch.autograd.Function):
+    """loss = sum_k c_k lam_k(S, M) as an autograd node over the parameters.
+
+    ``SpectralObjective.apply(model, features, weights, *model.parameters())``
+    returns the FP64 loss; its backward is the library's hand-written reverse
+    pass (no autograd tape of the forward)."""
+
+    @staticmethod
+    def forward(ctx, model, features, weights, *params):
+        res = spectral_step(model, features=features, weights=weights, training=True)
+        gW, gb = res.grads
+        ctx.save_for_backward(*gW, *gb)
+        return res.loss.clone()
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        grads = ctx.saved_tensors
+        return (None, None, None, *[g * grad_out.to(g.dtype) for g in grads])
