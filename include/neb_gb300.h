@@ -64,6 +64,19 @@ typedef struct neb_net {
 /* Thread-local message of the last failing call. */
 const char* neb_last_error(void);
 
+/* Instrumentation (the role of the reference's synchronised stage timers,
+ * VC:25-30 timed): neb_kernel_launches() counts every kernel this library has
+ * launched (its own kernels; cuSOLVER / cuBLAS calls count once each).
+ * Between neb_timing_begin() and neb_timing_end() every launch is bracketed
+ * by CUDA events on its stream; neb_timing_end synchronises those events and
+ * reports, per kernel name, the launch count, total milliseconds and the
+ * algorithmic flops and bytes of those launches (up to max_kernels entries;
+ * names are written as NUL-terminated strings of name_len bytes each). */
+unsigned long long neb_kernel_launches(void);
+int neb_timing_begin(void);
+int neb_timing_end(int max_kernels, char* names, int name_len, int* launches, double* total_ms,
+                   double* flops, double* bytes, int* n_kernels);
+
 /* Bytes of the activation tape (inputs and pre-activations of every layer,
  * in the precision's storage format) for n_points; and of the scratch
  * workspace every neb_* call below needs for n_points. */
@@ -171,6 +184,13 @@ int neb_backward_fields(const neb_net* net, const void* const* W, const double* 
                         const double* G_S, const void* qw, int64_t n_points,
                         const void* tape, void* const* gW, void* const* gb, int accumulate,
                         void* workspace, size_t workspace_bytes, neb_stream_t stream);
+
+/* Synchronises the stream and reports whether a bounded device-side wait of
+ * the tensor-core kernels gave up since the last neb_forward on this
+ * workspace (NEB_ERR_TIMEOUT), i.e. whether the step's results are invalid.
+ * NEB_OK for the SIMT precisions. */
+int neb_check_status(const neb_net* net, int64_t n_points, void* workspace,
+                     size_t workspace_bytes, neb_stream_t stream);
 
 /* One Adam transaction over n_tensors parameter tensors (float when dtype
  * is 0, double when 1): global gradient norm, clip scale min(1, clip/norm),

@@ -43,6 +43,10 @@ class NebNet(ctypes.Structure):
 # name -> (restype, argtypes)
 _SIGNATURES = {
     "neb_last_error": (ctypes.c_char_p, []),
+    "neb_kernel_launches": (ctypes.c_ulonglong, []),
+    "neb_timing_begin": (c_int, []),
+    "neb_timing_end": (c_int, [c_int, ctypes.c_char_p, c_int, POINTER(c_int), POINTER(c_double),
+                               POINTER(c_double), POINTER(c_double), POINTER(c_int)]),
     "neb_tape_bytes": (c_size_t, [POINTER(NebNet), c_int64]),
     "neb_workspace_bytes": (c_size_t, [POINTER(NebNet), c_int64]),
     "neb_features": (c_int, [POINTER(NebNet), c_int, c_int, POINTER(c_double), c_int, c_void_p,
@@ -72,6 +76,7 @@ _SIGNATURES = {
     "neb_backward_fields": (c_int, [POINTER(NebNet), POINTER(c_void_p), c_void_p, c_void_p,
                                     c_void_p, c_int64, c_void_p, POINTER(c_void_p),
                                     POINTER(c_void_p), c_int, c_void_p, c_size_t, c_void_p]),
+    "neb_check_status": (c_int, [POINTER(NebNet), c_int64, c_void_p, c_size_t, c_void_p]),
     "neb_adam_workspace_bytes": (c_size_t, []),
     "neb_adam": (c_int, [c_int, c_int, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p),
                          POINTER(c_void_p), POINTER(c_int64), c_int, c_double, c_double, c_double,
@@ -121,6 +126,31 @@ def check(status: int, what: str) -> None:
 
 def call(name: str, *args) -> None:
     check(getattr(load(), name)(*args), name)
+
+
+def kernel_launches() -> int:
+    return int(load().neb_kernel_launches())
+
+
+def timing_begin() -> None:
+    call("neb_timing_begin")
+
+
+def timing_end(max_kernels: int = 64) -> dict:
+    """Per-kernel {name: (launches, total_ms, flops, bytes)} since timing_begin."""
+    name_len = 64
+    names = ctypes.create_string_buffer(max_kernels * name_len)
+    launches = (c_int * max_kernels)()
+    ms = (c_double * max_kernels)()
+    fl = (c_double * max_kernels)()
+    by = (c_double * max_kernels)()
+    n = c_int(0)
+    call("neb_timing_end", max_kernels, names, name_len, launches, ms, fl, by, ctypes.byref(n))
+    out = {}
+    for k in range(n.value):
+        name = names.raw[k * name_len:(k + 1) * name_len].split(b"\0", 1)[0].decode()
+        out[name] = (launches[k], ms[k], fl[k], by[k])
+    return out
 
 
 def ptr_array(tensors) -> ctypes.Array:

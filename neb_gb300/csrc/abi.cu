@@ -13,6 +13,44 @@ namespace neb {
 
 thread_local std::string g_last_error;
 
+// ---------------------------------------------------------------- timing
+namespace {
+struct TimingEntry {
+  const char* name;
+  cudaEvent_t a, b;
+  double flops, bytes;
+};
+struct TimingState {
+  bool enabled = false;
+  std::vector<TimingEntry> entries;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  cudaEvent_t get() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+};
+TimingState g_timing;
+unsigned long long g_launches = 0;
+}  // namespace
+
+void count_launch() { __atomic_add_fetch(&g_launches, 1ull, __ATOMIC_RELAXED); }
+
+void timing_record(const char* name, cudaStream_t s, double flops, double bytes, bool begin) {
+  if (!g_timing.enabled) return;
+  cudaEvent_t e = g_timing.get();
+  cudaEventRecord(e, s);
+  if (begin) {
+    g_timing.entries.push_back({name, e, nullptr, flops, bytes});
+  } else if (!g_timing.entries.empty()) {
+    g_timing.entries.back().b = e;
+  }
+}
+
 void set_error(const char* fmt, ...) {
   char buf[1024];
   va_list ap;
@@ -57,6 +95,10 @@ struct TapeLayout {
 
 TapeLayout tape_layout(const neb_net* net, int64_t n) {
   TapeLayout t{};
+  if (net->precision == NEB_PREC_BF16X3) {
+    t.total = tc_tape_bytes(net, n, t.x_off, t.z_off);
+    return t;
+  }
   const int C = net_channels(net);
   const size_t es = master_size(net);
   size_t off = 0;
@@ -92,6 +134,10 @@ struct WsLayout {
 
 WsLayout ws_layout(const neb_net* net, int64_t n) {
   WsLayout w{};
+  if (net->precision == NEB_PREC_BF16X3) {
+    w.total = a256(tc_workspace_bytes(net, n));
+    return w;
+  }
   const int C = net_channels(net);
   const size_t es = master_size(net);
   const int mw = max_width(net);
@@ -116,6 +162,8 @@ int launch_fwd(const T* X, const T* W, const T* b, T* Z, T* Y, int64_t n, int K,
                cudaStream_t s) {
   using Tl = simt::Tile<C>;
   dim3 grid((unsigned)ceil_div(N, simt::kBN), (unsigned)ceil_div(n * C, Tl::BM));
+  KernelScope ks(Y ? "simt_jet_layer_fwd" : "simt_jet_output_fwd", s, 2.0 * n * C * K * N,
+                 (double)n * C * (K + (Y ? 2 : 1) * N) * sizeof(T));
   if (Y)
     simt::jet_gemm_fwd<T, C, true><<<grid, simt::kThreads, 0, s>>>(X, W, b, Z, Y, n, K, N, ldo);
   else
@@ -129,6 +177,9 @@ int launch_bwd(const T* A, const T* B0, const T* B1, const T* rowscale, T scale,
                T* Out, int64_t n, int K, int N, cudaStream_t s) {
   using Tl = simt::Tile<C>;
   dim3 grid((unsigned)ceil_div(N, simt::kBN), (unsigned)ceil_div(n * C, Tl::BM));
+  KernelScope ks(MAP ? "simt_gram_adjoint_bwd" : "simt_jet_layer_bwd_data", s,
+                 2.0 * n * (MAP ? 3 : C) * K * N,
+                 (double)n * C * (K + (Zprev ? 2 : 1) * N) * sizeof(T));
   if (Zprev)
     simt::jet_gemm_bwd<T, C, MAP, true>
         <<<grid, simt::kThreads, 0, s>>>(A, B0, B1, rowscale, scale, Zprev, Out, n, K, N);
@@ -150,14 +201,22 @@ int launch_rowsum(const T* P, int ldp, const T* Q, int ldq, const T* w, simt::Ch
   const int tiles = sym ? nt * (nt + 1) / 2 : mt * nt;
   if (sym) NEB_REQUIRE(M == N, "symmetric rowsum needs M == N");
   dim3 grid(tiles, chunks);
-  simt::rowsum_gemm<T, C><<<grid, simt::kThreads, 0, s>>>(P, ldp, Q, ldq, w, chans, n, cp, M, N,
-                                                          sym ? 1 : 0, part);
-  NEB_LAUNCH_CHECK();
+  {
+    KernelScope ks(sym ? "simt_gram" : "simt_weight_grad", s,
+                   (sym ? 1.0 : 2.0) * n * chans.n * (double)M * N,
+                   (double)n * chans.n * (M + N) * sizeof(T));
+    simt::rowsum_gemm<T, C><<<grid, simt::kThreads, 0, s>>>(P, ldp, Q, ldq, w, chans, n, cp, M, N,
+                                                            sym ? 1 : 0, part);
+    NEB_LAUNCH_CHECK();
+  }
   int64_t total = (int64_t)M * N;
   int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 4096);
-  simt::reduce_chunks<OutT><<<blocks, 256, 0, s>>>(part, chunks, M, N, sym ? 1 : 0, scale,
-                                                    accumulate, out);
-  NEB_LAUNCH_CHECK();
+  {
+    KernelScope ks("reduce_chunks", s, 0, (double)chunks * total * 8);
+    simt::reduce_chunks<OutT><<<blocks, 256, 0, s>>>(part, chunks, M, N, sym ? 1 : 0, scale,
+                                                      accumulate, out);
+    NEB_LAUNCH_CHECK();
+  }
   return NEB_OK;
 }
 
@@ -167,11 +226,17 @@ int launch_bias(const T* Zb, int64_t n, int N, double* partb, OutT* out, cudaStr
   const int64_t cp = chunk_points(n);
   const int chunks = (int)ceil_div(n, cp);
   dim3 grid((unsigned)ceil_div(N, 128), chunks);
-  simt::bias_partial<T, C><<<grid, 128, 0, s>>>(Zb, n, cp, N, partb);
-  NEB_LAUNCH_CHECK();
+  {
+    KernelScope ks("bias_grad", s, 0, (double)n * N * sizeof(T));
+    simt::bias_partial<T, C><<<grid, 128, 0, s>>>(Zb, n, cp, N, partb);
+    NEB_LAUNCH_CHECK();
+  }
   int blocks = (int)ceil_div(N, 256);
-  simt::reduce_chunks<OutT><<<blocks, 256, 0, s>>>(partb, chunks, 1, N, 0, 1.0, accumulate, out);
-  NEB_LAUNCH_CHECK();
+  {
+    KernelScope ks("reduce_chunks", s, 0, (double)chunks * N * 8);
+    simt::reduce_chunks<OutT><<<blocks, 256, 0, s>>>(partb, chunks, 1, N, 0, 1.0, accumulate, out);
+    NEB_LAUNCH_CHECK();
+  }
   return NEB_OK;
 }
 
@@ -239,9 +304,16 @@ int backward_hidden_simt(const neb_net* net, const void* const* W, const double*
   T* gS = gM + (size_t)H * H;
   int64_t hh = (int64_t)H * H;
   int blocks = (int)std::min<int64_t>(ceil_div(hh, 256), 4096);
-  convert_kernel<double, T><<<blocks, 256, 0, s>>>(GMh, gM, hh);
-  convert_kernel<double, T><<<blocks, 256, 0, s>>>(GSh, gS, hh);
-  NEB_LAUNCH_CHECK();
+  {
+    KernelScope ks("convert", s, 0, (double)hh * 2 * (8 + sizeof(T)));
+    convert_kernel<double, T><<<blocks, 256, 0, s>>>(GMh, gM, hh);
+    NEB_LAUNCH_CHECK();
+  }
+  {
+    KernelScope ks("convert", s, 0, (double)hh * (8 + sizeof(T)));
+    convert_kernel<double, T><<<blocks, 256, 0, s>>>(GSh, gS, hh);
+    NEB_LAUNCH_CHECK();
+  }
   // hbar = 2 w (h G) per channel, then the tanh-jet transpose of layer L
   const T* HL = (const T*)(tp + tl.x_off[L]);
   const T* ZL = (const T*)(tp + tl.z_off[L]);
@@ -311,6 +383,56 @@ using namespace neb;
 
 extern "C" const char* neb_last_error(void) { return g_last_error.c_str(); }
 
+extern "C" unsigned long long neb_kernel_launches(void) {
+  return __atomic_load_n(&g_launches, __ATOMIC_RELAXED);
+}
+
+extern "C" int neb_timing_begin(void) {
+  g_timing.entries.clear();
+  g_timing.used = 0;
+  g_timing.enabled = true;
+  return NEB_OK;
+}
+
+extern "C" int neb_timing_end(int max_kernels, char* names, int name_len, int* launches,
+                              double* total_ms, double* flops, double* bytes, int* n_kernels) {
+  g_timing.enabled = false;
+  std::vector<std::string> keys;
+  std::vector<int> cnt;
+  std::vector<double> ms, fl, by;
+  for (auto& e : g_timing.entries) {
+    if (!e.b) continue;
+    NEB_CUDA_CHECK(cudaEventSynchronize(e.b));
+    float t = 0.f;
+    NEB_CUDA_CHECK(cudaEventElapsedTime(&t, e.a, e.b));
+    size_t k = 0;
+    while (k < keys.size() && keys[k] != e.name) ++k;
+    if (k == keys.size()) {
+      keys.push_back(e.name);
+      cnt.push_back(0);
+      ms.push_back(0);
+      fl.push_back(0);
+      by.push_back(0);
+    }
+    cnt[k] += 1;
+    ms[k] += t;
+    fl[k] += e.flops;
+    by[k] += e.bytes;
+  }
+  int n = (int)keys.size() < max_kernels ? (int)keys.size() : max_kernels;
+  for (int k = 0; k < n; ++k) {
+    snprintf(names + (size_t)k * name_len, name_len, "%s", keys[k].c_str());
+    launches[k] = cnt[k];
+    total_ms[k] = ms[k];
+    flops[k] = fl[k];
+    bytes[k] = by[k];
+  }
+  *n_kernels = n;
+  g_timing.entries.clear();
+  g_timing.used = 0;
+  return NEB_OK;
+}
+
 extern "C" size_t neb_tape_bytes(const neb_net* net, int64_t n) {
   if (check_net(net) != NEB_OK || n <= 0) return 0;
   return tape_layout(net, n).total;
@@ -353,6 +475,7 @@ extern "C" int neb_features(const neb_net* net, int kind, int n_freq, const doub
   }
   int64_t total = n * F;
   int blocks = (int)ceil_div(total, 256);
+  KernelScope ks("features", s, 0, (double)total * net_channels(net) * master_size(net));
   if (net->precision == NEB_PREC_FP64) {
     if (net->dim == 2)
       features_kernel<double, 4><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
@@ -439,7 +562,7 @@ extern "C" int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n, co
     TapeLayout tl = tape_layout(net, n);
     WsLayout wl = ws_layout(net, n);
     return tc_hidden_gram(net, (const float*)qw, n, (const char*)tape + tl.x_off[net->n_hidden],
-                          AM, AS, (char*)ws + wl.part, (char*)ws + wl.tc, s);
+                          AM, AS, (char*)ws + wl.tc, s);
   }
   if (net->precision == NEB_PREC_FP64) return hidden_gram_simt<double, 4>(net, qw, n, tape, AM, AS, ws, s);
   return hidden_gram_simt<float, 4>(net, qw, n, tape, AM, AS, ws, s);
@@ -468,9 +591,8 @@ extern "C" int neb_backward_hidden(const neb_net* net, const void* const* W, con
       tt.x[l] = (char*)tape + tl.x_off[l];
       tt.z[l] = (char*)tape + tl.z_off[l];
     }
-    return tc_backward_hidden(net, (const float* const*)W, GMh, GSh, (const float*)qw, n, tt,
-                              (float* const*)gW, (float* const*)gb, (char*)ws, wl.zb1,
-                              (char*)ws + wl.part, (char*)ws + wl.partb, (char*)ws + wl.tc, s);
+    return tc_backward_hidden(net, GMh, GSh, (const float*)qw, n, tt, (float* const*)gW,
+                              (float* const*)gb, (char*)ws + wl.tc, s);
   }
   if (net->precision == NEB_PREC_FP64)
     return backward_hidden_simt<double, 4>(net, W, GMh, GSh, qw, n, tape, gW, gb, ws, s);
@@ -513,6 +635,26 @@ extern "C" int neb_backward_fields(const neb_net* net, const void* const* W, con
   return NEB_ERR_UNSUPPORTED;
 }
 
+extern "C" int neb_check_status(const neb_net* net, int64_t n, void* ws, size_t ws_bytes,
+                                neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  if (net->precision != NEB_PREC_BF16X3) return NEB_OK;
+  if (ws_bytes < ws_layout(net, n).total || !ws) {
+    set_error("neb_check_status: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  int code = 0;
+  st = tc_read_status(net, n, (char*)ws + ws_layout(net, n).tc, (cudaStream_t)stream, &code);
+  if (st) return st;
+  if (code) {
+    set_error("a bounded device-side wait gave up (status %d); results of this step are invalid",
+              code);
+    return NEB_ERR_TIMEOUT;
+  }
+  return NEB_OK;
+}
+
 extern "C" size_t neb_adam_workspace_bytes(void) { return 256; }
 
 extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* const* m,
@@ -546,15 +688,22 @@ extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* con
   NEB_CUDA_CHECK(cudaMemsetAsync(ws, 0, 128, s));
   int64_t total = t.off[n_tensors];
   int blocks = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(total, 256), 1), 1184);
-  if (dtype == 0) {
-    adam_norm<float><<<blocks, 256, 0, s>>>(t, acc, flag);
-    adam_update<float><<<blocks, 256, 0, s>>>(t, acc, flag, (double)step + 1, lr, clip, beta1,
-                                              beta2, eps, norm_out, committed_out);
-  } else {
-    adam_norm<double><<<blocks, 256, 0, s>>>(t, acc, flag);
-    adam_update<double><<<blocks, 256, 0, s>>>(t, acc, flag, (double)step + 1, lr, clip, beta1,
-                                               beta2, eps, norm_out, committed_out);
+  const double es = dtype == 0 ? 4.0 : 8.0;
+  {
+    KernelScope ks("adam_norm", s, 0, total * es);
+    if (dtype == 0) adam_norm<float><<<blocks, 256, 0, s>>>(t, acc, flag);
+    else adam_norm<double><<<blocks, 256, 0, s>>>(t, acc, flag);
+    NEB_LAUNCH_CHECK();
   }
-  NEB_LAUNCH_CHECK();
+  {
+    KernelScope ks("adam_update", s, 0, total * es * 7);
+    if (dtype == 0)
+      adam_update<float><<<blocks, 256, 0, s>>>(t, acc, flag, (double)step + 1, lr, clip, beta1,
+                                                beta2, eps, norm_out, committed_out);
+    else
+      adam_update<double><<<blocks, 256, 0, s>>>(t, acc, flag, (double)step + 1, lr, clip, beta1,
+                                                 beta2, eps, norm_out, committed_out);
+    NEB_LAUNCH_CHECK();
+  }
   return NEB_OK;
 }

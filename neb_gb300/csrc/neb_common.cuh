@@ -134,4 +134,25 @@ __device__ __forceinline__ void jet_act_backward(const T* z, T* yb) {
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Kernel instrumentation: every launch of this library goes through a
+// KernelScope, which counts it and, while timing is enabled
+// (neb_timing_begin / neb_timing_end), brackets it with CUDA events on the
+// launching stream and records its algorithmic flops and bytes.
+void timing_record(const char* name, cudaStream_t s, double flops, double bytes, bool begin);
+void count_launch();
+
+struct KernelScope {
+  const char* name;
+  cudaStream_t stream;
+  double flops, bytes;
+  KernelScope(const char* n, cudaStream_t s, double f = 0, double b = 0)
+      : name(n), stream(s), flops(f), bytes(b) {
+    timing_record(name, stream, flops, bytes, true);
+  }
+  ~KernelScope() {
+    count_launch();
+    timing_record(name, stream, flops, bytes, false);
+  }
+};
+
 }  // namespace neb

@@ -101,9 +101,13 @@ extern "C" int neb_spectral(int m, const double* M, const double* S, const doubl
   NEB_CUDA_CHECK(cudaMemcpyAsync(Mw, M, mm, cudaMemcpyDeviceToDevice, stream));
   NEB_CUDA_CHECK(cudaMemcpyAsync(V, S, mm, cudaMemcpyDeviceToDevice, stream));
   // S v = lam M v; on exit V (column-major) holds M-orthonormal eigenvectors
-  cusolverStatus_t cs = cusolverDnDsygvd(sol, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+  cusolverStatus_t cs;
+  {
+  KernelScope ks("cusolver_dsygvd", stream, 9.0 * m * (double)m * m, 0);
+  cs = cusolverDnDsygvd(sol, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
                                          CUBLAS_FILL_MODE_LOWER, m, V, m, Mw, m, lam, work, lwork,
                                          info);
+  }
   if (cs != CUSOLVER_STATUS_SUCCESS) {
     set_error("cusolverDnDsygvd failed (%d)", (int)cs);
     return NEB_ERR_SOLVER;
@@ -112,23 +116,38 @@ extern "C" int neb_spectral(int m, const double* M, const double* S, const doubl
   int blocks = (int)ceil_div((int64_t)m * m, threads);
   // G_S = V diag(c) V^T, G_M = -V diag(c lam) V^T (column-major V: column j =
   // eigenvector j; symmetric results)
-  scale_columns<<<blocks, threads, 0, stream>>>(V, c, nullptr, m, Tw);
-  NEB_LAUNCH_CHECK();
   double one = 1.0, zero = 0.0, mone = -1.0;
-  if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_T, m, m, m, &one, Tw, m, V, m, &zero, G_S, m) !=
-      CUBLAS_STATUS_SUCCESS) {
-    set_error("cublasDgemm (G_S) failed");
-    return NEB_ERR_CUDA;
+  {
+    KernelScope ks("scale_columns", stream, 0, 16.0 * m * m);
+    scale_columns<<<blocks, threads, 0, stream>>>(V, c, nullptr, m, Tw);
+    NEB_LAUNCH_CHECK();
   }
-  scale_columns<<<blocks, threads, 0, stream>>>(V, c, lam, m, Tw);
-  NEB_LAUNCH_CHECK();
-  if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_T, m, m, m, &mone, Tw, m, V, m, &zero, G_M, m) !=
-      CUBLAS_STATUS_SUCCESS) {
-    set_error("cublasDgemm (G_M) failed");
-    return NEB_ERR_CUDA;
+  {
+    KernelScope ks("cublas_dgemm", stream, 2.0 * m * (double)m * m, 24.0 * m * m);
+    if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_T, m, m, m, &one, Tw, m, V, m, &zero, G_S, m) !=
+        CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasDgemm (G_S) failed");
+      return NEB_ERR_CUDA;
+    }
   }
-  weighted_sum<<<1, 256, 0, stream>>>(c, lam, m, loss, info);
-  NEB_LAUNCH_CHECK();
+  {
+    KernelScope ks("scale_columns", stream, 0, 16.0 * m * m);
+    scale_columns<<<blocks, threads, 0, stream>>>(V, c, lam, m, Tw);
+    NEB_LAUNCH_CHECK();
+  }
+  {
+    KernelScope ks("cublas_dgemm", stream, 2.0 * m * (double)m * m, 24.0 * m * m);
+    if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_T, m, m, m, &mone, Tw, m, V, m, &zero, G_M, m) !=
+        CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasDgemm (G_M) failed");
+      return NEB_ERR_CUDA;
+    }
+  }
+  {
+    KernelScope ks("weighted_sum", stream, 0, 16.0 * m);
+    weighted_sum<<<1, 256, 0, stream>>>(c, lam, m, loss, info);
+    NEB_LAUNCH_CHECK();
+  }
   return NEB_OK;
 }
 

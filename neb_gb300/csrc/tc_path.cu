@@ -1,31 +1,896 @@
-// Tensor-core (tcgen05) path: placeholder entry points until the sm_103a
-// kernels land; they report NEB_ERR_UNSUPPORTED.
+// Tensor-core path of the jet MLP (NEB_PREC_BF16X3) on sm_103a.
+//
+// Every GEMM runs on tcgen05 with split-BF16 operands: a value x is stored as
+// hi = bf16(x), lo = bf16(x - hi) (16 significant bits), and a product is
+// accumulated in FP32 tensor memory as A_hi B_hi + A_lo B_hi + A_hi B_lo
+// (+ A_lo B_lo for the Grams, where the dropped term would bias every
+// diagonal the same way).
+// Operands arrive by TMA (128-byte swizzle, K-major) through an mbarrier ring;
+// one thread issues the MMAs, four warps run the epilogue from TMEM.
+//
+// Device layouts (n_pad = n rounded up to 128 points; "planar" = one matrix
+// per jet channel c in 0..3 = value, d/dx, d/dy, Laplacian):
+//   X_l   [2 planes hi/lo][C][n_pad][w_pad]  layer input, K-major for the next GEMM
+//   XT_l  [2][C][w_pad][n_pad]               its transpose, K-major over points
+//   Z_l   [C][n_pad][w]  float               pre-activation, for the reverse pass
+// Kernels:
+//   tc_jet_gemm<0>  forward layer:  Z = X W^T + b (value channel), X' = tanh-jet(Z)
+//   tc_jet_gemm<1>  reverse data:   Zbar' = tanh-jet^T(Z', Zbar W)
+//   tc_jet_gemm<2>  Gram adjoint:   Zbar_L = tanh-jet^T(Z_L, 2 w [0, h_x G_M, h_y G_M, h_lap G_S])
+//   tc_rowsum       sum over points of A[m][p] B[n][p] (Grams, weight gradients),
+//                   split over point ranges, FP64 partials reduced afterwards.
+#include <cudaTypedefs.h>
 #include "tc_path.cuh"
+#include "tc_ptx.cuh"
 
 namespace neb {
 
-size_t tc_workspace_bytes(const neb_net*, int64_t) { return 0; }
+namespace {
 
-int tc_forward(const neb_net*, const float* const*, const float* const*, const float*, int64_t,
-               const TcTape&, char*, cudaStream_t) {
-  set_error("NEB_PREC_BF16X3 forward not built");
-  return NEB_ERR_UNSUPPORTED;
+constexpr int C = 4;              // 2D jet channels
+constexpr int kTileBytes = 128 * 128;  // 128 rows x 64 bf16
+
+int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// ------------------------------------------------------------ host: maps
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int get_encode() {
+  if (g_encode) return NEB_OK;
+  cudaDriverEntryPointQueryResult q;
+  void* fn = nullptr;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                   cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+    set_error("cuTensorMapEncodeTiled unavailable");
+    return NEB_ERR_CUDA;
+  }
+  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  return NEB_OK;
 }
+
+// 2D bf16 map over a row-major [rows][cols] array, box {64 cols, box_rows}.
+int make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t cols, int box_rows) {
+  int st = get_encode();
+  if (st) return st;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (cols * 2) % 16) {
+    set_error("tensor map: base or row stride not 16-byte aligned");
+    return NEB_ERR_ARG;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+  cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d) rows=%lld cols=%lld", (int)r, (long long)rows,
+              (long long)cols);
+    return NEB_ERR_CUDA;
+  }
+  return NEB_OK;
+}
+
+__device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
+  uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  return reinterpret_cast<uint8_t*>((a + 1023) & ~uintptr_t(1023));
+}
+
+// -------------------------------------------------------- jet GEMM kernel
+struct JetGemmArgs {
+  int n_points, n_pad, K, N;
+  const float* bias;   // EPI 0: [N]
+  const float* zprev;  // EPI 1, 2: [C][n_pad][N] pre-activation of the target layer
+  const float* qw;     // EPI 2: [n_points] quadrature weights
+  float* z_out;        // EPI 0: [C][n_pad][N]
+  __nv_bfloat16* y_out;   // [2][C][n_pad][N]
+  __nv_bfloat16* yt_out;  // [2][C][N][n_pad]
+  int* status;
+};
+
+template <int EPI> struct JetCfg {
+  static constexpr int NB = EPI == 2 ? 2 : 1;    // distinct B matrices
+  static constexpr int NCH = EPI == 2 ? 3 : 4;   // accumulated channels
+  static constexpr int CH0 = EPI == 2 ? 1 : 0;
+  static constexpr int A_ST = EPI == 2 ? 3 : 4;
+  static constexpr int B_ST = 2;
+  static constexpr int B_BYTES = 2 * NB * kTileBytes;
+  static constexpr int SMEM = 1024 + A_ST * 2 * kTileBytes + B_ST * B_BYTES + 256;
+};
+
+__device__ __forceinline__ void store_split16(const float* v, __nv_bfloat16* hi_dst,
+                                              __nv_bfloat16* lo_dst) {
+  __align__(16) __nv_bfloat16 h[16], l[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) tc::split_bf16(v[j], h[j], l[j]);
+  uint4* hd = reinterpret_cast<uint4*>(hi_dst);
+  uint4* ld = reinterpret_cast<uint4*>(lo_dst);
+  hd[0] = reinterpret_cast<uint4*>(h)[0];
+  hd[1] = reinterpret_cast<uint4*>(h)[1];
+  ld[0] = reinterpret_cast<uint4*>(l)[0];
+  ld[1] = reinterpret_cast<uint4*>(l)[1];
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(192, 1)
+tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+            JetGemmArgs g) {
+  using Cfg = JetCfg<EPI>;
+  constexpr int NB = Cfg::NB, NCH = Cfg::NCH, CH0 = Cfg::CH0, A_ST = Cfg::A_ST,
+                B_ST = Cfg::B_ST;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* a_smem = smem;
+  uint8_t* b_smem = smem + A_ST * 2 * kTileBytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(b_smem + B_ST * Cfg::B_BYTES);
+  uint64_t* a_full = bars;
+  uint64_t* a_empty = bars + A_ST;
+  uint64_t* b_full = bars + 2 * A_ST;
+  uint64_t* b_empty = bars + 2 * A_ST + B_ST;
+  uint64_t* acc_full = bars + 2 * A_ST + 2 * B_ST;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_full + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n0 = blockIdx.x * 128, p0 = blockIdx.y * 128;
+  const int KC = g.K / 64;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < A_ST; ++i) {
+      tc::mbar_init(&a_full[i], 1);
+      tc::mbar_init(&a_empty[i], 1);
+    }
+    for (int i = 0; i < B_ST; ++i) {
+      tc::mbar_init(&b_full[i], 1);
+      tc::mbar_init(&b_empty[i], 1);
+    }
+    tc::mbar_init(acc_full, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(tmem_slot, 512);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    int ai = 0;
+    for (int kc = 0; kc < KC; ++kc) {
+      const int bs = kc % B_ST;
+      tc::mbar_wait(&b_empty[bs], ((kc / B_ST) & 1) ^ 1, g.status);
+      tc::mbar_expect_tx(&b_full[bs], Cfg::B_BYTES);
+      for (int b = 0; b < NB; ++b)
+        for (int pl = 0; pl < 2; ++pl)
+          tc::tma_load_2d(b_smem + bs * Cfg::B_BYTES + (b * 2 + pl) * kTileBytes, &tmB,
+                          &b_full[bs], kc * 64, (pl * NB + b) * g.N + n0);
+      for (int ci = 0; ci < NCH; ++ci, ++ai) {
+        const int as = ai % A_ST, c = CH0 + ci;
+        tc::mbar_wait(&a_empty[as], ((ai / A_ST) & 1) ^ 1, g.status);
+        tc::mbar_expect_tx(&a_full[as], 2 * kTileBytes);
+        for (int pl = 0; pl < 2; ++pl)
+          tc::tma_load_2d(a_smem + (as * 2 + pl) * kTileBytes, &tmA, &a_full[as], kc * 64,
+                          (pl * C + c) * g.n_pad + p0);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    constexpr uint32_t idesc = tc::idesc_bf16(128, 128);
+    int ai = 0;
+    for (int kc = 0; kc < KC; ++kc) {
+      const int bs = kc % B_ST;
+      tc::mbar_wait(&b_full[bs], (kc / B_ST) & 1, g.status);
+      tc::tc_fence_after();
+      for (int ci = 0; ci < NCH; ++ci, ++ai) {
+        const int as = ai % A_ST, c = CH0 + ci;
+        tc::mbar_wait(&a_full[as], (ai / A_ST) & 1, g.status);
+        tc::tc_fence_after();
+        const int bsel = (EPI == 2 && c == 3) ? 1 : 0;
+        const uint32_t a_hi = tc::smem_u32(a_smem + (as * 2) * kTileBytes);
+        const uint32_t a_lo = a_hi + kTileBytes;
+        const uint32_t b_hi = tc::smem_u32(b_smem + bs * Cfg::B_BYTES + (bsel * 2) * kTileBytes);
+        const uint32_t b_lo = b_hi + kTileBytes;
+        const uint32_t d = tmem + ci * 128;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const uint32_t off = kk * 32;
+          const uint64_t dah = tc::desc_sw128(a_hi + off), dal = tc::desc_sw128(a_lo + off);
+          const uint64_t dbh = tc::desc_sw128(b_hi + off), dbl = tc::desc_sw128(b_lo + off);
+          tc::mma_bf16(d, dah, dbh, idesc, (kc | kk) != 0);
+          tc::mma_bf16(d, dal, dbh, idesc, 1);
+          tc::mma_bf16(d, dah, dbl, idesc, 1);
+        }
+        tc::mma_commit(&a_empty[as]);
+      }
+      tc::mma_commit(&b_empty[bs]);
+    }
+    tc::mma_commit(acc_full);
+  } else if (warp >= 2) {
+    // ---------------- epilogue: one thread per point (TMEM lane)
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const int p = p0 + row;
+    tc::mbar_wait(acc_full, 0, g.status);
+    tc::tc_fence_after();
+    const size_t plane = (size_t)C * g.n_pad * g.N;  // elements of one hi or lo plane
+    float w2 = 0.f;
+    if constexpr (EPI == 2) w2 = p < g.n_points ? 2.f * g.qw[p] : 0.f;
+    for (int j0 = 0; j0 < 128; j0 += 16) {
+      float acc[NCH][16];
+#pragma unroll
+      for (int ci = 0; ci < NCH; ++ci)
+        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + ci * 128 + j0, acc[ci]);
+      const int col = n0 + j0;
+      float out[C][16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        float v[C];
+        if constexpr (EPI == 0) {
+#pragma unroll
+          for (int c = 0; c < C; ++c) v[c] = acc[c][j];
+          v[0] += g.bias[col + j];
+#pragma unroll
+          for (int c = 0; c < C; ++c) out[c][j] = v[c];  // pre-activation, stored below
+        } else {
+          float z[C];
+#pragma unroll
+          for (int c = 0; c < C; ++c) z[c] = g.zprev[((size_t)c * g.n_pad + p) * g.N + col + j];
+          if constexpr (EPI == 2) {
+            v[0] = 0.f;
+#pragma unroll
+            for (int c = 1; c < C; ++c) v[c] = w2 * acc[c - 1][j];
+          } else {
+#pragma unroll
+            for (int c = 0; c < C; ++c) v[c] = acc[c][j];
+          }
+          jet_act_backward<C>(z, v);
+#pragma unroll
+          for (int c = 0; c < C; ++c) out[c][j] = v[c];
+        }
+      }
+      if constexpr (EPI == 0) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          float4* zd = reinterpret_cast<float4*>(g.z_out + ((size_t)c * g.n_pad + p) * g.N + col);
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            zd[j] = make_float4(out[c][4 * j], out[c][4 * j + 1], out[c][4 * j + 2],
+                                out[c][4 * j + 3]);
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          float v[C];
+#pragma unroll
+          for (int c = 0; c < C; ++c) v[c] = out[c][j];
+          jet_act_forward<C>(v);
+#pragma unroll
+          for (int c = 0; c < C; ++c) out[c][j] = v[c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        size_t o = ((size_t)c * g.n_pad + p) * g.N + col;
+        store_split16(out[c], g.y_out + o, g.y_out + plane + o);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          __nv_bfloat16 h, l;
+          tc::split_bf16(out[c][j], h, l);
+          size_t t = ((size_t)c * g.N + col + j) * g.n_pad + p;
+          g.yt_out[t] = h;
+          g.yt_out[plane + t] = l;
+        }
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
+// ----------------------------------------------------------- rowsum kernel
+// part[z][m][n] = sum over K-chunks kq in split z of A(m, kq) . B(n, kq),
+// where the K index runs over (channel ci, point block): A rows
+// (pl * aC + a_ch0 + ci) * M + m, B rows (pl * bC + b_ch0 + ci) * N + n.
+struct RowsumArgs {
+  int M, N, n_pad, n_ch, a_ch0, b_ch0, aC, bC, splits, ldp;
+  int lo_lo;  // also accumulate A_lo B_lo: the Grams need it (without it the
+              // missing product acts as a systematic negative ridge)
+  double* part;
+  int* status;
+};
+
+template <int BN> struct RowCfg {
+  static constexpr int ST = 3;
+  static constexpr int A_BYTES = 2 * kTileBytes;
+  static constexpr int B_BYTES = 2 * BN * 128;
+  static constexpr int SMEM = 1024 + ST * (A_BYTES + B_BYTES) + 256;
+  static constexpr int TMEM = 2 * BN < 32 ? 32 : 2 * BN;  // two accumulator buffers
+};
+
+// The tensor cores' FP32 accumulation rounds toward zero, so a long run of
+// same-sign MMAs into one accumulator drifts (a few 1e-6 relative on a Gram
+// diagonal after a few hundred MMAs, which shows up as a ridge on the mass
+// matrix).  Each 64-point chunk is therefore accumulated in its own tensor
+// memory buffer (16 MMAs) and drained by the epilogue warps into
+// round-to-nearest FP32 register sums, double-buffered against the MMAs.
+template <int BN>
+__global__ void __launch_bounds__(320, 1)
+tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+          RowsumArgs g) {
+  using Cfg = RowCfg<BN>;
+  constexpr int ST = Cfg::ST;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* a_smem = smem;
+  uint8_t* b_smem = smem + ST * Cfg::A_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(b_smem + ST * Cfg::B_BYTES);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + ST;
+  uint64_t* acc_ready = bars + 2 * ST;      // [2]
+  uint64_t* acc_free = bars + 2 * ST + 2;   // [2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * ST + 4);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = g.N / BN;
+  const int m0 = (blockIdx.x / ntiles) * 128, n0 = (blockIdx.x % ntiles) * BN;
+  const int pblocks = g.n_pad / 64;
+  const int total = g.n_ch * pblocks;
+  const int per = (total + g.splits - 1) / g.splits;
+  const int k_begin = blockIdx.y * per;
+  const int k_end = min(total, k_begin + per);
+  const int n_it = k_end > k_begin ? k_end - k_begin : 0;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < ST; ++i) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&acc_ready[i], 1);
+      tc::mbar_init(&acc_free[i], 256);
+    }
+    tc::fence_mbar_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(tmem_slot, Cfg::TMEM);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    for (int it = 0; it < n_it; ++it) {
+      const int kq = k_begin + it, s = it % ST;
+      const int ci = kq / pblocks, pb = kq % pblocks;
+      tc::mbar_wait(&empty[s], ((it / ST) & 1) ^ 1, g.status);
+      tc::mbar_expect_tx(&full[s], Cfg::A_BYTES + Cfg::B_BYTES);
+      for (int pl = 0; pl < 2; ++pl) {
+        tc::tma_load_2d(a_smem + s * Cfg::A_BYTES + pl * kTileBytes, &tmA, &full[s], pb * 64,
+                        (pl * g.aC + g.a_ch0 + ci) * g.M + m0);
+        tc::tma_load_2d(b_smem + s * Cfg::B_BYTES + pl * (BN * 128), &tmB, &full[s], pb * 64,
+                        (pl * g.bC + g.b_ch0 + ci) * g.N + n0);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = tc::idesc_bf16(128, BN);
+    for (int it = 0; it < n_it; ++it) {
+      const int s = it % ST, buf = it & 1;
+      if (it >= 2) tc::mbar_wait(&acc_free[buf], ((it >> 1) & 1) ^ 1, g.status);
+      tc::mbar_wait(&full[s], (it / ST) & 1, g.status);
+      tc::tc_fence_after();
+      const uint32_t d = tmem + buf * BN;
+      const uint32_t a_hi = tc::smem_u32(a_smem + s * Cfg::A_BYTES), a_lo = a_hi + kTileBytes;
+      const uint32_t b_hi = tc::smem_u32(b_smem + s * Cfg::B_BYTES), b_lo = b_hi + BN * 128;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const uint32_t off = kk * 32;
+        const uint64_t dah = tc::desc_sw128(a_hi + off), dal = tc::desc_sw128(a_lo + off);
+        const uint64_t dbh = tc::desc_sw128(b_hi + off), dbl = tc::desc_sw128(b_lo + off);
+        tc::mma_bf16(d, dah, dbh, idesc, kk != 0);
+        tc::mma_bf16(d, dal, dbh, idesc, 1);
+        tc::mma_bf16(d, dah, dbl, idesc, 1);
+        if (g.lo_lo) tc::mma_bf16(d, dal, dbl, idesc, 1);
+      }
+      tc::mma_commit(&empty[s]);
+      tc::mma_commit(&acc_ready[buf]);
+    }
+  } else if (warp >= 2) {
+    // eight drain warps: lane quarter q = warp % 4, column half h
+    constexpr int HB = BN / 2;
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    const int m = m0 + q * 32 + lane;
+    float sum[HB];
+#pragma unroll
+    for (int j = 0; j < HB; ++j) sum[j] = 0.f;
+    for (int it = 0; it < n_it; ++it) {
+      const int buf = it & 1;
+      tc::mbar_wait(&acc_ready[buf], (it >> 1) & 1, g.status);
+      tc::tc_fence_after();
+#pragma unroll
+      for (int j0 = 0; j0 < HB; j0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * BN + h * HB + j0, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sum[j0 + j] += v[j];
+      }
+      tc::tc_fence_before();
+      tc::mbar_arrive(&acc_free[buf]);
+    }
+    double* out = g.part + ((size_t)blockIdx.y * g.M + m) * g.ldp + n0 + h * HB;
+#pragma unroll
+    for (int j = 0; j < HB; j += 2)
+      *reinterpret_cast<double2*>(out + j) = make_double2(sum[j], sum[j + 1]);
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, Cfg::TMEM);
+  }
+}
+
+// ------------------------------------------------------- helper kernels
+// Interleaved float features [n][C][F] -> split planar X_0 [2][C][n_pad][Fp]
+// and its transpose XT_0 [2][C][Fp][n_pad], zero padded.
+__global__ void prep_features(const float* __restrict__ f, int n, int F, int n_pad, int Fp,
+                              __nv_bfloat16* __restrict__ X, __nv_bfloat16* __restrict__ XT) {
+  const size_t total = (size_t)C * n_pad * Fp;
+  const size_t plane = total;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    // i enumerates (c, k, p) with p fastest so the transposed writes coalesce
+    int p = (int)(i % n_pad);
+    int k = (int)((i / n_pad) % Fp);
+    int c = (int)(i / ((size_t)n_pad * Fp));
+    float v = (p < n && k < F) ? f[((size_t)p * C + c) * F + k] : 0.f;
+    __nv_bfloat16 h, l;
+    tc::split_bf16(v, h, l);
+    size_t o = ((size_t)c * n_pad + p) * Fp + k;
+    X[o] = h;
+    X[plane + o] = l;
+    XT[i] = h;
+    XT[plane + i] = l;
+  }
+}
+
+// W [out][in] float -> Ws [2][out][inp] (zero padded), optionally WT [2][inp][out].
+__global__ void split_weight(const float* __restrict__ W, int out, int in, int inp,
+                             __nv_bfloat16* __restrict__ Ws, __nv_bfloat16* __restrict__ WT) {
+  const size_t total = (size_t)out * inp;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int o = (int)(i / inp), k = (int)(i % inp);
+    float v = k < in ? W[(size_t)o * in + k] : 0.f;
+    __nv_bfloat16 h, l;
+    tc::split_bf16(v, h, l);
+    Ws[i] = h;
+    Ws[total + i] = l;
+    if (WT) {
+      size_t t = (size_t)k * out + o;
+      WT[t] = h;
+      WT[total + t] = l;
+    }
+  }
+}
+
+// G_M, G_S (double [H][H]) -> [2 planes][2 (M, S)][H][H] bf16.
+__global__ void split_gram_adjoint(const double* __restrict__ GM, const double* __restrict__ GS,
+                                   int H, __nv_bfloat16* __restrict__ out) {
+  const size_t hh = (size_t)H * H;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 2 * hh;
+       i += (size_t)gridDim.x * blockDim.x) {
+    float v = (float)(i < hh ? GM[i] : GS[i - hh]);
+    __nv_bfloat16 h, l;
+    tc::split_bf16(v, h, l);
+    out[i] = h;
+    out[2 * hh + i] = l;
+  }
+}
+
+// wHT[pl][ci][f][p] = split(w_p * (XT_L[c = ci + 1][f][p])) for the three field
+// channels; w_p = 0 for padded points.
+__global__ void weighted_fields_t(const __nv_bfloat16* __restrict__ XT, const float* __restrict__ qw,
+                                  int n, int n_pad, int H, __nv_bfloat16* __restrict__ out) {
+  const size_t total = (size_t)3 * H * n_pad;
+  const size_t src_plane = (size_t)C * H * n_pad;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int p = (int)(i % n_pad);
+    size_t src = (size_t)H * n_pad + i;  // channel ci + 1
+    float v = __bfloat162float(XT[src]) + __bfloat162float(XT[src_plane + src]);
+    v *= p < n ? qw[p] : 0.f;
+    __nv_bfloat16 h, l;
+    tc::split_bf16(v, h, l);
+    out[i] = h;
+    out[total + i] = l;
+  }
+}
+
+// out[m * ldo + j] = sum_z part[(z * M + m) * ldp + j] for j < ncols.
+__global__ void reduce_parts(const double* __restrict__ part, int splits, int M, int ldp, int ncols,
+                             int ldo, int sym, float* __restrict__ outf, double* __restrict__ outd) {
+  const size_t total = (size_t)M * ncols;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int m = (int)(i / ncols), j = (int)(i % ncols);
+    double s = 0.0;
+    for (int z = 0; z < splits; ++z) s += part[((size_t)z * M + m) * ldp + j];
+    if (sym) {
+      double t = 0.0;
+      for (int z = 0; z < splits; ++z) t += part[((size_t)z * M + j) * ldp + m];
+      s = 0.5 * (s + t);
+    }
+    if (outf) outf[(size_t)m * ldo + j] = (float)s;
+    if (outd) outd[(size_t)m * ldo + j] = s;
+  }
+}
+
+// Bias gradient partials: partb[chunk][o] = sum over points of the value
+// plane of Zbar (hi + lo).
+__global__ void bias_partial_tc(const __nv_bfloat16* __restrict__ zb, int n_pad, int N,
+                                int chunk, double* __restrict__ partb) {
+  int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= N) return;
+  const size_t plane = (size_t)C * n_pad * N;
+  int p0 = blockIdx.y * chunk, p1 = min(n_pad, p0 + chunk);
+  double s = 0.0;
+  for (int p = p0; p < p1; ++p) {
+    size_t i = (size_t)p * N + o;  // channel 0
+    s += (double)__bfloat162float(zb[i]) + (double)__bfloat162float(zb[plane + i]);
+  }
+  partb[(size_t)blockIdx.y * N + o] = s;
+}
+
+// ---------------------------------------------------------- host helpers
+struct Dims {
+  int L, F, Fp, H;
+  int64_t n, n_pad;
+  int w[NEB_MAX_HIDDEN + 2];   // real widths
+  int wp[NEB_MAX_HIDDEN + 2];  // padded K widths
+};
+
+Dims dims_of(const neb_net* net, int64_t n) {
+  Dims d{};
+  d.L = net->n_hidden;
+  d.n = n;
+  d.n_pad = round_up(n, 128);
+  for (int l = 0; l <= d.L + 1; ++l) {
+    d.w[l] = net->widths[l];
+    d.wp[l] = l == 0 ? (int)round_up(net->widths[0], 64) : net->widths[l];
+  }
+  d.F = d.w[0];
+  d.Fp = d.wp[0];
+  d.H = d.w[d.L];
+  return d;
+}
+
+size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// TC workspace: [status][W splits per layer][WT splits][G split][wHT][Zbar A][Zbar B][ZbarT]
+//               [FP64 split partials][bias partials]
+constexpr int kMaxSplits = 32;
+constexpr int kBiasChunk = 512;
+struct TcWs {
+  size_t status, w[NEB_MAX_HIDDEN + 1], wt[NEB_MAX_HIDDEN + 1], gsplit, wht, zb0, zb1, zbt,
+      part, partb, total;
+};
+
+TcWs tc_ws(const Dims& d) {
+  TcWs t{};
+  size_t off = 0;
+  t.status = off;
+  off += 256;
+  int mw = 0;
+  for (int l = 1; l <= d.L; ++l) {
+    t.w[l] = off;
+    off += a256((size_t)2 * d.w[l] * d.wp[l - 1] * 2);
+    t.wt[l] = off;
+    off += l >= 2 ? a256((size_t)2 * d.w[l] * d.wp[l - 1] * 2) : 0;
+    mw = mw > d.w[l] ? mw : d.w[l];
+  }
+  t.gsplit = off;
+  off += a256((size_t)4 * d.H * d.H * 2);
+  t.wht = off;
+  off += a256((size_t)2 * 3 * d.H * d.n_pad * 2);
+  size_t zb = a256((size_t)2 * C * d.n_pad * mw * 2);
+  t.zb0 = off;
+  off += zb;
+  t.zb1 = off;
+  off += zb;
+  t.zbt = off;
+  off += zb;
+  int mx = mw > d.wp[0] ? mw : d.wp[0];
+  t.part = off;
+  off += a256((size_t)kMaxSplits * mx * mx * 8);
+  t.partb = off;
+  off += a256((size_t)((d.n_pad + kBiasChunk - 1) / kBiasChunk) * mw * 8);
+  t.total = off;
+  return t;
+}
+
+template <int EPI>
+int launch_jet(const CUtensorMap& A, const CUtensorMap& B, const JetGemmArgs& args, int n_tiles,
+               int p_tiles, cudaStream_t s, const char* name, double flops, double bytes) {
+  static bool configured = false;
+  if (!configured) {
+    NEB_CUDA_CHECK(cudaFuncSetAttribute(tc_jet_gemm<EPI>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        JetCfg<EPI>::SMEM));
+    configured = true;
+  }
+  KernelScope ks(name, s, flops, bytes);
+  tc_jet_gemm<EPI><<<dim3(n_tiles, p_tiles), 192, JetCfg<EPI>::SMEM, s>>>(A, B, args);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+// part = per-split partials of A . B^T over (channels, points); M rows of A,
+// N rows of B.
+template <int BN>
+int launch_rowsum_bn(const CUtensorMap& A, const CUtensorMap& B, RowsumArgs g, cudaStream_t s,
+                     const char* name, double flops, double bytes) {
+  static bool configured = false;
+  if (!configured) {
+    NEB_CUDA_CHECK(cudaFuncSetAttribute(tc_rowsum<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        RowCfg<BN>::SMEM));
+    configured = true;
+  }
+  KernelScope ks(name, s, flops, bytes);
+  dim3 grid((g.M / 128) * (g.N / BN), g.splits);
+  tc_rowsum<BN><<<grid, 320, RowCfg<BN>::SMEM, s>>>(A, B, g);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+int launch_rowsum(const void* a_base, int aC, int a_ch0, const void* b_base, int bC, int b_ch0,
+                  int n_ch, int M, int N, int64_t n_pad, double* part, int* status,
+                  cudaStream_t s, const char* name, double flops, int* splits_out,
+                  bool lo_lo = false) {
+  NEB_REQUIRE(M % 128 == 0, "tensor-core rowsum: M = %d must be a multiple of 128", M);
+  int BN = N % 128 == 0 ? 128 : (N % 64 == 0 ? 64 : 0);
+  NEB_REQUIRE(BN, "tensor-core rowsum: N = %d must be a multiple of 64", N);
+  int tiles = (M / 128) * (N / BN);
+  int total = n_ch * (int)(n_pad / 64);
+  int splits = (int)std::max(1, std::min(kMaxSplits, (2 * 148 + tiles - 1) / tiles));
+  splits = std::min(splits, total);
+  CUtensorMap ma, mb;
+  int st = make_map(&ma, a_base, (int64_t)2 * aC * M, n_pad, 128);
+  if (st) return st;
+  st = make_map(&mb, b_base, (int64_t)2 * bC * N, n_pad, BN);
+  if (st) return st;
+  RowsumArgs g{M, N, (int)n_pad, n_ch, a_ch0, b_ch0, aC, bC, splits, N, lo_lo ? 1 : 0, part,
+               status};
+  double bytes = (double)n_ch * n_pad * (M + N) * 4;
+  *splits_out = splits;
+  if (BN == 128) return launch_rowsum_bn<128>(ma, mb, g, s, name, flops, bytes);
+  return launch_rowsum_bn<64>(ma, mb, g, s, name, flops, bytes);
+}
+
+int reduce(const double* part, int splits, int M, int ldp, int ncols, int ldo, bool sym,
+           float* outf, double* outd, cudaStream_t s) {
+  KernelScope ks("reduce_chunks", s, 0, (double)splits * M * ncols * 8);
+  size_t total = (size_t)M * ncols;
+  int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
+  reduce_parts<<<blocks, 256, 0, s>>>(part, splits, M, ldp, ncols, ldo, sym ? 1 : 0, outf, outd);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+int check_dims(const neb_net* net) {
+  NEB_REQUIRE(net->dim == 2, "NEB_PREC_BF16X3: 2D scalar potential only");
+  for (int l = 1; l <= net->n_hidden; ++l)
+    NEB_REQUIRE(net->widths[l] % 128 == 0,
+                "NEB_PREC_BF16X3: hidden widths must be multiples of 128 (layer %d: %d)", l,
+                net->widths[l]);
+  return NEB_OK;
+}
+
+}  // namespace
+
+// ======================================================================
+size_t tc_tape_bytes(const neb_net* net, int64_t n, size_t* x_off, size_t* z_off) {
+  Dims d = dims_of(net, n);
+  size_t off = 0;
+  for (int l = 0; l <= d.L; ++l) {
+    if (l > 0) {
+      if (z_off) z_off[l] = off;
+      off += a256((size_t)C * d.n_pad * d.w[l] * 4);
+    }
+    if (x_off) x_off[l] = off;
+    off += 2 * a256((size_t)2 * C * d.n_pad * d.wp[l] * 2);  // X and XT
+  }
+  return off;
+}
+
+size_t tc_workspace_bytes(const neb_net* net, int64_t n) { return tc_ws(dims_of(net, n)).total; }
+
+int tc_forward(const neb_net* net, const float* const* W, const float* const* b, const float* feats,
+               int64_t n, const TcTape& tape, char* ws, cudaStream_t s) {
+  int st = check_dims(net);
+  if (st) return st;
+  Dims d = dims_of(net, n);
+  TcWs t = tc_ws(d);
+  int* status = (int*)(ws + t.status);
+  NEB_CUDA_CHECK(cudaMemsetAsync(status, 0, sizeof(int), s));
+  {
+    KernelScope ks("tc_prep_features", s, 0, (double)n * C * d.F * 4 + 8.0 * C * d.n_pad * d.Fp);
+    size_t total = (size_t)C * d.n_pad * d.Fp;
+    int blocks = (int)std::min<size_t>((total + 255) / 256, 8192);
+    __nv_bfloat16* X0 = (__nv_bfloat16*)tape.x[0];
+    size_t xsz = a256((size_t)2 * C * d.n_pad * d.Fp * 2);
+    prep_features<<<blocks, 256, 0, s>>>(feats, (int)n, d.F, (int)d.n_pad, d.Fp, X0,
+                                         (__nv_bfloat16*)((char*)tape.x[0] + xsz));
+    NEB_LAUNCH_CHECK();
+  }
+  for (int l = 1; l <= d.L; ++l) {
+    KernelScope ks("tc_split_weight", s, 0, (double)d.w[l] * d.wp[l - 1] * 12);
+    size_t total = (size_t)d.w[l] * d.wp[l - 1];
+    int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
+    split_weight<<<blocks, 256, 0, s>>>(W[l - 1], d.w[l], d.w[l - 1], d.wp[l - 1],
+                                        (__nv_bfloat16*)(ws + t.w[l]),
+                                        l >= 2 ? (__nv_bfloat16*)(ws + t.wt[l]) : nullptr);
+    NEB_LAUNCH_CHECK();
+  }
+  for (int l = 1; l <= d.L; ++l) {
+    const int K = d.wp[l - 1], N = d.w[l];
+    CUtensorMap ma, mb;
+    if ((st = make_map(&ma, tape.x[l - 1], (int64_t)2 * C * d.n_pad, K, 128))) return st;
+    if ((st = make_map(&mb, ws + t.w[l], (int64_t)2 * N, K, 128))) return st;
+    size_t xsz = a256((size_t)2 * C * d.n_pad * N * 2);
+    JetGemmArgs g{};
+    g.n_points = (int)n;
+    g.n_pad = (int)d.n_pad;
+    g.K = K;
+    g.N = N;
+    g.bias = b[l - 1];
+    g.z_out = (float*)tape.z[l];
+    g.y_out = (__nv_bfloat16*)tape.x[l];
+    g.yt_out = (__nv_bfloat16*)((char*)tape.x[l] + xsz);
+    g.status = status;
+    if ((st = launch_jet<0>(ma, mb, g, N / 128, (int)(d.n_pad / 128), s, "tc_jet_layer_fwd",
+                            2.0 * n * C * (double)d.w[l - 1] * N,
+                            (double)d.n_pad * C * (K * 4 + N * 12))))
+      return st;
+  }
+  return NEB_OK;
+}
+
+int tc_hidden_gram(const neb_net* net, const float* qw, int64_t n, const void* hl, double* AM,
+                   double* AS, char* ws, cudaStream_t s) {
+  int st = check_dims(net);
+  if (st) return st;
+  Dims d = dims_of(net, n);
+  TcWs t = tc_ws(d);
+  char* part = ws + t.part;
+  int* status = (int*)(ws + t.status);
+  const int H = d.H;
+  const char* XT = (const char*)hl + a256((size_t)2 * C * d.n_pad * H * 2);
+  __nv_bfloat16* wht = (__nv_bfloat16*)(ws + t.wht);
+  {
+    KernelScope ks("tc_weighted_fields", s, 0, 3.0 * H * d.n_pad * 8);
+    size_t total = (size_t)3 * H * d.n_pad;
+    int blocks = (int)std::min<size_t>((total + 255) / 256, 8192);
+    weighted_fields_t<<<blocks, 256, 0, s>>>((const __nv_bfloat16*)XT, qw, (int)n, (int)d.n_pad,
+                                             H, wht);
+    NEB_LAUNCH_CHECK();
+  }
+  int splits = 0;
+  // A_M: channels (d/dx, d/dy) = wHT channels 0, 1 against XT channels 1, 2
+  if ((st = launch_rowsum(wht, 3, 0, XT, C, 1, 2, H, H, d.n_pad, (double*)part, status, s,
+                          "tc_gram", 2.0 * 2 * n * (double)H * H, &splits, true)))
+    return st;
+  if ((st = reduce((double*)part, splits, H, H, H, H, true, nullptr, AM, s))) return st;
+  if ((st = launch_rowsum(wht, 3, 2, XT, C, 3, 1, H, H, d.n_pad, (double*)part, status, s,
+                          "tc_gram", 2.0 * n * (double)H * H, &splits, true)))
+    return st;
+  return reduce((double*)part, splits, H, H, H, H, true, nullptr, AS, s);
+}
+
+int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh, const float* qw,
+                       int64_t n, const TcTape& tape, float* const* gW, float* const* gb, char* ws,
+                       cudaStream_t s) {
+  int st = check_dims(net);
+  if (st) return st;
+  Dims d = dims_of(net, n);
+  TcWs t = tc_ws(d);
+  char* part = ws + t.part;
+  char* partb = ws + t.partb;
+  int* status = (int*)(ws + t.status);
+  const int L = d.L, H = d.H;
+  __nv_bfloat16* gs = (__nv_bfloat16*)(ws + t.gsplit);
+  {
+    KernelScope ks("tc_split_gram_adjoint", s, 0, (double)H * H * 2 * 12);
+    split_gram_adjoint<<<(int)std::min<size_t>((2ull * H * H + 255) / 256, 4096), 256, 0, s>>>(
+        GMh, GSh, H, gs);
+    NEB_LAUNCH_CHECK();
+  }
+  char* zb[2] = {ws + t.zb0, ws + t.zb1};
+  char* zbt = ws + t.zbt;
+  // Gram adjoint + tanh transpose of layer L
+  {
+    CUtensorMap ma, mb;
+    if ((st = make_map(&ma, tape.x[L], (int64_t)2 * C * d.n_pad, H, 128))) return st;
+    if ((st = make_map(&mb, gs, (int64_t)4 * H, H, 128))) return st;
+    JetGemmArgs g{};
+    g.n_points = (int)n;
+    g.n_pad = (int)d.n_pad;
+    g.K = H;
+    g.N = H;
+    g.zprev = (const float*)tape.z[L];
+    g.qw = qw;
+    g.y_out = (__nv_bfloat16*)zb[0];
+    g.yt_out = (__nv_bfloat16*)zbt;
+    g.status = status;
+    if ((st = launch_jet<2>(ma, mb, g, H / 128, (int)(d.n_pad / 128), s, "tc_gram_adjoint_bwd",
+                            2.0 * 3 * n * (double)H * H, (double)d.n_pad * C * H * 16)))
+      return st;
+  }
+  int cur = 0;
+  for (int l = L; l >= 1; --l) {
+    const int out = d.w[l], in = d.w[l - 1], inp = d.wp[l - 1];
+    // weight gradient: gW_l[o][i] = sum_c sum_p Zbar_l[c][p][o] X_{l-1}[c][p][i]
+    size_t xsz = a256((size_t)2 * C * d.n_pad * inp * 2);
+    const char* xt_prev = (const char*)tape.x[l - 1] + xsz;
+    int splits = 0;
+    if ((st = launch_rowsum(zbt, C, 0, xt_prev, C, 0, C, out, inp, d.n_pad, (double*)part, status,
+                            s, "tc_weight_grad", 2.0 * C * n * (double)out * in, &splits)))
+      return st;
+    if ((st = reduce((double*)part, splits, out, inp, in, in, false, gW[l - 1], nullptr, s)))
+      return st;
+    {
+      const int chunk = kBiasChunk;
+      const int chunks = (int)((d.n_pad + chunk - 1) / chunk);
+      KernelScope ks("bias_grad", s, 0, (double)d.n_pad * out * 4);
+      bias_partial_tc<<<dim3((out + 127) / 128, chunks), 128, 0, s>>>(
+          (const __nv_bfloat16*)zb[cur], (int)d.n_pad, out, chunk, (double*)partb);
+      NEB_LAUNCH_CHECK();
+      if ((st = reduce((double*)partb, chunks, 1, out, out, out, false, gb[l - 1], nullptr, s)))
+        return st;
+    }
+    if (l == 1) break;
+    // data gradient through W_l and the tanh transpose of layer l-1
+    CUtensorMap ma, mb;
+    if ((st = make_map(&ma, zb[cur], (int64_t)2 * C * d.n_pad, out, 128))) return st;
+    if ((st = make_map(&mb, ws + t.wt[l], (int64_t)2 * in, out, 128))) return st;
+    JetGemmArgs g{};
+    g.n_points = (int)n;
+    g.n_pad = (int)d.n_pad;
+    g.K = out;
+    g.N = in;
+    g.zprev = (const float*)tape.z[l - 1];
+    g.y_out = (__nv_bfloat16*)zb[cur ^ 1];
+    g.yt_out = (__nv_bfloat16*)zbt;
+    g.status = status;
+    if ((st = launch_jet<1>(ma, mb, g, in / 128, (int)(d.n_pad / 128), s,
+                            "tc_jet_layer_bwd_data", 2.0 * C * n * (double)out * in,
+                            (double)d.n_pad * C * (out * 4 + in * 12))))
+      return st;
+    cur ^= 1;
+  }
+  return NEB_OK;
+}
+
 int tc_output(const neb_net*, const float*, const float*, int, int, int64_t, const void*, void*,
               cudaStream_t) {
-  set_error("NEB_PREC_BF16X3 output not built");
+  set_error("NEB_PREC_BF16X3 stores no output-layer jets; evaluate them with NEB_PREC_FP32");
   return NEB_ERR_UNSUPPORTED;
 }
-int tc_hidden_gram(const neb_net*, const float*, int64_t, const void*, double*, double*, char*,
-                   char*, cudaStream_t) {
-  set_error("NEB_PREC_BF16X3 hidden gram not built");
-  return NEB_ERR_UNSUPPORTED;
-}
-int tc_backward_hidden(const neb_net*, const float* const*, const double*, const double*,
-                       const float*, int64_t, const TcTape&, float* const*, float* const*, char*,
-                       size_t, char*, char*, char*, cudaStream_t) {
-  set_error("NEB_PREC_BF16X3 backward not built");
-  return NEB_ERR_UNSUPPORTED;
+
+int tc_read_status(const neb_net* net, int64_t n, char* ws, cudaStream_t s, int* out) {
+  Dims d = dims_of(net, n);
+  TcWs t = tc_ws(d);
+  NEB_CUDA_CHECK(cudaMemcpyAsync(out, ws + t.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NEB_CUDA_CHECK(cudaStreamSynchronize(s));
+  return NEB_OK;
 }
 
 }  // namespace neb

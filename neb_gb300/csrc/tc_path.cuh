@@ -11,15 +11,18 @@ struct TcTape {
 };
 
 size_t tc_workspace_bytes(const neb_net* net, int64_t n);
+// Tape layout of the tensor-core path (offsets of X_l and Z_l); returns total bytes.
+size_t tc_tape_bytes(const neb_net* net, int64_t n, size_t* x_off, size_t* z_off);
+// Synchronises the stream and reads the bounded-wait status word (0 = ok).
+int tc_read_status(const neb_net* net, int64_t n, char* ws, cudaStream_t s, int* out);
 int tc_forward(const neb_net* net, const float* const* W, const float* const* b, const float* feats,
                int64_t n, const TcTape& tape, char* ws, cudaStream_t s);
 int tc_output(const neb_net* net, const float* Wout, const float* bout, int start, int stop,
               int64_t n, const void* tape, void* psi, cudaStream_t s);
 int tc_hidden_gram(const neb_net* net, const float* qw, int64_t n, const void* hl, double* AM,
-                   double* AS, char* part, char* ws, cudaStream_t s);
-int tc_backward_hidden(const neb_net* net, const float* const* W, const double* GMh,
-                       const double* GSh, const float* qw, int64_t n, const TcTape& tape,
-                       float* const* gW, float* const* gb, char* zbuf, size_t zb1_off, char* part,
-                       char* partb, char* ws, cudaStream_t s);
+                   double* AS, char* ws, cudaStream_t s);
+int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh, const float* qw,
+                       int64_t n, const TcTape& tape, float* const* gW, float* const* gb, char* ws,
+                       cudaStream_t s);
 
 }  // namespace neb

@@ -82,6 +82,10 @@ class Model:
         self.mb = [torch.zeros_like(b) for b in self.b]
         self.vb = [torch.zeros_like(b) for b in self.b]
         self.net = N.NebNet.make(cfg.dim, cfg.widths, precision)
+        # the reference-API forward/backward evaluate output-layer jets, which
+        # the tensor-core path does not store: they run the FP32 kernels
+        self.net_eval = self.net if precision != "bf16x3" else \
+            N.NebNet.make(cfg.dim, cfg.widths, "fp32")
         self._buf = _Buffers(self.device)
         N.load()
 
@@ -103,8 +107,10 @@ class Model:
             self.W[j].copy_(torch.as_tensor(np.asarray(W), dtype=self.dtype))
             self.b[j].copy_(torch.as_tensor(np.asarray(b), dtype=self.dtype))
 
-    def _ws(self, n: int) -> torch.Tensor:
-        return self._buf.get("ws", N.load().neb_workspace_bytes(ctypes.byref(self.net), n))
+    def _ws(self, n: int, net=None) -> torch.Tensor:
+        net = self.net if net is None else net
+        key = "ws" if net is self.net else "ws_eval"
+        return self._buf.get(key, N.load().neb_workspace_bytes(ctypes.byref(net), n))
 
     def features(self, points) -> torch.Tensor:
         """Input feature jets [n, C, F] (device, master dtype) of points [n, dim]."""
@@ -119,22 +125,31 @@ class Model:
                len(prm), pts.data_ptr(), n, out.data_ptr(), _stream())
         return out
 
-    def run_forward(self, feats: torch.Tensor) -> Tape:
+    def run_forward(self, feats: torch.Tensor, net=None) -> Tape:
         """Hidden layers over packed feature jets; returns the tape."""
+        net = self.net if net is None else net
         feats = feats.to(self.dtype).contiguous()
         n = feats.shape[0]
-        tape = self._buf.get("tape", N.load().neb_tape_bytes(ctypes.byref(self.net), n))
-        ws = self._ws(n)
-        N.call("neb_forward", ctypes.byref(self.net), N.ptr_array(self.W), N.ptr_array(self.b),
+        key = "tape" if net is self.net else "tape_eval"
+        tape = self._buf.get(key, N.load().neb_tape_bytes(ctypes.byref(net), n))
+        ws = self._ws(n, net)
+        N.call("neb_forward", ctypes.byref(net), N.ptr_array(self.W), N.ptr_array(self.b),
                feats.data_ptr(), n, tape.data_ptr(), ws.data_ptr(), ws.numel(), _stream())
         return Tape(tape, n, feats)
+
+    def check_device_status(self, n: int) -> None:
+        """Raise if a bounded device-side wait gave up during this step."""
+        ws = self._ws(n)
+        N.call("neb_check_status", ctypes.byref(self.net), n, ws.data_ptr(), ws.numel(),
+               _stream())
 
     def output(self, tape: Tape, start: int = 0, stop: int | None = None) -> torch.Tensor:
         stop = self.c.widths[-1] if stop is None else stop
         psi = torch.empty((tape.n_points, self.channels, stop - start), dtype=self.dtype,
                           device=self.device)
-        N.call("neb_output", ctypes.byref(self.net), self.W[-1].data_ptr(), self.b[-1].data_ptr(),
-               start, stop, tape.n_points, tape.buffer.data_ptr(), psi.data_ptr(), _stream())
+        N.call("neb_output", ctypes.byref(self.net_eval), self.W[-1].data_ptr(),
+               self.b[-1].data_ptr(), start, stop, tape.n_points, tape.buffer.data_ptr(),
+               psi.data_ptr(), _stream())
         return psi
 
     # ------------------------------------------------- reference backend API
@@ -147,7 +162,7 @@ class Model:
         _check_identity_envelope(data)
         feats = data.features
         feats = pack(feats, self.c.dim).to(self.device, self.dtype) if isinstance(feats, Jet) else feats
-        tape = self.run_forward(feats)
+        tape = self.run_forward(feats, self.net_eval)
         if cache:  # keep this tape: later calls must not overwrite it
             tape = Tape(tape.buffer.clone(), tape.n_points, tape.features)
         psi = self.output(tape, start, stop)
@@ -164,8 +179,8 @@ class Model:
             raise ValueError(f"adjoint shape {tuple(pb.shape)} does not match the outputs")
         gW = [torch.zeros_like(w) for w in self.W]
         gb = [torch.zeros_like(b) for b in self.b]
-        ws = self._ws(tape.n_points)
-        N.call("neb_backward_output", ctypes.byref(self.net), N.ptr_array(self.W), start, stop,
+        ws = self._ws(tape.n_points, self.net_eval)
+        N.call("neb_backward_output", ctypes.byref(self.net_eval), N.ptr_array(self.W), start, stop,
                pb.data_ptr(), tape.n_points, tape.buffer.data_ptr(), N.ptr_array(gW),
                N.ptr_array(gb), 0, ws.data_ptr(), ws.numel(), _stream())
         return gW, gb
@@ -330,6 +345,7 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
         res.grads = (gW, gb)
     if check:
         code = int(info.item())
+        model.check_device_status(n)
         if code != 0:
             raise FloatingPointError(
                 f"spectral stage failed (info={code}): the mass matrix is not positive definite "

@@ -134,7 +134,7 @@ def linear_backward(X, Zbar, W):
     """Transpose (hardcoded_backend.py:1115-1144): Xbar_c = Zbar_c W,
     gW = sum_c Zbar_c^T X_c, gb = sum_points Zbar_value."""
     Xbar = Zbar @ W
-    gW = np.einsum("cno,cni->oi", Zbar, X)
+    gW = np.tensordot(Zbar, X, axes=([0, 1], [0, 1]))
     gb = Zbar[0].sum(axis=0)
     return Xbar, gW, gb
 
