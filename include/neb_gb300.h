@@ -145,6 +145,20 @@ int neb_spectral(int m, const double* M, const double* S, const double* c, doubl
                  double* V, double* G_M, double* G_S, double* loss, int* info,
                  void* workspace, size_t workspace_bytes, neb_stream_t stream);
 
+/* Same contract as neb_spectral for m a multiple of 64 up to 512, computed
+ * with the precision where the conditioning lives: FP64 Cholesky of M and
+ * FP64 inverse factor L^-1; the reduced, well conditioned matrix
+ * C = L^-1 S L^-T formed by compensated FP32 GEMMs, rounded to FP32 and
+ * reduced to tridiagonal form in FP32 by one 8-CTA thread-block cluster; eigenvectors of
+ * the tridiagonal by FP32 twisted factorisations and eigenvalues as their FP64
+ * Rayleigh quotients; FP32 back-transformation and adjoints.  Eigenvalue
+ * relative error ~ eps_32 cond(C) (1e-6 on the periodic training pencil).
+ * Replaces the same reference functions as neb_spectral. */
+size_t neb_spectral_mixed_workspace_bytes(int m);
+int neb_spectral_mixed(int m, const double* M, const double* S, const double* c, double* lam,
+                       double* V, double* G_M, double* G_S, double* loss, int* info,
+                       void* workspace, size_t workspace_bytes, neb_stream_t stream);
+
 /* K x H output weights between the hidden pencil and the K x K pencil
  * (FP64): M = W A_M W^T, S = W A_S W^T; and back: G_Mh = W^T G_M W,
  * G_Sh = W^T G_S W, gW = 2 (G_M W A_M + G_S W A_S). */

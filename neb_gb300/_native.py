@@ -62,6 +62,10 @@ _SIGNATURES = {
     "neb_spectral_workspace_bytes": (c_size_t, [c_int]),
     "neb_spectral": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "neb_spectral_mixed_workspace_bytes": (c_size_t, [c_int]),
+    "neb_spectral_mixed": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                                   c_void_p]),
     "neb_pencil_workspace_bytes": (c_size_t, [c_int, c_int]),
     "neb_pencil_project": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_size_t, c_void_p]),

@@ -38,7 +38,7 @@ TimingState g_timing;
 unsigned long long g_launches = 0;
 }  // namespace
 
-void count_launch() { __atomic_add_fetch(&g_launches, 1ull, __ATOMIC_RELAXED); }
+void count_launch(int n) { __atomic_add_fetch(&g_launches, (unsigned long long)n, __ATOMIC_RELAXED); }
 
 void timing_record(const char* name, cudaStream_t s, double flops, double bytes, bool begin) {
   if (!g_timing.enabled) return;

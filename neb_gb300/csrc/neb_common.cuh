@@ -139,18 +139,19 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // (neb_timing_begin / neb_timing_end), brackets it with CUDA events on the
 // launching stream and records its algorithmic flops and bytes.
 void timing_record(const char* name, cudaStream_t s, double flops, double bytes, bool begin);
-void count_launch();
+void count_launch(int n = 1);
 
 struct KernelScope {
   const char* name;
   cudaStream_t stream;
   double flops, bytes;
-  KernelScope(const char* n, cudaStream_t s, double f = 0, double b = 0)
-      : name(n), stream(s), flops(f), bytes(b) {
+  int launches;
+  KernelScope(const char* n, cudaStream_t s, double f = 0, double b = 0, int nl = 1)
+      : name(n), stream(s), flops(f), bytes(b), launches(nl) {
     timing_record(name, stream, flops, bytes, true);
   }
   ~KernelScope() {
-    count_launch();
+    count_launch(launches);
     timing_record(name, stream, flops, bytes, false);
   }
 };

@@ -62,9 +62,17 @@ class Model:
     """Shared tanh MLP with analytic spatial jets (reference backend API)."""
 
     def __init__(self, cfg: NebConfig, K: int | None = None, seed: int = 0,
-                 precision: str = "bf16x3", device: str | torch.device = "cuda"):
+                 precision: str = "bf16x3", device: str | torch.device = "cuda",
+                 spectral: str | None = None):
         if precision not in N.PREC:
             raise ValueError(f"precision must be one of {tuple(N.PREC)}")
+        # spectral stage: "mixed" (FP64 Cholesky and inverse factor, FP32
+        # tridiagonalisation, FP64 tridiagonal eigensolve) or "fp64"
+        # (cuSOLVER sygvd); the FP64 form defaults to "fp64"
+        spectral = spectral or ("fp64" if precision == "fp64" else "mixed")
+        if spectral not in ("mixed", "fp64"):
+            raise ValueError("spectral must be 'mixed' or 'fp64'")
+        self.spectral = spectral
         if K is not None:
             cfg = cfg.scaled(outputs=K * (3 if cfg.dim == 3 else 1))
         self.c = cfg
@@ -319,8 +327,10 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
     lam, V, GM, GS = _f64((m,), dev), _f64((m, m), dev), _f64((m, m), dev), _f64((m, m), dev)
     loss = _f64((), dev)
     info = torch.zeros((), dtype=torch.int32, device=dev)
-    sws = st.buf.get("spectral", lib.neb_spectral_workspace_bytes(m))
-    N.call("neb_spectral", m, PM.data_ptr(), PS.data_ptr(), c.data_ptr(), lam.data_ptr(),
+    mixed_bytes = lib.neb_spectral_mixed_workspace_bytes(m) if model.spectral == "mixed" else 0
+    name = "neb_spectral_mixed" if mixed_bytes else "neb_spectral"
+    sws = st.buf.get(name, mixed_bytes or lib.neb_spectral_workspace_bytes(m))
+    N.call(name, m, PM.data_ptr(), PS.data_ptr(), c.data_ptr(), lam.data_ptr(),
            V.data_ptr(), GM.data_ptr(), GS.data_ptr(), loss.data_ptr(), info.data_ptr(),
            sws.data_ptr(), sws.numel(), s)
     res = SpectralResult(loss, lam, V, m, info, M=M, S=S, A_M=AM, A_S=AS)

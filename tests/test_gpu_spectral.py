@@ -1,0 +1,100 @@
+"""Mixed-precision spectral stage (neb_spectral_mixed) against the FP64 oracle
+(GB300 only).  Its eigenvalue error is about eps_32 * cond(C) for the reduced
+matrix C = L^-1 S L^-T; the pencils here have cond(M) = 1e4 and cond(C) = 40
+like the training pencils.  Tolerances: eigenvalues 1e-5 relative, objective
+adjoints 1e-4 relative (norm)."""
+import ctypes
+
+import numpy as np
+import pytest
+import scipy.linalg as sla
+import torch
+
+from oracle import neb_oracle as O
+from neb_gb300 import _native as N
+from neb_gb300 import configs as CF
+
+pytestmark = pytest.mark.gpu
+
+
+def _pencil(m, seed, cond=1e4, lam_range=(30.0, 1200.0)):
+    """A pencil shaped like the training pencils: mass matrix of condition
+    ``cond``, generalized eigenvalues spread over ``lam_range``."""
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.normal(size=(m, m)))
+    ev = np.logspace(0, np.log10(cond), m)
+    M = (Q * ev) @ Q.T
+    M = 0.5 * (M + M.T)
+    P, _ = np.linalg.qr(rng.normal(size=(m, m)))
+    lam = np.sort(rng.uniform(*lam_range, m))
+    L = np.linalg.cholesky(M)
+    S = L @ ((P * lam) @ P.T) @ L.T
+    return M, 0.5 * (S + S.T)
+
+
+def _run(name, M, S, c):
+    m = len(M)
+    dev = "cuda"
+    t = lambda a: torch.tensor(a, dtype=torch.float64, device=dev).contiguous()
+    Md, Sd, cd = t(M), t(S), t(c)
+    lam = torch.empty(m, dtype=torch.float64, device=dev)
+    V, GM, GS = (torch.empty((m, m), dtype=torch.float64, device=dev) for _ in range(3))
+    loss = torch.empty((), dtype=torch.float64, device=dev)
+    info = torch.zeros((), dtype=torch.int32, device=dev)
+    lib = N.load()
+    nbytes = getattr(lib, name + "_workspace_bytes")(m)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    N.call(name, m, Md.data_ptr(), Sd.data_ptr(), cd.data_ptr(), lam.data_ptr(), V.data_ptr(),
+           GM.data_ptr(), GS.data_ptr(), loss.data_ptr(), info.data_ptr(), ws.data_ptr(),
+           ws.numel(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return (int(info.item()), lam.cpu().numpy(), V.cpu().numpy(), GM.cpu().numpy(),
+            GS.cpu().numpy(), float(loss.item()))
+
+
+@pytest.mark.parametrize("m", [64, 256, 512])
+@pytest.mark.parametrize("kind", ["trace", "ordering"])
+def test_mixed_spectral_matches_fp64(m, kind):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    M, S = _pencil(m, m)
+    ref = O.spectral_objective(M, S, kind)
+    info, lam, V, GM, GS, loss = _run("neb_spectral_mixed", M, S, ref["lam"] * 0 + O.objective_weights(kind, m))
+    assert info == 0
+    np.testing.assert_allclose(lam, ref["lam"], rtol=1e-5)
+    assert abs(loss - ref["loss"]) <= 1e-5 * abs(ref["loss"])
+    # the adjoints come from FP32 eigenvectors: about eps_32 cond(L) relative
+    for g, r in ((GM, ref["GM"]), (GS, ref["GS"])):
+        assert np.linalg.norm(g - r) <= 5e-4 * np.linalg.norm(r)
+    # rows of V are M-orthonormal generalized eigenvectors (FP32 vectors,
+    # so orthonormality to about eps_32 cond(M))
+    assert np.abs(V @ M @ V.T - np.eye(m)).max() < 1e-2
+    R = V @ S - lam[:, None] * (V @ M)
+    assert np.abs(R).max() <= 1e-4 * np.abs(S).max()
+
+
+def test_mixed_spectral_on_periodic_hidden_pencil():
+    """The K = 1024 periodic training pencil (cond(A_M) ~ 1.5e4)."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    cfg = CF.CONFIGS["periodic_train"]
+    pts, w = CF.sample(cfg)
+    p = O.glorot_init(list(cfg.widths), 0)
+    xs, _, _ = O.mlp_forward(p, O.features_periodic(pts, 16), 2)
+    AM, AS = O.hidden_grams_2d(xs[-1], w[0])
+    ref = O.spectral_objective(AM, AS, "ordering")
+    info, lam, V, GM, GS, loss = _run("neb_spectral_mixed", AM, AS, O.objective_weights("ordering", 512))
+    assert info == 0
+    assert np.max(np.abs(lam - ref["lam"]) / ref["lam"]) < 1e-5
+    assert np.linalg.norm(GM - ref["GM"]) <= 1e-4 * np.linalg.norm(ref["GM"])
+    assert np.linalg.norm(GS - ref["GS"]) <= 1e-4 * np.linalg.norm(ref["GS"])
+
+
+def test_mixed_spectral_flags_a_singular_mass_matrix():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    M, S = _pencil(64, 3)
+    M[:, 5] = 0.0
+    M[5, :] = 0.0
+    info, *_ = _run("neb_spectral_mixed", M, S, np.ones(64))
+    assert info > 64
