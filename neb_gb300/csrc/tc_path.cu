@@ -114,7 +114,7 @@ __device__ __forceinline__ void store_split16(const float* v, __nv_bfloat16* hi_
 }
 
 template <int EPI>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(320, 1)
 tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             JetGemmArgs g) {
   using Cfg = JetCfg<EPI>;
@@ -210,49 +210,34 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     }
     tc::mma_commit(acc_full);
   } else if (warp >= 2) {
-    // ---------------- epilogue: one thread per point (TMEM lane)
-    const int q = warp & 3;
+    // ---------------- epilogue: eight warps, one thread per point (TMEM lane);
+    // warp w reads lane quarter w % 4 and column half (w - 2) / 4.
+    const int q = warp & 3, half = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     const int p = p0 + row;
     tc::mbar_wait(acc_full, 0, g.status);
     tc::tc_fence_after();
     const size_t plane = (size_t)C * g.n_pad * g.N;  // elements of one hi or lo plane
+    // transposed outputs are staged per warp through the (now idle) operand
+    // buffers: [C][2 planes][16 columns][32 points] bf16 = 8 KB per warp
+    __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(smem) + (size_t)(warp - 2) * 4096;
     float w2 = 0.f;
     if constexpr (EPI == 2) w2 = p < g.n_points ? 2.f * g.qw[p] : 0.f;
-    for (int j0 = 0; j0 < 128; j0 += 16) {
+    for (int jc = 0; jc < 4; ++jc) {
+      const int j0 = half * 64 + jc * 16;
       float acc[NCH][16];
 #pragma unroll
       for (int ci = 0; ci < NCH; ++ci)
         tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + ci * 128 + j0, acc[ci]);
       const int col = n0 + j0;
       float out[C][16];
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        float v[C];
-        if constexpr (EPI == 0) {
-#pragma unroll
-          for (int c = 0; c < C; ++c) v[c] = acc[c][j];
-          v[0] += g.bias[col + j];
-#pragma unroll
-          for (int c = 0; c < C; ++c) out[c][j] = v[c];  // pre-activation, stored below
-        } else {
-          float z[C];
-#pragma unroll
-          for (int c = 0; c < C; ++c) z[c] = g.zprev[((size_t)c * g.n_pad + p) * g.N + col + j];
-          if constexpr (EPI == 2) {
-            v[0] = 0.f;
-#pragma unroll
-            for (int c = 1; c < C; ++c) v[c] = w2 * acc[c - 1][j];
-          } else {
-#pragma unroll
-            for (int c = 0; c < C; ++c) v[c] = acc[c][j];
-          }
-          jet_act_backward<C>(z, v);
-#pragma unroll
-          for (int c = 0; c < C; ++c) out[c][j] = v[c];
-        }
-      }
       if constexpr (EPI == 0) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+#pragma unroll
+          for (int c = 0; c < C; ++c) out[c][j] = acc[c][j];
+          out[0][j] += g.bias[col + j];
+        }
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           float4* zd = reinterpret_cast<float4*>(g.z_out + ((size_t)c * g.n_pad + p) * g.N + col);
@@ -270,7 +255,39 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 #pragma unroll
           for (int c = 0; c < C; ++c) out[c][j] = v[c];
         }
+      } else {
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const float4* zs =
+              reinterpret_cast<const float4*>(g.zprev + ((size_t)c * g.n_pad + p) * g.N + col);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            float4 z4 = zs[j];
+            out[c][4 * j] = z4.x;
+            out[c][4 * j + 1] = z4.y;
+            out[c][4 * j + 2] = z4.z;
+            out[c][4 * j + 3] = z4.w;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          float z[C], v[C];
+#pragma unroll
+          for (int c = 0; c < C; ++c) z[c] = out[c][j];
+          if constexpr (EPI == 2) {
+            v[0] = 0.f;
+#pragma unroll
+            for (int c = 1; c < C; ++c) v[c] = w2 * acc[c - 1][j];
+          } else {
+#pragma unroll
+            for (int c = 0; c < C; ++c) v[c] = acc[c][j];
+          }
+          jet_act_backward<C>(z, v);
+#pragma unroll
+          for (int c = 0; c < C; ++c) out[c][j] = v[c];
+        }
       }
+      // planar split outputs (row-contiguous per point), transposed via smem
 #pragma unroll
       for (int c = 0; c < C; ++c) {
         size_t o = ((size_t)c * g.n_pad + p) * g.N + col;
@@ -279,11 +296,22 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         for (int j = 0; j < 16; ++j) {
           __nv_bfloat16 h, l;
           tc::split_bf16(out[c][j], h, l);
-          size_t t = ((size_t)c * g.N + col + j) * g.n_pad + p;
-          g.yt_out[t] = h;
-          g.yt_out[plane + t] = l;
+          stage[((c * 2 + 0) * 16 + j) * 32 + lane] = h;
+          stage[((c * 2 + 1) * 16 + j) * 32 + lane] = l;
         }
       }
+      __syncwarp();
+      const uint4* st4 = reinterpret_cast<const uint4*>(stage);
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const int u = lane + 32 * t;       // 512 vectors of 8 points
+        const int r = u >> 2, quad = u & 3;  // r = (c * 2 + plane) * 16 + j
+        const int c = r >> 5, pl = (r >> 4) & 1, j = r & 15;
+        const size_t gi = (size_t)pl * plane + ((size_t)c * g.N + col + j) * g.n_pad + p0 +
+                          q * 32 + quad * 8;
+        *reinterpret_cast<uint4*>(g.yt_out + gi) = st4[u];
+      }
+      __syncwarp();
     }
   }
   tc::tc_fence_before();
@@ -628,7 +656,7 @@ int launch_jet(const CUtensorMap& A, const CUtensorMap& B, const JetGemmArgs& ar
     configured = true;
   }
   KernelScope ks(name, s, flops, bytes);
-  tc_jet_gemm<EPI><<<dim3(n_tiles, p_tiles), 192, JetCfg<EPI>::SMEM, s>>>(A, B, args);
+  tc_jet_gemm<EPI><<<dim3(n_tiles, p_tiles), 320, JetCfg<EPI>::SMEM, s>>>(A, B, args);
   NEB_LAUNCH_CHECK();
   return NEB_OK;
 }
