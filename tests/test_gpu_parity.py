@@ -12,7 +12,7 @@ import pytest
 import torch
 
 from oracle import neb_oracle as O
-from neb_gb300 import CONFIGS, Jet, Model, spectral_step, train_step
+from neb_gb300 import CONFIGS, Jet, Model, SpectralObjective, spectral_step, train_step
 from neb_gb300 import configs as CF
 
 pytestmark = pytest.mark.gpu
@@ -206,3 +206,33 @@ def test_training_loop_decreases_loss_fp32():
         losses.append(float(res.loss))
     assert model.epoch == 6
     assert losses[-1] < losses[0]
+
+
+def test_spectral_objective_autograd_matches_oracle(tmp_path):
+    """SpectralObjective as a torch.autograd.Function: loss and parameter
+    gradients through torch.autograd.grad equal the oracle's (FP64 form)."""
+    _needs_gpu()
+    cfg = CONFIGS["periodic_small"].scaled(hidden=32, outputs=24, grid_n=20)
+    pts, w = CF.sample(cfg)
+    model = Model(cfg, precision="fp64", seed=5)
+    params = [p.detach().requires_grad_() for p in model.parameters()]
+    feats = model.features(pts)
+    loss = SpectralObjective.apply(model, feats, torch.as_tensor(w, device="cuda"), *params)
+    grads = torch.autograd.grad(2.0 * loss, params)
+    ref = O.objective_and_grad_factored(_params64(model), _oracle_features(cfg, pts), w,
+                                        cfg.objective)
+    assert abs(float(loss.detach()) - ref.loss) <= 1e-9 * abs(ref.loss)
+    L = len(model.W)
+    got = ([g / 2.0 for g in grads[:L]], [g / 2.0 for g in grads[L:]])
+    assert _grad_rel(got, ref.grads) < 1e-8
+    # save / load round trip keeps parameters, moments and epoch (NCC keys)
+    gW, gb = got
+    model.adam(gW, gb, 1e-3)
+    path = tmp_path / "state.npz"
+    model.save(path)
+    other = Model(cfg, precision="fp64", seed=9)
+    other.load(path)
+    assert other.epoch == model.epoch == 1
+    for name in ("W", "b", "mW", "vW", "mb", "vb"):
+        for a, b in zip(getattr(model, name), getattr(other, name)):
+            assert torch.equal(a, b)
