@@ -121,6 +121,16 @@ int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n_points,
                     const void* tape, double* A_M, double* A_S, void* workspace,
                     size_t workspace_bytes, neb_stream_t stream);
 
+/* neb_hidden_gram for FP32 / FP64 networks without a workspace argument: no
+ * counterpart in the reference (its CuPy code always has a memory pool).
+ * For hosts that cannot pass a workspace; allocates nothing.  The per-chunk
+ * partials live in a fixed 8 MiB device array: chunks x H x H doubles must
+ * fit (H <= 128 at any n_points), else NEB_ERR_ARG.  The first call on each
+ * device sets up the array's address and should come before any stream
+ * capture; calls overlapping in time on one device race on the array. */
+int neb_hidden_gram_static(const neb_net* net, const void* qw, int64_t n_points,
+                           const void* tape, double* A_M, double* A_S, neb_stream_t stream);
+
 /* FP64 K x K Grams of the fields of output rows [0, widths[L+1]) assembled
  * from the output jets without storing them: 2D u = (psi_y, -psi_x),
  * omega = -lap psi; 3D u = curl A, omega = curl curl A (VTJ2:93-98).

@@ -57,6 +57,8 @@ _SIGNATURES = {
                            c_void_p, c_void_p]),
     "neb_hidden_gram": (c_int, [POINTER(NebNet), c_void_p, c_int64, c_void_p, c_void_p, c_void_p,
                                 c_void_p, c_size_t, c_void_p]),
+    "neb_hidden_gram_static": (c_int, [POINTER(NebNet), c_void_p, c_int64, c_void_p, c_void_p,
+                                       c_void_p, c_void_p]),
     "neb_fields_gram": (c_int, [POINTER(NebNet), c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                                 c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "neb_spectral_workspace_bytes": (c_size_t, [c_int]),

@@ -3,6 +3,7 @@
 // NEB_PREC_BF16X3 runs the tcgen05 kernels of tc_path.cu.
 #include <cstdarg>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 #include "simt_kernels.cuh"
@@ -706,4 +707,96 @@ extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* con
     NEB_LAUNCH_CHECK();
   }
   return NEB_OK;
+}
+
+// ------------------------------------------- allocation-free hidden Grams
+// neb_hidden_gram_static computes what neb_hidden_gram computes for the
+// FP32 and FP64 networks, but takes no workspace: its per-chunk FP64
+// partial Grams live in the fixed device array below, so the call allocates
+// no device memory at all.  It exists for callers that cannot hand the
+// library a workspace: a plain C or ctypes host with no PyTorch or CuPy
+// memory pool to carve one from, for which a cudaMalloc / cudaFree pair per
+// call would also synchronise the whole device.
+//
+// The array holds at most kStaticScratchBytes (8 MiB):
+// chunks x H x H doubles with chunks = ceil(n / max(256, ceil(n / 32))),
+// i.e. H <= 128 at any n, H = 256 up to n = 4096.  Larger requests are
+// rejected with NEB_ERR_ARG before anything is launched.  Nothing in the
+// array needs to start at zero: every partial the reduction reads is
+// written by the chunk kernel of the same call.
+//
+// The first call on each device looks up the array's device address with
+// cudaGetSymbolAddress (with that device current) and caches it; make that
+// first call before any stream capture begins.  There is one array per
+// device, so calls that overlap in time on one device (two streams, two
+// host threads) race on it: serialise them, e.g. on one stream.
+static __device__ __align__(256) unsigned char g_gram_scratch[8u << 20];
+
+namespace neb {
+namespace {
+constexpr size_t kStaticScratchBytes = sizeof(g_gram_scratch);
+constexpr int kMaxScratchDevices = 64;
+std::mutex g_scratch_mutex;
+void* g_scratch_ptr[kMaxScratchDevices] = {};
+
+int static_scratch(void** out) {
+  int dev = -1;
+  NEB_CUDA_CHECK(cudaGetDevice(&dev));
+  NEB_REQUIRE(dev >= 0 && dev < kMaxScratchDevices,
+              "neb_hidden_gram_static: device ordinal %d beyond %d", dev, kMaxScratchDevices);
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_gram_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("neb_hidden_gram_static: cudaGetSymbolAddress on device %d: %s", dev,
+                cudaGetErrorString(e));
+      return NEB_ERR_CUDA;
+    }
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return NEB_OK;
+}
+
+template <typename T>
+int hidden_gram_fixed(const neb_net* net, const void* qw, int64_t n, const void* tape,
+                      double* AM, double* AS, double* part, cudaStream_t s) {
+  const int L = net->n_hidden, H = net->widths[L];
+  TapeLayout tl = tape_layout(net, n);
+  const T* HL = (const T*)((const char*)tape + tl.x_off[L]);
+  simt::ChanSet grad{2, {1, 2}};
+  simt::ChanSet lap{1, {3}};
+  int st = launch_rowsum<T, 4, double>(HL, H, HL, H, (const T*)qw, grad, n, H, H, true, 1.0, part,
+                                       AM, s);
+  if (st) return st;
+  return launch_rowsum<T, 4, double>(HL, H, HL, H, (const T*)qw, lap, n, H, H, true, 1.0, part,
+                                     AS, s);
+}
+}  // namespace
+}  // namespace neb
+
+extern "C" int neb_hidden_gram_static(const neb_net* net, const void* qw, int64_t n,
+                                      const void* tape, double* AM, double* AS,
+                                      neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  NEB_REQUIRE(net->dim == 2, "neb_hidden_gram_static: 2D scalar potential only");
+  NEB_REQUIRE(net->precision == NEB_PREC_FP32 || net->precision == NEB_PREC_FP64,
+              "neb_hidden_gram_static: FP32 or FP64 networks only");
+  NEB_REQUIRE(n > 0 && qw && tape && AM && AS, "neb_hidden_gram_static: bad arguments");
+  const int H = net->widths[net->n_hidden];
+  const int64_t chunks = ceil_div(n, chunk_points(n));
+  const size_t need = (size_t)chunks * H * H * sizeof(double);
+  NEB_REQUIRE(need <= kStaticScratchBytes,
+              "neb_hidden_gram_static: %lld points x width %d need %zu bytes of scratch "
+              "(%lld chunks x %d x %d doubles); the fixed array holds %zu",
+              (long long)n, H, need, (long long)chunks, H, H, kStaticScratchBytes);
+  void* part = nullptr;
+  st = static_scratch(&part);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (net->precision == NEB_PREC_FP64)
+    return hidden_gram_fixed<double>(net, qw, n, tape, AM, AS, (double*)part, s);
+  return hidden_gram_fixed<float>(net, qw, n, tape, AM, AS, (double*)part, s);
 }
