@@ -24,6 +24,7 @@ struct TimingEntry {
 struct TimingState {
   bool enabled = false;
   std::vector<TimingEntry> entries;
+  std::vector<size_t> open;  // entries whose scope has not ended (scopes nest)
   std::vector<cudaEvent_t> pool;
   size_t used = 0;
   cudaEvent_t get() {
@@ -46,9 +47,11 @@ void timing_record(const char* name, cudaStream_t s, double flops, double bytes,
   cudaEvent_t e = g_timing.get();
   cudaEventRecord(e, s);
   if (begin) {
+    g_timing.open.push_back(g_timing.entries.size());
     g_timing.entries.push_back({name, e, nullptr, flops, bytes});
-  } else if (!g_timing.entries.empty()) {
-    g_timing.entries.back().b = e;
+  } else if (!g_timing.open.empty()) {
+    g_timing.entries[g_timing.open.back()].b = e;
+    g_timing.open.pop_back();
   }
 }
 
@@ -390,6 +393,7 @@ extern "C" unsigned long long neb_kernel_launches(void) {
 
 extern "C" int neb_timing_begin(void) {
   g_timing.entries.clear();
+  g_timing.open.clear();
   g_timing.used = 0;
   g_timing.enabled = true;
   return NEB_OK;
@@ -430,6 +434,7 @@ extern "C" int neb_timing_end(int max_kernels, char* names, int name_len, int* l
   }
   *n_kernels = n;
   g_timing.entries.clear();
+  g_timing.open.clear();
   g_timing.used = 0;
   return NEB_OK;
 }

@@ -562,20 +562,31 @@ __global__ void reduce_parts(const double* __restrict__ part, int splits, int M,
   }
 }
 
-// Bias gradient partials: partb[chunk][o] = sum over points of the value
-// plane of Zbar (hi + lo).
+// Bias gradient partials: partb[chunk][o] = sum over the chunk's points of
+// the value plane of Zbar (hi + lo).  hi + lo is exact in FP32; four
+// independent FP32 accumulators over a 256-point chunk keep the dependent
+// add chain short, and the chunk sums are combined in FP64 by reduce_parts.
 __global__ void bias_partial_tc(const __nv_bfloat16* __restrict__ zb, int n_pad, int N,
                                 int chunk, double* __restrict__ partb) {
   int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= N) return;
   const size_t plane = (size_t)C * n_pad * N;
   int p0 = blockIdx.y * chunk, p1 = min(n_pad, p0 + chunk);
-  double s = 0.0;
-  for (int p = p0; p < p1; ++p) {
-    size_t i = (size_t)p * N + o;  // channel 0
-    s += (double)__bfloat162float(zb[i]) + (double)__bfloat162float(zb[plane + i]);
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  int p = p0;
+  for (; p + 4 <= p1; p += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      size_t i = (size_t)(p + u) * N + o;  // channel 0
+      acc[u] += __bfloat162float(zb[i]) + __bfloat162float(zb[plane + i]);
+    }
   }
-  partb[(size_t)blockIdx.y * N + o] = s;
+  for (; p < p1; ++p) {
+    size_t i = (size_t)p * N + o;
+    acc[0] += __bfloat162float(zb[i]) + __bfloat162float(zb[plane + i]);
+  }
+  partb[(size_t)blockIdx.y * N + o] = ((double)acc[0] + (double)acc[1]) +
+                                      ((double)acc[2] + (double)acc[3]);
 }
 
 // ---------------------------------------------------------- host helpers
@@ -606,7 +617,7 @@ size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 // TC workspace: [status][W splits per layer][WT splits][G split][wHT][Zbar A][Zbar B][ZbarT]
 //               [FP64 split partials][bias partials]
 constexpr int kMaxSplits = 32;
-constexpr int kBiasChunk = 512;
+constexpr int kBiasChunk = 256;
 struct TcWs {
   size_t status, w[NEB_MAX_HIDDEN + 1], wt[NEB_MAX_HIDDEN + 1], gsplit, wht, zb0, zb1, zbt,
       part, partb, total;
@@ -877,10 +888,12 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
     {
       const int chunk = kBiasChunk;
       const int chunks = (int)((d.n_pad + chunk - 1) / chunk);
-      KernelScope ks("bias_grad", s, 0, (double)d.n_pad * out * 4);
-      bias_partial_tc<<<dim3((out + 127) / 128, chunks), 128, 0, s>>>(
-          (const __nv_bfloat16*)zb[cur], (int)d.n_pad, out, chunk, (double*)partb);
-      NEB_LAUNCH_CHECK();
+      {
+        KernelScope ks("bias_grad", s, 0, (double)d.n_pad * out * 4);
+        bias_partial_tc<<<dim3((out + 127) / 128, chunks), 128, 0, s>>>(
+            (const __nv_bfloat16*)zb[cur], (int)d.n_pad, out, chunk, (double*)partb);
+        NEB_LAUNCH_CHECK();
+      }
       if ((st = reduce((double*)partb, chunks, 1, out, out, out, false, gb[l - 1], nullptr, s)))
         return st;
     }
