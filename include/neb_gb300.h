@@ -131,11 +131,15 @@ int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n_points,
 int neb_hidden_gram_static(const neb_net* net, const void* qw, int64_t n_points,
                            const void* tape, double* A_M, double* A_S, neb_stream_t stream);
 
-/* FP64 K x K Grams of the fields of output rows [0, widths[L+1]) assembled
- * from the output jets without storing them: 2D u = (psi_y, -psi_x),
- * omega = -lap psi; 3D u = curl A, omega = curl curl A (VTJ2:93-98).
- * M = sum_p w u_i.u_j, S = sum_p w omega_i.omega_j (ROLL:178-179, VC:40-46).
- * accumulate != 0 adds into M and S (point chunks). */
+/* Direct route: FP64 K x K Grams of the fields of every mode, from the
+ * output jets psi = W_out h of this call's points (kept in the workspace,
+ * FP32 / FP64 networks): 2D K = widths[L+1] scalar potentials,
+ * u = (psi_y, -psi_x), omega = -lap psi; 3D K = widths[L+1] / 3 vector
+ * potentials A_k = (psi_3k, psi_3k+1, psi_3k+2), u = curl A,
+ * omega = curl curl A (VTJ2:93-98, VC:32-38).  M = sum_p w u_i.u_j,
+ * S = sum_p w omega_i.omega_j (ROLL:178-179, VC:40-46).  accumulate != 0
+ * adds into M and S, so a large point set is processed in chunks, each chunk
+ * with its own neb_forward (the recompute of VC:88-99). */
 int neb_fields_gram(const neb_net* net, const void* W_out, const void* qw,
                     int64_t n_points, const void* tape, double* M, double* S, int accumulate,
                     void* workspace, size_t workspace_bytes, neb_stream_t stream);
@@ -154,6 +158,20 @@ size_t neb_spectral_workspace_bytes(int m);
 int neb_spectral(int m, const double* M, const double* S, const double* c, double* lam,
                  double* V, double* G_M, double* G_S, double* loss, int* info,
                  void* workspace, size_t workspace_bytes, neb_stream_t stream);
+
+/* Finite pencil of a possibly singular mass matrix, FP64 (cuSOLVER syevd):
+ * M = Q diag(e) Q^T; the r = #{e_i > rank_rtol * e_max} leading directions
+ * span range(M) (the eigenvalue-ratio rank test of ROLL:180-186, which
+ * rejects where this restricts); lam[0..r) ascending eigenvalues of
+ * (S, M) on that range, rows 0..r-1 of V their M-orthonormal eigenvectors,
+ * loss = sum_{k<r} c_k lam_k, G_S = V^T diag(c) V, G_M = -V^T diag(c lam) V.
+ * Equal to neb_spectral when r = m.  Synchronises the stream once (the rank
+ * sizes the reduced problem) and writes r to *rank (host pointer). */
+size_t neb_spectral_range_workspace_bytes(int m);
+int neb_spectral_range(int m, const double* M, const double* S, const double* c,
+                       double rank_rtol, double* lam, double* V, double* G_M, double* G_S,
+                       double* loss, int* rank, int* info, void* workspace,
+                       size_t workspace_bytes, neb_stream_t stream);
 
 /* Same contract as neb_spectral for m a multiple of 64 up to 512, computed
  * with the precision where the conditioning lives: FP64 Cholesky of M and
@@ -202,8 +220,10 @@ int neb_backward_output(const neb_net* net, const void* const* W, int start, int
                         size_t workspace_bytes, neb_stream_t stream);
 
 /* Reverse pass from the K x K Gram adjoints G_M, G_S of neb_fields_gram:
- * field adjoints 2 w u G_M, 2 w omega G_S, their transpose onto the output
- * jets, and then every layer.  gW, gb: n_hidden + 1 device pointers. */
+ * recomputes this call's output jets and fields from the tape, field
+ * adjoints 2 w u G_M, 2 w omega G_S (VTJ2:114-116, VC:94-95), their
+ * transpose onto the output jets (VTJ2:102-106), then every layer.  gW, gb:
+ * n_hidden + 1 device pointers; accumulate != 0 adds (point chunks). */
 int neb_backward_fields(const neb_net* net, const void* const* W, const double* G_M,
                         const double* G_S, const void* qw, int64_t n_points,
                         const void* tape, void* const* gW, void* const* gb, int accumulate,

@@ -64,6 +64,10 @@ _SIGNATURES = {
     "neb_spectral_workspace_bytes": (c_size_t, [c_int]),
     "neb_spectral": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "neb_spectral_range_workspace_bytes": (c_size_t, [c_int]),
+    "neb_spectral_range": (c_int, [c_int, c_void_p, c_void_p, c_void_p, ctypes.c_double, c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, POINTER(c_int),
+                                   c_void_p, c_void_p, c_size_t, c_void_p]),
     "neb_spectral_mixed_workspace_bytes": (c_size_t, [c_int]),
     "neb_spectral_mixed": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,

@@ -9,6 +9,7 @@
 #include "simt_kernels.cuh"
 #include "elementwise.cuh"
 #include "tc_path.cuh"
+#include "fields.cuh"
 
 namespace neb {
 
@@ -133,8 +134,15 @@ int max_width(const neb_net* net) {
 
 // Workspace: [Zbar ping][Zbar pong][partials][bias partials][G casts][tc scratch]
 struct WsLayout {
-  size_t zb0, zb1, part, partb, gcast, tc, total;
+  size_t zb0, zb1, part, partb, gcast, fld, psib, tc, total;
 };
+
+// Modes of the output layer: K = widths[L+1] scalar potentials in 2D,
+// widths[L+1] / 3 vector potentials in 3D.
+int n_modes(const neb_net* net) {
+  const int Ko = net->widths[net->n_hidden + 1];
+  return net->dim == 2 ? Ko : Ko / 3;
+}
 
 WsLayout ws_layout(const neb_net* net, int64_t n) {
   WsLayout w{};
@@ -150,14 +158,18 @@ WsLayout ws_layout(const neb_net* net, int64_t n) {
   size_t part = a256((size_t)chunks * mw * mw * sizeof(double));
   size_t partb = a256((size_t)chunks * mw * sizeof(double));
   size_t gcast = a256((size_t)2 * mw * mw * es);
-  size_t tc = net->precision == NEB_PREC_BF16X3 ? a256(tc_workspace_bytes(net, n)) : 0;
+  // direct route: fields F [n][C][K] and output-jet adjoints [n][C][Ko]
+  size_t fld = a256((size_t)n * C * n_modes(net) * es);
+  size_t psib = a256((size_t)n * C * net->widths[net->n_hidden + 1] * es);
   w.zb0 = 0;
   w.zb1 = zb;
   w.part = 2 * zb;
   w.partb = w.part + part;
   w.gcast = w.partb + partb;
-  w.tc = w.gcast + gcast;
-  w.total = w.tc + tc;
+  w.fld = w.gcast + gcast;
+  w.psib = w.fld + fld;
+  w.tc = w.psib + psib;
+  w.total = w.tc;
   return w;
 }
 
@@ -182,7 +194,7 @@ int launch_bwd(const T* A, const T* B0, const T* B1, const T* rowscale, T scale,
   using Tl = simt::Tile<C>;
   dim3 grid((unsigned)ceil_div(N, simt::kBN), (unsigned)ceil_div(n * C, Tl::BM));
   KernelScope ks(MAP ? "simt_gram_adjoint_bwd" : "simt_jet_layer_bwd_data", s,
-                 2.0 * n * (MAP ? 3 : C) * K * N,
+                 2.0 * n * (MAP == 0 ? C : (MAP == 1 ? 3 : 6)) * K * N,
                  (double)n * C * (K + (Zprev ? 2 : 1) * N) * sizeof(T));
   if (Zprev)
     simt::jet_gemm_bwd<T, C, MAP, true>
@@ -373,6 +385,89 @@ int hidden_gram_simt(const neb_net* net, const void* qw, int64_t n, const void* 
   if (st) return st;
   return launch_rowsum<T, C, double>(HL, H, HL, H, (const T*)qw, lap, n, H, H, true, 1.0, part, AS,
                                      s);
+}
+
+// ------------------------------------------------------ direct route
+// Output jets Psi = W_out h (no bias: the fields use derivative channels
+// only) into psi, then the fields F of every mode.
+template <typename T, int C>
+int fields_forward_simt(const neb_net* net, const void* Wout, int64_t n, const void* tape,
+                        T* psi, T* F, cudaStream_t s) {
+  const int L = net->n_hidden, H = net->widths[L], Ko = net->widths[L + 1];
+  const int K = n_modes(net);
+  TapeLayout tl = tape_layout(net, n);
+  const T* HL = (const T*)((const char*)tape + tl.x_off[L]);
+  int st = launch_fwd<T, C>(HL, (const T*)Wout, nullptr, psi, nullptr, n, H, Ko, Ko, s);
+  if (st) return st;
+  const int64_t total = n * K;
+  KernelScope ks("fields_extract", s, 0, (double)n * C * (Ko + K) * sizeof(T));
+  fields_extract<T, C><<<(unsigned)ceil_div(total, 256), 256, 0, s>>>(psi, F, n, K, Ko);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+// M (+)= sum_p w_p u_i . u_j, S (+)= sum_p w_p omega_i . omega_j over the
+// modes i, j (K x K, FP64).
+template <typename T, int C>
+int fields_gram_simt(const neb_net* net, const void* Wout, const void* qw, int64_t n,
+                     const void* tape, double* M, double* S, int accumulate, void* ws,
+                     cudaStream_t s) {
+  WsLayout wl = ws_layout(net, n);
+  char* w = (char*)ws;
+  T* psi = (T*)(w + wl.zb0);
+  T* F = (T*)(w + wl.fld);
+  double* part = (double*)(w + wl.part);
+  const int K = n_modes(net);
+  int st = fields_forward_simt<T, C>(net, Wout, n, tape, psi, F, s);
+  if (st) return st;
+  simt::ChanSet vel = C == 4 ? simt::ChanSet{2, {1, 2}} : simt::ChanSet{3, {1, 2, 3}};
+  simt::ChanSet vor = C == 4 ? simt::ChanSet{1, {3}} : simt::ChanSet{3, {4, 5, 6}};
+  st = launch_rowsum<T, C, double>(F, K, F, K, (const T*)qw, vel, n, K, K, true, 1.0, part, M, s,
+                                   accumulate);
+  if (st) return st;
+  return launch_rowsum<T, C, double>(F, K, F, K, (const T*)qw, vor, n, K, K, true, 1.0, part, S,
+                                     s, accumulate);
+}
+
+// Reverse of fields_gram + objective adjoints G_M, G_S: field adjoints
+// Fbar = 2 w F G (velocity rows with G_M, vorticity rows with G_S), their
+// transpose to output-jet adjoints, then the output and hidden layers.
+template <typename T, int C>
+int backward_fields_simt(const neb_net* net, const void* const* W, const double* GM,
+                         const double* GS, const void* qw, int64_t n, const void* tape,
+                         void* const* gW, void* const* gb, int accumulate, void* ws,
+                         cudaStream_t s) {
+  const int L = net->n_hidden, Ko = net->widths[L + 1];
+  const int K = n_modes(net);
+  WsLayout wl = ws_layout(net, n);
+  char* w = (char*)ws;
+  T* psi = (T*)(w + wl.zb0);
+  T* Fb = (T*)(w + wl.zb1);
+  T* F = (T*)(w + wl.fld);
+  T* Pb = (T*)(w + wl.psib);
+  T* gM = (T*)(w + wl.gcast);
+  T* gS = gM + (size_t)K * K;
+  int st = fields_forward_simt<T, C>(net, W[L], n, tape, psi, F, s);
+  if (st) return st;
+  const int64_t kk = (int64_t)K * K;
+  const int blocks = (int)std::min<int64_t>(ceil_div(kk, 256), 4096);
+  {
+    KernelScope ks("convert", s, 0, (double)kk * 2 * (8 + sizeof(T)), 2);
+    convert_kernel<double, T><<<blocks, 256, 0, s>>>(GM, gM, kk);
+    NEB_LAUNCH_CHECK();
+    convert_kernel<double, T><<<blocks, 256, 0, s>>>(GS, gS, kk);
+    NEB_LAUNCH_CHECK();
+  }
+  constexpr int MAP = C == 4 ? 1 : 2;
+  st = launch_bwd<T, C, MAP>(F, gM, gS, (const T*)qw, T(2), nullptr, Fb, n, K, K, s);
+  if (st) return st;
+  {
+    const int64_t total = n * K;
+    KernelScope ks("fields_adjoint", s, 0, (double)n * C * (Ko + K) * sizeof(T));
+    fields_adjoint<T, C><<<(unsigned)ceil_div(total, 256), 256, 0, s>>>(Fb, Pb, n, K, Ko);
+    NEB_LAUNCH_CHECK();
+  }
+  return backward_output_simt<T, C>(net, W, 0, Ko, Pb, n, tape, gW, gb, ws, s, accumulate);
 }
 
 }  // namespace
@@ -629,16 +724,37 @@ extern "C" int neb_backward_output(const neb_net* net, const void* const* W, int
 extern "C" int neb_fields_gram(const neb_net* net, const void* Wout, const void* qw, int64_t n,
                                const void* tape, double* M, double* S, int accumulate, void* ws,
                                size_t ws_bytes, neb_stream_t stream) {
-  set_error("neb_fields_gram: direct-route Grams are not built yet");
-  return NEB_ERR_UNSUPPORTED;
+  int st = check_net(net);
+  if (st) return st;
+  NEB_REQUIRE(n > 0 && Wout && qw && tape && M && S, "neb_fields_gram: bad arguments");
+  NEB_REQUIRE(net->precision != NEB_PREC_BF16X3,
+              "neb_fields_gram: the direct route runs in NEB_PREC_FP32 or NEB_PREC_FP64");
+  if (ws_bytes < ws_layout(net, n).total || !ws) {
+    set_error("neb_fields_gram: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  return NEB_DISPATCH(net, fields_gram_simt, net, Wout, qw, n, tape, M, S, accumulate, ws,
+                      (cudaStream_t)stream);
 }
 
 extern "C" int neb_backward_fields(const neb_net* net, const void* const* W, const double* GM,
                                    const double* GS, const void* qw, int64_t n, const void* tape,
                                    void* const* gW, void* const* gb, int accumulate, void* ws,
                                    size_t ws_bytes, neb_stream_t stream) {
-  set_error("neb_backward_fields: direct-route reverse pass is not built yet");
-  return NEB_ERR_UNSUPPORTED;
+  int st = check_net(net);
+  if (st) return st;
+  NEB_REQUIRE(n > 0 && W && GM && GS && qw && tape && gW && gb,
+              "neb_backward_fields: bad arguments");
+  for (int l = 0; l <= net->n_hidden; ++l)
+    NEB_REQUIRE(W[l] && gW[l] && gb[l], "neb_backward_fields: null pointer at layer %d", l);
+  NEB_REQUIRE(net->precision != NEB_PREC_BF16X3,
+              "neb_backward_fields: the direct route runs in NEB_PREC_FP32 or NEB_PREC_FP64");
+  if (ws_bytes < ws_layout(net, n).total || !ws) {
+    set_error("neb_backward_fields: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  return NEB_DISPATCH(net, backward_fields_simt, net, W, GM, GS, qw, n, tape, gW, gb, accumulate,
+                      ws, (cudaStream_t)stream);
 }
 
 extern "C" int neb_check_status(const neb_net* net, int64_t n, void* ws, size_t ws_bytes,

@@ -173,13 +173,15 @@ jet_gemm_fwd(const T* __restrict__ X, const T* __restrict__ W, const T* __restri
 // Out[r][n] = s_p * sum_k A[r][k] B_{map(c)}[k][n], then (if Zprev) the
 // tanh-jet transpose with the pre-activation Zprev.  A: [n*C][K];
 // B0, B1: [K][N] row-major; map (compile time): MAP == 0 -> every channel uses
-// B0; MAP == 1 -> 2D hidden-Gram adjoint: value channel zero, gradient
-// channels B0 (G_M), Laplacian B1 (G_S).  rowscale: per-point s_p (nullable)
-// times scale.
+// B0; MAP == 1 -> 2D Gram adjoint: value channel zero, gradient channels B0
+// (G_M), Laplacian B1 (G_S); MAP == 2 -> 3D field adjoint on the field layout
+// of fields.cuh: channels 1-3 (velocity) B0 (G_M), 4-6 (vorticity) B1 (G_S),
+// the rest zero.  rowscale: per-point s_p (nullable) times scale.
 // ---------------------------------------------------------------------------
 template <int MAP, int C> __device__ __forceinline__ int chan_b(int c) {
   if constexpr (MAP == 0) return 0;
-  else return c == 0 ? -1 : (c == 3 ? 1 : 0);
+  else if constexpr (MAP == 1) return c == 0 ? -1 : (c == 3 ? 1 : 0);
+  else return (c >= 1 && c <= 3) ? 0 : ((c >= 4 && c <= 6) ? 1 : -1);
 }
 
 template <typename T, int C, int MAP, bool ACT>

@@ -6,6 +6,8 @@
 // coincide; eigenvectors are returned with row k holding eigenvector k.
 #include <cublas_v2.h>
 #include <cusolverDn.h>
+#include <cmath>
+#include <vector>
 #include "elementwise.cuh"
 
 namespace neb {
@@ -198,6 +200,195 @@ extern "C" int neb_pencil_pullback(int K, int H, const double* W, const double* 
     // gW = 2 (G_M W A_M + G_S W A_S) = 2 (T1 A_M + T2 A_S)
     if ((st = gemm_rm(blas, false, false, K, H, H, 2.0, T1, H, A_M, H, 0.0, gW, H))) return st;
     if ((st = gemm_rm(blas, false, false, K, H, H, 2.0, T2, H, A_S, H, 1.0, gW, H))) return st;
+  }
+  return NEB_OK;
+}
+
+// --------------------------------------------------- finite (range) pencil
+// Rank-revealing FP64 route for pencils whose mass matrix may be singular:
+// M = Q diag(e) Q^T (ascending e); the r eigenvalues above rank_rtol * e_max
+// span range(M) (the eigenvalue-ratio rank test of paper_rollout.py:180-186);
+// the finite pencil is C = Q_r^T S Q_r with Q_r = Q[:, m-r:] diag(e^-1/2),
+// C = Y diag(lam) Y^T, V = Q_r Y (M-orthonormal), the objective and its
+// adjoints over those r pairs.  When r = m this equals the sygvd route.
+namespace neb {
+namespace {
+__global__ void range_basis(const double* __restrict__ Q, const double* __restrict__ e, int m,
+                            int r, double* __restrict__ Qr) {
+  int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)m * r) return;
+  int j = (int)(idx / m);
+  int col = m - r + j;
+  Qr[idx] = Q[(int64_t)col * m + idx % m] / sqrt(e[col]);
+}
+
+// out[i + j rows] = V[i + j rows] * c_j (* lam_j)
+__global__ void scale_cols(const double* __restrict__ V, int rows, int cols,
+                           const double* __restrict__ c, const double* __restrict__ lam,
+                           double* __restrict__ out) {
+  int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)rows * cols) return;
+  int j = (int)(idx / rows);
+  out[idx] = V[idx] * c[j] * (lam ? lam[j] : 1.0);
+}
+
+int syevd_lwork(cusolverDnHandle_t s, int n, int* lwork) {
+  if (cusolverDnDsyevd_bufferSize(s, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, nullptr,
+                                  n, nullptr, lwork) != CUSOLVER_STATUS_SUCCESS) {
+    set_error("cusolverDnDsyevd_bufferSize failed");
+    return NEB_ERR_CUDA;
+  }
+  return NEB_OK;
+}
+}  // namespace
+}  // namespace neb
+
+extern "C" size_t neb_spectral_range_workspace_bytes(int m) {
+  if (m <= 0) return 0;
+  cusolverDnHandle_t s;
+  if (handles(nullptr, &s, nullptr) != NEB_OK) return 0;
+  int lwork = 0;
+  if (syevd_lwork(s, m, &lwork) != NEB_OK) return 0;
+  size_t mm = align256((size_t)m * m * sizeof(double));
+  return 4 * mm + align256((size_t)m * sizeof(double)) + 256 +
+         align256((size_t)lwork * sizeof(double));
+}
+
+extern "C" int neb_spectral_range(int m, const double* M, const double* S, const double* c,
+                                  double rank_rtol, double* lam, double* V, double* G_M,
+                                  double* G_S, double* loss, int* rank, int* info,
+                                  void* workspace, size_t workspace_bytes,
+                                  neb_stream_t stream_) {
+  NEB_REQUIRE(m > 0 && rank_rtol >= 0.0, "neb_spectral_range: bad arguments");
+  NEB_REQUIRE(M && S && c && lam && V && G_M && G_S && loss && rank && info,
+              "neb_spectral_range: null pointer");
+  cudaStream_t stream = (cudaStream_t)stream_;
+  cusolverDnHandle_t sol;
+  cublasHandle_t blas;
+  int st = handles(stream, &sol, &blas);
+  if (st) return st;
+  if (workspace_bytes < neb_spectral_range_workspace_bytes(m) || !workspace) {
+    set_error("neb_spectral_range: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  int lwork = 0;
+  if ((st = syevd_lwork(sol, m, &lwork))) return st;
+  const size_t mm = align256((size_t)m * m * sizeof(double));
+  char* ws = (char*)workspace;
+  double* Q = (double*)ws;
+  double* Qr = (double*)(ws + mm);
+  double* T = (double*)(ws + 2 * mm);
+  double* Cm = (double*)(ws + 3 * mm);
+  double* e = (double*)(ws + 4 * mm);
+  int* dinfo = (int*)(ws + 4 * mm + align256((size_t)m * sizeof(double)));
+  double* work = (double*)(ws + 4 * mm + align256((size_t)m * sizeof(double)) + 256);
+  NEB_CUDA_CHECK(cudaMemcpyAsync(Q, M, (size_t)m * m * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 stream));
+  {
+    KernelScope ks("cusolver_dsyevd", stream, 9.0 * m * (double)m * m, 0);
+    if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, Q, m, e, work,
+                         lwork, dinfo) != CUSOLVER_STATUS_SUCCESS) {
+      set_error("cusolverDnDsyevd (mass matrix) failed");
+      return NEB_ERR_SOLVER;
+    }
+  }
+  // the rank decides the size of the finite pencil: read e (m doubles) back
+  std::vector<double> eh((size_t)m);
+  int ih = 0;
+  NEB_CUDA_CHECK(cudaMemcpyAsync(eh.data(), e, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost,
+                                 stream));
+  NEB_CUDA_CHECK(cudaMemcpyAsync(&ih, dinfo, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  NEB_CUDA_CHECK(cudaStreamSynchronize(stream));
+  if (ih != 0) {
+    set_error("neb_spectral_range: eigensolve of the mass matrix failed (info %d)", ih);
+    return NEB_ERR_SOLVER;
+  }
+  const double emax = eh[(size_t)m - 1];
+  if (!std::isfinite(emax)) {
+    set_error("neb_spectral_range: non-finite mass matrix");
+    return NEB_ERR_NONFINITE;
+  }
+  int r = 0;
+  for (int i = 0; i < m; ++i) r += eh[(size_t)i] > rank_rtol * emax ? 1 : 0;
+  *rank = r;
+  if (r == 0 || !(emax > 0.0)) {
+    set_error("neb_spectral_range: the mass matrix has no positive eigenvalue");
+    return NEB_ERR_NOT_PD;
+  }
+  int lwork_r = 0;
+  if ((st = syevd_lwork(sol, r, &lwork_r))) return st;
+  NEB_REQUIRE(lwork_r <= lwork, "neb_spectral_range: solver workspace for rank %d exceeds m", r);
+  const int threads = 256;
+  {
+    KernelScope ks("range_basis", stream, 0, 16.0 * m * r);
+    range_basis<<<(unsigned)ceil_div((int64_t)m * r, threads), threads, 0, stream>>>(Q, e, m, r,
+                                                                                      Qr);
+    NEB_LAUNCH_CHECK();
+  }
+  double one = 1.0, zero = 0.0, mone = -1.0;
+  {
+    KernelScope ks("cublas_dgemm", stream, 2.0 * m * (double)m * r + 2.0 * r * (double)r * m,
+                   8.0 * (m * (double)m + 2.0 * m * r + r * (double)r), 2);
+    // T = S Qr (m x r), C = Qr^T T (r x r)
+    if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, m, r, m, &one, S, m, Qr, m, &zero, T, m) !=
+            CUBLAS_STATUS_SUCCESS ||
+        cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, r, r, m, &one, Qr, m, T, m, &zero, Cm, r) !=
+            CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasDgemm (finite pencil) failed");
+      return NEB_ERR_CUDA;
+    }
+  }
+  {
+    KernelScope ks("cusolver_dsyevd", stream, 9.0 * r * (double)r * r, 0);
+    if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r, Cm, r, lam,
+                         work, lwork, info) != CUSOLVER_STATUS_SUCCESS) {
+      set_error("cusolverDnDsyevd (finite pencil) failed");
+      return NEB_ERR_SOLVER;
+    }
+  }
+  // V = Qr Y (m x r, column k = eigenvector k = row k of the row-major output)
+  NEB_CUDA_CHECK(cudaMemsetAsync(V, 0, (size_t)m * m * sizeof(double), stream));
+  {
+    KernelScope ks("cublas_dgemm", stream, 2.0 * m * (double)r * r, 8.0 * (2.0 * m * r + r * r));
+    if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, m, r, r, &one, Qr, m, Cm, r, &zero, V, m) !=
+        CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasDgemm (eigenvectors) failed");
+      return NEB_ERR_CUDA;
+    }
+  }
+  const unsigned blocks = (unsigned)ceil_div((int64_t)m * r, threads);
+  {
+    KernelScope ks("scale_columns", stream, 0, 16.0 * m * r);
+    scale_cols<<<blocks, threads, 0, stream>>>(V, m, r, c, nullptr, T);
+    NEB_LAUNCH_CHECK();
+  }
+  {
+    KernelScope ks("cublas_dgemm", stream, 2.0 * m * (double)m * r, 8.0 * (2.0 * m * r + m * m));
+    if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_T, m, m, r, &one, T, m, V, m, &zero, G_S, m) !=
+        CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasDgemm (G_S) failed");
+      return NEB_ERR_CUDA;
+    }
+  }
+  {
+    KernelScope ks("scale_columns", stream, 0, 16.0 * m * r);
+    scale_cols<<<blocks, threads, 0, stream>>>(V, m, r, c, lam, T);
+    NEB_LAUNCH_CHECK();
+  }
+  {
+    KernelScope ks("cublas_dgemm", stream, 2.0 * m * (double)m * r, 8.0 * (2.0 * m * r + m * m));
+    if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_T, m, m, r, &mone, T, m, V, m, &zero, G_M, m) !=
+        CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasDgemm (G_M) failed");
+      return NEB_ERR_CUDA;
+    }
+  }
+  if (r < m)
+    NEB_CUDA_CHECK(cudaMemsetAsync(lam + r, 0, (size_t)(m - r) * sizeof(double), stream));
+  {
+    KernelScope ks("weighted_sum", stream, 0, 16.0 * r);
+    weighted_sum<<<1, 256, 0, stream>>>(c, lam, r, loss, info);
+    NEB_LAUNCH_CHECK();
   }
   return NEB_OK;
 }

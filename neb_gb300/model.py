@@ -62,13 +62,17 @@ class Model:
     """Shared tanh MLP with analytic spatial jets (reference backend API)."""
 
     def __init__(self, cfg: NebConfig, K: int | None = None, seed: int = 0,
-                 precision: str = "bf16x3", device: str | torch.device = "cuda",
+                 precision: str | None = None, device: str | torch.device = "cuda",
                  spectral: str | None = None):
+        # split-BF16 tensor cores for the 2D hidden-layer route; the 3D curl
+        # fields take the direct route, which runs the FP32 kernels
+        precision = precision or ("bf16x3" if cfg.dim == 2 else "fp32")
         if precision not in N.PREC:
             raise ValueError(f"precision must be one of {tuple(N.PREC)}")
-        # spectral stage: "mixed" (FP64 Cholesky and inverse factor, FP32
-        # tridiagonalisation, FP64 tridiagonal eigensolve) or "fp64"
-        # (cuSOLVER sygvd); the FP64 form defaults to "fp64"
+        # spectral stage: "mixed" (compensated-FP32 Cholesky and reduction,
+        # FP32 tridiagonalisation and tridiagonal eigenvectors, FP64
+        # Rayleigh-quotient eigenvalues) or "fp64" (cuSOLVER sygvd); the FP64
+        # form defaults to "fp64"
         spectral = spectral or ("fp64" if precision == "fp64" else "mixed")
         if spectral not in ("mixed", "fp64"):
             raise ValueError("spectral must be 'mixed' or 'fp64'")
@@ -279,22 +283,93 @@ def _f64(shape, device):
     return torch.empty(shape, dtype=torch.float64, device=device)
 
 
+def _solve(model: Model, m: int, PM, PS, kind: str):
+    """Spectral stage on the m x m pencil (PS, PM): eigenpairs, objective
+    and its Gram adjoints, all on the device."""
+    lib = N.load()
+    dev = model.device
+    st = getattr(model, "_spectral", None) or SpectralState(model)
+    model._spectral = st
+    c = torch.as_tensor(objective_weights(kind, m), dtype=torch.float64, device=dev)
+    lam, V, GM, GS = _f64((m,), dev), _f64((m, m), dev), _f64((m, m), dev), _f64((m, m), dev)
+    loss = _f64((), dev)
+    info = torch.zeros((), dtype=torch.int32, device=dev)
+    mixed_bytes = lib.neb_spectral_mixed_workspace_bytes(m) if model.spectral == "mixed" else 0
+    name = "neb_spectral_mixed" if mixed_bytes else "neb_spectral"
+    sws = st.buf.get(name, mixed_bytes or lib.neb_spectral_workspace_bytes(m))
+    N.call(name, m, PM.data_ptr(), PS.data_ptr(), c.data_ptr(), lam.data_ptr(),
+           V.data_ptr(), GM.data_ptr(), GS.data_ptr(), loss.data_ptr(), info.data_ptr(),
+           sws.data_ptr(), sws.numel(), _stream())
+    return loss, lam, V, GM, GS, info
+
+
+RANK_RTOL = 1e-10
+
+
+def _solve_range(model: Model, m: int, PM, PS, kind: str, rank_rtol: float = RANK_RTOL):
+    """FP64 finite pencil of a possibly singular M (rank from the eigenvalue
+    ratio test); returns the r finite pairs.  Reads the rank back (one
+    stream synchronisation)."""
+    lib = N.load()
+    dev = model.device
+    st = getattr(model, "_spectral", None) or SpectralState(model)
+    model._spectral = st
+    c = torch.as_tensor(objective_weights(kind, m), dtype=torch.float64, device=dev)
+    lam, V, GM, GS = _f64((m,), dev), _f64((m, m), dev), _f64((m, m), dev), _f64((m, m), dev)
+    loss = _f64((), dev)
+    info = torch.zeros((), dtype=torch.int32, device=dev)
+    rank = ctypes.c_int(0)
+    sws = st.buf.get("range", lib.neb_spectral_range_workspace_bytes(m))
+    N.call("neb_spectral_range", m, PM.data_ptr(), PS.data_ptr(), c.data_ptr(), rank_rtol,
+           lam.data_ptr(), V.data_ptr(), GM.data_ptr(), GS.data_ptr(), loss.data_ptr(),
+           ctypes.byref(rank), info.data_ptr(), sws.data_ptr(), sws.numel(), _stream())
+    r = rank.value
+    return loss, lam[:r], V[:r], GM, GS, info, r
+
+
+def _raise_on_info(info) -> None:
+    code = int(info.item())
+    if code != 0:
+        raise FloatingPointError(
+            f"spectral stage failed (info={code}): the mass matrix is not positive definite "
+            "or the eigensolver did not converge; no update")
+
+
 def spectral_step(model: Model, points=None, weights=None, training: bool = True,
                   objective: str | None = None, return_grams: bool = False,
-                  features: torch.Tensor | None = None, check: bool = True) -> SpectralResult:
+                  features: torch.Tensor | None = None, check: bool = True,
+                  route: str | None = None, chunk_points: int | None = None) -> SpectralResult:
     """One objective (+ gradient) evaluation of the eigenfluid basis.
 
     points [n, dim] and weights [n] (host arrays or device tensors), or
-    ``features`` (packed jets) with ``weights``.  2D scalar potentials use
-    the hidden-layer pencil: A_M, A_S (H x H) from the last hidden layer,
-    and M = W_out A_M W_out^T, S = W_out A_S W_out^T.  When K >= H the finite
-    eigenvalues of (S, M) are those of (A_S, A_M) (the K fields span the H
-    hidden fields); otherwise the K x K pencil is solved.  ``check`` reads
-    the solver status back (one 4-byte D2H) and raises FloatingPointError.
+    ``features`` (packed jets) with ``weights``.
+
+    route "factored" (the 2D default): the hidden-layer pencil A_M, A_S
+    (H x H) from the last hidden layer, and M = W_out A_M W_out^T,
+    S = W_out A_S W_out^T.  When K >= H the finite eigenvalues of (S, M) are
+    those of (A_S, A_M) (the K fields span the H hidden fields); otherwise
+    the K x K pencil is solved.
+
+    route "direct" (the 3D default, FP32 / FP64 networks): the K x K Grams of
+    the velocity and vorticity fields of every mode, accumulated over point
+    chunks of ``chunk_points``; the reverse pass recomputes each chunk's
+    activations instead of keeping them (velocity/core.py:88-99).  The
+    pencil is solved in FP64 on range(M) (rank from the eigenvalue ratio
+    test, RANK_RTOL), so a mass matrix whose fields are nearly dependent
+    gives the r finite eigenvalues rather than noise; ``rank`` reports r.
+
+    ``check`` reads the solver status back (one 4-byte D2H) and raises
+    FloatingPointError.
     """
     cfg = model.c
+    route = route or ("factored" if cfg.dim == 2 else "direct")
+    if route == "direct":
+        return _spectral_step_direct(model, points, weights, training, objective, return_grams,
+                                     features, check, chunk_points)
+    if route != "factored":
+        raise ValueError("route must be 'factored' or 'direct'")
     if cfg.dim != 2:
-        raise NotImplementedError("spectral_step: the 3D curl path uses the direct Grams")
+        raise ValueError("the factored route is the 2D scalar-potential route")
     kind = objective or cfg.objective
     dev = model.device
     feats = model.features(points) if features is None else features
@@ -323,16 +398,7 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
         m, PM, PS = H, AM, AS
     else:
         m, PM, PS = K, M, S
-    c = torch.as_tensor(objective_weights(kind, m), dtype=torch.float64, device=dev)
-    lam, V, GM, GS = _f64((m,), dev), _f64((m, m), dev), _f64((m, m), dev), _f64((m, m), dev)
-    loss = _f64((), dev)
-    info = torch.zeros((), dtype=torch.int32, device=dev)
-    mixed_bytes = lib.neb_spectral_mixed_workspace_bytes(m) if model.spectral == "mixed" else 0
-    name = "neb_spectral_mixed" if mixed_bytes else "neb_spectral"
-    sws = st.buf.get(name, mixed_bytes or lib.neb_spectral_workspace_bytes(m))
-    N.call(name, m, PM.data_ptr(), PS.data_ptr(), c.data_ptr(), lam.data_ptr(),
-           V.data_ptr(), GM.data_ptr(), GS.data_ptr(), loss.data_ptr(), info.data_ptr(),
-           sws.data_ptr(), sws.numel(), s)
+    loss, lam, V, GM, GS, info = _solve(model, m, PM, PS, kind)
     res = SpectralResult(loss, lam, V, m, info, M=M, S=S, A_M=AM, A_S=AS)
     if training:
         L = model.n_hidden
@@ -354,12 +420,62 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
                N.ptr_array(gW[:L]), N.ptr_array(gb[:L]), ws.data_ptr(), ws.numel(), s)
         res.grads = (gW, gb)
     if check:
-        code = int(info.item())
         model.check_device_status(n)
-        if code != 0:
-            raise FloatingPointError(
-                f"spectral stage failed (info={code}): the mass matrix is not positive definite "
-                "or the eigensolver did not converge; no update")
+        _raise_on_info(info)
+    return res
+
+
+DEFAULT_CHUNK_POINTS = 1 << 17
+
+
+def _spectral_step_direct(model: Model, points, weights, training, objective, return_grams,
+                          features, check, chunk_points) -> SpectralResult:
+    cfg = model.c
+    if model.precision == "bf16x3":
+        raise NotImplementedError(
+            "the direct (field-Gram) route runs the FP32 or FP64 kernels: build the Model with "
+            "precision='fp32' or 'fp64'")
+    kind = objective or cfg.objective
+    dev = model.device
+    n = int(features.shape[0]) if features is not None else len(points)
+    qw = torch.as_tensor(weights, device=dev).to(model.dtype).contiguous()
+    if qw.shape != (n,):
+        raise ValueError("weights must be [n]")
+    chunk = int(chunk_points or DEFAULT_CHUNK_POINTS)
+    if chunk <= 0:
+        raise ValueError("chunk_points must be positive")
+    bounds = [(a, min(n, a + chunk)) for a in range(0, n, chunk)]
+    K = model.K
+    s = _stream()
+
+    def forward_chunk(a, b):
+        feats = features[a:b] if features is not None else model.features(points[a:b])
+        return model.run_forward(feats)
+
+    M, S = _f64((K, K), dev), _f64((K, K), dev)
+    tape = None
+    for i, (a, b) in enumerate(bounds):
+        tape = forward_chunk(a, b)
+        ws = model._ws(b - a)
+        N.call("neb_fields_gram", ctypes.byref(model.net), model.W[-1].data_ptr(),
+               qw[a:b].data_ptr(), b - a, tape.buffer.data_ptr(), M.data_ptr(), S.data_ptr(),
+               int(i > 0), ws.data_ptr(), ws.numel(), s)
+    loss, lam, V, GM, GS, info, r = _solve_range(model, K, M, S, kind)
+    res = SpectralResult(loss, lam, V, r, info, M=M, S=S)
+    if training:
+        gW = [torch.empty_like(w) for w in model.W]
+        gb = [torch.empty_like(b) for b in model.b]
+        for i, (a, b) in enumerate(bounds):
+            if len(bounds) > 1:  # recompute this chunk's activations
+                tape = forward_chunk(a, b)
+            ws = model._ws(b - a)
+            N.call("neb_backward_fields", ctypes.byref(model.net), N.ptr_array(model.W),
+                   GM.data_ptr(), GS.data_ptr(), qw[a:b].data_ptr(), b - a,
+                   tape.buffer.data_ptr(), N.ptr_array(gW), N.ptr_array(gb), int(i > 0),
+                   ws.data_ptr(), ws.numel(), s)
+        res.grads = (gW, gb)
+    if check:
+        _raise_on_info(info)
     return res
 
 
