@@ -54,6 +54,12 @@ def parse():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="periodic_train",
+                    choices=["periodic_train", "periodic_small", "periodic_eval", "multihole",
+                             "metaball3d"],
+                    help="periodic_train is the headline line; the others print one line "
+                         "each for the remaining configurations (timing and FP64-oracle "
+                         "errors), not the headline metric")
     return ap.parse_args()
 
 
@@ -181,11 +187,243 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------- the other configurations
+def _rel_max(a, b) -> float:
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+
+
+def _grad_rel(grads, ref_grads) -> float:
+    num = den = 0.0
+    for gs, rs in zip(grads, zip(*ref_grads)):
+        for g, r in zip(gs, rs):
+            d = g.detach().cpu().double().numpy() - r
+            num += float((d * d).sum())
+            den += float((r * r).sum())
+    return math.sqrt(num / den)
+
+
+def _params64(model):
+    return [(a.detach().cpu().double().numpy(), b.detach().cpu().double().numpy())
+            for a, b in zip(model.W, model.b)]
+
+
+def _eig_rel(lam, ref_lam) -> float:
+    lam = np.asarray(lam, dtype=np.float64)
+    ref_lam = np.asarray(ref_lam, dtype=np.float64)
+    if lam.shape != ref_lam.shape:
+        return float("nan")
+    return float(np.max(np.abs(lam - ref_lam) / np.abs(ref_lam)))
+
+
+# rank tolerances of the finite pencil reported for the configurations
+# whose mass matrix is numerically singular at init: the FP64 rule, and one
+# above the FP32 noise floor of the Grams
+RTOLS = (1e-10, 1e-6)
+
+
+def _pencil_errors(r, ref) -> dict:
+    return {"rank": int(r.rank), "oracle_rank": int(ref.rank),
+            "eig_rel_err_max": _eig_rel(r.eigenvalues.cpu().numpy(), ref.lam),
+            "gram_M_rel_err": _rel_max(r.M.cpu().numpy(), ref.M),
+            "gram_S_rel_err": _rel_max(r.S.cpu().numpy(), ref.S),
+            "grad_rel_err": _grad_rel(r.grads, ref.grads),
+            "loss_rel_err": abs(float(r.loss) - ref.loss) / abs(ref.loss)}
+
+
+def _timed(step, W, K):
+    """ms per step over K steps after W warm-up steps (CUDA events)."""
+    import torch
+    for i in range(W):
+        step(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(W, W + K):
+        step(i)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / K
+
+
+def _kernel_table(N, step, K):
+    """Per-kernel ms per step of K further steps (library timers)."""
+    import torch
+    torch.cuda.synchronize()
+    N.timing_begin()
+    for i in range(K):
+        step(i)
+    torch.cuda.synchronize()
+    kern = N.timing_end()
+    return {k: round(v[1] / K, 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][1])[:12]}
+
+
+def run_workload(args, world, rank, local):
+    """One line per configuration other than the headline: device-timed
+    steps, the plain FP32 form where the configuration asks for it, and the
+    errors of eigenvalues, Gram entries and gradients against the FP64
+    oracle (the checker) on the same seeded inputs."""
+    import torch
+    sys.path.insert(0, str(ROOT))
+    from neb_gb300 import CONFIGS, Model, spectral_step, train_step
+    from neb_gb300 import _native as N
+    from neb_gb300 import configs as CF
+    from oracle import neb_oracle as O
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    name = args.workload
+    cfg = CONFIGS[name]
+    W, K = max(args.warmup, 1), args.steps
+    line = {"workload": name, "n_gpus": 1, "steps": K, "warmup": W,
+            "data": "synthetic: seeded samples of the configuration, Glorot-normal init",
+            "widths": list(cfg.widths), "objective": cfg.objective}
+
+    def dev_inputs(pts, w):
+        return torch.tensor(pts, device=dev), torch.tensor(w, device=dev)
+
+    if name == "periodic_small":
+        pts, w = CF.sample(cfg)
+        dp, dw = dev_inputs(pts, w)
+        model = Model(cfg, precision="fp64", seed=0, device=dev)
+        ms = _timed(lambda i: train_step(model, dp, dw, check=False), W, K)
+        kern = _kernel_table(N, lambda i: train_step(model, dp, dw, check=False), 2)
+        m0 = Model(cfg, precision="fp64", seed=0, device=dev)
+        r = spectral_step(m0, dp, dw, training=True, return_grams=True)
+        X0 = O.features_periodic(pts, cfg.n_freq, cfg.period)
+        t0 = time.perf_counter()
+        ref = O.objective_and_grad(_params64(m0), X0, w, 2, cfg.objective)
+        O.adam_step(_params64(m0), O.zero_moments(_params64(m0)), ref.grads, 0, cfg.lr, cfg.clip)
+        t_cpu = time.perf_counter() - t0
+        line.update({
+            "metric": "objective+grad steps/s, FP64, K=64, 64^2 grid (trace objective)",
+            "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "f64",
+            "kernels_ms_per_step": kern,
+            "accuracy": {"eig_rel_err_max": _eig_rel(r.eigenvalues.cpu().numpy(), ref.lam),
+                         "gram_M_rel_err": _rel_max(r.M.cpu().numpy(), ref.M),
+                         "gram_S_rel_err": _rel_max(r.S.cpu().numpy(), ref.S),
+                         "grad_rel_err": _grad_rel(r.grads, ref.grads),
+                         "loss_rel_err": abs(float(r.loss) - ref.loss) / abs(ref.loss)},
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": cpu_threads(),
+                             "kind": "port", "sample": "1 full step of the FP64 NumPy "
+                             "restatement (direct K x K route) + Adam"}})
+    elif name == "periodic_eval":
+        pts, w = CF.sample(cfg)
+        dp, dw = dev_inputs(pts, w)
+        n = len(w)
+        X0 = O.features_periodic(pts, cfg.n_freq, cfg.period)
+        arms, acc = {}, {}
+        for prec in ("bf16x3", "fp32"):
+            model = Model(cfg, precision=prec, seed=0, device=dev)
+            step = (lambda i, m=model: spectral_step(m, dp, dw, training=False,
+                                                     return_grams=True, check=False))
+            ms = _timed(step, W, K)
+            arms[prec] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms,
+                          "point_mode_evals_per_s": n * cfg.K / (ms / 1e3),
+                          "kernels_ms_per_step": _kernel_table(N, step, 2)}
+        for seed in (0, 1, 2):
+            ref = None
+            for prec in ("bf16x3", "fp32"):
+                model = Model(cfg, precision=prec, seed=seed, device=dev)
+                r = spectral_step(model, dp, dw, training=False, return_grams=True)
+                if ref is None:
+                    ref = O.objective_and_grad_factored(_params64(model), X0, w, cfg.objective,
+                                                        want_grad=False)
+                acc[f"{prec}_seed{seed}"] = {
+                    "eig_rel_err_max": _eig_rel(r.eigenvalues.cpu().numpy(), ref.lam),
+                    "gram_M_rel_err": _rel_max(r.M.cpu().numpy(), ref.M),
+                    "gram_S_rel_err": _rel_max(r.S.cpu().numpy(), ref.S),
+                    "n_eigenvalues": int(r.rank)}
+        ms = arms["bf16x3"]["ms_per_step"]
+        line.update({
+            "metric": "forward + Gram + eigensolve steps/s, K=1024, 256^2 grid",
+            "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "bf16x3",
+            "point_mode_evals_per_s": n * cfg.K / (ms / 1e3),
+            "fp32_plain": arms["fp32"], "split_bf16": arms["bf16x3"],
+            "speedup_vs_fp32_plain": arms["fp32"]["ms_per_step"] / ms, "accuracy": acc})
+    elif name == "multihole":
+        pts, w = CF.sample(cfg)
+        dp, dw = dev_inputs(pts, w)
+        X0 = O.features_multihole(pts, np.asarray(cfg.centres))
+        arms, acc, ref = {}, {}, None
+        for prec in ("bf16x3", "fp32"):
+            model = Model(cfg, precision=prec, seed=0, device=dev)
+            step = (lambda i, m=model: train_step(m, dp, dw, check=False))
+            ms = _timed(step, W, K)
+            arms[prec] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms,
+                          "kernels_ms_per_step": _kernel_table(N, step, 2)}
+            if ref is None:
+                m0 = Model(cfg, precision=prec, seed=0, device=dev)
+                t0 = time.perf_counter()
+                ref = {rt: O.objective_and_grad_factored(_params64(m0), X0, w, cfg.objective,
+                                                         rank_rtol=rt) for rt in RTOLS}
+                t_cpu = (time.perf_counter() - t0) / len(RTOLS)
+            for rt in RTOLS:
+                m0 = Model(cfg, precision=prec, seed=0, device=dev)
+                m0.rank_rtol = rt
+                r = spectral_step(m0, dp, dw, training=True, return_grams=True)
+                acc[f"{prec}_rank_rtol_{rt:g}"] = _pencil_errors(r, ref[rt])
+        ms = arms["bf16x3"]["ms_per_step"]
+        line.update({
+            "metric": "objective+grad steps/s, K=1024, multiply connected domain, 200k points",
+            "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "bf16x3",
+            "fp32_plain": arms["fp32"], "split_bf16": arms["bf16x3"],
+            "speedup_vs_fp32_plain": arms["fp32"]["ms_per_step"] / ms, "accuracy": acc,
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": cpu_threads(),
+                             "kind": "port", "sample": "1 full step (200,000 points) of the "
+                             "FP64 NumPy restatement, factored route, without Adam"}})
+    elif name == "metaball3d":
+        pts, w = CF.sample(cfg)
+        dp, dw = dev_inputs(pts, w)
+        n = len(w)
+        model = Model(cfg, precision="fp32", seed=0, device=dev)
+
+        def step(i):
+            r = spectral_step(model, dp, dw, training=True, check=False)
+            model.adam_async(*r.grads, lr=cfg.lr, clip=cfg.clip)
+            return r
+
+        ms = _timed(step, W, K)
+        kern = _kernel_table(N, step, 1)
+        r_full = spectral_step(Model(cfg, precision="fp32", seed=0, device=dev), dp, dw,
+                               training=False)
+        # errors on a seeded subsample that the FP64 oracle finishes in about a minute
+        sub = np.random.default_rng(7).choice(n, size=min(n, 8192), replace=False)
+        ps, ws_ = pts[sub], w[sub] * (n / len(sub))
+        X0 = O.features_raw3d(ps)
+        acc = {}
+        m0 = Model(cfg, precision="fp64", seed=0, device=dev)
+        ref = {rt: O.objective_and_grad(_params64(m0), X0, ws_, 3, cfg.objective, rank_rtol=rt)
+               for rt in RTOLS}
+        for prec in ("fp32", "fp64"):
+            for rt in RTOLS:
+                m0 = Model(cfg, precision=prec, seed=0, device=dev)
+                m0.rank_rtol = rt
+                r = spectral_step(m0, torch.tensor(ps, device=dev),
+                                  torch.tensor(ws_, device=dev), training=True)
+                acc[f"{prec}_rank_rtol_{rt:g}"] = _pencil_errors(r, ref[rt])
+        line.update({
+            "metric": "objective+grad steps/s, 3D curl basis K=512, 1,599,754 points",
+            "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "f32",
+            "points": n, "chunk_points": 1 << 17, "rank_at_init": int(r_full.rank),
+            "kernels_ms_per_step": kern, "accuracy_subsample_8192": acc,
+            "note": "FP32 SIMT kernels with point-chunked recompute; at Glorot init the "
+                    "curl fields are nearly dependent, so M is numerically singular and the "
+                    "pencil is solved on range(M) in FP64"})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload != "periodic_train":
+        run_workload(args, world, rank, local)
         return
     import torch
     import torch.distributed as dist

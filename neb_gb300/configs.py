@@ -47,6 +47,10 @@ class NebConfig:
     lr: float = 1e-3
     steps: int = 0
     clip: float = 8.0
+    # spectral stage: "mixed" for pencils that stay well conditioned (the
+    # periodic Fourier-feature bases), "range" (FP64, rank-revealing) where
+    # raw-coordinate inputs make the fields nearly dependent at init
+    spectral: str = "mixed"
 
     @property
     def K(self) -> int:
@@ -84,9 +88,10 @@ CONFIGS = {
                                 "ordering", n_freq=16, sampler="uniform", n_points=128 * 128,
                                 steps=25, lr=1e-3),
     "multihole": NebConfig("multihole", 2, "multihole", (5, 256, 256, 256, 256, 1024), "ordering",
-                           centres=MULTIHOLE_CENTRES, sampler="multihole", n_points=200_000),
+                           centres=MULTIHOLE_CENTRES, sampler="multihole", n_points=200_000,
+                           spectral="range"),
     "metaball3d": NebConfig("metaball3d", 3, "raw3d", (3, 512, 512, 512, 512, 1536), "ordering",
-                            sampler="metaball", n_points=1_599_754),
+                            sampler="metaball", n_points=1_599_754, spectral="range"),
 }
 
 

@@ -73,10 +73,16 @@ class Model:
         # FP32 tridiagonalisation and tridiagonal eigenvectors, FP64
         # Rayleigh-quotient eigenvalues) or "fp64" (cuSOLVER sygvd); the FP64
         # form defaults to "fp64"
-        spectral = spectral or ("fp64" if precision == "fp64" else "mixed")
-        if spectral not in ("mixed", "fp64"):
-            raise ValueError("spectral must be 'mixed' or 'fp64'")
+        # "range" (cuSOLVER syevd on M, FP64 finite pencil on range(M)) for
+        # configurations whose mass matrix may be numerically singular
+        if spectral is None:
+            spectral = cfg.spectral if cfg.spectral == "range" else \
+                ("fp64" if precision == "fp64" else "mixed")
+        if spectral not in ("mixed", "fp64", "range"):
+            raise ValueError("spectral must be 'mixed', 'fp64' or 'range'")
         self.spectral = spectral
+        # range solves keep the eigen-directions of M above rank_rtol * max
+        self.rank_rtol = RANK_RTOL
         if K is not None:
             cfg = cfg.scaled(outputs=K * (3 if cfg.dim == 3 else 1))
         self.c = cfg
@@ -262,7 +268,7 @@ class SpectralResult:
     loss: torch.Tensor            # device scalar (FP64)
     eigenvalues: torch.Tensor     # [m] FP64, ascending
     eigenvectors: torch.Tensor    # [m][m] FP64, row k = eigenvector k (pencil coordinates)
-    rank: int                     # m: dimension of the span of the K fields
+    rank: int                     # number of finite eigenpairs (dimension of range(M))
     info: torch.Tensor            # device int: solver status
     grads: tuple | None = None    # (gW list, gb list) when training
     M: torch.Tensor | None = None
@@ -398,8 +404,12 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
         m, PM, PS = H, AM, AS
     else:
         m, PM, PS = K, M, S
-    loss, lam, V, GM, GS, info = _solve(model, m, PM, PS, kind)
-    res = SpectralResult(loss, lam, V, m, info, M=M, S=S, A_M=AM, A_S=AS)
+    if model.spectral == "range":
+        loss, lam, V, GM, GS, info, r = _solve_range(model, m, PM, PS, kind, model.rank_rtol)
+    else:
+        loss, lam, V, GM, GS, info = _solve(model, m, PM, PS, kind)
+        r = m
+    res = SpectralResult(loss, lam, V, r, info, M=M, S=S, A_M=AM, A_S=AS)
     if training:
         L = model.n_hidden
         gW = [torch.empty_like(w) for w in model.W]
@@ -460,7 +470,7 @@ def _spectral_step_direct(model: Model, points, weights, training, objective, re
         N.call("neb_fields_gram", ctypes.byref(model.net), model.W[-1].data_ptr(),
                qw[a:b].data_ptr(), b - a, tape.buffer.data_ptr(), M.data_ptr(), S.data_ptr(),
                int(i > 0), ws.data_ptr(), ws.numel(), s)
-    loss, lam, V, GM, GS, info, r = _solve_range(model, K, M, S, kind)
+    loss, lam, V, GM, GS, info, r = _solve_range(model, K, M, S, kind, model.rank_rtol)
     res = SpectralResult(loss, lam, V, r, info, M=M, S=S)
     if training:
         gW = [torch.empty_like(w) for w in model.W]

@@ -399,7 +399,8 @@ def hidden_grams_2d(H, w):
     return 0.5 * (AM + AM.T), 0.5 * (AS + AS.T)
 
 
-def objective_and_grad_factored(params, X0, w, kind, act="tanh", want_grad=True):
+def objective_and_grad_factored(params, X0, w, kind, act="tanh", want_grad=True,
+                                rank_rtol=1e-10):
     """Factored route for the 2D scalar potential: Grams in the span of the
     last hidden layer.  When K >= H the finite eigenvalues of (S, M) are those
     of (A_S, A_M) (W_out of full column rank) and dL/dW_out = 0; otherwise the
@@ -412,7 +413,7 @@ def objective_and_grad_factored(params, X0, w, kind, act="tanh", want_grad=True)
     K, Hn = W_out.shape
     AM, AS = hidden_grams_2d(H, w)
     if K >= Hn:
-        obj = spectral_objective(AM, AS, kind)
+        obj = spectral_objective(AM, AS, kind, rank_rtol)
         GMh, GSh = obj["GM"], obj["GS"]
         M = W_out @ AM @ W_out.T
         S = W_out @ AS @ W_out.T
@@ -420,7 +421,7 @@ def objective_and_grad_factored(params, X0, w, kind, act="tanh", want_grad=True)
     else:
         M = W_out @ AM @ W_out.T
         S = W_out @ AS @ W_out.T
-        obj = spectral_objective(M, S, kind)
+        obj = spectral_objective(M, S, kind, rank_rtol)
         GMh = W_out.T @ obj["GM"] @ W_out
         GSh = W_out.T @ obj["GS"] @ W_out
         gWout = 2.0 * (obj["GM"] @ W_out @ AM + obj["GS"] @ W_out @ AS)

@@ -153,3 +153,20 @@ def test_direct_route_rejects_split_bf16_model():
     pts, w = CF.sample(cfg)
     with pytest.raises(NotImplementedError):
         spectral_step(model, pts, w, route="direct")
+
+
+def test_factored_route_rank_deficient_multihole_fp64():
+    """Multihole basis (raw coordinates and hole angles), 128-wide hidden
+    layer, K = 256 > H: the hidden mass Gram has 97 eigenvalues above 1e-10
+    of its largest (neighbours 1.36e-10 and 9.4e-11), so the range solve keeps
+    97 finite pairs, as the oracle does; tolerance as for the 3D case."""
+    _needs_gpu()
+    cfg = CONFIGS["multihole"].scaled(hidden=128, outputs=256, n_points=4000)
+    pts, w = CF.sample(cfg)
+    model = Model(cfg, precision="fp64", seed=0)
+    assert model.spectral == "range"
+    res = spectral_step(model, pts, w, training=True)
+    ref = O.objective_and_grad_factored(_params64(model), _oracle_features(cfg, pts), w,
+                                        cfg.objective)
+    assert res.rank == ref.rank == 97
+    np.testing.assert_allclose(res.eigenvalues.cpu().numpy(), ref.lam, rtol=1e-4)
