@@ -20,8 +20,9 @@
 // Pipeline (one stream, no host synchronisation):
 //   chol_diag / chol_panel / chol_update   blocked Cholesky, 32 x 32 blocks,
 //                                          compensated FP32 (FP64-class)
-//   2 x df_trsm                            C = L^-1 S L^-T by two triangular
-//                                          solves, compensated FP32
+//   2 x df_solve                           C = L^-1 S L^-T by two blocked triangular
+//                                          solves with inverse diagonal blocks,
+//                                          compensated FP32
 //   tridiag_cluster                        FP32 Householder tridiagonalisation in
 //                                          one 8-CTA cluster, the matrix held in
 //                                          distributed shared memory, 2 cluster
@@ -29,8 +30,9 @@
 //   tri_eigvals                            eigenvalue brackets of T, warp per eigenvalue
 //   tri_eigvecs                            eigenvectors of T by twisted factorisations,
 //                                          eigenvalues refined to FP64 Rayleigh quotients
-//   householder_apply                      x_k = Q z_k (FP32), warp per vector
-//   df_trsm, SGEMMs                        V rows = (L^-T x_k)^T, G_S, G_M
+//   wy_factor / wy_apply                   x_k = Q z_k (FP32), 32 reflectors per
+//                                          block in compact WY form
+//   df_solve, SGEMMs                       V rows = (L^-T x_k)^T, G_S, G_M
 #include <cooperative_groups.h>
 #include <cublas_v2.h>
 #include "elementwise.cuh"
@@ -98,76 +100,88 @@ __device__ __forceinline__ df df_shfl_xor(df x, int o) {
 }
 
 // ------------------------------------------------------------ Cholesky
-// Blocked right-looking Cholesky of the FP64 matrix A (lower factor written
-// back in FP64), 32 x 32 blocks, compensated FP32 arithmetic.
-__global__ void __launch_bounds__(1024) chol_diag(double* __restrict__ A, int m, int p,
-                                                  double* __restrict__ Linv_pp,
-                                                  int* __restrict__ info) {
-  __shared__ df a[kCB][kCB + 1];
-  __shared__ df x[kCB][kCB + 1];
-  __shared__ df rpiv[kCB];
-  __shared__ int bad;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int r0 = p * kCB;
-  a[ty][tx] = df_from(A[(size_t)(r0 + ty) * m + r0 + tx]);
-  if (threadIdx.x == 0) bad = 0;
+// Blocked right-looking Cholesky of the FP64 matrix A, 32 x 32 tiles,
+// compensated FP32 arithmetic, one launch per panel.  chol_step(p) has one
+// CTA per trailing lower tile (i, j), p < j <= i: it forms the panel tiles
+// L_ip = A_ip L_pp^-T (and L_jp) from the inverse diagonal factor, updates
+// A_ij -= L_ip L_jp^T, writes L_ip (the CTA with j = p + 1) to the factor
+// matrix Lw, and the CTA of tile (p + 1, p + 1) goes on to factor that tile
+// and invert it for the next panel.  A keeps only trailing updates; the
+// factor lives in Lw (lower tiles), the inverse diagonal tiles in linv_pp.
+
+// Factor the SPD tile a (shared, 1024 threads: thread (i, j) = (ty, tx))
+// into L and its inverse X = L^-1 (both lower).  One barrier per column: every
+// thread forms r = 1 / sqrt(a_kk) itself, column k of L is a_ik r, and the
+// trailing entries take a_ij -= (a_ik r)(a_jk r).  The inverse is built by
+// doubling: [[X11, 0], [X21, X22]] with X21 = -X22 L21 X11, on blocks of
+// 1, 2, 4, 8, 16.  Returns (through *bad) the first failing pivot + 1.
+__device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1],
+                            df (*Tm)[kCB + 1], df* rinv, int* bad) {
+  const int j = threadIdx.x & 31, i = threadIdx.x >> 5;
+  L[i][j] = df{0.f, 0.f};
+  X[i][j] = df{0.f, 0.f};
   __syncthreads();
   for (int k = 0; k < kCB; ++k) {
-    if (threadIdx.x == 0) {
-      df v = a[k][k];
-      if (!(v.h > 0.f)) {  // not positive definite (or NaN)
-        if (!bad) bad = k + 1;
-        v = df{1.f, 0.f};
-      }
-      df sq = df_sqrt(v);
-      a[k][k] = sq;
-      rpiv[k] = df_recip(sq);
+    df akk = a[k][k];
+    if (!(akk.h > 0.f)) {  // not positive definite (or NaN)
+      if (threadIdx.x == 0 && *bad == 0) *bad = k + 1;
+      akk = df{1.f, 0.f};
     }
-    __syncthreads();
-    if (ty == 0 && tx > k) a[tx][k] = df_mul(a[tx][k], rpiv[k]);
-    __syncthreads();
-    if (ty > k && tx > k && tx <= ty) a[ty][tx] = df_add(a[ty][tx], df_neg(df_mul(a[ty][k], a[tx][k])));
+    const df r = df_recip(df_sqrt(akk));
+    const df lik = df_mul(a[i][k], r);
+    if (j == k && i >= k) L[i][k] = lik;
+    if (threadIdx.x == 0) rinv[k] = r;
+    if (j > k && i >= j) a[i][j] = df_add(a[i][j], df_neg(df_mul(lik, df_mul(a[j][k], r))));
     __syncthreads();
   }
-  if (tx <= ty) A[(size_t)(r0 + ty) * m + r0 + tx] = df_to(a[ty][tx]);
-  // inverse of the diagonal block, row by row (column j per lane of warp 0)
-  for (int i = 0; i < kCB; ++i) {
-    if (ty == 0) {
-      const int j = tx;
-      df s = (i == j) ? df{1.f, 0.f} : df{0.f, 0.f};
-      for (int k = j; k < i; ++k) s = df_add(s, df_neg(df_mul(a[i][k], x[k][j])));
-      x[i][j] = i < j ? df{0.f, 0.f} : df_mul(s, rpiv[i]);
-    }
-    __syncwarp();
-  }
+  if (i == j) X[i][i] = rinv[i];
   __syncthreads();
-  Linv_pp[ty * kCB + tx] = df_to(x[ty][tx]);
-  if (threadIdx.x == 0 && bad && *info == 0) *info = m + r0 + bad;
+  for (int s = 1; s < kCB; s <<= 1) {
+    // block pair starting at o = 2 s q: rows o+s..o+2s-1, columns o..o+s-1
+    const bool in21 = (i / (2 * s) == j / (2 * s)) && (i % (2 * s) >= s) && (j % (2 * s) < s);
+    const int o = (i / (2 * s)) * 2 * s;
+    if (in21) {  // Tm = L21 X11
+      df acc{0.f, 0.f};
+      for (int t = 0; t < s; ++t) acc = df_add(acc, df_mul(L[i][o + t], X[o + t][j]));
+      Tm[i][j] = acc;
+    }
+    __syncthreads();
+    if (in21) {  // X21 = -X22 Tm
+      df acc{0.f, 0.f};
+      for (int t = s; t < 2 * s; ++t) acc = df_add(acc, df_mul(X[i][o + t], Tm[o + t][j]));
+      X[i][j] = df_neg(acc);
+    }
+    __syncthreads();
+  }
 }
 
-// L_ip = A_ip L_pp^-T for the row blocks below the diagonal block.
-__global__ void __launch_bounds__(1024) chol_panel(double* __restrict__ A, int m, int p,
-                                                   const double* __restrict__ Linv_pp) {
-  __shared__ df a[kCB][kCB + 1];
-  __shared__ df li[kCB][kCB + 1];
+__global__ void __launch_bounds__(1024) chol_first(const double* __restrict__ A, int m,
+                                                   double* __restrict__ Lw,
+                                                   double* __restrict__ linv_pp,
+                                                   int* __restrict__ info) {
+  __shared__ df a[kCB][kCB + 1], L[kCB][kCB + 1], X[kCB][kCB + 1], Tm[kCB][kCB + 1];
+  __shared__ df rinv[kCB];
+  __shared__ int bad;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int rb = (p + 1 + blockIdx.x) * kCB, cb = p * kCB;
-  a[ty][tx] = df_from(A[(size_t)(rb + ty) * m + cb + tx]);
-  li[ty][tx] = df_from(Linv_pp[ty * kCB + tx]);
+  a[ty][tx] = df_from(A[(size_t)ty * m + tx]);
+  if (threadIdx.x == 0) bad = 0;
   __syncthreads();
-  df s0{0.f, 0.f}, s1{0.f, 0.f};
-#pragma unroll
-  for (int k = 0; k < kCB; k += 2) {
-    s0 = df_add(s0, df_mul(a[ty][k], li[tx][k]));
-    s1 = df_add(s1, df_mul(a[ty][k + 1], li[tx][k + 1]));
-  }
-  A[(size_t)(rb + ty) * m + cb + tx] = df_to(df_add(s0, s1));
+  tile_factor(a, L, X, Tm, rinv, &bad);
+  Lw[(size_t)ty * m + tx] = df_to(L[ty][tx]);
+  linv_pp[ty * kCB + tx] = df_to(X[ty][tx]);
+  if (threadIdx.x == 0 && bad && *info == 0) *info = m + bad;
 }
 
-// A_ij -= L_ip L_jp^T for the lower-triangle tiles p < j <= i.
-__global__ void __launch_bounds__(1024) chol_update(double* __restrict__ A, int m, int p) {
-  __shared__ df li[kCB][kCB + 1];
-  __shared__ df lj[kCB][kCB + 1];
+__global__ void __launch_bounds__(1024) chol_step(double* __restrict__ A, int m, int p,
+                                                  double* __restrict__ Lw,
+                                                  double* __restrict__ linv_pp,
+                                                  int* __restrict__ info) {
+  __shared__ df xi[kCB][kCB + 1];  // L_pp^-1, later L of the next diagonal tile
+  __shared__ df li[kCB][kCB + 1];  // A_ip, then L_ip
+  __shared__ df lj[kCB][kCB + 1];  // A_jp, then L_jp
+  __shared__ df tl[kCB][kCB + 1];  // the updated tile
+  __shared__ df rinv[kCB];
+  __shared__ int bad;
   int t = blockIdx.x, bi = p + 1;
   while (t >= bi - p) {  // tile index -> (bi, bj) with p < bj <= bi
     t -= bi - p;
@@ -176,17 +190,44 @@ __global__ void __launch_bounds__(1024) chol_update(double* __restrict__ A, int 
   const int bj = p + 1 + t;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int cb = p * kCB;
-  li[ty][tx] = df_from(A[(size_t)(bi * kCB + ty) * m + cb + tx]);
-  lj[ty][tx] = df_from(A[(size_t)(bj * kCB + ty) * m + cb + tx]);
+  xi[ty][tx] = df_from(linv_pp[(size_t)p * kCB * kCB + ty * kCB + tx]);
+  const df aip = df_from(A[(size_t)(bi * kCB + ty) * m + cb + tx]);
+  const df ajp = bj == bi ? aip : df_from(A[(size_t)(bj * kCB + ty) * m + cb + tx]);
+  const df aij = df_from(A[(size_t)(bi * kCB + ty) * m + bj * kCB + tx]);
+  if (threadIdx.x == 0) bad = 0;
   __syncthreads();
+  // L_ip[r][c] = sum_k A_ip[r][k] X[c][k] (X lower: k <= c)
   df s0{0.f, 0.f}, s1{0.f, 0.f};
+  li[ty][tx] = aip;
+  lj[ty][tx] = ajp;
+  __syncthreads();
+  for (int k = 0; k <= tx; ++k) s0 = df_add(s0, df_mul(li[ty][k], xi[tx][k]));
+  if (bj != bi)
+    for (int k = 0; k <= tx; ++k) s1 = df_add(s1, df_mul(lj[ty][k], xi[tx][k]));
+  __syncthreads();
+  li[ty][tx] = s0;
+  lj[ty][tx] = bj != bi ? s1 : s0;
+  if (bj == p + 1) Lw[(size_t)(bi * kCB + ty) * m + cb + tx] = df_to(s0);
+  __syncthreads();
+  df u0{0.f, 0.f}, u1{0.f, 0.f};
 #pragma unroll
   for (int k = 0; k < kCB; k += 2) {
-    s0 = df_add(s0, df_mul(li[ty][k], lj[tx][k]));
-    s1 = df_add(s1, df_mul(li[ty][k + 1], lj[tx][k + 1]));
+    u0 = df_add(u0, df_mul(li[ty][k], lj[tx][k]));
+    u1 = df_add(u1, df_mul(li[ty][k + 1], lj[tx][k + 1]));
   }
-  double* o = A + (size_t)(bi * kCB + ty) * m + bj * kCB + tx;
-  *o = df_to(df_add(df_from(*o), df_neg(df_add(s0, s1))));
+  const df upd = df_add(aij, df_neg(df_add(u0, u1)));
+  if (!(bi == p + 1 && bj == p + 1)) {
+    A[(size_t)(bi * kCB + ty) * m + bj * kCB + tx] = df_to(upd);
+    return;
+  }
+  // the next diagonal tile: factor and invert it here
+  tl[ty][tx] = upd;
+  __syncthreads();
+  tile_factor(tl, xi, li, lj, rinv, &bad);
+  const int r0 = (p + 1) * kCB;
+  Lw[(size_t)(r0 + ty) * m + r0 + tx] = df_to(xi[ty][tx]);
+  linv_pp[(size_t)(p + 1) * kCB * kCB + ty * kCB + tx] = df_to(li[ty][tx]);
+  if (threadIdx.x == 0 && bad && *info == 0) *info = m + r0 + bad;
 }
 
 // The lower factor as float pairs, and its transpose (so both solves read
@@ -206,80 +247,93 @@ __global__ void split_factor(const double* __restrict__ L, int m, df* __restrict
     LTd[(size_t)(bx + r) * m + by + threadIdx.x] = t[threadIdx.x][r];
 }
 
-// Blocked triangular solves, compensated FP32, 8 right-hand-side columns per
-// 256-thread block:
-//   upper == 0:  L Y = B   (forward;  T = L as float pairs, rows of L)
-//   upper == 1:  L^T Y = B (backward; T = L^T as float pairs, rows of L^T)
-// Per 32-row block: the contribution of every solved row is a small
-// matrix product over 32 x 32 tiles of T staged in shared memory (one output
-// per thread, two accumulation chains); then the 32 x 32 diagonal block is
-// solved by one warp per column with shuffles.  B(r, c) = b_trans ? B[c][r] :
-// B[r][c] (FP64 or FP32); Y(r, c) goes to out[r][c] or, with out_trans,
-// out[c][r] (FP64 or FP32).
-constexpr int kTrsmCols = 8;
-__global__ void __launch_bounds__(256) df_trsm(const df* __restrict__ T, int m, int upper,
-                                               const void* __restrict__ B, int b_f32, int b_trans,
-                                               void* __restrict__ out, int out_f32, int out_trans) {
-  extern __shared__ df ys[];  // [m][kTrsmCols] solved values
-  __shared__ df tile[32][33];
-  __shared__ df acc[32][kTrsmCols + 1];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int c0 = blockIdx.x * kTrsmCols;
-  const int r_t = tid >> 3, c_t = tid & 7;  // phase-1 output (row in block, column)
-  const int nb = m / 32;
+// Inverses of the 32 x 32 diagonal blocks of L as float pairs, for both
+// solves: DL[b] = L_bb^-1 (lower), DU[b] = (L_bb^-1)^T = (L^T)_bb^-1 (upper).
+__global__ void __launch_bounds__(1024) split_dinv(const double* __restrict__ linv_pp,
+                                                   df* __restrict__ DL, df* __restrict__ DU) {
+  const int b = blockIdx.x, r = threadIdx.x >> 5, c = threadIdx.x & 31;
+  const size_t base = (size_t)b * kCB * kCB;
+  const df v = df_from(linv_pp[base + r * kCB + c]);
+  DL[base + r * kCB + c] = v;
+  DU[base + c * kCB + r] = v;
+}
+
+// Blocked triangular solves, compensated FP32, kSolveCols right-hand-side
+// columns per 256-thread block (128 blocks at m = 512):
+//   upper == 0:  L Y = B   (forward;  T = L as float pairs, D = DL)
+//   upper == 1:  L^T Y = B (backward; T = L^T as float pairs, D = DU)
+// Per 32-row block b: acc = B_b - T_b,solved y_solved (thread = row x column
+// x half of the solved range, two accumulation chains each), then
+// y_b = D_b acc (a 32 x 32 product with the inverse diagonal block, no
+// sequential substitution).  B(r, c) = b_trans ? B[c][r] : B[r][c] (FP64 or
+// FP32); Y(r, c) goes to out[r][c] or, with out_trans, out[c][r].
+constexpr int kSolveCols = 4;
+__global__ void __launch_bounds__(256) df_solve(const df* __restrict__ T,
+                                                const df* __restrict__ D, int m, int upper,
+                                                const void* __restrict__ B, int b_f32,
+                                                int b_trans, void* __restrict__ out, int out_f32,
+                                                int out_trans) {
+  extern __shared__ df ys[];  // [m][kSolveCols] solved values, then the T rows
+  df* tt = ys + (size_t)m * kSolveCols;  // [32][ncols + 1] rows of T being used
+  __shared__ df part[kCB][kSolveCols];
+  __shared__ df acc[kCB][kSolveCols];
+  const int tid = threadIdx.x;
+  const int row = tid & 31, col = (tid >> 5) & (kSolveCols - 1), half = tid >> 7;
+  const int c = blockIdx.x * kSolveCols + col;
+  const int nb = m / kCB;
   for (int bb = 0; bb < nb; ++bb) {
-    const int b = upper ? nb - 1 - bb : bb;  // block of rows being solved
-    const int rb0 = b * 32;
-    // phase 1: acc = B - sum over solved blocks of T[rows][solved] y[solved]
-    const int r = rb0 + r_t, c = c0 + c_t;
-    {
-      const size_t bi = b_trans ? (size_t)c * m + r : (size_t)r * m + c;
-      const double bv = b_f32 ? (double)((const float*)B)[bi] : ((const double*)B)[bi];
-      df s0 = df_from(bv), s1{0.f, 0.f};
-      for (int kk = 0; kk < bb; ++kk) {
-        const int kb = upper ? nb - 1 - kk : kk;
-        __syncthreads();
-        for (int t = tid; t < 32 * 32; t += 256) {
-          const int tr = t >> 5, tc = t & 31;
-          tile[tr][tc] = T[(size_t)(rb0 + tr) * m + kb * 32 + tc];
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int q = 0; q < 32; q += 2) {
-          s0 = df_add(s0, df_neg(df_mul(tile[r_t][q], ys[(size_t)(kb * 32 + q) * kTrsmCols + c_t])));
-          s1 = df_add(s1, df_neg(df_mul(tile[r_t][q + 1], ys[(size_t)(kb * 32 + q + 1) * kTrsmCols + c_t])));
-        }
-      }
-      __syncthreads();
-      acc[r_t][c_t] = df_add(s0, s1);
-      for (int t = tid; t < 32 * 32; t += 256) {
-        const int tr = t >> 5, tc = t & 31;
-        tile[tr][tc] = T[(size_t)(rb0 + tr) * m + rb0 + tc];
-      }
-      __syncthreads();
-    }
-    // phase 2: solve the diagonal block, warp w -> column c0 + w, lane -> row
-    if (warp < kTrsmCols) {
-      df v = acc[lane][warp];
-      for (int step = 0; step < 32; ++step) {
-        const int q = upper ? 31 - step : step;  // row finalised at this step
-        df yq{0.f, 0.f};
-        if (lane == q) {
-          yq = df_mul(v, df_recip(tile[q][q]));
-          ys[(size_t)(rb0 + q) * kTrsmCols + warp] = yq;
-        }
-        yq.h = __shfl_sync(0xffffffffu, yq.h, q);
-        yq.l = __shfl_sync(0xffffffffu, yq.l, q);
-        const bool pending = upper ? lane < q : lane > q;
-        if (pending) v = df_add(v, df_neg(df_mul(tile[lane][q], yq)));
-      }
+    const int b = upper ? nb - 1 - bb : bb;
+    const int rb0 = b * kCB;
+    // solved rows: [0, rb0) (forward) or [rb0 + 32, m) (backward)
+    const int lo = upper ? rb0 + kCB : 0, hi = upper ? m : rb0;
+    const int ncols = hi - lo, ld = ncols + 1;  // odd pitch: two wavefronts per warp
+    for (int t = tid; t < kCB * ncols; t += 256) {
+      const int r = t / ncols, k = t - r * ncols;
+      tt[r * ld + k] = T[(size_t)(rb0 + r) * m + lo + k];
     }
     __syncthreads();
+    const int mid = ncols >> 1;
+    const int k0 = half ? mid : 0, k1 = half ? ncols : mid;
+    const df* trow = tt + row * ld;
+    const df* yb = ys + (size_t)lo * kSolveCols + col;
+    df s0{0.f, 0.f}, s1{0.f, 0.f};
+    int k = k0;
+#pragma unroll 2
+    for (; k + 1 < k1; k += 2) {
+      s0 = df_add(s0, df_mul(trow[k], yb[(size_t)k * kSolveCols]));
+      s1 = df_add(s1, df_mul(trow[k + 1], yb[(size_t)(k + 1) * kSolveCols]));
+    }
+    if (k < k1) s0 = df_add(s0, df_mul(trow[k], yb[(size_t)k * kSolveCols]));
+    const df s = df_add(s0, s1);
+    if (half) part[row][col] = s;
+    __syncthreads();
+    if (!half) {
+      const int r = rb0 + row;
+      const size_t bi = b_trans ? (size_t)c * m + r : (size_t)r * m + c;
+      const double bv = b_f32 ? (double)((const float*)B)[bi] : ((const double*)B)[bi];
+      acc[row][col] = df_add(df_from(bv), df_neg(df_add(s, part[row][col])));
+    }
+    __syncthreads();
+    // y_b = D_b acc: half 0 sums j < 16, half 1 j >= 16
+    const df* drow = D + ((size_t)b * kCB + row) * kCB;
+    df y0{0.f, 0.f}, y1{0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+      const int jj = half * 16 + j;
+      y0 = df_add(y0, df_mul(drow[jj], acc[jj][col]));
+      y1 = df_add(y1, df_mul(drow[jj + 1], acc[jj + 1][col]));
+    }
+    const df y = df_add(y0, y1);
+    if (half) part[row][col] = y;
+    __syncthreads();
+    if (!half) ys[(size_t)(rb0 + row) * kSolveCols + col] = df_add(y, part[row][col]);
+    __syncthreads();
   }
-  for (int t = tid; t < m * kTrsmCols; t += 256) {
-    const int rr = t / kTrsmCols, cc = t % kTrsmCols;
+  for (int t = tid; t < m * kSolveCols; t += 256) {
+    const int rr = t / kSolveCols, cc = t % kSolveCols;
     const df y = ys[t];
-    const size_t oi = out_trans ? (size_t)(c0 + cc) * m + rr : (size_t)rr * m + c0 + cc;
+    const int cc_g = blockIdx.x * kSolveCols + cc;
+    const size_t oi = out_trans ? (size_t)cc_g * m + rr : (size_t)rr * m + cc_g;
     if (out_f32) ((float*)out)[oi] = y.h + y.l;
     else ((double*)out)[oi] = df_to(y);
   }
@@ -528,39 +582,53 @@ __global__ void __launch_bounds__(256) tri_eigvals(const double* __restrict__ d,
 
 // Thread per eigenvector: twisted factorisation of T - lam I in FP32 (forward
 // and backward pivots, twist at the smallest |gamma|); the eigenvalue is then
-// refined to the FP64 Rayleigh quotient z^T T z / z^T z (error below
-// (eps_32 |T|)^2 / gap).  Z[i][k] (column k) FP32.  The pivots of the 32
-// threads of a block live in shared memory, [i][thread].
+// refined to the Rayleigh quotient z^T T z / z^T z, accumulated in
+// compensated FP32 (T is FP32, so every product is exact as a float pair),
+// with an error below (eps_32 |T|)^2 / gap.  Z[i][k] (column k) FP32.  T is
+// staged in shared memory as floats; the pivots of the 32 threads of a block
+// live there too, [i][thread].
+__device__ __forceinline__ df two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+
 __global__ void __launch_bounds__(32) tri_eigvecs(const double* __restrict__ d,
                                                   const double* __restrict__ e, int m,
                                                   double* __restrict__ lam, float* __restrict__ Z) {
-  extern __shared__ float piv[];  // dp [m][32], dm [m][32]
+  extern __shared__ float piv[];  // dp [m][32], dm [m][32], dd [m], ee [m]
+  float* dp = piv + threadIdx.x;                   // dp[i * 32]
+  float* dm = piv + (size_t)m * 32 + threadIdx.x;  // dm[i * 32]
+  float* dd = piv + (size_t)m * 64;
+  float* ee = dd + m;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    dd[i] = (float)d[i];
+    ee[i] = i + 1 < m ? (float)e[i] : 0.f;
+  }
+  __syncthreads();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= m) return;
-  float* dp = piv + threadIdx.x - (size_t)0;      // dp[i * 32]
-  float* dm = piv + (size_t)m * 32 + threadIdx.x;  // dm[i * 32]
   const float l = (float)lam[k];
   const float tiny = 1e-30f;
-  float q = (float)d[0] - l;
+  float q = dd[0] - l;
   if (fabsf(q) < tiny) q = tiny;
   dp[0] = q;
   for (int i = 1; i < m; ++i) {
-    const float ei = (float)e[i - 1];
-    q = ((float)d[i] - l) - __fdividef(ei * ei, q);
+    const float ei = ee[i - 1];
+    q = (dd[i] - l) - __fdividef(ei * ei, q);
     if (fabsf(q) < tiny) q = tiny;
     dp[i * 32] = q;
   }
-  q = (float)d[m - 1] - l;
+  q = dd[m - 1] - l;
   if (fabsf(q) < tiny) q = tiny;
   dm[(m - 1) * 32] = q;
-  float best = fabsf(dp[(m - 1) * 32] + q - ((float)d[m - 1] - l));
+  float best = fabsf(dp[(m - 1) * 32] + q - (dd[m - 1] - l));
   int r = m - 1;
   for (int i = m - 2; i >= 0; --i) {
-    const float ei = (float)e[i];
-    q = ((float)d[i] - l) - __fdividef(ei * ei, q);
+    const float ei = ee[i];
+    q = (dd[i] - l) - __fdividef(ei * ei, q);
     if (fabsf(q) < tiny) q = tiny;
     dm[i * 32] = q;
-    const float g = fabsf(dp[i * 32] + q - ((float)d[i] - l));
+    const float g = fabsf(dp[i * 32] + q - (dd[i] - l));
     if (g < best) {
       best = g;
       r = i;
@@ -569,88 +637,153 @@ __global__ void __launch_bounds__(32) tri_eigvecs(const double* __restrict__ d,
   float z = 1.f;
   Z[(size_t)r * m + k] = 1.f;
   for (int i = r - 1; i >= 0; --i) {
-    z = -__fdividef((float)e[i], dp[i * 32]) * z;
+    z = -__fdividef(ee[i], dp[i * 32]) * z;
     if (fabsf(z) < 1e-30f) z = 0.f;
     Z[(size_t)i * m + k] = z;
   }
   z = 1.f;
   for (int i = r + 1; i < m; ++i) {
-    z = -__fdividef((float)e[i - 1], dm[i * 32]) * z;
+    z = -__fdividef(ee[i - 1], dm[i * 32]) * z;
     if (fabsf(z) < 1e-30f) z = 0.f;
     Z[(size_t)i * m + k] = z;
   }
-  // FP64 norm and Rayleigh quotient, four independent partial sums
-  double n0 = 0, n1 = 0, q0 = 0, q1 = 0;
-  double zp = 0.0;
+  // Rayleigh quotient and norm in compensated FP32, two chains each
+  df n0{0.f, 0.f}, n1{0.f, 0.f}, q0{0.f, 0.f}, q1{0.f, 0.f};
+  float zp = 0.f;
   for (int i = 0; i < m; ++i) {
-    const double zi = (double)Z[(size_t)i * m + k];
+    const float zi = Z[(size_t)i * m + k];
+    df t = df_mul(two_prod(dd[i], zi), df{zi, 0.f});
+    if (i > 0) t = df_add(t, df_mul(two_prod(2.f * ee[i - 1], zp), df{zi, 0.f}));
     if (i & 1) {
-      n1 += zi * zi;
-      q1 += zi * (d[i] * zi + 2.0 * (i > 0 ? e[i - 1] * zp : 0.0));
+      n1 = df_add(n1, two_prod(zi, zi));
+      q1 = df_add(q1, t);
     } else {
-      n0 += zi * zi;
-      q0 += zi * (d[i] * zi + 2.0 * (i > 0 ? e[i - 1] * zp : 0.0));
+      n0 = df_add(n0, two_prod(zi, zi));
+      q0 = df_add(q0, t);
     }
     zp = zi;
   }
-  const double nrm = n0 + n1;
-  lam[k] = (q0 + q1) / nrm;
+  const double nrm = df_to(df_add(n0, n1));
+  lam[k] = df_to(df_add(q0, q1)) / nrm;
   const float sc = (float)(1.0 / sqrt(nrm));
   for (int i = 0; i < m; ++i) Z[(size_t)i * m + k] *= sc;
 }
 
-// Warp per eigenvector: x_k = H_0 ... H_{m-3} z_k, applying the reflectors
-// from the last to the first; reflector rows are staged through shared
-// memory 16 at a time for the 4 warps of a block.  X row k = x_k (FP32).
-constexpr int kHChunk = 16;
-__global__ void __launch_bounds__(128) householder_apply(const float* __restrict__ Vh,
-                                                         const float* __restrict__ tau, int m,
-                                                         const float* __restrict__ Z,
-                                                         float* __restrict__ X) {
-  extern __shared__ float vs[];  // [kHChunk][m]
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = blockIdx.x * 4 + warp;
-  const bool active = k < m;
-  float z[kMaxM / 32];
-  const int per = (m + 31) / 32;
-#pragma unroll
-  for (int t = 0; t < kMaxM / 32; ++t) {
-    int i = lane + 32 * t;
-    z[t] = (active && t < per && i < m) ? Z[(size_t)i * m + k] : 0.f;
+// Back-transformation x_k = H_0 H_1 ... H_{m-3} z_k in blocks of 32
+// reflectors (compact WY form, FP32): Q_B = H_j0 ... H_j0+31 = I - V T V^T
+// with T upper triangular (T_aa = tau_a, T[0:a, a] = -tau_a T[0:a, 0:a]
+// V^T v_a), applied from the last block to the first as
+// Z <- Z - V (T (V^T Z)).
+constexpr int kWY = 32;
+
+// T_B for every block B (one CTA per block): the Gram V_B^T V_B, then the
+// column recursion by one warp.  Vh row j = reflector j (zero up to j).
+__global__ void __launch_bounds__(1024) wy_factor(const float* __restrict__ Vh,
+                                                  const float* __restrict__ tau, int m,
+                                                  float* __restrict__ Tw) {
+  extern __shared__ float vsh[];  // [kWY][m + 1] (padded rows: no bank conflicts)
+  __shared__ float G[kWY][kWY + 1];
+  __shared__ float T[kWY][kWY + 1];
+  const int B = blockIdx.x, j0 = B * kWY, ld = m + 1;
+  const int cnt = min(kWY, m - 2 - j0);
+  for (int t = threadIdx.x; t < kWY * m; t += blockDim.x) {
+    const int a = t / m, i = t % m;
+    vsh[a * ld + i] = a < cnt ? Vh[(size_t)(j0 + a) * m + i] : 0.f;
   }
-  for (int j_hi = m - 3; j_hi >= 0; j_hi -= kHChunk) {
-    const int j_lo = max(0, j_hi - kHChunk + 1);
-    const int cnt = j_hi - j_lo + 1;
-    __syncthreads();
-    for (int q = warp; q < cnt; q += 4)
-      for (int i = lane; i < m; i += 32) vs[(size_t)q * m + i] = Vh[(size_t)(j_hi - q) * m + i];
-    __syncthreads();
-    for (int q = 0; q < cnt; ++q) {
-      const int j = j_hi - q;
-      const float tj = tau[j];
-      const float* v = vs + (size_t)q * m;
-      float s = 0.f;
-#pragma unroll
-      for (int t = 0; t < kMaxM / 32; ++t) {
-        int i = lane + 32 * t;
-        if (t < per && i > j && i < m) s += v[i] * z[t];
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      s *= tj;
-#pragma unroll
-      for (int t = 0; t < kMaxM / 32; ++t) {
-        int i = lane + 32 * t;
-        if (t < per && i > j && i < m) z[t] -= s * v[i];
-      }
+  __syncthreads();
+  {
+    const int a = threadIdx.x >> 5, b = threadIdx.x & 31;
+    float g = 0.f;
+    for (int i = j0 + 1; i < m; ++i) g = fmaf(vsh[a * ld + i], vsh[b * ld + i], g);
+    G[a][b] = g;
+    T[a][b] = 0.f;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int i = threadIdx.x;
+    for (int a = 0; a < cnt; ++a) {
+      const float ta = tau[j0 + a];
+      float t = 0.f;
+      if (i < a)
+        for (int k = i; k < a; ++k) t = fmaf(T[i][k], G[k][a], t);
+      __syncwarp();
+      if (i < a) T[i][a] = -ta * t;
+      if (i == a) T[a][a] = ta;
+      __syncwarp();
     }
   }
-  if (active)
+  __syncthreads();
+  Tw[(size_t)B * kWY * kWY + threadIdx.x] = T[threadIdx.x >> 5][threadIdx.x & 31];
+}
+
+// X row k = Q z_k for kSolveCols eigenvectors per 256-thread block.
+__global__ void __launch_bounds__(256) wy_apply(const float* __restrict__ Vh,
+                                                const float* __restrict__ Tw, int m,
+                                                const float* __restrict__ Z,
+                                                float* __restrict__ X) {
+  extern __shared__ float zc[];  // [kSolveCols][m], then the block's reflectors [kWY][m]
+  float* vb = zc + (size_t)kSolveCols * m;
+  __shared__ float W[kWY][kSolveCols];
+  __shared__ float W2[kWY][kSolveCols];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int k0 = blockIdx.x * kSolveCols;
+  for (int t = tid; t < kSolveCols * m; t += 256) {
+    const int c = t % kSolveCols, i = t / kSolveCols;
+    zc[c * m + i] = Z[(size_t)i * m + k0 + c];
+  }
+  const int nblk = (m - 2 + kWY - 1) / kWY;
+  for (int B = nblk - 1; B >= 0; --B) {
+    const int j0 = B * kWY;
+    const int cnt = min(kWY, m - 2 - j0);
+    __syncthreads();
+    for (int t = tid; t < cnt * m; t += 256) vb[t] = Vh[(size_t)j0 * m + t];
+    __syncthreads();
+    // W = V^T Z: warp w takes reflectors a = w, w + 8, ...; lanes over rows
+    for (int a = warp; a < kWY; a += 8) {
+      float acc[kSolveCols] = {};
+      if (a < cnt) {
+        const float* v = vb + (size_t)a * m;
+        for (int i = j0 + 1 + lane; i < m; i += 32) {
+          const float vi = v[i];
 #pragma unroll
-    for (int t = 0; t < kMaxM / 32; ++t) {
-      int i = lane + 32 * t;
-      if (t < per && i < m) X[(size_t)k * m + i] = z[t];
+          for (int c = 0; c < kSolveCols; ++c) acc[c] = fmaf(vi, zc[c * m + i], acc[c]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < kSolveCols; ++c) {
+        float x = acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) W[a][c] = x;
+      }
     }
+    __syncthreads();
+    // W2 = T W (T upper triangular)
+    if (tid < kWY * kSolveCols) {
+      const int a = tid & 31, c = tid >> 5;
+      const float* tr = Tw + (size_t)B * kWY * kWY + a * kWY;
+      float x = 0.f;
+      for (int b = a; b < kWY; ++b) x = fmaf(tr[b], W[b][c], x);
+      W2[a][c] = x;
+    }
+    __syncthreads();
+    // Z -= V W2
+    for (int i = j0 + 1 + tid; i < m; i += 256) {
+      float acc[kSolveCols] = {};
+      for (int a = 0; a < cnt; ++a) {
+        const float vi = vb[(size_t)a * m + i];
+#pragma unroll
+        for (int c = 0; c < kSolveCols; ++c) acc[c] = fmaf(vi, W2[a][c], acc[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < kSolveCols; ++c) zc[c * m + i] -= acc[c];
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < kSolveCols * m; t += 256) {
+    const int c = t / m, i = t % m;
+    X[(size_t)(k0 + c) * m + i] = zc[c * m + i];
+  }
 }
 
 // Scale rows of E by f_k = c_k (G_S) or c_k lam_k (G_M) into Es.
@@ -694,7 +827,7 @@ __global__ void mixed_loss(const double* __restrict__ c, const double* __restric
 }
 
 struct MixedWs {
-  size_t Mw, linv_pp, LT, Y, C, Vh, tau, d, e, Z, X, E, Es, G, total;
+  size_t Mw, Lw, linv_pp, Dinv, LT, Y, C, Vh, tau, Tw, d, e, Z, X, E, Es, G, total;
 };
 
 MixedWs mixed_ws(int m) {
@@ -706,12 +839,15 @@ MixedWs mixed_ws(int m) {
     return o;
   };
   w.Mw = take(mm * 8);
+  w.Lw = take(mm * 8);  // Cholesky factor (lower tiles)
   w.linv_pp = take((size_t)(m / kCB) * kCB * kCB * 8);
+  w.Dinv = take((size_t)2 * (m / kCB) * kCB * kCB * sizeof(df));  // DL, DU
   w.LT = take(mm * 8 * 2);   // L and L^T as float pairs
   w.Y = take(mm * 8);    // L^-1 S (FP64)
   w.C = take(mm * 4);
   w.Vh = take(mm * 4);
   w.tau = take((size_t)m * 4);
+  w.Tw = take((size_t)((m - 2 + kWY - 1) / kWY) * kWY * kWY * 4);
   w.d = take((size_t)m * 8);
   w.e = take((size_t)m * 8);
   w.Z = take(mm * 4);
@@ -774,6 +910,7 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   cudaStream_t s = (cudaStream_t)stream_;
   char* ws = (char*)workspace;
   double* Mw = (double*)(ws + w.Mw);
+  double* Lw = (double*)(ws + w.Lw);
   double* linv_pp = (double*)(ws + w.linv_pp);
   df* Ld = (df*)(ws + w.LT);
   df* LTd = Ld + (size_t)m * m;
@@ -781,6 +918,7 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   float* C = (float*)(ws + w.C);
   float* Vh = (float*)(ws + w.Vh);
   float* tau = (float*)(ws + w.tau);
+  float* Tw = (float*)(ws + w.Tw);
   double* d = (double*)(ws + w.d);
   double* e = (double*)(ws + w.e);
   float* Z = (float*)(ws + w.Z);
@@ -794,29 +932,44 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   NEB_CUDA_CHECK(cudaMemsetAsync(info, 0, sizeof(int), s));
   NEB_CUDA_CHECK(cudaMemcpyAsync(Mw, M, mm * 8, cudaMemcpyDeviceToDevice, s));
   {
-    KernelScope ks("spec_cholesky_df", s, (double)m * m * m / 3.0, 16.0 * mm, 3 * nb - 2);
-    for (int p = 0; p < nb; ++p) {
-      chol_diag<<<1, 1024, 0, s>>>(Mw, m, p, linv_pp + (size_t)p * kCB * kCB, info);
+    KernelScope ks("spec_cholesky_df", s, (double)m * m * m / 3.0, 16.0 * mm, nb);
+    chol_first<<<1, 1024, 0, s>>>(Mw, m, Lw, linv_pp, info);
+    NEB_LAUNCH_CHECK();
+    for (int p = 0; p + 1 < nb; ++p) {
+      const int tiles = (nb - p - 1) * (nb - p) / 2;
+      chol_step<<<tiles, 1024, 0, s>>>(Mw, m, p, Lw, linv_pp, info);
       NEB_LAUNCH_CHECK();
-      if (p + 1 < nb) {
-        chol_panel<<<nb - p - 1, 1024, 0, s>>>(Mw, m, p, linv_pp + (size_t)p * kCB * kCB);
-        NEB_LAUNCH_CHECK();
-        int tiles = (nb - p - 1) * (nb - p) / 2;
-        chol_update<<<tiles, 1024, 0, s>>>(Mw, m, p);
-        NEB_LAUNCH_CHECK();
-      }
     }
   }
   int st;
-  const size_t trsm_smem = (size_t)kTrsmCols * m * sizeof(df);
+  const size_t solve_smem = ((size_t)kSolveCols * m + (size_t)kCB * m) * sizeof(df);
+  {
+    static bool solve_configured = false;
+    if (!solve_configured) {
+      NEB_CUDA_CHECK(cudaFuncSetAttribute(df_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (kSolveCols * kMaxM + kCB * kMaxM) * (int)sizeof(df)));
+      solve_configured = true;
+    }
+  }
+  df* DL = (df*)(ws + w.Dinv);
+  df* DU = DL + (size_t)nb * kCB * kCB;
   {
     // C = L^-1 S L^-T as two solves: Y = L^-1 S, C = L^-1 Y^T (S symmetric)
-    KernelScope ks("spec_reduce_df", s, 2.0 * m * mm, 32.0 * mm, 3);
-    split_factor<<<dim3(m / 32, m / 32), dim3(32, 8), 0, s>>>(Mw, m, Ld, LTd);
-    NEB_LAUNCH_CHECK();
-    df_trsm<<<m / kTrsmCols, 256, trsm_smem, s>>>(Ld, m, 0, S, 0, 0, Y, 0, 0);
-    NEB_LAUNCH_CHECK();
-    df_trsm<<<m / kTrsmCols, 256, trsm_smem, s>>>(Ld, m, 0, Y, 0, 1, C, 1, 0);
+    KernelScope ks("spec_reduce_df", s, 2.0 * m * mm, 32.0 * mm, 4);
+    {
+      KernelScope k1("split_factor", s, 0, 0, 0);
+      split_factor<<<dim3(m / 32, m / 32), dim3(32, 8), 0, s>>>(Lw, m, Ld, LTd);
+      NEB_LAUNCH_CHECK();
+      split_dinv<<<nb, 1024, 0, s>>>(linv_pp, DL, DU);
+      NEB_LAUNCH_CHECK();
+    }
+    {
+      KernelScope k2("df_solve", s, 0, 0, 0);
+      df_solve<<<m / kSolveCols, 256, solve_smem, s>>>(Ld, DL, m, 0, S, 0, 0, Y, 0, 0);
+      NEB_LAUNCH_CHECK();
+    }
+    KernelScope k3("df_solve", s, 0, 0, 0);
+    df_solve<<<m / kSolveCols, 256, solve_smem, s>>>(Ld, DL, m, 0, Y, 0, 1, C, 1, 0);
     NEB_LAUNCH_CHECK();
   }
   cublasHandle_t h;
@@ -838,27 +991,50 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   }
   {
     KernelScope ks("spec_tridiag_eig", s, 0, 16.0 * m, 2);
-    tri_eigvals<<<(m * 32 + 255) / 256, 256, (size_t)2 * m * 4, s>>>(d, e, m, lam);
-    NEB_LAUNCH_CHECK();
+    {
+      KernelScope k1("tri_eigvals", s, 0, 0, 0);
+      tri_eigvals<<<(m * 32 + 255) / 256, 256, (size_t)2 * m * 4, s>>>(d, e, m, lam);
+      NEB_LAUNCH_CHECK();
+    }
     static bool vec_configured = false;
     if (!vec_configured) {
       NEB_CUDA_CHECK(cudaFuncSetAttribute(tri_eigvecs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          2 * kMaxM * 32 * (int)sizeof(float)));
+                                          (2 * kMaxM * 32 + 2 * kMaxM) * (int)sizeof(float)));
       vec_configured = true;
     }
-    tri_eigvecs<<<(m + 31) / 32, 32, (size_t)2 * m * 32 * sizeof(float), s>>>(d, e, m, lam, Z);
+    tri_eigvecs<<<(m + 31) / 32, 32, ((size_t)2 * m * 32 + 2 * m) * sizeof(float), s>>>(d, e, m,
+                                                                                        lam, Z);
     NEB_LAUNCH_CHECK();
   }
   {
-    KernelScope ks("spec_backtransform_fp32", s, 2.0 * m * mm, 4.0 * mm * ((m + 3) / 4));
-    householder_apply<<<(m + 3) / 4, 128, (size_t)kHChunk * m * 4, s>>>(Vh, tau, m, Z, X);
+    KernelScope ks("spec_backtransform_fp32", s, 4.0 * m * mm, 4.0 * mm * (m / kSolveCols), 2);
+    static bool wy_configured = false;
+    if (!wy_configured) {
+      NEB_CUDA_CHECK(cudaFuncSetAttribute(wy_factor, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kWY * (kMaxM + 1) * (int)sizeof(float)));
+      wy_configured = true;
+    }
+    const int nblk = (m - 2 + kWY - 1) / kWY;
+    wy_factor<<<nblk, 1024, (size_t)kWY * (m + 1) * sizeof(float), s>>>(Vh, tau, m, Tw);
+    NEB_LAUNCH_CHECK();
+    static bool wya_configured = false;
+    if (!wya_configured) {
+      NEB_CUDA_CHECK(cudaFuncSetAttribute(wy_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (kSolveCols + kWY) * kMaxM * (int)sizeof(float)));
+      wya_configured = true;
+    }
+    wy_apply<<<m / kSolveCols, 256, (size_t)(kSolveCols + kWY) * m * sizeof(float), s>>>(
+        Vh, Tw, m, Z, X);
     NEB_LAUNCH_CHECK();
   }
   {
     KernelScope ks("spec_adjoints_fp32", s, 6.0 * m * mm, 24.0 * mm, 9);
     // rows of V: e_k = (L^-T x_k)^T, a backward solve with L^T on the columns of X^T
-    df_trsm<<<m / kTrsmCols, 256, trsm_smem, s>>>(LTd, m, 1, X, 1, 1, E, 1, 1);
-    NEB_LAUNCH_CHECK();
+    {
+      KernelScope k1("df_solve", s, 0, 0, 0);
+      df_solve<<<m / kSolveCols, 256, solve_smem, s>>>(LTd, DU, m, 1, X, 1, 1, E, 1, 1);
+      NEB_LAUNCH_CHECK();
+    }
     int blocks = (int)std::min<size_t>((mm + 255) / 256, 2048);
     f32_to_f64<<<blocks, 256, 0, s>>>(E, V, mm, 1.0);
     NEB_LAUNCH_CHECK();
