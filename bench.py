@@ -524,13 +524,11 @@ def main():
             dist.destroy_process_group()
         return
 
-    # roofline of the dominant jet-MLP kernel (by total time).  The spectral
-    # stage (spec_*, cuSOLVER) works on a 512 x 512 pencil: it is bound by
+    # roofline of the dominant jet-MLP kernel (by total time; tc_* / simt_*
+    # timers).  The spectral stage works on a 512 x 512 pencil: it is bound by
     # dependent-operation latency and barriers, not by the tensor pipe or HBM,
     # and is reported separately below.
-    own = {k: v for k, v in kernels.items()
-           if not k.startswith(("cusolver", "cublas", "spec_", "reduce_", "adam", "scale_",
-                                "weighted_sum", "convert"))}
+    own = {k: v for k, v in kernels.items() if k.startswith(("tc_", "simt_"))}
     dom = max(own, key=lambda k: own[k][1])
     launches_dom, total_ms_dom, flops_dom, bytes_dom = own[dom]
     per_launch_s = total_ms_dom / launches_dom / 1e3

@@ -49,6 +49,26 @@ constexpr int kTriThreads = 512;
 
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Asynchronous global -> shared copies (cp.async): a staging loop issues all
+// of its copies before waiting once, instead of one dependent load per
+// element.
+__device__ __forceinline__ uint32_t sh_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sh_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sh_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sh_u32(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
+}
+
 // ------------------------------------------------ compensated FP32 ("df")
 // A value is an unevaluated sum hi + lo of two floats (about 48 significant
 // bits).  Products use TwoProd through fma, sums TwoSum: every operation runs
@@ -120,18 +140,32 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
   const int j = threadIdx.x & 31, i = threadIdx.x >> 5;
   L[i][j] = df{0.f, 0.f};
   X[i][j] = df{0.f, 0.f};
-  __syncthreads();
-  for (int k = 0; k < kCB; ++k) {
-    df akk = a[k][k];
-    if (!(akk.h > 0.f)) {  // not positive definite (or NaN)
-      if (threadIdx.x == 0 && *bad == 0) *bad = k + 1;
-      akk = df{1.f, 0.f};
+  if (threadIdx.x == 0) {
+    df a00 = a[0][0];
+    if (!(a00.h > 0.f)) {  // not positive definite (or NaN)
+      if (*bad == 0) *bad = 1;
+      a00 = df{1.f, 0.f};
     }
-    const df r = df_recip(df_sqrt(akk));
+    rinv[0] = df_recip(df_sqrt(a00));
+  }
+  __syncthreads();
+  // step k: r = 1 / l_kk comes from the thread that finalised a_kk in step
+  // k - 1, so the reciprocal square root is taken once per column
+  for (int k = 0; k < kCB; ++k) {
+    const df r = rinv[k];
     const df lik = df_mul(a[i][k], r);
     if (j == k && i >= k) L[i][k] = lik;
-    if (threadIdx.x == 0) rinv[k] = r;
-    if (j > k && i >= j) a[i][j] = df_add(a[i][j], df_neg(df_mul(lik, df_mul(a[j][k], r))));
+    if (j > k && i >= j) {
+      df v = df_add(a[i][j], df_neg(df_mul(lik, df_mul(a[j][k], r))));
+      a[i][j] = v;
+      if (i == k + 1 && j == k + 1) {
+        if (!(v.h > 0.f)) {
+          if (*bad == 0) *bad = k + 2;
+          v = df{1.f, 0.f};
+        }
+        rinv[k + 1] = df_recip(df_sqrt(v));
+      }
+    }
     __syncthreads();
   }
   if (i == j) X[i][i] = rinv[i];
@@ -289,8 +323,9 @@ __global__ void __launch_bounds__(256) df_solve(const df* __restrict__ T,
     const int ncols = hi - lo, ld = ncols + 1;  // odd pitch: two wavefronts per warp
     for (int t = tid; t < kCB * ncols; t += 256) {
       const int r = t / ncols, k = t - r * ncols;
-      tt[r * ld + k] = T[(size_t)(rb0 + r) * m + lo + k];
+      cp_async8(tt + r * ld + k, T + (size_t)(rb0 + r) * m + lo + k);
     }
+    cp_async_wait_all();
     __syncthreads();
     const int mid = ncols >> 1;
     const int k0 = half ? mid : 0, k1 = half ? ncols : mid;
@@ -688,8 +723,10 @@ __global__ void __launch_bounds__(1024) wy_factor(const float* __restrict__ Vh,
   const int cnt = min(kWY, m - 2 - j0);
   for (int t = threadIdx.x; t < kWY * m; t += blockDim.x) {
     const int a = t / m, i = t % m;
-    vsh[a * ld + i] = a < cnt ? Vh[(size_t)(j0 + a) * m + i] : 0.f;
+    if (a < cnt) cp_async4(vsh + a * ld + i, Vh + (size_t)(j0 + a) * m + i);
+    else vsh[a * ld + i] = 0.f;
   }
+  cp_async_wait_all();
   __syncthreads();
   {
     const int a = threadIdx.x >> 5, b = threadIdx.x & 31;
@@ -736,7 +773,8 @@ __global__ void __launch_bounds__(256) wy_apply(const float* __restrict__ Vh,
     const int j0 = B * kWY;
     const int cnt = min(kWY, m - 2 - j0);
     __syncthreads();
-    for (int t = tid; t < cnt * m; t += 256) vb[t] = Vh[(size_t)j0 * m + t];
+    for (int t = 4 * tid; t < cnt * m; t += 4 * 256) cp_async16(vb + t, Vh + (size_t)j0 * m + t);
+    cp_async_wait_all();
     __syncthreads();
     // W = V^T Z: warp w takes reflectors a = w, w + 8, ...; lanes over rows
     for (int a = warp; a < kWY; a += 8) {

@@ -6,13 +6,19 @@
 // (+ A_lo B_lo for the Grams, where the dropped term would bias every
 // diagonal the same way).
 // Operands arrive by TMA (128-byte swizzle, K-major) through an mbarrier ring;
-// one thread issues the MMAs, four warps run the epilogue from TMEM.
+// one thread issues the MMAs, eight warps run the epilogue from TMEM.  The
+// jet GEMM is persistent (one CTA per SM, 128 x 64 tiles round-robin) with
+// its accumulators double-buffered in TMEM, so epilogue and MMAs overlap.
 //
 // Device layouts (n_pad = n rounded up to 128 points; "planar" = one matrix
-// per jet channel c in 0..3 = value, d/dx, d/dy, Laplacian):
-//   X_l   [2 planes hi/lo][C][n_pad][w_pad]  layer input, K-major for the next GEMM
-//   XT_l  [2][C][w_pad][n_pad]               its transpose, K-major over points
-//   Z_l   [C][n_pad][w]  float               pre-activation, for the reverse pass
+// per jet channel c in 0..3 = value, d/dx, d/dy, Laplacian), points
+// contiguous so that a warp (32 TMEM lanes = 32 points) stores whole
+// 128-byte lines:
+//   X_l   [2 planes hi/lo][C][w_pad][n_pad]  layer output: MN-major A operand
+//                                            of the next layer, K-major
+//                                            (over points) for the weight
+//                                            gradient and the Grams
+//   Z_l   [C][w][n_pad]  float               pre-activation, for the reverse pass
 // Kernels:
 //   tc_jet_gemm<0>  forward layer:  Z = X W^T + b (value channel), X' = tanh-jet(Z)
 //   tc_jet_gemm<1>  reverse data:   Zbar' = tanh-jet^T(Z', Zbar W)
@@ -82,59 +88,59 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
 struct JetGemmArgs {
   int n_points, n_pad, K, N;
   const float* bias;   // EPI 0: [N]
-  const float* zprev;  // EPI 1, 2: [C][n_pad][N] pre-activation of the target layer
+  const float* zprev;  // EPI 1, 2: [C][N][n_pad] pre-activation of the target layer
   const float* qw;     // EPI 2: [n_points] quadrature weights
-  float* z_out;        // EPI 0: [C][n_pad][N]
-  __nv_bfloat16* y_out;   // [2][C][n_pad][N]
-  __nv_bfloat16* yt_out;  // [2][C][N][n_pad]
+  float* z_out;        // EPI 0: [C][N][n_pad]
+  __nv_bfloat16* yt_out;  // [2][C][N][n_pad] split output
   int* status;
 };
 
 template <int EPI> struct JetCfg {
+  static constexpr int BN = 64;                  // output columns per tile
   static constexpr int NB = EPI == 2 ? 2 : 1;    // distinct B matrices
   static constexpr int NCH = EPI == 2 ? 3 : 4;   // accumulated channels
   static constexpr int CH0 = EPI == 2 ? 1 : 0;
   static constexpr int A_ST = EPI == 2 ? 3 : 4;
   static constexpr int B_ST = 2;
-  static constexpr int B_BYTES = 2 * NB * kTileBytes;
-  static constexpr int SMEM = 1024 + A_ST * 2 * kTileBytes + B_ST * B_BYTES + 256;
+  static constexpr int B_TILE = BN * 128;        // 64 rows x 64 bf16
+  static constexpr int B_BYTES = 2 * NB * B_TILE;
+  static constexpr int STAGE = 8 * 8192;         // epilogue transpose staging, 8 warps
+  static constexpr int SMEM = 1024 + A_ST * 2 * kTileBytes + B_ST * B_BYTES + STAGE + 256;
+  static constexpr int TBUF = 256;               // TMEM columns per accumulator buffer
 };
 
-__device__ __forceinline__ void store_split16(const float* v, __nv_bfloat16* hi_dst,
-                                              __nv_bfloat16* lo_dst) {
-  __align__(16) __nv_bfloat16 h[16], l[16];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) tc::split_bf16(v[j], h[j], l[j]);
-  uint4* hd = reinterpret_cast<uint4*>(hi_dst);
-  uint4* ld = reinterpret_cast<uint4*>(lo_dst);
-  hd[0] = reinterpret_cast<uint4*>(h)[0];
-  hd[1] = reinterpret_cast<uint4*>(h)[1];
-  ld[0] = reinterpret_cast<uint4*>(l)[0];
-  ld[1] = reinterpret_cast<uint4*>(l)[1];
-}
 
+// Persistent tcgen05 jet GEMM: tiles of 128 points x 64 outputs (all jet
+// channels) are dealt round-robin to the CTAs (one per SM); the accumulators
+// are double-buffered in tensor memory (2 x 256 columns), so the epilogue of
+// one tile overlaps the MMAs of the next.  Roles: warp 0 lane 0 issues TMA
+// loads, warp 1 lane 0 issues MMAs, warps 2-9 run the epilogue (lane quarter
+// w % 4, column half (w - 2) / 4).
 template <int EPI>
 __global__ void __launch_bounds__(320, 1)
 tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             JetGemmArgs g) {
   using Cfg = JetCfg<EPI>;
-  constexpr int NB = Cfg::NB, NCH = Cfg::NCH, CH0 = Cfg::CH0, A_ST = Cfg::A_ST,
+  constexpr int BN = Cfg::BN, NB = Cfg::NB, NCH = Cfg::NCH, CH0 = Cfg::CH0, A_ST = Cfg::A_ST,
                 B_ST = Cfg::B_ST;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* a_smem = smem;
   uint8_t* b_smem = smem + A_ST * 2 * kTileBytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(b_smem + B_ST * Cfg::B_BYTES);
+  uint8_t* st_smem = b_smem + B_ST * Cfg::B_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(st_smem + Cfg::STAGE);
   uint64_t* a_full = bars;
   uint64_t* a_empty = bars + A_ST;
   uint64_t* b_full = bars + 2 * A_ST;
   uint64_t* b_empty = bars + 2 * A_ST + B_ST;
-  uint64_t* acc_full = bars + 2 * A_ST + 2 * B_ST;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_full + 1);
+  uint64_t* acc_full = bars + 2 * A_ST + 2 * B_ST;   // [2]
+  uint64_t* acc_empty = acc_full + 2;                // [2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n0 = blockIdx.x * 128, p0 = blockIdx.y * 128;
   const int KC = g.K / 64;
+  const int n_tiles = g.N / BN;
+  const int total = n_tiles * (g.n_pad / 128);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < A_ST; ++i) {
@@ -145,7 +151,10 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       tc::mbar_init(&b_full[i], 1);
       tc::mbar_init(&b_empty[i], 1);
     }
-    tc::mbar_init(acc_full, 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&acc_full[i], 1);
+      tc::mbar_init(&acc_empty[i], 8);  // one arrival per epilogue warp
+    }
     tc::fence_mbar_init();
   }
   if (warp == 1) {
@@ -159,159 +168,170 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer
-    int ai = 0;
-    for (int kc = 0; kc < KC; ++kc) {
-      const int bs = kc % B_ST;
-      tc::mbar_wait(&b_empty[bs], ((kc / B_ST) & 1) ^ 1, g.status);
-      tc::mbar_expect_tx(&b_full[bs], Cfg::B_BYTES);
-      for (int b = 0; b < NB; ++b)
-        for (int pl = 0; pl < 2; ++pl)
-          tc::tma_load_2d(b_smem + bs * Cfg::B_BYTES + (b * 2 + pl) * kTileBytes, &tmB,
-                          &b_full[bs], kc * 64, (pl * NB + b) * g.N + n0);
-      for (int ci = 0; ci < NCH; ++ci, ++ai) {
-        const int as = ai % A_ST, c = CH0 + ci;
-        tc::mbar_wait(&a_empty[as], ((ai / A_ST) & 1) ^ 1, g.status);
-        tc::mbar_expect_tx(&a_full[as], 2 * kTileBytes);
-        for (int pl = 0; pl < 2; ++pl)
-          tc::tma_load_2d(a_smem + (as * 2 + pl) * kTileBytes, &tmA, &a_full[as], kc * 64,
-                          (pl * C + c) * g.n_pad + p0);
+    int ai = 0, bi = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+      const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
+      for (int kc = 0; kc < KC; ++kc, ++bi) {
+        const int bs = bi % B_ST;
+        tc::mbar_wait(&b_empty[bs], ((bi / B_ST) & 1) ^ 1, g.status);
+        tc::mbar_expect_tx(&b_full[bs], Cfg::B_BYTES);
+        for (int b = 0; b < NB; ++b)
+          for (int pl = 0; pl < 2; ++pl)
+            tc::tma_load_2d(b_smem + bs * Cfg::B_BYTES + (b * 2 + pl) * Cfg::B_TILE, &tmB,
+                            &b_full[bs], kc * 64, (pl * NB + b) * g.N + n0);
+        for (int ci = 0; ci < NCH; ++ci, ++ai) {
+          const int as = ai % A_ST, c = CH0 + ci;
+          tc::mbar_wait(&a_empty[as], ((ai / A_ST) & 1) ^ 1, g.status);
+          tc::mbar_expect_tx(&a_full[as], 2 * kTileBytes);
+          // A is MN-major: [plane][channel][k][point]; a tile is two boxes of
+          // 64 points x 64 k rows
+          for (int pl = 0; pl < 2; ++pl)
+            for (int hb = 0; hb < 2; ++hb)
+              tc::tma_load_2d(a_smem + (as * 2 + pl) * kTileBytes + hb * (kTileBytes / 2), &tmA,
+                              &a_full[as], p0 + hb * 64, (pl * C + c) * g.K + kc * 64);
+        }
       }
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
-    constexpr uint32_t idesc = tc::idesc_bf16(128, 128);
-    int ai = 0;
-    for (int kc = 0; kc < KC; ++kc) {
-      const int bs = kc % B_ST;
-      tc::mbar_wait(&b_full[bs], (kc / B_ST) & 1, g.status);
+    constexpr uint32_t idesc = tc::idesc_bf16(128, BN, true);
+    int ai = 0, bi = 0, it = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
+      const int buf = it & 1;
+      tc::mbar_wait(&acc_empty[buf], ((it >> 1) & 1) ^ 1, g.status);
       tc::tc_fence_after();
-      for (int ci = 0; ci < NCH; ++ci, ++ai) {
-        const int as = ai % A_ST, c = CH0 + ci;
-        tc::mbar_wait(&a_full[as], (ai / A_ST) & 1, g.status);
+      for (int kc = 0; kc < KC; ++kc, ++bi) {
+        const int bs = bi % B_ST;
+        tc::mbar_wait(&b_full[bs], (bi / B_ST) & 1, g.status);
         tc::tc_fence_after();
-        const int bsel = (EPI == 2 && c == 3) ? 1 : 0;
-        const uint32_t a_hi = tc::smem_u32(a_smem + (as * 2) * kTileBytes);
-        const uint32_t a_lo = a_hi + kTileBytes;
-        const uint32_t b_hi = tc::smem_u32(b_smem + bs * Cfg::B_BYTES + (bsel * 2) * kTileBytes);
-        const uint32_t b_lo = b_hi + kTileBytes;
-        const uint32_t d = tmem + ci * 128;
+        for (int ci = 0; ci < NCH; ++ci, ++ai) {
+          const int as = ai % A_ST, c = CH0 + ci;
+          tc::mbar_wait(&a_full[as], (ai / A_ST) & 1, g.status);
+          tc::tc_fence_after();
+          const int bsel = (EPI == 2 && c == 3) ? 1 : 0;
+          const uint32_t a_hi = tc::smem_u32(a_smem + (as * 2) * kTileBytes);
+          const uint32_t a_lo = a_hi + kTileBytes;
+          const uint32_t b_hi =
+              tc::smem_u32(b_smem + bs * Cfg::B_BYTES + (bsel * 2) * Cfg::B_TILE);
+          const uint32_t b_lo = b_hi + Cfg::B_TILE;
+          const uint32_t d = tmem + buf * Cfg::TBUF + ci * BN;
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const uint32_t off = kk * 32;
-          const uint64_t dah = tc::desc_sw128(a_hi + off), dal = tc::desc_sw128(a_lo + off);
-          const uint64_t dbh = tc::desc_sw128(b_hi + off), dbl = tc::desc_sw128(b_lo + off);
-          tc::mma_bf16(d, dah, dbh, idesc, (kc | kk) != 0);
-          tc::mma_bf16(d, dal, dbh, idesc, 1);
-          tc::mma_bf16(d, dah, dbl, idesc, 1);
+          for (int kk = 0; kk < 4; ++kk) {
+            // K step of 16: 16 rows of the MN-major A tile, 32 bytes of the K-major B rows
+            const uint32_t aoff = kk * 2048, boff = kk * 32;
+            const uint64_t dah = tc::desc_mn_sw128(a_hi + aoff, kTileBytes / 2);
+            const uint64_t dal = tc::desc_mn_sw128(a_lo + aoff, kTileBytes / 2);
+            const uint64_t dbh = tc::desc_sw128(b_hi + boff), dbl = tc::desc_sw128(b_lo + boff);
+            tc::mma_bf16(d, dah, dbh, idesc, (kc | kk) != 0);
+            tc::mma_bf16(d, dal, dbh, idesc, 1);
+            tc::mma_bf16(d, dah, dbl, idesc, 1);
+          }
+          tc::mma_commit(&a_empty[as]);
         }
-        tc::mma_commit(&a_empty[as]);
+        tc::mma_commit(&b_empty[bs]);
       }
-      tc::mma_commit(&b_empty[bs]);
+      tc::mma_commit(&acc_full[buf]);
     }
-    tc::mma_commit(acc_full);
   } else if (warp >= 2) {
-    // ---------------- epilogue: eight warps, one thread per point (TMEM lane);
-    // warp w reads lane quarter w % 4 and column half (w - 2) / 4.
+    // ---------------- epilogue: eight warps, one thread per point (TMEM lane)
     const int q = warp & 3, half = (warp - 2) >> 2;
     const int row = q * 32 + lane;
-    const int p = p0 + row;
-    tc::mbar_wait(acc_full, 0, g.status);
-    tc::tc_fence_after();
     const size_t plane = (size_t)C * g.n_pad * g.N;  // elements of one hi or lo plane
-    // transposed outputs are staged per warp through the (now idle) operand
-    // buffers: [C][2 planes][16 columns][32 points] bf16 = 8 KB per warp
-    __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(smem) + (size_t)(warp - 2) * 4096;
-    float w2 = 0.f;
-    if constexpr (EPI == 2) w2 = p < g.n_points ? 2.f * g.qw[p] : 0.f;
-    for (int jc = 0; jc < 4; ++jc) {
-      const int j0 = half * 64 + jc * 16;
-      float acc[NCH][16];
+    // transposed outputs are staged per warp: [C][2 planes][16 columns][32 points]
+    __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(st_smem) + (size_t)(warp - 2) * 4096;
+    int it = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
+      const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
+      const int p = p0 + row;
+      const int buf = it & 1;
+      tc::mbar_wait(&acc_full[buf], (it >> 1) & 1, g.status);
+      tc::tc_fence_after();
+      float w2 = 0.f;
+      if constexpr (EPI == 2) w2 = p < g.n_points ? 2.f * g.qw[p] : 0.f;
+      for (int jc = 0; jc < 2; ++jc) {
+        const int j0 = half * 32 + jc * 16;
+        float acc[NCH][16];
 #pragma unroll
-      for (int ci = 0; ci < NCH; ++ci)
-        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + ci * 128 + j0, acc[ci]);
-      const int col = n0 + j0;
-      float out[C][16];
-      if constexpr (EPI == 0) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-#pragma unroll
-          for (int c = 0; c < C; ++c) out[c][j] = acc[c][j];
-          out[0][j] += g.bias[col + j];
+        for (int ci = 0; ci < NCH; ++ci)
+          tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * Cfg::TBUF + ci * BN + j0,
+                        acc[ci]);
+        if (jc == 1) {  // this warp's columns of the buffer are drained
+          tc::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
         }
+        const int col = n0 + j0;
+        float out[C][16];
+        if constexpr (EPI == 0) {
 #pragma unroll
-        for (int c = 0; c < C; ++c) {
-          float4* zd = reinterpret_cast<float4*>(g.z_out + ((size_t)c * g.n_pad + p) * g.N + col);
+          for (int j = 0; j < 16; ++j) {
 #pragma unroll
-          for (int j = 0; j < 4; ++j)
-            zd[j] = make_float4(out[c][4 * j], out[c][4 * j + 1], out[c][4 * j + 2],
-                                out[c][4 * j + 3]);
-        }
+            for (int c = 0; c < C; ++c) out[c][j] = acc[c][j];
+            out[0][j] += g.bias[col + j];
+          }
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          float v[C];
+          for (int c = 0; c < C; ++c)
 #pragma unroll
-          for (int c = 0; c < C; ++c) v[c] = out[c][j];
-          jet_act_forward<C>(v);
+            for (int j = 0; j < 16; ++j)  // [C][N][n_pad]: a warp stores 32 points
+              g.z_out[((size_t)c * g.N + col + j) * g.n_pad + p] = out[c][j];
 #pragma unroll
-          for (int c = 0; c < C; ++c) out[c][j] = v[c];
-        }
-      } else {
+          for (int j = 0; j < 16; ++j) {
+            float v[C];
 #pragma unroll
-        for (int c = 0; c < C; ++c) {
-          const float4* zs =
-              reinterpret_cast<const float4*>(g.zprev + ((size_t)c * g.n_pad + p) * g.N + col);
+            for (int c = 0; c < C; ++c) v[c] = out[c][j];
+            jet_act_forward<C>(v);
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            float4 z4 = zs[j];
-            out[c][4 * j] = z4.x;
-            out[c][4 * j + 1] = z4.y;
-            out[c][4 * j + 2] = z4.z;
-            out[c][4 * j + 3] = z4.w;
+            for (int c = 0; c < C; ++c) out[c][j] = v[c];
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < C; ++c)
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              out[c][j] = g.zprev[((size_t)c * g.N + col + j) * g.n_pad + p];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float z[C], v[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) z[c] = out[c][j];
+            if constexpr (EPI == 2) {
+              v[0] = 0.f;
+#pragma unroll
+              for (int c = 1; c < C; ++c) v[c] = w2 * acc[c - 1][j];
+            } else {
+#pragma unroll
+              for (int c = 0; c < C; ++c) v[c] = acc[c][j];
+            }
+            jet_act_backward<C>(z, v);
+#pragma unroll
+            for (int c = 0; c < C; ++c) out[c][j] = v[c];
           }
         }
+        // split outputs [2][C][N][n_pad] (points contiguous), staged through
+        // shared memory into 16-byte vectors of 8 points
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          float z[C], v[C];
+        for (int c = 0; c < C; ++c) {
 #pragma unroll
-          for (int c = 0; c < C; ++c) z[c] = out[c][j];
-          if constexpr (EPI == 2) {
-            v[0] = 0.f;
-#pragma unroll
-            for (int c = 1; c < C; ++c) v[c] = w2 * acc[c - 1][j];
-          } else {
-#pragma unroll
-            for (int c = 0; c < C; ++c) v[c] = acc[c][j];
+          for (int j = 0; j < 16; ++j) {
+            __nv_bfloat16 h, l;
+            tc::split_bf16(out[c][j], h, l);
+            stage[((c * 2 + 0) * 16 + j) * 32 + lane] = h;
+            stage[((c * 2 + 1) * 16 + j) * 32 + lane] = l;
           }
-          jet_act_backward<C>(z, v);
-#pragma unroll
-          for (int c = 0; c < C; ++c) out[c][j] = v[c];
         }
-      }
-      // planar split outputs (row-contiguous per point), transposed via smem
+        __syncwarp();
+        const uint4* st4 = reinterpret_cast<const uint4*>(stage);
 #pragma unroll
-      for (int c = 0; c < C; ++c) {
-        size_t o = ((size_t)c * g.n_pad + p) * g.N + col;
-        store_split16(out[c], g.y_out + o, g.y_out + plane + o);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          __nv_bfloat16 h, l;
-          tc::split_bf16(out[c][j], h, l);
-          stage[((c * 2 + 0) * 16 + j) * 32 + lane] = h;
-          stage[((c * 2 + 1) * 16 + j) * 32 + lane] = l;
+        for (int u8 = 0; u8 < 16; ++u8) {
+          const int u = lane + 32 * u8;        // 512 vectors of 8 points
+          const int r = u >> 2, quad = u & 3;  // r = (c * 2 + plane) * 16 + j
+          const int c = r >> 5, pl = (r >> 4) & 1, j = r & 15;
+          const size_t gi = (size_t)pl * plane + ((size_t)c * g.N + col + j) * g.n_pad + p0 +
+                            q * 32 + quad * 8;
+          *reinterpret_cast<uint4*>(g.yt_out + gi) = st4[u];
         }
+        __syncwarp();
       }
-      __syncwarp();
-      const uint4* st4 = reinterpret_cast<const uint4*>(stage);
-#pragma unroll
-      for (int t = 0; t < 16; ++t) {
-        const int u = lane + 32 * t;       // 512 vectors of 8 points
-        const int r = u >> 2, quad = u & 3;  // r = (c * 2 + plane) * 16 + j
-        const int c = r >> 5, pl = (r >> 4) & 1, j = r & 15;
-        const size_t gi = (size_t)pl * plane + ((size_t)c * g.N + col + j) * g.n_pad + p0 +
-                          q * 32 + quad * 8;
-        *reinterpret_cast<uint4*>(g.yt_out + gi) = st4[u];
-      }
-      __syncwarp();
     }
   }
   tc::tc_fence_before();
@@ -470,21 +490,18 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
 // Interleaved float features [n][C][F] -> split planar X_0 [2][C][n_pad][Fp]
 // and its transpose XT_0 [2][C][Fp][n_pad], zero padded.
 __global__ void prep_features(const float* __restrict__ f, int n, int F, int n_pad, int Fp,
-                              __nv_bfloat16* __restrict__ X, __nv_bfloat16* __restrict__ XT) {
+                              __nv_bfloat16* __restrict__ XT) {
   const size_t total = (size_t)C * n_pad * Fp;
   const size_t plane = total;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
-    // i enumerates (c, k, p) with p fastest so the transposed writes coalesce
+    // i enumerates (c, k, p) with p fastest so the writes coalesce
     int p = (int)(i % n_pad);
     int k = (int)((i / n_pad) % Fp);
     int c = (int)(i / ((size_t)n_pad * Fp));
     float v = (p < n && k < F) ? f[((size_t)p * C + c) * F + k] : 0.f;
     __nv_bfloat16 h, l;
     tc::split_bf16(v, h, l);
-    size_t o = ((size_t)c * n_pad + p) * Fp + k;
-    X[o] = h;
-    X[plane + o] = l;
     XT[i] = h;
     XT[plane + i] = l;
   }
@@ -562,31 +579,29 @@ __global__ void reduce_parts(const double* __restrict__ part, int splits, int M,
   }
 }
 
-// Bias gradient partials: partb[chunk][o] = sum over the chunk's points of
-// the value plane of Zbar (hi + lo).  hi + lo is exact in FP32; four
-// independent FP32 accumulators over a 256-point chunk keep the dependent
-// add chain short, and the chunk sums are combined in FP64 by reduce_parts.
-__global__ void bias_partial_tc(const __nv_bfloat16* __restrict__ zb, int n_pad, int N,
-                                int chunk, double* __restrict__ partb) {
-  int o = blockIdx.x * blockDim.x + threadIdx.x;
+// Bias gradient: gb[o] = sum over points of the value plane of Zbar (hi +
+// lo), Zbar in [2][C][N][n_pad] (points contiguous): one warp per output,
+// 16-byte loads, FP32 sums of 8-point groups accumulated in FP64.
+__global__ void bias_rows_tc(const __nv_bfloat16* __restrict__ zb, int n_pad, int N,
+                             double* __restrict__ out) {
+  const int o = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (o >= N) return;
-  const size_t plane = (size_t)C * n_pad * N;
-  int p0 = blockIdx.y * chunk, p1 = min(n_pad, p0 + chunk);
-  float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  int p = p0;
-  for (; p + 4 <= p1; p += 4) {
+  const size_t plane = (size_t)C * N * n_pad;
+  const uint4* hi = reinterpret_cast<const uint4*>(zb + (size_t)o * n_pad);
+  const uint4* lo = reinterpret_cast<const uint4*>(zb + plane + (size_t)o * n_pad);
+  double acc = 0.0;
+  for (int v = lane; v < n_pad / 8; v += 32) {
+    const uint4 a = hi[v], b = lo[v];
+    const __nv_bfloat16* ha = reinterpret_cast<const __nv_bfloat16*>(&a);
+    const __nv_bfloat16* lb = reinterpret_cast<const __nv_bfloat16*>(&b);
+    float s8 = 0.f;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      size_t i = (size_t)(p + u) * N + o;  // channel 0
-      acc[u] += __bfloat162float(zb[i]) + __bfloat162float(zb[plane + i]);
-    }
+    for (int t = 0; t < 8; ++t) s8 += __bfloat162float(ha[t]) + __bfloat162float(lb[t]);
+    acc += (double)s8;
   }
-  for (; p < p1; ++p) {
-    size_t i = (size_t)p * N + o;
-    acc[0] += __bfloat162float(zb[i]) + __bfloat162float(zb[plane + i]);
-  }
-  partb[(size_t)blockIdx.y * N + o] = ((double)acc[0] + (double)acc[1]) +
-                                      ((double)acc[2] + (double)acc[3]);
+#pragma unroll
+  for (int sh = 16; sh > 0; sh >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, sh);
+  if (lane == 0) out[o] = acc;
 }
 
 // ---------------------------------------------------------- host helpers
@@ -614,13 +629,12 @@ Dims dims_of(const neb_net* net, int64_t n) {
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// TC workspace: [status][W splits per layer][WT splits][G split][wHT][Zbar A][Zbar B][ZbarT]
-//               [FP64 split partials][bias partials]
+// TC workspace: [status][W splits per layer][WT splits][G split][wHT][Zbar A][Zbar B]
+//               [FP64 split partials][bias sums]
 constexpr int kMaxSplits = 32;
-constexpr int kBiasChunk = 256;
 struct TcWs {
-  size_t status, w[NEB_MAX_HIDDEN + 1], wt[NEB_MAX_HIDDEN + 1], gsplit, wht, zb0, zb1, zbt,
-      part, partb, total;
+  size_t status, w[NEB_MAX_HIDDEN + 1], wt[NEB_MAX_HIDDEN + 1], gsplit, wht, zb0, zb1, part,
+      partb, total;
 };
 
 TcWs tc_ws(const Dims& d) {
@@ -645,13 +659,11 @@ TcWs tc_ws(const Dims& d) {
   off += zb;
   t.zb1 = off;
   off += zb;
-  t.zbt = off;
-  off += zb;
   int mx = mw > d.wp[0] ? mw : d.wp[0];
   t.part = off;
   off += a256((size_t)kMaxSplits * mx * mx * 8);
   t.partb = off;
-  off += a256((size_t)((d.n_pad + kBiasChunk - 1) / kBiasChunk) * mw * 8);
+  off += a256((size_t)mw * 8);
   t.total = off;
   return t;
 }
@@ -666,8 +678,18 @@ int launch_jet(const CUtensorMap& A, const CUtensorMap& B, const JetGemmArgs& ar
                                         JetCfg<EPI>::SMEM));
     configured = true;
   }
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    NEB_CUDA_CHECK(cudaGetDevice(&dev));
+    NEB_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  (void)n_tiles;
+  NEB_REQUIRE(args.N % JetCfg<EPI>::BN == 0, "jet GEMM: N = %d must be a multiple of %d", args.N,
+              JetCfg<EPI>::BN);
+  const int tiles = (args.N / JetCfg<EPI>::BN) * p_tiles;
   KernelScope ks(name, s, flops, bytes);
-  tc_jet_gemm<EPI><<<dim3(n_tiles, p_tiles), 320, JetCfg<EPI>::SMEM, s>>>(A, B, args);
+  tc_jet_gemm<EPI><<<std::min(tiles, sms), 320, JetCfg<EPI>::SMEM, s>>>(A, B, args);
   NEB_LAUNCH_CHECK();
   return NEB_OK;
 }
@@ -745,7 +767,7 @@ size_t tc_tape_bytes(const neb_net* net, int64_t n, size_t* x_off, size_t* z_off
       off += a256((size_t)C * d.n_pad * d.w[l] * 4);
     }
     if (x_off) x_off[l] = off;
-    off += 2 * a256((size_t)2 * C * d.n_pad * d.wp[l] * 2);  // X and XT
+    off += a256((size_t)2 * C * d.n_pad * d.wp[l] * 2);  // X, points contiguous
   }
   return off;
 }
@@ -764,10 +786,8 @@ int tc_forward(const neb_net* net, const float* const* W, const float* const* b,
     KernelScope ks("tc_prep_features", s, 0, (double)n * C * d.F * 4 + 8.0 * C * d.n_pad * d.Fp);
     size_t total = (size_t)C * d.n_pad * d.Fp;
     int blocks = (int)std::min<size_t>((total + 255) / 256, 8192);
-    __nv_bfloat16* X0 = (__nv_bfloat16*)tape.x[0];
-    size_t xsz = a256((size_t)2 * C * d.n_pad * d.Fp * 2);
-    prep_features<<<blocks, 256, 0, s>>>(feats, (int)n, d.F, (int)d.n_pad, d.Fp, X0,
-                                         (__nv_bfloat16*)((char*)tape.x[0] + xsz));
+    prep_features<<<blocks, 256, 0, s>>>(feats, (int)n, d.F, (int)d.n_pad, d.Fp,
+                                         (__nv_bfloat16*)tape.x[0]);
     NEB_LAUNCH_CHECK();
   }
   for (int l = 1; l <= d.L; ++l) {
@@ -782,9 +802,8 @@ int tc_forward(const neb_net* net, const float* const* W, const float* const* b,
   for (int l = 1; l <= d.L; ++l) {
     const int K = d.wp[l - 1], N = d.w[l];
     CUtensorMap ma, mb;
-    if ((st = make_map(&ma, tape.x[l - 1], (int64_t)2 * C * d.n_pad, K, 128))) return st;
-    if ((st = make_map(&mb, ws + t.w[l], (int64_t)2 * N, K, 128))) return st;
-    size_t xsz = a256((size_t)2 * C * d.n_pad * N * 2);
+    if ((st = make_map(&ma, tape.x[l - 1], (int64_t)2 * C * K, d.n_pad, 64))) return st;
+    if ((st = make_map(&mb, ws + t.w[l], (int64_t)2 * N, K, JetCfg<0>::BN))) return st;
     JetGemmArgs g{};
     g.n_points = (int)n;
     g.n_pad = (int)d.n_pad;
@@ -792,12 +811,11 @@ int tc_forward(const neb_net* net, const float* const* W, const float* const* b,
     g.N = N;
     g.bias = b[l - 1];
     g.z_out = (float*)tape.z[l];
-    g.y_out = (__nv_bfloat16*)tape.x[l];
-    g.yt_out = (__nv_bfloat16*)((char*)tape.x[l] + xsz);
+    g.yt_out = (__nv_bfloat16*)tape.x[l];
     g.status = status;
     if ((st = launch_jet<0>(ma, mb, g, N / 128, (int)(d.n_pad / 128), s, "tc_jet_layer_fwd",
                             2.0 * n * C * (double)d.w[l - 1] * N,
-                            (double)d.n_pad * C * (K * 4 + N * 12))))
+                            (double)d.n_pad * C * (K * 4 + N * 8))))
       return st;
   }
   return NEB_OK;
@@ -812,7 +830,7 @@ int tc_hidden_gram(const neb_net* net, const float* qw, int64_t n, const void* h
   char* part = ws + t.part;
   int* status = (int*)(ws + t.status);
   const int H = d.H;
-  const char* XT = (const char*)hl + a256((size_t)2 * C * d.n_pad * H * 2);
+  const char* XT = (const char*)hl;
   __nv_bfloat16* wht = (__nv_bfloat16*)(ws + t.wht);
   {
     KernelScope ks("tc_weighted_fields", s, 0, 3.0 * H * d.n_pad * 8);
@@ -852,13 +870,13 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
         GMh, GSh, H, gs);
     NEB_LAUNCH_CHECK();
   }
+  // Zbar of the current layer and the next, [2][C][w][n_pad] (points contiguous)
   char* zb[2] = {ws + t.zb0, ws + t.zb1};
-  char* zbt = ws + t.zbt;
   // Gram adjoint + tanh transpose of layer L
   {
     CUtensorMap ma, mb;
-    if ((st = make_map(&ma, tape.x[L], (int64_t)2 * C * d.n_pad, H, 128))) return st;
-    if ((st = make_map(&mb, gs, (int64_t)4 * H, H, 128))) return st;
+    if ((st = make_map(&ma, tape.x[L], (int64_t)2 * C * H, d.n_pad, 64))) return st;
+    if ((st = make_map(&mb, gs, (int64_t)4 * H, H, JetCfg<2>::BN))) return st;
     JetGemmArgs g{};
     g.n_points = (int)n;
     g.n_pad = (int)d.n_pad;
@@ -866,50 +884,46 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
     g.N = H;
     g.zprev = (const float*)tape.z[L];
     g.qw = qw;
-    g.y_out = (__nv_bfloat16*)zb[0];
-    g.yt_out = (__nv_bfloat16*)zbt;
+    g.yt_out = (__nv_bfloat16*)zb[0];
     g.status = status;
     if ((st = launch_jet<2>(ma, mb, g, H / 128, (int)(d.n_pad / 128), s, "tc_gram_adjoint_bwd",
-                            2.0 * 3 * n * (double)H * H, (double)d.n_pad * C * H * 16)))
+                            2.0 * 3 * n * (double)H * H, (double)d.n_pad * C * H * 12)))
       return st;
   }
   int cur = 0;
   for (int l = L; l >= 1; --l) {
     const int out = d.w[l], in = d.w[l - 1], inp = d.wp[l - 1];
-    // weight gradient: gW_l[o][i] = sum_c sum_p Zbar_l[c][p][o] X_{l-1}[c][p][i]
-    size_t xsz = a256((size_t)2 * C * d.n_pad * inp * 2);
-    const char* xt_prev = (const char*)tape.x[l - 1] + xsz;
+    // weight gradient: gW_l[o][i] = sum_c sum_p Zbar_l[c][o][p] X_{l-1}[c][i][p]
+    const char* x_prev = (const char*)tape.x[l - 1];
     int splits = 0;
-    if ((st = launch_rowsum(zbt, C, 0, xt_prev, C, 0, C, out, inp, d.n_pad, (double*)part, status,
-                            s, "tc_weight_grad", 2.0 * C * n * (double)out * in, &splits)))
+    if ((st = launch_rowsum(zb[cur], C, 0, x_prev, C, 0, C, out, inp, d.n_pad, (double*)part,
+                            status, s, "tc_weight_grad", 2.0 * C * n * (double)out * in,
+                            &splits)))
       return st;
     if ((st = reduce((double*)part, splits, out, inp, in, in, false, gW[l - 1], nullptr, s)))
       return st;
     {
-      const int chunk = kBiasChunk;
-      const int chunks = (int)((d.n_pad + chunk - 1) / chunk);
       {
         KernelScope ks("bias_grad", s, 0, (double)d.n_pad * out * 4);
-        bias_partial_tc<<<dim3((out + 127) / 128, chunks), 128, 0, s>>>(
-            (const __nv_bfloat16*)zb[cur], (int)d.n_pad, out, chunk, (double*)partb);
+        bias_rows_tc<<<(out + 7) / 8, 256, 0, s>>>((const __nv_bfloat16*)zb[cur], (int)d.n_pad,
+                                                   out, (double*)partb);
         NEB_LAUNCH_CHECK();
       }
-      if ((st = reduce((double*)partb, chunks, 1, out, out, out, false, gb[l - 1], nullptr, s)))
+      if ((st = reduce((double*)partb, 1, 1, out, out, out, false, gb[l - 1], nullptr, s)))
         return st;
     }
     if (l == 1) break;
     // data gradient through W_l and the tanh transpose of layer l-1
     CUtensorMap ma, mb;
-    if ((st = make_map(&ma, zb[cur], (int64_t)2 * C * d.n_pad, out, 128))) return st;
-    if ((st = make_map(&mb, ws + t.wt[l], (int64_t)2 * in, out, 128))) return st;
+    if ((st = make_map(&ma, zb[cur], (int64_t)2 * C * out, d.n_pad, 64))) return st;
+    if ((st = make_map(&mb, ws + t.wt[l], (int64_t)2 * in, out, JetCfg<1>::BN))) return st;
     JetGemmArgs g{};
     g.n_points = (int)n;
     g.n_pad = (int)d.n_pad;
     g.K = out;
     g.N = in;
     g.zprev = (const float*)tape.z[l - 1];
-    g.y_out = (__nv_bfloat16*)zb[cur ^ 1];
-    g.yt_out = (__nv_bfloat16*)zbt;
+    g.yt_out = (__nv_bfloat16*)zb[cur ^ 1];
     g.status = status;
     if ((st = launch_jet<1>(ma, mb, g, in / 128, (int)(d.n_pad / 128), s,
                             "tc_jet_layer_bwd_data", 2.0 * C * n * (double)out * in,

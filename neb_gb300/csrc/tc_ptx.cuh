@@ -134,11 +134,28 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t smem_addr) {
   return d;
 }
 
-// Instruction descriptor: kind::f16 with bf16 A and B, f32 D, K-major A and B.
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+// Shared-memory matrix descriptor of an MN-major bf16 tile with the 128-byte
+// swizzle: each K row holds 64 MN-contiguous elements (128 bytes, the layout
+// a TMA box {64 MN elements, K rows} with CU_TENSOR_MAP_SWIZZLE_128B writes),
+// 8-row K groups 1024 bytes apart (stride byte offset) and 64-element MN
+// blocks mn_stride bytes apart (leading byte offset).
+__device__ __forceinline__ uint64_t desc_mn_sw128(uint32_t smem_addr, uint32_t mn_stride) {
+  uint64_t d = 0;
+  d |= (uint64_t)((smem_addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((mn_stride >> 4) & 0x3FFF) << 16;  // leading byte offset: MN blocks
+  d |= (uint64_t)((1024 >> 4) & 0x3FFF) << 32;        // stride byte offset: K groups
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor: kind::f16 with bf16 A and B, f32 D, K-major B; A
+// K-major, or MN-major when a_mn (bit 15, transpose A).
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool a_mn = false) {
   return (1u << 4)                         // D = f32
          | (1u << 7)                       // A = bf16
          | (1u << 10)                      // B = bf16
+         | ((a_mn ? 1u : 0u) << 15)        // A major-ness
          | ((uint32_t)(N >> 3) << 17)      // N / 8
          | ((uint32_t)(M >> 4) << 24);     // M / 16
 }
