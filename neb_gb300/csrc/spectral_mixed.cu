@@ -394,16 +394,30 @@ __device__ __forceinline__ float block_sum(float v, float* red) {
 // C: [m][m] FP32 (symmetrised on load).  Outputs: d[m], e[m-1] (FP64 of the
 // FP32 tridiagonal), Vh[m][m] (row k = Householder vector of step k, zero up
 // to index k), tau[m].  Rows are dealt cyclically (row i on CTA i % 8) so
-// every CTA keeps a share of the shrinking trailing matrix.  Per column:
-// push the column and its squared norm, cluster barrier, p = tau A v on own
-// rows and push it, cluster barrier, rank-2 update of own rows, block
-// barrier.  The first entry of v (x1 - alpha) is applied through scalar
-// corrections so no extra barrier is needed to patch it.
+// every CTA keeps a share of the shrinking trailing matrix; eight threads
+// share a row.  Every CTA also keeps a replica of the current pivot row k,
+// so the Householder vector of column k (= row k by symmetry) is formed
+// locally, and one cluster barrier per column suffices:
+//   x = rowk[k+1:], sigma = |x|^2, alpha, tau (block reduction, every CTA);
+//   p_i = tau A_i v on own rows (8-lane reductions); push p_i, per-warp
+//   partial p.v, and (owner of row k+1) row k+1 to every CTA; cluster barrier;
+//   rank-2 update A -= v p^T + w v^T, w = p - tau (p.v) v, of own rows and of
+//   the replica of row k+1, which becomes the next pivot row.
+// Remote stores go through mapa / st.shared::cluster.  v_{k+1} = x1 - alpha
+// is applied through scalar corrections, so vloc holds the raw row.
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+
+__device__ __forceinline__ void st_cluster(float* local_addr, int rank, float v) {
+  uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(local_addr)), ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
+}
+
+constexpr int kTriWarps = kTriThreads / 32;
 
 __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kTriThreads, 1)
 tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
@@ -412,133 +426,135 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
   const int rank = (int)cluster.block_rank();
   const int rb = m / kCluster;  // local rows; global row of local li is li * 8 + rank
   extern __shared__ __align__(16) float sm[];
-  float* Aloc = sm;                              // [rb][m]
-  float* vbuf = Aloc + (size_t)rb * m;           // [2][m]
-  float* pbuf = vbuf + 2 * m;                    // [2][m]
-  float* sig = pbuf + 2 * m;                     // [2][kCluster]
+  float* Aloc = sm;                                  // [rb][m]
+  float* vloc = Aloc + (size_t)rb * m;               // [m] raw pivot row (replica)
+  float* pbuf = vloc + m;                            // [2][m] p, pushed
+  float* nrow = pbuf + 2 * m;                        // [2][m] next pivot row, pushed
+  float* kps = nrow + 2 * m;                         // [2][kCluster * kTriWarps]
+  float* red = kps + 2 * kCluster * kTriWarps;       // [kTriWarps] block reduction
   const int tid = threadIdx.x, nthr = blockDim.x;
-  const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int li = tid >> 3, sub = tid & 7;  // row of this thread, its share of the row
+  const bool has_row = li < rb;
+  const int gi = li * kCluster + rank;     // global row
   const int m4 = m >> 2;
+  const int nslot = kCluster * kTriWarps;
 
-  for (int li = warp; li < rb; li += nwarps) {
-    const int i = li * kCluster + rank;
+  for (int r = warp; r < rb; r += kTriWarps) {
+    const int i = r * kCluster + rank;
     for (int j = lane; j < m; j += 32)
-      Aloc[(size_t)li * m + j] = 0.5f * (C[(size_t)i * m + j] + C[(size_t)j * m + i]);
+      Aloc[(size_t)r * m + j] = 0.5f * (C[(size_t)i * m + j] + C[(size_t)j * m + i]);
   }
-  __syncthreads();
+  for (int j = tid; j < m; j += nthr) vloc[j] = 0.5f * (C[j] + C[(size_t)j * m]);  // row 0
+  cluster.sync();  // every CTA of the cluster runs before remote stores begin
+  float* Ai = Aloc + (size_t)(has_row ? li : 0) * m;
+  float4* Ai4 = reinterpret_cast<float4*>(Ai);
+  const float4* v4 = reinterpret_cast<const float4*>(vloc);
 
   for (int k = 0; k + 2 < m; ++k) {
     const int par = k & 1;
-    float* vb = vbuf + par * m;
     float* pb = pbuf + par * m;
-    float* sg = sig + par * kCluster;
-    // own rows i > k are local indices li >= lo
-    const int lo = (k + 1 - rank + kCluster - 1) / kCluster > 0 ? (k + 1 - rank + kCluster - 1) / kCluster : 0;
-    // (a) push column k of own rows; warp 0 pushes the squared norm
-    for (int li = lo + warp; li < rb; li += nwarps)
-      if (lane < kCluster) {
-        float* rv = cluster.map_shared_rank(vb, lane);
-        rv[li * kCluster + rank] = Aloc[(size_t)li * m + k];
-      }
-    if (warp == 0) {
-      float part = 0.f;
-      for (int li = lo + lane; li < rb; li += 32) {
-        float x = Aloc[(size_t)li * m + k];
-        part += x * x;
-      }
-      part = warp_sum(part);
-      if (lane < kCluster) {
-        float* rs = cluster.map_shared_rank(sg, lane);
-        rs[rank] = part;
-      }
+    float* nr = nrow + par * m;
+    float* kp = kps + par * nslot;
+    // (a) sigma = |rowk[k+1:]|^2 (one element per thread), Householder scalars
+    {
+      const float xj = (tid > k && tid < m) ? vloc[tid] : 0.f;
+      const float part = warp_sum(xj * xj);
+      if (lane == 0) red[warp] = part;
     }
-    cluster.sync();
-    // (b) Householder vector v = x - alpha e_1 (x1 = vb[k + 1] is left unpatched)
-    float sigma = 0.f;
-#pragma unroll
-    for (int c = 0; c < kCluster; ++c) sigma += sg[c];
-    const float x1 = vb[k + 1];
+    __syncthreads();
+    float sigma = lane < kTriWarps ? red[lane] : 0.f;
+    sigma = warp_sum(sigma);
+    const float x1 = vloc[k + 1];
     const float alpha = sigma > 0.f ? -copysignf(sqrtf(sigma), x1) : 0.f;
     const float v1 = x1 - alpha;
     const float vv = sigma - x1 * x1 + v1 * v1;
     const float tau = vv > 0.f ? 2.f / vv : 0.f;
-    if (tid == 0) {
-      if (rank == 0) {
+    if (rank == 0) {
+      if (tid == 0) {
         e_out[k] = alpha;
         tau_out[k] = tau;
+        d_out[k] = vloc[k];
       }
-      if (k % kCluster == rank) d_out[k] = Aloc[(size_t)(k / kCluster) * m + k];
+      for (int j = tid; j < m; j += nthr)
+        Vh[(size_t)k * m + j] = j <= k ? 0.f : (j == k + 1 ? v1 : vloc[j]);
     }
-    for (int li = lo + tid; li < rb; li += nthr) {
-      const int i = li * kCluster + rank;
-      Vh[(size_t)k * m + i] = i == k + 1 ? v1 : vb[i];
-    }
-    if (rank == 0)
-      for (int i = tid; i <= k; i += nthr) Vh[(size_t)k * m + i] = 0.f;
-    // (c) p_i = tau (A_i . v) on own rows (v_{k+1} = x1 - alpha by correction)
+    // (b) p_i = tau (A_i . v) on own rows, 8 threads per row
+    const bool active = has_row && gi > k;
     const int j4 = (k + 1) >> 2;
-    const float4* vb4 = reinterpret_cast<const float4*>(vb);
-    for (int li = lo + warp; li < rb; li += nwarps) {
-      const float* Ai = Aloc + (size_t)li * m;
-      const float4* Ai4 = reinterpret_cast<const float4*>(Ai);
-      float sacc = 0.f;
-      for (int q = j4 + lane; q < m4; q += 32) {
-        float4 a = Ai4[q], v = vb4[q];
+    float pi = 0.f, vi = 0.f, sacc = 0.f;
+    if (active) {
+      for (int q = j4 + sub; q < m4; q += 8) {
+        const float4 a = Ai4[q], v = v4[q];
         const int j = q << 2;
         sacc += (j >= k + 1 ? a.x * v.x : 0.f) + (j + 1 >= k + 1 ? a.y * v.y : 0.f) +
                 (j + 2 >= k + 1 ? a.z * v.z : 0.f) + (j + 3 >= k + 1 ? a.w * v.w : 0.f);
       }
-      sacc = warp_sum(sacc);
-      const float p = tau * (sacc - alpha * Ai[k + 1]);
-      if (lane < kCluster) {
-        float* rp = cluster.map_shared_rank(pb, lane);
-        rp[li * kCluster + rank] = p;
+    }
+    sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
+    sacc += __shfl_xor_sync(0xffffffffu, sacc, 2);
+    sacc += __shfl_xor_sync(0xffffffffu, sacc, 4);
+    if (active) {
+      pi = tau * (sacc - alpha * Ai[k + 1]);
+      vi = gi == k + 1 ? v1 : vloc[gi];
+      st_cluster(pb + gi, sub, pi);
+    }
+    {
+      const float part = warp_sum(sub == 0 ? pi * vi : 0.f);
+      if (lane < kCluster) st_cluster(kp + rank * kTriWarps + warp, lane, part);
+    }
+    // the owner of row k+1 sends it (as it stands before this column's update)
+    if ((k + 1) % kCluster == rank) {
+      const float* r1 = Aloc + (size_t)((k + 1) / kCluster) * m;
+      for (int t = tid; t < (m - k - 1) * kCluster; t += nthr) {
+        const int j = k + 1 + t / kCluster, dst = t % kCluster;
+        st_cluster(nr + j, dst, r1[j]);
       }
     }
     cluster.sync();
-    // (d) 2K = tau p^T v (each warp redundantly), then A -= v p^T + w v^T
-    float kp = 0.f;
+    // (c) K2 = tau p^T v, then A -= v p^T + w v^T on own rows and on row k+1
+    float pv = 0.f;
+    for (int c = lane; c < nslot; c += 32) pv += kp[c];
+    const float K2 = tau * warp_sum(pv);
     const float4* pb4 = reinterpret_cast<const float4*>(pb);
-    for (int q = j4 + lane; q < m4; q += 32) {
-      float4 a = pb4[q], v = vb4[q];
-      const int j = q << 2;
-      kp += (j >= k + 1 ? a.x * v.x : 0.f) + (j + 1 >= k + 1 ? a.y * v.y : 0.f) +
-            (j + 2 >= k + 1 ? a.z * v.z : 0.f) + (j + 3 >= k + 1 ? a.w * v.w : 0.f);
-    }
-    const float K2 = tau * (warp_sum(kp) - alpha * pb[k + 1]);
-    for (int li = lo + warp; li < rb; li += nwarps) {
-      const int i = li * kCluster + rank;
-      float* Ai = Aloc + (size_t)li * m;
-      float4* Ai4 = reinterpret_cast<float4*>(Ai);
-      const float vi = i == k + 1 ? v1 : vb[i];
-      const float pi = pb[i];
+    if (active) {
       const float wi = pi - K2 * vi;
-      for (int q = j4 + lane; q < m4; q += 32) {  // entries j <= k are dead
-        float4 a = Ai4[q], p = pb4[q], v = vb4[q];
+      for (int q = j4 + sub; q < m4; q += 8) {  // entries j <= k are dead
+        float4 a = Ai4[q];
+        const float4 p = pb4[q], v = v4[q];
         a.x -= vi * p.x + wi * v.x;
         a.y -= vi * p.y + wi * v.y;
         a.z -= vi * p.z + wi * v.z;
         a.w -= vi * p.w + wi * v.w;
         Ai4[q] = a;
       }
-      __syncwarp();
-      if (lane == 0) Ai[k + 1] += wi * alpha;  // v_{k+1} = vb[k+1] - alpha
+      // v_{k+1} = vloc[k+1] - alpha; column k+1 lies in chunk j4, which sub 0 updated
+      if (sub == 0) Ai[k + 1] += wi * alpha;
     }
+    // next pivot row: row k+1 updated the same way (v_{k+1} = v1, w_{k+1})
+    const float w1 = pb[k + 1] - K2 * v1;
+    float nv = 0.f;
+    const int j = tid;
+    if (j > k && j < m) {
+      nv = nr[j] - (v1 * pb[j] + w1 * vloc[j]);
+      if (j == k + 1) nv += w1 * alpha;
+    }
+    __syncthreads();  // every thread is done reading vloc for this column
+    if (j > k && j < m) vloc[j] = nv;
     __syncthreads();
   }
-  if (tid == 0) {
-    if ((m - 2) % kCluster == rank) {
-      const float* Ar = Aloc + (size_t)((m - 2) / kCluster) * m;
-      d_out[m - 2] = Ar[m - 2];
-      e_out[m - 2] = Ar[m - 1];
-    }
-    if ((m - 1) % kCluster == rank) d_out[m - 1] = Aloc[(size_t)((m - 1) / kCluster) * m + m - 1];
+  if (tid == 0 && rank == 0) {
+    d_out[m - 2] = vloc[m - 2];
+    e_out[m - 2] = vloc[m - 1];
+    tau_out[m - 2] = 0.f;
+    tau_out[m - 1] = 0.f;
   }
   if (rank == 0)
-    for (int k = m - 2; k < m; ++k) {
-      if (tid == 0) tau_out[k] = 0.f;
+    for (int k = m - 2; k < m; ++k)
       for (int i = tid; i < m; i += nthr) Vh[(size_t)k * m + i] = 0.f;
-    }
+  // d_{m-1}: the last diagonal entry, after the final update of row m-1
+  if (tid == 0 && (m - 1) % kCluster == rank)
+    d_out[m - 1] = Aloc[(size_t)((m - 1) / kCluster) * m + m - 1];
   cluster.sync();
 }
 
@@ -1015,12 +1031,14 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   {
     static bool configured = false;
     const int rb = m / kCluster;
-    const size_t smem = ((size_t)rb * m + 4 * m + 2 * kCluster) * sizeof(float);
+    const size_t smem =
+        ((size_t)rb * m + 5 * m + 2 * kCluster * kTriWarps + kTriWarps) * sizeof(float);
     if (!configured) {
       NEB_CUDA_CHECK(cudaFuncSetAttribute(tridiag_cluster,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(((size_t)kMaxM / kCluster * kMaxM + 4 * kMaxM +
-                                                 2 * kCluster + 64) * sizeof(float))));
+                                          (int)(((size_t)kMaxM / kCluster * kMaxM + 5 * kMaxM +
+                                                 2 * kCluster * kTriWarps + kTriWarps) *
+                                                sizeof(float))));
       configured = true;
     }
     KernelScope ks("spec_tridiag_cluster_fp32", s, 4.0 / 3.0 * m * mm, 8.0 * mm);
