@@ -1,6 +1,7 @@
 // extern "C" entry points of the jet MLP, the Grams and the reverse pass.
 // Precision dispatch: NEB_PREC_FP32 / NEB_PREC_FP64 run the SIMT kernels;
 // NEB_PREC_BF16X3 runs the tcgen05 kernels of tc_path.cu.
+#include <cmath>
 #include <cstdarg>
 #include <cstring>
 #include <mutex>
@@ -817,14 +818,19 @@ extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* con
     else adam_norm<double><<<blocks, 256, 0, s>>>(t, acc, flag);
     NEB_LAUNCH_CHECK();
   }
+  double* scal = (double*)((char*)ws + 128);
   {
-    KernelScope ks("adam_update", s, 0, total * es * 7);
+    KernelScope ks("adam_update", s, 0, total * es * 7, 2);
+    adam_finalize<<<1, 1, 0, s>>>(acc, flag, clip, norm_out, committed_out, scal);
+    NEB_LAUNCH_CHECK();
+    const double step1 = (double)step + 1;
+    const double lr_c1 = lr / (1.0 - std::pow(beta1, step1));
+    const double inv_c2 = 1.0 / (1.0 - std::pow(beta2, step1));
     if (dtype == 0)
-      adam_update<float><<<blocks, 256, 0, s>>>(t, acc, flag, (double)step + 1, lr, clip, beta1,
-                                                beta2, eps, norm_out, committed_out);
+      adam_update<float><<<blocks, 256, 0, s>>>(t, scal, (float)lr_c1, (float)inv_c2,
+                                                (float)beta1, (float)beta2, (float)eps);
     else
-      adam_update<double><<<blocks, 256, 0, s>>>(t, acc, flag, (double)step + 1, lr, clip, beta1,
-                                                 beta2, eps, norm_out, committed_out);
+      adam_update<double><<<blocks, 256, 0, s>>>(t, scal, lr_c1, inv_c2, beta1, beta2, eps);
     NEB_LAUNCH_CHECK();
   }
   return NEB_OK;

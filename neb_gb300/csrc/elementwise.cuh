@@ -28,7 +28,18 @@ __global__ void features_kernel(int kind, int n_freq, double period, FeaturePara
     double w = 2.0 * 3.14159265358979323846 * k / period;
     double s = pts[p * 2 + axis];
     double sn, cs;
-    sincos(w * s, &sn, &cs);
+    if constexpr (sizeof(T) == 4) {
+      // FP32 outputs: reduce the phase to [-pi, pi] in FP64 (three FP64
+      // operations), then the FP32 sine and cosine
+      const double a = w * s;
+      const double red = fma(-rint(a * 0.15915494309189535), 6.283185307179586, a);
+      float sf, cf;
+      sincosf((float)red, &sf, &cf);
+      sn = sf;
+      cs = cf;
+    } else {
+      sincos(w * s, &sn, &cs);
+    }
     double v = (r & 1) ? cs : sn;
     out[0] = v;
     out[1 + axis] = (r & 1) ? -w * sn : w * cs;
@@ -95,21 +106,28 @@ __global__ void adam_norm(AdamTable t, double* __restrict__ acc, int* __restrict
   }
 }
 
-// Masked Adam update: commits only when the gradients are finite and the
-// global norm positive (the transaction of hardcoded_backend.py:2184-2277).
-template <typename T>
-__global__ void adam_update(AdamTable t, const double* __restrict__ acc, const int* __restrict__ flag,
-                            double step1, double lr, double clip, double b1, double b2, double eps,
-                            double* __restrict__ norm_out, int* __restrict__ committed_out) {
+// The transaction's scalars, once: global norm, commit decision (finite
+// gradients and a positive norm, hardcoded_backend.py:2184-2277) and the clip
+// scale min(1, clip / norm); scal[0] = 0 means "do not commit".
+static __global__ void adam_finalize(const double* __restrict__ acc, const int* __restrict__ flag,
+                              double clip, double* __restrict__ norm_out,
+                              int* __restrict__ committed_out, double* __restrict__ scal) {
   const double norm = sqrt(acc[0]);
   const bool ok = (flag[0] == 0) && isfinite(norm) && norm > 0.0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (norm_out) *norm_out = norm;
-    if (committed_out) *committed_out = ok ? 1 : 0;
-  }
-  if (!ok) return;
-  const double scale = fmin(1.0, clip / fmax(norm, 1e-30));
-  const double c1 = 1.0 - pow(b1, step1), c2 = 1.0 - pow(b2, step1);
+  if (norm_out) *norm_out = norm;
+  if (committed_out) *committed_out = ok ? 1 : 0;
+  scal[0] = ok ? fmin(1.0, clip / fmax(norm, 1e-30)) : 0.0;
+}
+
+// Masked Adam update with the scalars of adam_finalize; lr_c1 = lr / (1 -
+// beta1^step), inv_c2 = 1 / (1 - beta2^step) come from the host, so no
+// per-element double-precision work remains for the FP32 form.
+template <typename T>
+__global__ void adam_update(AdamTable t, const double* __restrict__ scal, T lr_c1, T inv_c2,
+                            T b1, T b2, T eps) {
+  const double sc = scal[0];
+  if (sc == 0.0) return;
+  const T scale = (T)sc, ob1 = T(1) - b1, ob2 = T(1) - b2;
   const int64_t total = t.off[t.n];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -118,12 +136,12 @@ __global__ void adam_update(AdamTable t, const double* __restrict__ acc, const i
     T* p = static_cast<T*>(t.p[k]);
     T* m = static_cast<T*>(t.m[k]);
     T* v = static_cast<T*>(t.v[k]);
-    T g = static_cast<const T*>(t.g[k])[j] * (T)scale;
-    T mn = (T)b1 * m[j] + (T)(1.0 - b1) * g;
-    T vn = (T)b2 * v[j] + (T)(1.0 - b2) * g * g;
+    T g = static_cast<const T*>(t.g[k])[j] * scale;
+    T mn = b1 * m[j] + ob1 * g;
+    T vn = b2 * v[j] + ob2 * g * g;
     m[j] = mn;
     v[j] = vn;
-    p[j] -= (T)lr * (mn / (T)c1) / (sqrt(vn / (T)c2) + (T)eps);
+    p[j] -= lr_c1 * mn / (sqrt(vn * inv_c2) + eps);
   }
 }
 

@@ -580,28 +580,43 @@ __global__ void reduce_parts(const double* __restrict__ part, int splits, int M,
 }
 
 // Bias gradient: gb[o] = sum over points of the value plane of Zbar (hi +
-// lo), Zbar in [2][C][N][n_pad] (points contiguous): one warp per output,
-// 16-byte loads, FP32 sums of 8-point groups accumulated in FP64.
-__global__ void bias_rows_tc(const __nv_bfloat16* __restrict__ zb, int n_pad, int N,
-                             double* __restrict__ out) {
-  const int o = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (o >= N) return;
-  const size_t plane = (size_t)C * N * n_pad;
-  const uint4* hi = reinterpret_cast<const uint4*>(zb + (size_t)o * n_pad);
-  const uint4* lo = reinterpret_cast<const uint4*>(zb + plane + (size_t)o * n_pad);
+// lo), Zbar in [2][C][N][n_pad] (points contiguous).  A 256-thread block
+// takes two outputs, four warps each over a quarter of the points (16-byte
+// loads, FP32 sums of 8-point groups accumulated in FP64), combined in
+// shared memory.
+__global__ void __launch_bounds__(256) bias_rows_tc(const __nv_bfloat16* __restrict__ zb,
+                                                   int n_pad, int N, double* __restrict__ out) {
+  __shared__ double part[8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int o = blockIdx.x * 2 + (warp >> 2), quarter = warp & 3;
   double acc = 0.0;
-  for (int v = lane; v < n_pad / 8; v += 32) {
-    const uint4 a = hi[v], b = lo[v];
-    const __nv_bfloat16* ha = reinterpret_cast<const __nv_bfloat16*>(&a);
-    const __nv_bfloat16* lb = reinterpret_cast<const __nv_bfloat16*>(&b);
-    float s8 = 0.f;
+  if (o < N) {
+    const size_t plane = (size_t)C * N * n_pad;
+    const uint4* hi = reinterpret_cast<const uint4*>(zb + (size_t)o * n_pad);
+    const uint4* lo = reinterpret_cast<const uint4*>(zb + plane + (size_t)o * n_pad);
+    const int nv = n_pad / 8, per = (nv + 3) / 4;
+    const int v0 = quarter * per, v1 = min(nv, v0 + per);
+    for (int v = v0 + lane; v < v1; v += 32) {
+      const uint4 a = hi[v], b = lo[v];
+      const __nv_bfloat16* ha = reinterpret_cast<const __nv_bfloat16*>(&a);
+      const __nv_bfloat16* lb = reinterpret_cast<const __nv_bfloat16*>(&b);
+      float s8 = 0.f;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) s8 += __bfloat162float(ha[t]) + __bfloat162float(lb[t]);
-    acc += (double)s8;
+      for (int t = 0; t < 8; ++t) s8 += __bfloat162float(ha[t]) + __bfloat162float(lb[t]);
+      acc += (double)s8;
+    }
   }
 #pragma unroll
   for (int sh = 16; sh > 0; sh >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, sh);
-  if (lane == 0) out[o] = acc;
+  if (lane == 0) part[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    const int oo = blockIdx.x * 2 + threadIdx.x;
+    if (oo < N) {
+      const double* q = part + threadIdx.x * 4;
+      out[oo] = (q[0] + q[1]) + (q[2] + q[3]);
+    }
+  }
 }
 
 // ---------------------------------------------------------- host helpers
@@ -905,7 +920,7 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
     {
       {
         KernelScope ks("bias_grad", s, 0, (double)d.n_pad * out * 4);
-        bias_rows_tc<<<(out + 7) / 8, 256, 0, s>>>((const __nv_bfloat16*)zb[cur], (int)d.n_pad,
+        bias_rows_tc<<<(out + 1) / 2, 256, 0, s>>>((const __nv_bfloat16*)zb[cur], (int)d.n_pad,
                                                    out, (double*)partb);
         NEB_LAUNCH_CHECK();
       }
