@@ -119,6 +119,14 @@ __device__ __forceinline__ df df_shfl_xor(df x, int o) {
   return {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
 }
 
+// FP64 -> float pairs (the Cholesky works on float pairs in memory, so its
+// per-panel kernels do no FP64 conversions).
+__global__ void to_df(const double* __restrict__ a, df* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    b[i] = df_from(a[i]);
+}
+
 // ------------------------------------------------------------ Cholesky
 // Blocked right-looking Cholesky of the FP64 matrix A, 32 x 32 tiles,
 // compensated FP32 arithmetic, one launch per panel.  chol_step(p) has one
@@ -189,26 +197,24 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
   }
 }
 
-__global__ void __launch_bounds__(1024) chol_first(const double* __restrict__ A, int m,
-                                                   double* __restrict__ Lw,
-                                                   double* __restrict__ linv_pp,
+__global__ void __launch_bounds__(1024) chol_first(const df* __restrict__ A, int m,
+                                                   df* __restrict__ Lw, df* __restrict__ linv_pp,
                                                    int* __restrict__ info) {
   __shared__ df a[kCB][kCB + 1], L[kCB][kCB + 1], X[kCB][kCB + 1], Tm[kCB][kCB + 1];
   __shared__ df rinv[kCB];
   __shared__ int bad;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  a[ty][tx] = df_from(A[(size_t)ty * m + tx]);
+  a[ty][tx] = A[(size_t)ty * m + tx];
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   tile_factor(a, L, X, Tm, rinv, &bad);
-  Lw[(size_t)ty * m + tx] = df_to(L[ty][tx]);
-  linv_pp[ty * kCB + tx] = df_to(X[ty][tx]);
+  Lw[(size_t)ty * m + tx] = L[ty][tx];
+  linv_pp[ty * kCB + tx] = X[ty][tx];
   if (threadIdx.x == 0 && bad && *info == 0) *info = m + bad;
 }
 
-__global__ void __launch_bounds__(1024) chol_step(double* __restrict__ A, int m, int p,
-                                                  double* __restrict__ Lw,
-                                                  double* __restrict__ linv_pp,
+__global__ void __launch_bounds__(1024) chol_step(df* __restrict__ A, int m, int p,
+                                                  df* __restrict__ Lw, df* __restrict__ linv_pp,
                                                   int* __restrict__ info) {
   __shared__ df xi[kCB][kCB + 1];  // L_pp^-1, later L of the next diagonal tile
   __shared__ df li[kCB][kCB + 1];  // A_ip, then L_ip
@@ -224,10 +230,10 @@ __global__ void __launch_bounds__(1024) chol_step(double* __restrict__ A, int m,
   const int bj = p + 1 + t;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int cb = p * kCB;
-  xi[ty][tx] = df_from(linv_pp[(size_t)p * kCB * kCB + ty * kCB + tx]);
-  const df aip = df_from(A[(size_t)(bi * kCB + ty) * m + cb + tx]);
-  const df ajp = bj == bi ? aip : df_from(A[(size_t)(bj * kCB + ty) * m + cb + tx]);
-  const df aij = df_from(A[(size_t)(bi * kCB + ty) * m + bj * kCB + tx]);
+  xi[ty][tx] = linv_pp[(size_t)p * kCB * kCB + ty * kCB + tx];
+  const df aip = A[(size_t)(bi * kCB + ty) * m + cb + tx];
+  const df ajp = bj == bi ? aip : A[(size_t)(bj * kCB + ty) * m + cb + tx];
+  const df aij = A[(size_t)(bi * kCB + ty) * m + bj * kCB + tx];
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   // L_ip[r][c] = sum_k A_ip[r][k] X[c][k] (X lower: k <= c)
@@ -241,7 +247,7 @@ __global__ void __launch_bounds__(1024) chol_step(double* __restrict__ A, int m,
   __syncthreads();
   li[ty][tx] = s0;
   lj[ty][tx] = bj != bi ? s1 : s0;
-  if (bj == p + 1) Lw[(size_t)(bi * kCB + ty) * m + cb + tx] = df_to(s0);
+  if (bj == p + 1) Lw[(size_t)(bi * kCB + ty) * m + cb + tx] = s0;
   __syncthreads();
   df u0{0.f, 0.f}, u1{0.f, 0.f};
 #pragma unroll
@@ -251,7 +257,7 @@ __global__ void __launch_bounds__(1024) chol_step(double* __restrict__ A, int m,
   }
   const df upd = df_add(aij, df_neg(df_add(u0, u1)));
   if (!(bi == p + 1 && bj == p + 1)) {
-    A[(size_t)(bi * kCB + ty) * m + bj * kCB + tx] = df_to(upd);
+    A[(size_t)(bi * kCB + ty) * m + bj * kCB + tx] = upd;
     return;
   }
   // the next diagonal tile: factor and invert it here
@@ -259,20 +265,20 @@ __global__ void __launch_bounds__(1024) chol_step(double* __restrict__ A, int m,
   __syncthreads();
   tile_factor(tl, xi, li, lj, rinv, &bad);
   const int r0 = (p + 1) * kCB;
-  Lw[(size_t)(r0 + ty) * m + r0 + tx] = df_to(xi[ty][tx]);
-  linv_pp[(size_t)(p + 1) * kCB * kCB + ty * kCB + tx] = df_to(li[ty][tx]);
+  Lw[(size_t)(r0 + ty) * m + r0 + tx] = xi[ty][tx];
+  linv_pp[(size_t)(p + 1) * kCB * kCB + ty * kCB + tx] = li[ty][tx];
   if (threadIdx.x == 0 && bad && *info == 0) *info = m + r0 + bad;
 }
 
 // The lower factor as float pairs, and its transpose (so both solves read
 // rows): Ld[i][j] = L[i][j] (j <= i, else 0), LTd[j][i] = L[i][j].
-__global__ void split_factor(const double* __restrict__ L, int m, df* __restrict__ Ld,
+__global__ void split_factor(const df* __restrict__ L, int m, df* __restrict__ Ld,
                              df* __restrict__ LTd) {
   __shared__ df t[32][33];
   const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
   for (int r = threadIdx.y; r < 32; r += blockDim.y) {
     const int i = by + r, j = bx + threadIdx.x;
-    df v = i >= j ? df_from(L[(size_t)i * m + j]) : df{0.f, 0.f};
+    df v = i >= j ? L[(size_t)i * m + j] : df{0.f, 0.f};
     Ld[(size_t)i * m + j] = v;
     t[r][threadIdx.x] = v;
   }
@@ -283,11 +289,11 @@ __global__ void split_factor(const double* __restrict__ L, int m, df* __restrict
 
 // Inverses of the 32 x 32 diagonal blocks of L as float pairs, for both
 // solves: DL[b] = L_bb^-1 (lower), DU[b] = (L_bb^-1)^T = (L^T)_bb^-1 (upper).
-__global__ void __launch_bounds__(1024) split_dinv(const double* __restrict__ linv_pp,
+__global__ void __launch_bounds__(1024) split_dinv(const df* __restrict__ linv_pp,
                                                    df* __restrict__ DL, df* __restrict__ DU) {
   const int b = blockIdx.x, r = threadIdx.x >> 5, c = threadIdx.x & 31;
   const size_t base = (size_t)b * kCB * kCB;
-  const df v = df_from(linv_pp[base + r * kCB + c]);
+  const df v = linv_pp[base + r * kCB + c];
   DL[base + r * kCB + c] = v;
   DU[base + c * kCB + r] = v;
 }
@@ -963,9 +969,9 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   }
   cudaStream_t s = (cudaStream_t)stream_;
   char* ws = (char*)workspace;
-  double* Mw = (double*)(ws + w.Mw);
-  double* Lw = (double*)(ws + w.Lw);
-  double* linv_pp = (double*)(ws + w.linv_pp);
+  df* Mw = (df*)(ws + w.Mw);  // working copy of M, float pairs
+  df* Lw = (df*)(ws + w.Lw);  // Cholesky factor (lower tiles), float pairs
+  df* linv_pp = (df*)(ws + w.linv_pp);
   df* Ld = (df*)(ws + w.LT);
   df* LTd = Ld + (size_t)m * m;
   double* Y = (double*)(ws + w.Y);
@@ -984,9 +990,10 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   const int nb = m / kCB;
 
   NEB_CUDA_CHECK(cudaMemsetAsync(info, 0, sizeof(int), s));
-  NEB_CUDA_CHECK(cudaMemcpyAsync(Mw, M, mm * 8, cudaMemcpyDeviceToDevice, s));
   {
-    KernelScope ks("spec_cholesky_df", s, (double)m * m * m / 3.0, 16.0 * mm, nb);
+    KernelScope ks("spec_cholesky_df", s, (double)m * m * m / 3.0, 16.0 * mm, nb + 1);
+    to_df<<<(int)std::min<size_t>((mm + 255) / 256, 1024), 256, 0, s>>>(M, Mw, mm);
+    NEB_LAUNCH_CHECK();
     chol_first<<<1, 1024, 0, s>>>(Mw, m, Lw, linv_pp, info);
     NEB_LAUNCH_CHECK();
     for (int p = 0; p + 1 < nb; ++p) {
