@@ -350,7 +350,7 @@ struct RowsumArgs {
   int M, N, n_pad, n_ch, a_ch0, b_ch0, aC, bC, splits, ldp;
   int lo_lo;  // also accumulate A_lo B_lo: the Grams need it (without it the
               // missing product acts as a systematic negative ridge)
-  double* part;
+  float* part;  // FP32 chunk-group partials, combined with compensation by reduce_parts
   int* status;
 };
 
@@ -473,10 +473,10 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
       tc::tc_fence_before();
       tc::mbar_arrive(&acc_free[buf]);
     }
-    double* out = g.part + ((size_t)blockIdx.y * g.M + m) * g.ldp + n0 + h * HB;
+    float* out = g.part + ((size_t)blockIdx.y * g.M + m) * g.ldp + n0 + h * HB;
 #pragma unroll
-    for (int j = 0; j < HB; j += 2)
-      *reinterpret_cast<double2*>(out + j) = make_double2(sum[j], sum[j + 1]);
+    for (int j = 0; j < HB; j += 4)
+      *reinterpret_cast<float4*>(out + j) = make_float4(sum[j], sum[j + 1], sum[j + 2], sum[j + 3]);
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -560,22 +560,34 @@ __global__ void weighted_fields_t(const __nv_bfloat16* __restrict__ XT, const fl
   }
 }
 
-// out[m * ldo + j] = sum_z part[(z * M + m) * ldp + j] for j < ncols.
-__global__ void reduce_parts(const double* __restrict__ part, int splits, int M, int ldp, int ncols,
+// out[m * ldo + j] = sum_z part[(z * M + m) * ldp + j] for j < ncols: the
+// FP32 partials are summed with an error term (TwoSum), so the sum keeps
+// about twice FP32 precision without double-precision arithmetic; sym
+// averages the sum with its transpose.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = hi + x, bb = s - hi;
+  lo += (hi - (s - bb)) + (x - bb);
+  hi = s;
+}
+
+__global__ void reduce_parts(const float* __restrict__ part, int splits, int M, int ldp, int ncols,
                              int ldo, int sym, float* __restrict__ outf, double* __restrict__ outd) {
   const size_t total = (size_t)M * ncols;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     int m = (int)(i / ncols), j = (int)(i % ncols);
-    double s = 0.0;
-    for (int z = 0; z < splits; ++z) s += part[((size_t)z * M + m) * ldp + j];
+    float hi = 0.f, lo = 0.f;
+    for (int z = 0; z < splits; ++z) two_sum_acc(hi, lo, part[((size_t)z * M + m) * ldp + j]);
     if (sym) {
-      double t = 0.0;
-      for (int z = 0; z < splits; ++z) t += part[((size_t)z * M + j) * ldp + m];
-      s = 0.5 * (s + t);
+      float th = 0.f, tl = 0.f;
+      for (int z = 0; z < splits; ++z) two_sum_acc(th, tl, part[((size_t)z * M + j) * ldp + m]);
+      two_sum_acc(hi, lo, th);
+      lo += tl;
+      hi *= 0.5f;
+      lo *= 0.5f;
     }
-    if (outf) outf[(size_t)m * ldo + j] = (float)s;
-    if (outd) outd[(size_t)m * ldo + j] = s;
+    if (outf) outf[(size_t)m * ldo + j] = hi + lo;
+    if (outd) outd[(size_t)m * ldo + j] = (double)hi + (double)lo;
   }
 }
 
@@ -585,7 +597,7 @@ __global__ void reduce_parts(const double* __restrict__ part, int splits, int M,
 // loads, FP32 sums of 8-point groups accumulated in FP64), combined in
 // shared memory.
 __global__ void __launch_bounds__(256) bias_rows_tc(const __nv_bfloat16* __restrict__ zb,
-                                                   int n_pad, int N, double* __restrict__ out) {
+                                                   int n_pad, int N, float* __restrict__ out) {
   __shared__ double part[8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int o = blockIdx.x * 2 + (warp >> 2), quarter = warp & 3;
@@ -614,7 +626,7 @@ __global__ void __launch_bounds__(256) bias_rows_tc(const __nv_bfloat16* __restr
     const int oo = blockIdx.x * 2 + threadIdx.x;
     if (oo < N) {
       const double* q = part + threadIdx.x * 4;
-      out[oo] = (q[0] + q[1]) + (q[2] + q[3]);
+      out[oo] = (float)((q[0] + q[1]) + (q[2] + q[3]));
     }
   }
 }
@@ -728,7 +740,7 @@ int launch_rowsum_bn(const CUtensorMap& A, const CUtensorMap& B, RowsumArgs g, c
 }
 
 int launch_rowsum(const void* a_base, int aC, int a_ch0, const void* b_base, int bC, int b_ch0,
-                  int n_ch, int M, int N, int64_t n_pad, double* part, int* status,
+                  int n_ch, int M, int N, int64_t n_pad, float* part, int* status,
                   cudaStream_t s, const char* name, double flops, int* splits_out,
                   bool lo_lo = false) {
   NEB_REQUIRE(M % 128 == 0, "tensor-core rowsum: M = %d must be a multiple of 128", M);
@@ -751,9 +763,9 @@ int launch_rowsum(const void* a_base, int aC, int a_ch0, const void* b_base, int
   return launch_rowsum_bn<64>(ma, mb, g, s, name, flops, bytes);
 }
 
-int reduce(const double* part, int splits, int M, int ldp, int ncols, int ldo, bool sym,
+int reduce(const float* part, int splits, int M, int ldp, int ncols, int ldo, bool sym,
            float* outf, double* outd, cudaStream_t s) {
-  KernelScope ks("reduce_chunks", s, 0, (double)splits * M * ncols * 8);
+  KernelScope ks("reduce_chunks", s, 0, (double)splits * M * ncols * 4);
   size_t total = (size_t)M * ncols;
   int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
   reduce_parts<<<blocks, 256, 0, s>>>(part, splits, M, ldp, ncols, ldo, sym ? 1 : 0, outf, outd);
@@ -857,14 +869,14 @@ int tc_hidden_gram(const neb_net* net, const float* qw, int64_t n, const void* h
   }
   int splits = 0;
   // A_M: channels (d/dx, d/dy) = wHT channels 0, 1 against XT channels 1, 2
-  if ((st = launch_rowsum(wht, 3, 0, XT, C, 1, 2, H, H, d.n_pad, (double*)part, status, s,
+  if ((st = launch_rowsum(wht, 3, 0, XT, C, 1, 2, H, H, d.n_pad, (float*)part, status, s,
                           "tc_gram", 2.0 * 2 * n * (double)H * H, &splits, true)))
     return st;
-  if ((st = reduce((double*)part, splits, H, H, H, H, true, nullptr, AM, s))) return st;
-  if ((st = launch_rowsum(wht, 3, 2, XT, C, 3, 1, H, H, d.n_pad, (double*)part, status, s,
+  if ((st = reduce((float*)part, splits, H, H, H, H, true, nullptr, AM, s))) return st;
+  if ((st = launch_rowsum(wht, 3, 2, XT, C, 3, 1, H, H, d.n_pad, (float*)part, status, s,
                           "tc_gram", 2.0 * n * (double)H * H, &splits, true)))
     return st;
-  return reduce((double*)part, splits, H, H, H, H, true, nullptr, AS, s);
+  return reduce((float*)part, splits, H, H, H, H, true, nullptr, AS, s);
 }
 
 int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh, const float* qw,
@@ -875,7 +887,6 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
   Dims d = dims_of(net, n);
   TcWs t = tc_ws(d);
   char* part = ws + t.part;
-  char* partb = ws + t.partb;
   int* status = (int*)(ws + t.status);
   const int L = d.L, H = d.H;
   __nv_bfloat16* gs = (__nv_bfloat16*)(ws + t.gsplit);
@@ -911,21 +922,19 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
     // weight gradient: gW_l[o][i] = sum_c sum_p Zbar_l[c][o][p] X_{l-1}[c][i][p]
     const char* x_prev = (const char*)tape.x[l - 1];
     int splits = 0;
-    if ((st = launch_rowsum(zb[cur], C, 0, x_prev, C, 0, C, out, inp, d.n_pad, (double*)part,
+    if ((st = launch_rowsum(zb[cur], C, 0, x_prev, C, 0, C, out, inp, d.n_pad, (float*)part,
                             status, s, "tc_weight_grad", 2.0 * C * n * (double)out * in,
                             &splits)))
       return st;
-    if ((st = reduce((double*)part, splits, out, inp, in, in, false, gW[l - 1], nullptr, s)))
+    if ((st = reduce((float*)part, splits, out, inp, in, in, false, gW[l - 1], nullptr, s)))
       return st;
     {
       {
         KernelScope ks("bias_grad", s, 0, (double)d.n_pad * out * 4);
         bias_rows_tc<<<(out + 1) / 2, 256, 0, s>>>((const __nv_bfloat16*)zb[cur], (int)d.n_pad,
-                                                   out, (double*)partb);
+                                                   out, gb[l - 1]);
         NEB_LAUNCH_CHECK();
       }
-      if ((st = reduce((double*)partb, 1, 1, out, out, out, false, gb[l - 1], nullptr, s)))
-        return st;
     }
     if (l == 1) break;
     // data gradient through W_l and the tanh transpose of layer l-1
