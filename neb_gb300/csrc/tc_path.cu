@@ -244,30 +244,53 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
       const int p = p0 + row;
       const int buf = it & 1;
-      tc::mbar_wait(&acc_full[buf], (it >> 1) & 1, g.status);
-      tc::tc_fence_after();
       float w2 = 0.f;
       if constexpr (EPI == 2) w2 = p < g.n_points ? 2.f * g.qw[p] : 0.f;
       for (int jc = 0; jc < 2; ++jc) {
         const int j0 = half * 32 + jc * 16;
-        float acc[NCH][16];
+        const int col = n0 + j0;
+        // global operands first (bias, or the pre-activations of the target
+        // layer), so their latency overlaps the accumulator wait and loads
+        float out[C][16];
+        float bias16[16];
+        if constexpr (EPI == 0) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) bias16[j] = __ldg(g.bias + col + j);
+        } else {
+#pragma unroll
+          for (int c = 0; c < C; ++c)
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              out[c][j] = __ldg(g.zprev + ((size_t)c * g.N + col + j) * g.n_pad + p);
+        }
+        if (jc == 0) {
+          tc::mbar_wait(&acc_full[buf], (it >> 1) & 1, g.status);
+          tc::tc_fence_after();
+        }
+        uint32_t raw[NCH][16];
 #pragma unroll
         for (int ci = 0; ci < NCH; ++ci)
-          tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * Cfg::TBUF + ci * BN + j0,
-                        acc[ci]);
+          tc::tmem_ld16_issue(tmem + ((uint32_t)(q * 32) << 16) + buf * Cfg::TBUF + ci * BN + j0,
+                              raw[ci]);
+        tc::tmem_ld_wait();
+        float acc[NCH][16];
+#pragma unroll
+        for (int ci = 0; ci < NCH; ++ci) {
+          tc::tmem_ld_fence(raw[ci]);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) acc[ci][j] = __uint_as_float(raw[ci][j]);
+        }
         if (jc == 1) {  // this warp's columns of the buffer are drained
           tc::tc_fence_before();
           __syncwarp();
           if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
         }
-        const int col = n0 + j0;
-        float out[C][16];
         if constexpr (EPI == 0) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
 #pragma unroll
             for (int c = 0; c < C; ++c) out[c][j] = acc[c][j];
-            out[0][j] += g.bias[col + j];
+            out[0][j] += bias16[j];
           }
 #pragma unroll
           for (int c = 0; c < C; ++c)
@@ -284,11 +307,6 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             for (int c = 0; c < C; ++c) out[c][j] = v[c];
           }
         } else {
-#pragma unroll
-          for (int c = 0; c < C; ++c)
-#pragma unroll
-            for (int j = 0; j < 16; ++j)
-              out[c][j] = g.zprev[((size_t)c * g.N + col + j) * g.n_pad + p];
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             float z[C], v[C];
@@ -463,12 +481,17 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
       const int buf = it & 1;
       tc::mbar_wait(&acc_ready[buf], (it >> 1) & 1, g.status);
       tc::tc_fence_after();
+      uint32_t raw[HB / 16][16];
 #pragma unroll
-      for (int j0 = 0; j0 < HB; j0 += 16) {
-        float v[16];
-        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * BN + h * HB + j0, v);
+      for (int c16 = 0; c16 < HB / 16; ++c16)
+        tc::tmem_ld16_issue(tmem + ((uint32_t)(q * 32) << 16) + buf * BN + h * HB + c16 * 16,
+                            raw[c16]);
+      tc::tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 16; ++j) sum[j0 + j] += v[j];
+      for (int c16 = 0; c16 < HB / 16; ++c16) {
+        tc::tmem_ld_fence(raw[c16]);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sum[c16 * 16 + j] += __uint_as_float(raw[c16][j]);
       }
       tc::tc_fence_before();
       tc::mbar_arrive(&acc_free[buf]);
