@@ -96,24 +96,30 @@ struct JetGemmArgs {
 };
 
 template <int EPI> struct JetCfg {
-  static constexpr int BN = 64;                  // output columns per tile
+  // output columns per tile: 128 for the layer GEMMs (single accumulator
+  // buffer, wider MMAs); 64 for the Gram adjoint (three channels, so two
+  // buffers fit and its epilogue overlaps the next tile's MMAs)
+  static constexpr int BN = EPI == 2 ? 64 : 128;
   static constexpr int NB = EPI == 2 ? 2 : 1;    // distinct B matrices
   static constexpr int NCH = EPI == 2 ? 3 : 4;   // accumulated channels
   static constexpr int CH0 = EPI == 2 ? 1 : 0;
-  static constexpr int A_ST = EPI == 2 ? 3 : 4;
+  // accumulator buffers in the 512 TMEM columns (double-buffered when they fit)
+  static constexpr int NBUF = 2 * NCH * BN <= 512 ? 2 : 1;
+  static constexpr int TBUF = 512 / NBUF;        // TMEM columns per accumulator buffer
+  static constexpr int A_ST = 3;
   static constexpr int B_ST = 2;
-  static constexpr int B_TILE = BN * 128;        // 64 rows x 64 bf16
+  static constexpr int B_TILE = BN * 128;        // BN rows x 64 bf16
   static constexpr int B_BYTES = 2 * NB * B_TILE;
   static constexpr int STAGE = 8 * 8192;         // epilogue transpose staging, 8 warps
   static constexpr int SMEM = 1024 + A_ST * 2 * kTileBytes + B_ST * B_BYTES + STAGE + 256;
-  static constexpr int TBUF = 256;               // TMEM columns per accumulator buffer
 };
 
 
-// Persistent tcgen05 jet GEMM: tiles of 128 points x 64 outputs (all jet
-// channels) are dealt round-robin to the CTAs (one per SM); the accumulators
-// are double-buffered in tensor memory (2 x 256 columns), so the epilogue of
-// one tile overlaps the MMAs of the next.  Roles: warp 0 lane 0 issues TMA
+// Persistent tcgen05 jet GEMM: tiles of 128 points x BN outputs (all jet
+// channels) are dealt round-robin to the CTAs (one per SM).  The producer
+// keeps loading operand stages across tile boundaries; the accumulators are
+// double-buffered in tensor memory when 2 x NCH x BN columns fit in 512, so
+// the epilogue of one tile can overlap the MMAs of the next.  Roles: warp 0 lane 0 issues TMA
 // loads, warp 1 lane 0 issues MMAs, warps 2-9 run the epilogue (lane quarter
 // w % 4, column half (w - 2) / 4).
 template <int EPI>
@@ -197,8 +203,8 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     constexpr uint32_t idesc = tc::idesc_bf16(128, BN, true);
     int ai = 0, bi = 0, it = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
-      const int buf = it & 1;
-      tc::mbar_wait(&acc_empty[buf], ((it >> 1) & 1) ^ 1, g.status);
+      const int buf = it % Cfg::NBUF, use = it / Cfg::NBUF;
+      tc::mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status);
       tc::tc_fence_after();
       for (int kc = 0; kc < KC; ++kc, ++bi) {
         const int bs = bi % B_ST;
@@ -243,11 +249,12 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
       const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
       const int p = p0 + row;
-      const int buf = it & 1;
+      const int buf = it % Cfg::NBUF, use = it / Cfg::NBUF;
       float w2 = 0.f;
       if constexpr (EPI == 2) w2 = p < g.n_points ? 2.f * g.qw[p] : 0.f;
-      for (int jc = 0; jc < 2; ++jc) {
-        const int j0 = half * 32 + jc * 16;
+      constexpr int kChunks = BN / 32;  // 16-column chunks of this warp's half
+      for (int jc = 0; jc < kChunks; ++jc) {
+        const int j0 = half * (BN / 2) + jc * 16;
         const int col = n0 + j0;
         // global operands first (bias, or the pre-activations of the target
         // layer), so their latency overlaps the accumulator wait and loads
@@ -264,7 +271,7 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
               out[c][j] = __ldg(g.zprev + ((size_t)c * g.N + col + j) * g.n_pad + p);
         }
         if (jc == 0) {
-          tc::mbar_wait(&acc_full[buf], (it >> 1) & 1, g.status);
+          tc::mbar_wait(&acc_full[buf], use & 1, g.status);
           tc::tc_fence_after();
         }
         uint32_t raw[NCH][16];
@@ -280,7 +287,7 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 #pragma unroll
           for (int j = 0; j < 16; ++j) acc[ci][j] = __uint_as_float(raw[ci][j]);
         }
-        if (jc == 1) {  // this warp's columns of the buffer are drained
+        if (jc == kChunks - 1) {  // this warp's columns of the buffer are drained
           tc::tc_fence_before();
           __syncwarp();
           if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
