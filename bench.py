@@ -138,6 +138,28 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# ------------------------------------------------------------- replicas
+# N GPUs run N independent replicas of the step (the path has no exchange
+# without an all-reduce of the Grams): each rank draws its own point batches,
+# times its own steps, and rank 0 reports the whole job from the slowest rank.
+def replica_seed(base_seed: int, rank: int) -> int:
+    return base_seed + 1000 * rank
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_steps_per_s(world: int, steps: int, ms_max: float) -> float:
+    return world * steps / (ms_max / 1e3)
+
+
 def cpu_threads():
     return os.cpu_count() or 1
 
@@ -441,17 +463,13 @@ def main():
         if world > 1:
             dist.barrier()
 
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    def max_ms(x: float) -> float:
+        return max_over_ranks(x, world, dev)
 
     cfg = CONFIGS["periodic_train"]
     K, W = args.steps, args.warmup
     n = cfg.n_points
-    batches = [CF.sample(cfg, step=s, seed=cfg.seed + 1000 * rank) for s in range(K + W)]
+    batches = [CF.sample(cfg, step=s, seed=replica_seed(cfg.seed, rank)) for s in range(K + W)]
     dev_batches = [(torch.tensor(p, device=dev), torch.tensor(w, device=dev, dtype=torch.float32))
                    for p, w in batches]
 
@@ -480,8 +498,8 @@ def main():
     pk = peaks()
     with ClockSampler(local) as clocks:
         model, res, ms, kernels, launches = device_timed(args.precision, timing=True)
-    ms_max = max_over_ranks(ms)
-    value = world * K / (ms_max / 1e3)
+    ms_max = max_ms(ms)
+    value = whole_job_steps_per_s(world, K, ms_max)
     clk = clocks.summary()
     info_ok = int(res.info.item()) == 0
 
@@ -489,7 +507,7 @@ def main():
     fp32 = None
     if not args.no_fp32_plain and args.precision != "fp32":
         _, _, ms32, _, _ = device_timed("fp32")
-        ms32 = max_over_ranks(ms32)
+        ms32 = max_ms(ms32)
         fp32 = {"value": world * K / (ms32 / 1e3), "ms_per_step": ms32 / K}
 
     # end to end through the public API: host (pinned) points and weights in,
@@ -513,7 +531,7 @@ def main():
             losses.append(float(r.loss))
         e1.record()
         torch.cuda.synchronize()
-        ms_e = max_over_ranks(e0.elapsed_time(e1))
+        ms_e = max_ms(e0.elapsed_time(e1))
         h2d = host[0][0].numel() * 8 + host[0][1].numel() * 4
         d2h = 4 + 4 + 8  # solver status, Adam commit flag, loss
         e2e = {"value": world * K / (ms_e / 1e3), "unit": "steps/s", "h2d_bytes_per_step": h2d,
