@@ -550,15 +550,18 @@ def main():
     dom = max(own, key=lambda k: own[k][1])
     launches_dom, total_ms_dom, flops_dom, bytes_dom = own[dom]
     per_launch_s = total_ms_dom / launches_dom / 1e3
-    tensor = flops_dom > 0
+    flops_l, bytes_l = flops_dom / launches_dom, bytes_dom / launches_dom
+    # the binding roof for this kernel: whichever of its algorithmic flops at
+    # the bf16 peak and its algorithmic bytes at the copy bandwidth takes longer
+    t_tensor = flops_l / (pk["bf16"] * 1e12)
+    t_hbm = bytes_l / (pk["hbm"] * 1e9)
+    tensor_frac = t_tensor / per_launch_s
+    hbm_frac = t_hbm / per_launch_s
+    tensor = t_tensor >= t_hbm
     if tensor:
-        achieved = flops_dom / launches_dom / per_launch_s / 1e12
-        peak_v = pk["bf16"]
-        unit = "TFLOP/s"
+        achieved, peak_v, unit = flops_l / per_launch_s / 1e12, pk["bf16"], "TFLOP/s"
     else:
-        achieved = bytes_dom / launches_dom / per_launch_s / 1e9
-        peak_v = pk["hbm"]
-        unit = "GB/s"
+        achieved, peak_v, unit = bytes_l / per_launch_s / 1e9, pk["hbm"], "GB/s"
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
@@ -567,7 +570,9 @@ def main():
                 "peak": peak_v, "unit": unit, "frac": achieved / peak_v, "traffic": traffic,
                 "peak_source": pk["source"],
                 "per_launch_ms": per_launch_s * 1e3,
-                "algorithmic_per_launch": (flops_dom if tensor else bytes_dom) / launches_dom}
+                "algorithmic_flops_per_launch": flops_l,
+                "algorithmic_bytes_per_launch": bytes_l,
+                "tensor_frac": tensor_frac, "hbm_frac": hbm_frac}
     stages = {k: {"launches_per_step": v[0] / K, "ms_per_step": v[1] / K} for k, v in
               sorted(kernels.items(), key=lambda kv: -kv[1][1])}
     spectral_ms = sum(v[1] for k, v in kernels.items()
