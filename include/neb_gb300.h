@@ -174,13 +174,15 @@ int neb_spectral_range(int m, const double* M, const double* S, const double* c,
                        size_t workspace_bytes, neb_stream_t stream);
 
 /* Same contract as neb_spectral for m a multiple of 64 up to 512, computed
- * with the precision where the conditioning lives: FP64 Cholesky of M and
- * FP64 inverse factor L^-1; the reduced, well conditioned matrix
- * C = L^-1 S L^-T formed by compensated FP32 GEMMs, rounded to FP32 and
- * reduced to tridiagonal form in FP32 by one 8-CTA thread-block cluster; eigenvectors of
- * the tridiagonal by FP32 twisted factorisations and eigenvalues as their FP64
- * Rayleigh quotients; FP32 back-transformation and adjoints.  Eigenvalue
- * relative error ~ eps_32 cond(C) (1e-6 on the periodic training pencil).
+ * with the precision where the conditioning lives: the Cholesky of M and the
+ * reduction C = L^-1 S L^-T in compensated FP32 (value = hi + lo, FP64-class
+ * accuracy); the reduced, well conditioned C rounded to FP32 and reduced to
+ * tridiagonal form in FP32 by one 16-CTA thread-block cluster; eigenvalues of
+ * the tridiagonal by FP32 Sturm multisection, eigenvectors by FP32 twisted
+ * factorisations, eigenvalues refined to their Rayleigh quotients; FP32
+ * back-transformation and adjoints.  Eigenvalue relative error
+ * ~ eps_32 cond(C) (1e-6 on the periodic training pencil).  info as for
+ * neb_spectral, plus -2 = the cluster's exchange stalled (bounded wait).
  * Replaces the same reference functions as neb_spectral. */
 size_t neb_spectral_mixed_workspace_bytes(int m);
 int neb_spectral_mixed(int m, const double* M, const double* S, const double* c, double* lam,

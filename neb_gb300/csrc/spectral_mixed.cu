@@ -18,15 +18,16 @@
 // FP32 (they only feed the reverse pass).
 //
 // Pipeline (one stream, no host synchronisation):
-//   chol_diag / chol_panel / chol_update   blocked Cholesky, 32 x 32 blocks,
+//   chol_first / chol_step                 blocked Cholesky, 32-column panels,
 //                                          compensated FP32 (FP64-class)
 //   2 x df_solve                           C = L^-1 S L^-T by two blocked triangular
 //                                          solves with inverse diagonal blocks,
 //                                          compensated FP32
 //   tridiag_cluster                        FP32 Householder tridiagonalisation in
-//                                          one 8-CTA cluster, the matrix held in
-//                                          distributed shared memory, 2 cluster
-//                                          barriers per column
+//                                          one 16-CTA cluster, the rows held in
+//                                          registers, per-column exchange by
+//                                          st.async into mbarrier-guarded
+//                                          shared memory
 //   tri_eigvals                            eigenvalue brackets of T, warp per eigenvalue
 //   tri_eigvecs                            eigenvectors of T by twisted factorisations,
 //                                          eigenvalues refined to FP64 Rayleigh quotients
@@ -44,8 +45,6 @@ namespace {
 
 constexpr int kCB = 32;          // Cholesky block
 constexpr int kMaxM = 512;
-constexpr int kCluster = 8;
-constexpr int kTriThreads = 512;
 
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -403,186 +402,281 @@ __global__ void __launch_bounds__(256) df_solve(const df* __restrict__ T,
 }
 
 // ------------------------------------------------- cluster tridiagonalisation
-struct TriShared {
-  int rb, m;
-};
-
-__device__ __forceinline__ float block_sum(float v, float* red) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __syncthreads();
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  float s = 0.f;
-  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-  return s;
-}
-
 // C: [m][m] FP32 (symmetrised on load).  Outputs: d[m], e[m-1] (FP64 of the
 // FP32 tridiagonal), Vh[m][m] (row k = Householder vector of step k, zero up
-// to index k), tau[m].  Rows are dealt cyclically (row i on CTA i % 8) so
-// every CTA keeps a share of the shrinking trailing matrix; eight threads
-// share a row.  Every CTA also keeps a replica of the current pivot row k,
-// so the Householder vector of column k (= row k by symmetry) is formed
-// locally, and one cluster barrier per column suffices:
-//   x = rowk[k+1:], sigma = |x|^2, alpha, tau (block reduction, every CTA);
-//   p_i = tau A_i v on own rows (8-lane reductions); push p_i, per-warp
-//   partial p.v, and (owner of row k+1) row k+1 to every CTA; cluster barrier;
-//   rank-2 update A -= v p^T + w v^T, w = p - tau (p.v) v, of own rows and of
-//   the replica of row k+1, which becomes the next pivot row.
-// Remote stores go through mapa / st.shared::cluster.  v_{k+1} = x1 - alpha
-// is applied through scalar corrections, so vloc holds the raw row.
+// to index k), tau[m].
+//
+// One cluster of kTriCluster CTAs on kTriCluster SMs.  Rows are dealt
+// cyclically (row i on CTA i % kTriCluster) and live in REGISTERS: eight
+// threads share a row, thread `sub` holding chunks of four columns
+// q = sub + 8 t as a[t] (16 float4 at m = 512).  Every CTA keeps a replica of
+// the current pivot row, so the Householder vector of column k (row k by
+// symmetry) is formed locally.  Per column k:
+//   sigma = |row_k[k+1:]|^2 (warp partials left by the previous column),
+//   alpha, tau;
+//   one pass over the own rows applies the pending rank-2 update of column
+//   k-1 (A -= v p^T + w v^T, w = p - K2 v) and forms p_i = tau A_i v;
+//   every row owner pushes p_i and A_{i,k+1} (column k+1 before update k,
+//   = row k+1 by symmetry) to every CTA, plus one warp partial of p.v, by
+//   st.async, which completes on the receiver's mbarrier (no cluster
+//   barrier): the receivers wait for the byte count of the column;
+//   K2 = tau p.v; the next pivot row, row k+1 after update k, is formed by
+//   every CTA from the pushed column; one __syncthreads.
+// The update is lazy by one column, so each element of the trailing matrix
+// is read and written once per column.  Every 32 columns the front chunk of
+// every thread dies and the register array shifts down by one, so the chunk
+// holding column k+1 is always a[0] of thread (k+1)/4 % 8 (no dynamic
+// register indexing).  v_{k+1} = x1 - alpha is applied through scalar
+// corrections, so the replica holds the raw row.
+constexpr int kTriCluster = 16;
+constexpr int kTriThreads = 8 * kMaxM / kTriCluster;  // 8 threads per row
+constexpr int kTriWarps = kTriThreads / 32;
+constexpr int kTriSlots = kTriCluster * kTriWarps;    // p.v partials per column
+constexpr int kTriPush = kTriCluster / 8;              // CTAs each thread pushes to
+constexpr int kTriChunks = kMaxM / 32;                 // float4 per thread
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-
-__device__ __forceinline__ void st_cluster(float* local_addr, int rank, float v) {
-  uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(local_addr)), ra;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
-  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint32_t cluster_map(uint32_t a, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+// 4-byte store into another CTA's shared memory that completes (complete_tx,
+// release at cluster scope) on that CTA's mbarrier
+__device__ __forceinline__ void st_async_f32(uint32_t raddr, float v, uint32_t rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];"
+               ::"r"(raddr), "r"(__float_as_uint(v)), "r"(rbar) : "memory");
+}
+// Bounded wait (acquire at cluster scope) for the phase of parity `parity`;
+// the thread sleeps in the hardware up to 20 us per try; false after ~2^32
+// cycles (about two seconds).
+__device__ __forceinline__ bool cluster_bar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  uint32_t done;
+  do {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], "
+        "%2, %3;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity), "r"(20000u)
+        : "memory");
+    if (done) return true;
+  } while (clock64() - t0 < (1ll << 32));
+  return false;
 }
 
-constexpr int kTriWarps = kTriThreads / 32;
-
-__global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kTriThreads, 1)
+__global__ void __launch_bounds__(kTriThreads, 1)
 tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
-                double* __restrict__ e_out, float* __restrict__ Vh, float* __restrict__ tau_out) {
+                double* __restrict__ e_out, float* __restrict__ Vh, float* __restrict__ tau_out,
+                int* __restrict__ info) {
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
-  const int rb = m / kCluster;  // local rows; global row of local li is li * 8 + rank
+  const int rb = m / kTriCluster;
   extern __shared__ __align__(16) float sm[];
-  float* Aloc = sm;                                  // [rb][m]
-  float* vloc = Aloc + (size_t)rb * m;               // [m] raw pivot row (replica)
-  float* pbuf = vloc + m;                            // [2][m] p, pushed
-  float* nrow = pbuf + 2 * m;                        // [2][m] next pivot row, pushed
-  float* kps = nrow + 2 * m;                         // [2][kCluster * kTriWarps]
-  float* red = kps + 2 * kCluster * kTriWarps;       // [kTriWarps] block reduction
-  const int tid = threadIdx.x, nthr = blockDim.x;
+  float* vrow = sm;                 // [2][m] pivot rows k (parity k & 1), zero at j <= k
+  float* pbuf = vrow + 2 * m;       // [2][m] p of column k, pushed
+  float* nrow = pbuf + 2 * m;       // [2][m] column k+1 before update k, pushed
+  float* kps = nrow + 2 * m;        // [2][kTriSlots] warp partials of p.v, pushed
+  float* red = kps + 2 * kTriSlots; // [2][kTriWarps] partials of sigma
+  __shared__ __align__(8) unsigned long long bars[2];
+  const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const int li = tid >> 3, sub = tid & 7;  // row of this thread, its share of the row
+  const int li = tid >> 3, sub = tid & 7;
   const bool has_row = li < rb;
-  const int gi = li * kCluster + rank;     // global row
-  const int m4 = m >> 2;
-  const int nslot = kCluster * kTriWarps;
+  const int gi = li * kTriCluster + rank;  // global row of this thread
+  const int m4 = m >> 2, nsub = m4 >> 3;   // float4 chunks per row, per thread
 
-  for (int r = warp; r < rb; r += kTriWarps) {
-    const int i = r * kCluster + rank;
-    for (int j = lane; j < m; j += 32)
-      Aloc[(size_t)r * m + j] = 0.5f * (C[(size_t)i * m + j] + C[(size_t)j * m + i]);
+  float4 a[kTriChunks];
+#pragma unroll
+  for (int t = 0; t < kTriChunks; ++t) {
+    a[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (has_row && t < nsub) {
+      const int j = 4 * (sub + 8 * t);
+      const float* ci = C + (size_t)gi * m + j;
+      a[t].x = 0.5f * (ci[0] + C[(size_t)(j + 0) * m + gi]);
+      a[t].y = 0.5f * (ci[1] + C[(size_t)(j + 1) * m + gi]);
+      a[t].z = 0.5f * (ci[2] + C[(size_t)(j + 2) * m + gi]);
+      a[t].w = 0.5f * (ci[3] + C[(size_t)(j + 3) * m + gi]);
+    }
   }
-  for (int j = tid; j < m; j += nthr) vloc[j] = 0.5f * (C[j] + C[(size_t)j * m]);  // row 0
-  cluster.sync();  // every CTA of the cluster runs before remote stores begin
-  float* Ai = Aloc + (size_t)(has_row ? li : 0) * m;
-  float4* Ai4 = reinterpret_cast<float4*>(Ai);
-  const float4* v4 = reinterpret_cast<const float4*>(vloc);
+  {  // pivot row 0 and its sigma partials
+    float part = 0.f;
+    for (int j = tid; j < m; j += kTriThreads) {
+      const float x0 = 0.5f * (C[j] + C[(size_t)j * m]);
+      if (j == 0 && rank == 0) d_out[0] = x0;
+      const float x = j > 0 ? x0 : 0.f;
+      vrow[j] = x;
+      vrow[m + j] = 0.f;
+      pbuf[j] = 0.f;
+      pbuf[m + j] = 0.f;
+      part += x * x;
+    }
+    part = warp_sum(part);
+    if (lane == 0) red[warp] = part;
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  const uint32_t base = smem_addr(sm);
+  uint32_t rsub[kTriPush];  // shared window of CTAs sub + 8 d
+#pragma unroll
+  for (int d = 0; d < kTriPush; ++d) rsub[d] = cluster_map(base, sub + 8 * d);
+  const uint32_t rlane = cluster_map(base, lane % kTriCluster);
+  const uint32_t bar_off = smem_addr(&bars[0]) - base;  // the same in every CTA
+  bool failed = false;
+  cluster.sync();  // barriers initialised and every CTA running before the first push
+  float pprev = 0.f, vprev = 0.f, K2prev = 0.f;  // this row's p, v and K2 of column k-1
 
   for (int k = 0; k + 2 < m; ++k) {
-    const int par = k & 1;
-    float* pb = pbuf + par * m;
-    float* nr = nrow + par * m;
-    float* kp = kps + par * nslot;
-    // (a) sigma = |rowk[k+1:]|^2 (one element per thread), Householder scalars
+    const int par = k & 1, npar = par ^ 1;
+    const float* vcur = vrow + par * m;
+    float* vprv = vrow + npar * m;
+    const float* pb = pbuf + par * m;
+    const float* pbp = pbuf + npar * m;
+    const float* nr = nrow + par * m;
+    const float* kp = kps + par * kTriSlots;
+    float sigma = 0.f;
     {
-      const float xj = (tid > k && tid < m) ? vloc[tid] : 0.f;
-      const float part = warp_sum(xj * xj);
-      if (lane == 0) red[warp] = part;
+      const float4* r4 = reinterpret_cast<const float4*>(red + par * kTriWarps);
+#pragma unroll
+      for (int c = 0; c < kTriWarps / 4; ++c) {
+        const float4 r = r4[c];
+        sigma += (r.x + r.y) + (r.z + r.w);
+      }
     }
-    __syncthreads();
-    float sigma = lane < kTriWarps ? red[lane] : 0.f;
-    sigma = warp_sum(sigma);
-    const float x1 = vloc[k + 1];
-    const float alpha = sigma > 0.f ? -copysignf(sqrtf(sigma), x1) : 0.f;
+    const float x1 = vcur[k + 1];
+    const float alpha = sigma > 0.f ? -copysignf(sigma * rsqrtf(sigma), x1) : 0.f;
     const float v1 = x1 - alpha;
     const float vv = sigma - x1 * x1 + v1 * v1;
-    const float tau = vv > 0.f ? 2.f / vv : 0.f;
-    if (rank == 0) {
-      if (tid == 0) {
-        e_out[k] = alpha;
-        tau_out[k] = tau;
-        d_out[k] = vloc[k];
-      }
-      for (int j = tid; j < m; j += nthr)
-        Vh[(size_t)k * m + j] = j <= k ? 0.f : (j == k + 1 ? v1 : vloc[j]);
+    const float tau = vv > 0.f ? __fdividef(2.f, vv) : 0.f;
+    if (tid == 0)
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                       smem_addr(&bars[par])),
+                   "r"(8u * (m - k - 1) + 4u * kTriSlots)
+                   : "memory");
+    if (rank == 0 && tid == 0) {
+      e_out[k] = alpha;
+      tau_out[k] = tau;
     }
-    // (b) p_i = tau (A_i . v) on own rows, 8 threads per row
+    if (tid < rb) {
+      const int j = rank * rb + tid;
+      Vh[(size_t)k * m + j] = j == k + 1 ? v1 : vcur[j];
+    }
+    // pending update of column k-1 fused with p_i = tau A_i v of column k
+    if (k > 0 && ((k + 1) & 31) == 0) {
+#pragma unroll
+      for (int t = 0; t < kTriChunks - 1; ++t) a[t] = a[t + 1];
+    }
+    const int j4 = (k + 1) >> 2, T = j4 >> 3, sk = j4 & 7;  // a[t] = chunk sub + 8 (t + T)
     const bool active = has_row && gi > k;
-    const int j4 = (k + 1) >> 2;
     float pi = 0.f, vi = 0.f, sacc = 0.f;
     if (active) {
-      for (int q = j4 + sub; q < m4; q += 8) {
-        const float4 a = Ai4[q], v = v4[q];
-        const int j = q << 2;
-        sacc += (j >= k + 1 ? a.x * v.x : 0.f) + (j + 1 >= k + 1 ? a.y * v.y : 0.f) +
-                (j + 2 >= k + 1 ? a.z * v.z : 0.f) + (j + 3 >= k + 1 ? a.w * v.w : 0.f);
+      const float wprev = pprev - K2prev * vprev;
+      const float4* vc4 = reinterpret_cast<const float4*>(vcur);
+      const float4* vp4 = reinterpret_cast<const float4*>(vprv);
+      const float4* pp4 = reinterpret_cast<const float4*>(pbp);
+      float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+      for (int t = 0; t < kTriChunks; ++t) {
+        if ((t > 0 || sub >= sk) && t + T < nsub) {
+          const int q = sub + 8 * (t + T);
+          const float4 pp = pp4[q], vp = vp4[q], vc = vc4[q];
+          a[t].x = fmaf(-wprev, vp.x, fmaf(-vprev, pp.x, a[t].x));
+          a[t].y = fmaf(-wprev, vp.y, fmaf(-vprev, pp.y, a[t].y));
+          a[t].z = fmaf(-wprev, vp.z, fmaf(-vprev, pp.z, a[t].z));
+          a[t].w = fmaf(-wprev, vp.w, fmaf(-vprev, pp.w, a[t].w));
+          s0 = fmaf(a[t].x, vc.x, s0);
+          s1 = fmaf(a[t].y, vc.y, s1);
+          s0 = fmaf(a[t].z, vc.z, s0);
+          s1 = fmaf(a[t].w, vc.w, s1);
+        }
       }
+      sacc = s0 + s1;
     }
     sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
     sacc += __shfl_xor_sync(0xffffffffu, sacc, 2);
     sacc += __shfl_xor_sync(0xffffffffu, sacc, 4);
+    const int ck = (k + 1) & 3;  // A_{i,k+1}: component ck of a[0] of thread sk
+    const float own = ck == 0 ? a[0].x : ck == 1 ? a[0].y : ck == 2 ? a[0].z : a[0].w;
+    const float aik1 = __shfl_sync(0xffffffffu, own, (lane & ~7) | sk);
     if (active) {
-      pi = tau * (sacc - alpha * Ai[k + 1]);
-      vi = gi == k + 1 ? v1 : vloc[gi];
-      st_cluster(pb + gi, sub, pi);
+      pi = tau * (sacc - alpha * aik1);
+      vi = gi == k + 1 ? v1 : vcur[gi];
+#pragma unroll
+      for (int d = 0; d < kTriPush; ++d) {
+        const uint32_t rbar = rsub[d] + bar_off + 8u * par;
+        st_async_f32(rsub[d] + 4u * (uint32_t)(pb + gi - sm), pi, rbar);
+        st_async_f32(rsub[d] + 4u * (uint32_t)(nr + gi - sm), aik1, rbar);
+      }
     }
+    {  // every lane of a row holds its p_i v_i: two levels sum the warp's four rows
+      float part = pi * vi;
+      part += __shfl_xor_sync(0xffffffffu, part, 8);
+      part += __shfl_xor_sync(0xffffffffu, part, 16);
+      if (lane < kTriCluster)
+        st_async_f32(rlane + 4u * (uint32_t)(kp + rank * kTriWarps + warp - sm), part,
+                     rlane + bar_off + 8u * par);
+    }
+    failed = !cluster_bar_wait(smem_addr(&bars[par]), (uint32_t)(k >> 1) & 1u);
+    float pv;
     {
-      const float part = warp_sum(sub == 0 ? pi * vi : 0.f);
-      if (lane < kCluster) st_cluster(kp + rank * kTriWarps + warp, lane, part);
+      static_assert(kTriSlots == 128, "one float4 of p.v partials per lane");
+      const float4 q = reinterpret_cast<const float4*>(kp)[lane];
+      pv = warp_sum((q.x + q.y) + (q.z + q.w));
     }
-    // the owner of row k+1 sends it (as it stands before this column's update)
-    if ((k + 1) % kCluster == rank) {
-      const float* r1 = Aloc + (size_t)((k + 1) / kCluster) * m;
-      for (int t = tid; t < (m - k - 1) * kCluster; t += nthr) {
-        const int j = k + 1 + t / kCluster, dst = t % kCluster;
-        st_cluster(nr + j, dst, r1[j]);
-      }
-    }
-    cluster.sync();
-    // (c) K2 = tau p^T v, then A -= v p^T + w v^T on own rows and on row k+1
-    float pv = 0.f;
-    for (int c = lane; c < nslot; c += 32) pv += kp[c];
-    const float K2 = tau * warp_sum(pv);
-    const float4* pb4 = reinterpret_cast<const float4*>(pb);
-    if (active) {
-      const float wi = pi - K2 * vi;
-      for (int q = j4 + sub; q < m4; q += 8) {  // entries j <= k are dead
-        float4 a = Ai4[q];
-        const float4 p = pb4[q], v = v4[q];
-        a.x -= vi * p.x + wi * v.x;
-        a.y -= vi * p.y + wi * v.y;
-        a.z -= vi * p.z + wi * v.z;
-        a.w -= vi * p.w + wi * v.w;
-        Ai4[q] = a;
-      }
-      // v_{k+1} = vloc[k+1] - alpha; column k+1 lies in chunk j4, which sub 0 updated
-      if (sub == 0) Ai[k + 1] += wi * alpha;
-    }
-    // next pivot row: row k+1 updated the same way (v_{k+1} = v1, w_{k+1})
+    const float K2 = tau * pv;
+    // pivot row k+1 after update k, from column k+1 as it stood before it
     const float w1 = pb[k + 1] - K2 * v1;
-    float nv = 0.f;
-    const int j = tid;
-    if (j > k && j < m) {
-      nv = nr[j] - (v1 * pb[j] + w1 * vloc[j]);
-      if (j == k + 1) nv += w1 * alpha;
+    float part = 0.f;
+    for (int j = tid; j < m; j += kTriThreads) {
+      float nv = 0.f;
+      if (j > k) {
+        nv = nr[j] - (v1 * pb[j] + w1 * vcur[j]);
+        if (j == k + 1) {
+          if (rank == 0) d_out[k + 1] = nv + w1 * alpha;
+          nv = 0.f;
+        }
+      }
+      part += nv * nv;
+      vprv[j] = nv;
     }
-    __syncthreads();  // every thread is done reading vloc for this column
-    if (j > k && j < m) vloc[j] = nv;
-    __syncthreads();
+    part = warp_sum(part);
+    if (lane == 0) red[npar * kTriWarps + warp] = part;
+    pprev = pi;
+    vprev = vi;
+    K2prev = K2;
+    failed = __syncthreads_or(failed);
+    if (failed) break;
   }
+  if (failed) {
+    // a stalled exchange: report it, and let pushes still in flight land
+    // before any CTA of the cluster exits
+    if (tid == 0) atomicExch(info, -2);
+    __nanosleep(50000);
+  }
+  const int pl = (m - 3) & 1;  // parity of the last column
   if (tid == 0 && rank == 0) {
-    d_out[m - 2] = vloc[m - 2];
-    e_out[m - 2] = vloc[m - 1];
+    e_out[m - 2] = vrow[(pl ^ 1) * m + m - 1];
     tau_out[m - 2] = 0.f;
     tau_out[m - 1] = 0.f;
   }
   if (rank == 0)
     for (int k = m - 2; k < m; ++k)
-      for (int i = tid; i < m; i += nthr) Vh[(size_t)k * m + i] = 0.f;
-  // d_{m-1}: the last diagonal entry, after the final update of row m-1
-  if (tid == 0 && (m - 1) % kCluster == rank)
-    d_out[m - 1] = Aloc[(size_t)((m - 1) / kCluster) * m + m - 1];
+      for (int i = tid; i < m; i += kTriThreads) Vh[(size_t)k * m + i] = 0.f;
+  // d_{m-1}: row m-1 (a[0].w of its last thread) with the pending update
+  if (has_row && gi == m - 1 && sub == 7) {
+    const float w = pprev - K2prev * vprev;
+    d_out[m - 1] = a[0].w - (vprev * pbuf[pl * m + m - 1] + w * vrow[pl * m + m - 1]);
+  }
   cluster.sync();
 }
 
@@ -1058,20 +1152,30 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   cublasHandle_t h;
   if ((st = blas32(s, &h))) return st;
   {
-    static bool configured = false;
-    const int rb = m / kCluster;
-    const size_t smem =
-        ((size_t)rb * m + 5 * m + 2 * kCluster * kTriWarps + kTriWarps) * sizeof(float);
-    if (!configured) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kTriCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kTriCluster);
+    cfg.blockDim = dim3(kTriThreads);
+    cfg.dynamicSmemBytes = ((size_t)6 * m + 2 * kTriSlots + 2 * kTriWarps) * sizeof(float);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    static int clusters = -1;  // co-resident 16-CTA clusters (non-portable size)
+    if (clusters < 0) {
       NEB_CUDA_CHECK(cudaFuncSetAttribute(tridiag_cluster,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(((size_t)kMaxM / kCluster * kMaxM + 5 * kMaxM +
-                                                 2 * kCluster * kTriWarps + kTriWarps) *
-                                                sizeof(float))));
-      configured = true;
+                                          cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      NEB_CUDA_CHECK(cudaOccupancyMaxActiveClusters(&clusters, tridiag_cluster, &cfg));
     }
+    NEB_REQUIRE(clusters >= 1,
+                "neb_spectral_mixed: the GPU cannot co-schedule a %d-CTA thread-block cluster",
+                kTriCluster);
     KernelScope ks("spec_tridiag_cluster_fp32", s, 4.0 / 3.0 * m * mm, 8.0 * mm);
-    tridiag_cluster<<<kCluster, kTriThreads, smem, s>>>(C, m, d, e, Vh, tau);
+    NEB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, tridiag_cluster, (const float*)C, m, d, e, Vh, tau,
+                                      info));
     NEB_LAUNCH_CHECK();
   }
   {
