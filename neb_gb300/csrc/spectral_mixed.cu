@@ -20,9 +20,9 @@
 // Pipeline (one stream, no host synchronisation):
 //   chol_first / chol_step                 blocked Cholesky, 32-column panels,
 //                                          compensated FP32 (FP64-class)
-//   2 x df_solve                           C = L^-1 S L^-T by two blocked triangular
-//                                          solves with inverse diagonal blocks,
-//                                          compensated FP32
+//   2 x df_solve_rl                        C = L^-1 S L^-T by two right-looking
+//                                          blocked triangular solves with inverse
+//                                          diagonal blocks, compensated FP32
 //   tridiag_cluster                        FP32 Householder tridiagonalisation in
 //                                          one 16-CTA cluster, the rows held in
 //                                          registers, per-column exchange by
@@ -33,7 +33,7 @@
 //                                          eigenvalues refined to FP64 Rayleigh quotients
 //   wy_factor / wy_apply                   x_k = Q z_k (FP32), 32 reflectors per
 //                                          block in compact WY form
-//   df_solve, SGEMMs                       V rows = (L^-T x_k)^T, G_S, G_M
+//   df_solve_rl, SGEMMs                    V rows = (L^-T x_k)^T, G_S, G_M
 #include <cooperative_groups.h>
 #include <cublas_v2.h>
 #include "elementwise.cuh"
@@ -319,85 +319,90 @@ __global__ void __launch_bounds__(1024) split_dinv(const df* __restrict__ linv_p
   DU[base + c * kCB + r] = v;
 }
 
-// Blocked triangular solves, compensated FP32, kSolveCols right-hand-side
-// columns per 256-thread block (128 blocks at m = 512):
-//   upper == 0:  L Y = B   (forward;  T = L as float pairs, D = DL)
-//   upper == 1:  L^T Y = B (backward; T = L^T as float pairs, D = DU)
-// Per 32-row block b: acc = B_b - T_b,solved y_solved (thread = row x column
-// x half of the solved range, two accumulation chains each), then
-// y_b = D_b acc (a 32 x 32 product with the inverse diagonal block, no
-// sequential substitution).  B(r, c) = b_trans ? B[c][r] : B[r][c] (FP64 or
-// FP32); Y(r, c) goes to out[r][c] or, with out_trans, out[c][r].
-constexpr int kSolveCols = 4;
-__global__ void __launch_bounds__(256) df_solve(const df* __restrict__ T,
-                                                const df* __restrict__ D, int m, int upper,
-                                                const void* __restrict__ B, int b_f32,
-                                                int b_trans, void* __restrict__ out, int out_f32,
-                                                int out_trans) {
-  extern __shared__ df ys[];  // [m][kSolveCols] solved values, then the T rows
-  df* tt = ys + (size_t)m * kSolveCols;  // [32][ncols + 1] rows of T being used
-  __shared__ df part[kCB][kSolveCols];
-  __shared__ df acc[kCB][kSolveCols];
-  const int tid = threadIdx.x;
-  const int row = tid & 31, col = (tid >> 5) & (kSolveCols - 1), half = tid >> 7;
-  const int c = blockIdx.x * kSolveCols + col;
+constexpr int kSolveCols = 4;  // eigenvectors per block of the back-transformation
+
+// Right-looking blocked triangular solve, compensated FP32: A Y = B with
+// A = L (upper == 0, forward) or A = L^T (upper == 1, backward), kRLCols
+// right-hand sides per CTA, one thread per row (m <= 512).  F holds the
+// columns of A as rows, F[j][i] = A[i][j] (L^T as float pairs for the
+// forward solve, L for the backward one), so the update reads of a warp are
+// coalesced.  Per 32-row block b, in elimination order:
+//   the warp owning block b forms y_b = D_b acc_b (its accumulators, staged
+//   through shared memory, times the inverse diagonal block);
+//   every row i still pending subtracts A_i,b y_b (32-term Dot2 sums, one
+//   per right-hand side, the 32 factor entries loaded before the barrier).
+// Each row keeps its accumulators in registers from the load of B to the
+// store of Y; the only sequential chain is the 16 blocks (at m = 512), with
+// one barrier each.  B(r, c) = b_trans ? B[c][r] : B[r][c] (FP64 or FP32);
+// Y(r, c) goes to out[r][c] or, with out_trans, out[c][r].
+constexpr int kRLCols = 4;
+__global__ void __launch_bounds__(kMaxM) df_solve_rl(const df* __restrict__ F,
+                                                     const df* __restrict__ D, int m, int upper,
+                                                     const void* __restrict__ B, int b_f32,
+                                                     int b_trans, void* __restrict__ out,
+                                                     int out_f32, int out_trans) {
+  __shared__ df stage[kCB][kRLCols];     // accumulators of the block being finished
+  __shared__ df ys[2][kCB][kRLCols];     // y of the finished block, by parity
+  const int i = threadIdx.x, lane = i & 31, wb = i >> 5;  // row, its block
+  const int c0 = blockIdx.x * kRLCols;
   const int nb = m / kCB;
-  for (int bb = 0; bb < nb; ++bb) {
-    const int b = upper ? nb - 1 - bb : bb;
-    const int rb0 = b * kCB;
-    // solved rows: [0, rb0) (forward) or [rb0 + 32, m) (backward)
-    const int lo = upper ? rb0 + kCB : 0, hi = upper ? m : rb0;
-    const int ncols = hi - lo, ld = ncols + 1;  // odd pitch: two wavefronts per warp
-    for (int t = tid; t < kCB * ncols; t += 256) {
-      const int r = t / ncols, k = t - r * ncols;
-      cp_async8(tt + r * ld + k, T + (size_t)(rb0 + r) * m + lo + k);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    const int mid = ncols >> 1;
-    const int k0 = half ? mid : 0, k1 = half ? ncols : mid;
-    const df* trow = tt + row * ld;
-    const df* yb = ys + (size_t)lo * kSolveCols + col;
-    dot2 s0, s1;
-    int k = k0;
-#pragma unroll 2
-    for (; k + 1 < k1; k += 2) {
-      dot2_add(s0, trow[k], yb[(size_t)k * kSolveCols]);
-      dot2_add(s1, trow[k + 1], yb[(size_t)(k + 1) * kSolveCols]);
-    }
-    if (k < k1) dot2_add(s0, trow[k], yb[(size_t)k * kSolveCols]);
-    const df s = dot2_sum(s0, s1);
-    if (half) part[row][col] = s;
-    __syncthreads();
-    if (!half) {
-      const int r = rb0 + row;
-      const size_t bi = b_trans ? (size_t)c * m + r : (size_t)r * m + c;
-      const double bv = b_f32 ? (double)((const float*)B)[bi] : ((const double*)B)[bi];
-      acc[row][col] = df_add(df_from(bv), df_neg(df_add(s, part[row][col])));
-    }
-    __syncthreads();
-    // y_b = D_b acc: half 0 sums j < 16, half 1 j >= 16
-    const df* drow = D + ((size_t)b * kCB + row) * kCB;
-    dot2 y0, y1;
+  const bool has = i < m;
+  df acc[kRLCols];
 #pragma unroll
-    for (int j = 0; j < 16; j += 2) {
-      const int jj = half * 16 + j;
-      dot2_add(y0, drow[jj], acc[jj][col]);
-      dot2_add(y1, drow[jj + 1], acc[jj + 1][col]);
+  for (int c = 0; c < kRLCols; ++c) {
+    acc[c] = df{0.f, 0.f};
+    if (has) {
+      const size_t bi = b_trans ? (size_t)(c0 + c) * m + i : (size_t)i * m + c0 + c;
+      acc[c] = df_from(b_f32 ? (double)((const float*)B)[bi] : ((const double*)B)[bi]);
     }
-    const df y = dot2_sum(y0, y1);
-    if (half) part[row][col] = y;
-    __syncthreads();
-    if (!half) ys[(size_t)(rb0 + row) * kSolveCols + col] = df_add(y, part[row][col]);
-    __syncthreads();
   }
-  for (int t = tid; t < m * kSolveCols; t += 256) {
-    const int rr = t / kSolveCols, cc = t % kSolveCols;
-    const df y = ys[t];
-    const int cc_g = blockIdx.x * kSolveCols + cc;
-    const size_t oi = out_trans ? (size_t)cc_g * m + rr : (size_t)rr * m + cc_g;
-    if (out_f32) ((float*)out)[oi] = y.h + y.l;
-    else ((double*)out)[oi] = df_to(y);
+  for (int bb = 0; bb < nb; ++bb) {
+    const int b = upper ? nb - 1 - bb : bb, par = bb & 1;
+    const int r0 = b * kCB;
+    const bool pending = has && (upper ? wb < b : wb > b);
+    if (wb == b) {
+      const df* dp = D + ((size_t)b * kCB + lane) * kCB;  // row lane of D_b
+#pragma unroll
+      for (int c = 0; c < kRLCols; ++c) stage[lane][c] = acc[c];
+      __syncwarp();
+      dot2 y[kRLCols];
+#pragma unroll 8
+      for (int j = 0; j < kCB; ++j) {
+        const df d = dp[j];
+#pragma unroll
+        for (int c = 0; c < kRLCols; ++c) dot2_add(y[c], d, stage[j][c]);
+      }
+#pragma unroll
+      for (int c = 0; c < kRLCols; ++c) {
+        acc[c] = dot2_df(y[c]);  // this row's solution
+        ys[par][lane][c] = acc[c];
+      }
+    }
+    df f[kCB];  // A_i,r0+j, loaded while the block's warp finishes
+    if (pending) {
+#pragma unroll
+      for (int j = 0; j < kCB; ++j) f[j] = F[(size_t)(r0 + j) * m + i];
+    }
+    __syncthreads();
+    if (pending) {
+      dot2 u[kRLCols];
+#pragma unroll
+      for (int j = 0; j < kCB; ++j)
+#pragma unroll
+        for (int c = 0; c < kRLCols; ++c) dot2_add(u[c], f[j], ys[par][j][c]);
+#pragma unroll
+      for (int c = 0; c < kRLCols; ++c) acc[c] = df_add(acc[c], df_neg(dot2_df(u[c])));
+    }
+    // ys[par] is rewritten two blocks later, after the next barrier; stage is
+    // rewritten by the next block's warp, whose own reads of it are done
+  }
+  if (has) {
+#pragma unroll
+    for (int c = 0; c < kRLCols; ++c) {
+      const size_t oi = out_trans ? (size_t)(c0 + c) * m + i : (size_t)i * m + c0 + c;
+      if (out_f32) ((float*)out)[oi] = acc[c].h + acc[c].l;
+      else ((double*)out)[oi] = df_to(acc[c]);
+    }
   }
 }
 
@@ -1119,15 +1124,6 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     }
   }
   int st;
-  const size_t solve_smem = ((size_t)kSolveCols * m + (size_t)kCB * m) * sizeof(df);
-  {
-    static bool solve_configured = false;
-    if (!solve_configured) {
-      NEB_CUDA_CHECK(cudaFuncSetAttribute(df_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (kSolveCols * kMaxM + kCB * kMaxM) * (int)sizeof(df)));
-      solve_configured = true;
-    }
-  }
   df* DL = (df*)(ws + w.Dinv);
   df* DU = DL + (size_t)nb * kCB * kCB;
   {
@@ -1141,12 +1137,12 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
       NEB_LAUNCH_CHECK();
     }
     {
-      KernelScope k2("df_solve", s, 0, 0, 0);
-      df_solve<<<m / kSolveCols, 256, solve_smem, s>>>(Ld, DL, m, 0, S, 0, 0, Y, 0, 0);
+      KernelScope k2("df_solve_rl", s, 0, 0, 0);
+      df_solve_rl<<<m / kRLCols, kMaxM, 0, s>>>(LTd, DL, m, 0, S, 0, 0, Y, 0, 0);
       NEB_LAUNCH_CHECK();
     }
-    KernelScope k3("df_solve", s, 0, 0, 0);
-    df_solve<<<m / kSolveCols, 256, solve_smem, s>>>(Ld, DL, m, 0, Y, 0, 1, C, 1, 0);
+    KernelScope k3("df_solve_rl", s, 0, 0, 0);
+    df_solve_rl<<<m / kRLCols, kMaxM, 0, s>>>(LTd, DL, m, 0, Y, 0, 1, C, 1, 0);
     NEB_LAUNCH_CHECK();
   }
   cublasHandle_t h;
@@ -1220,8 +1216,8 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     KernelScope ks("spec_adjoints_fp32", s, 6.0 * m * mm, 24.0 * mm, 9);
     // rows of V: e_k = (L^-T x_k)^T, a backward solve with L^T on the columns of X^T
     {
-      KernelScope k1("df_solve", s, 0, 0, 0);
-      df_solve<<<m / kSolveCols, 256, solve_smem, s>>>(LTd, DU, m, 1, X, 1, 1, E, 1, 1);
+      KernelScope k1("df_solve_rl", s, 0, 0, 0);
+      df_solve_rl<<<m / kRLCols, kMaxM, 0, s>>>(Ld, DU, m, 1, X, 1, 1, E, 1, 1);
       NEB_LAUNCH_CHECK();
     }
     int blocks = (int)std::min<size_t>((mm + 255) / 256, 2048);
