@@ -575,23 +575,24 @@ extern "C" int neb_features(const neb_net* net, int kind, int n_freq, const doub
     dprm.n = n_params;
     for (int i = 0; i < n_params; ++i) dprm.v[i] = params[i];
   }
+  const double inv_period = kind == NEB_FEAT_PERIODIC ? 1.0 / period : 0.0;
   int64_t total = n * F;
   int blocks = (int)ceil_div(total, 256);
   KernelScope ks("features", s, 0, (double)total * net_channels(net) * master_size(net));
   if (net->precision == NEB_PREC_FP64) {
     if (net->dim == 2)
-      features_kernel<double, 4><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
-                                                        (double*)feats);
+      features_kernel<double, 4><<<blocks, 256, 0, s>>>(
+          kind, n_freq, period, inv_period, dprm, points, n, F, (double*)feats);
     else
-      features_kernel<double, 10><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
-                                                         (double*)feats);
+      features_kernel<double, 10><<<blocks, 256, 0, s>>>(
+          kind, n_freq, period, inv_period, dprm, points, n, F, (double*)feats);
   } else {
     if (net->dim == 2)
-      features_kernel<float, 4><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
-                                                       (float*)feats);
+      features_kernel<float, 4><<<blocks, 256, 0, s>>>(
+          kind, n_freq, period, inv_period, dprm, points, n, F, (float*)feats);
     else
-      features_kernel<float, 10><<<blocks, 256, 0, s>>>(kind, n_freq, period, dprm, points, n, F,
-                                                        (float*)feats);
+      features_kernel<float, 10><<<blocks, 256, 0, s>>>(
+          kind, n_freq, period, inv_period, dprm, points, n, F, (float*)feats);
   }
   NEB_LAUNCH_CHECK();
   return NEB_OK;

@@ -12,34 +12,53 @@ struct FeatureParams {
 };
 
 // One thread per (point, feature): writes the C jet channels of the feature.
+// Periodic features with FP32 outputs reduce the phase in turns in FP64
+// (t = k s / period, t - rint(t): four FP64 operations, exact to ~1e-16
+// turns) and evaluate sin / cos (pi * 2 (t - rint t)) in FP32; inv_period =
+// 1 / period comes from the host, so no FP64 division runs per element.
 template <typename T, int C>
-__global__ void features_kernel(int kind, int n_freq, double period, FeatureParams prm,
-                                const double* __restrict__ pts, int64_t n, int F, T* __restrict__ X0) {
-  int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (idx >= n * F) return;
-  int64_t p = idx / F;
-  int f = (int)(idx % F);
+__global__ void features_kernel(int kind, int n_freq, double period, double inv_period,
+                                FeatureParams prm, const double* __restrict__ pts, int64_t n,
+                                int F, T* __restrict__ X0) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t total = n * F;
+  if (idx >= total) return;
+  int64_t p;
+  int f;
+  if (total < ((int64_t)1 << 31)) {
+    const int i32 = (int)idx;
+    p = i32 / F;
+    f = i32 - (int)p * F;
+  } else {
+    p = idx / F;
+    f = (int)(idx % F);
+  }
+  if constexpr (sizeof(T) == 4 && C == 4) {
+    if (kind == NEB_FEAT_PERIODIC) {
+      // for axis in (x, y), for k = 1..n_freq, (sin, cos) of 2 pi k s / period
+      const int axis = f / (2 * n_freq), r = f % (2 * n_freq), k = r / 2 + 1;
+      const double t = (double)k * (pts[p * 2 + axis] * inv_period);
+      const float red2 = 2.f * (float)(t - rint(t));  // in [-1, 1]
+      float sn, cs;
+      sincospif(red2, &sn, &cs);
+      const float w = (float)(6.283185307179586 * inv_period) * (float)k;
+      const float v = (r & 1) ? cs : sn;
+      float* o = X0 + (p * C) * (int64_t)F + f;
+      o[0] = v;
+      o[(int64_t)(1 + axis) * F] = (r & 1) ? -w * sn : w * cs;
+      o[(int64_t)(2 - axis) * F] = 0.f;
+      o[(int64_t)3 * F] = -w * w * v;
+      return;
+    }
+  }
   double out[C];
 #pragma unroll
   for (int c = 0; c < C; ++c) out[c] = 0.0;
   if (kind == NEB_FEAT_PERIODIC) {
-    // for axis in (x, y), for k = 1..n_freq, (sin, cos) of 2 pi k s / period
     int axis = f / (2 * n_freq), r = f % (2 * n_freq), k = r / 2 + 1;
     double w = 2.0 * 3.14159265358979323846 * k / period;
-    double s = pts[p * 2 + axis];
     double sn, cs;
-    if constexpr (sizeof(T) == 4) {
-      // FP32 outputs: reduce the phase to [-pi, pi] in FP64 (three FP64
-      // operations), then the FP32 sine and cosine
-      const double a = w * s;
-      const double red = fma(-rint(a * 0.15915494309189535), 6.283185307179586, a);
-      float sf, cf;
-      sincosf((float)red, &sf, &cf);
-      sn = sf;
-      cs = cf;
-    } else {
-      sincos(w * s, &sn, &cs);
-    }
+    sincos(w * pts[p * 2 + axis], &sn, &cs);
     double v = (r & 1) ? cs : sn;
     out[0] = v;
     out[1 + axis] = (r & 1) ? -w * sn : w * cs;

@@ -203,15 +203,15 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
     const bool in21 = (i / (2 * s) == j / (2 * s)) && (i % (2 * s) >= s) && (j % (2 * s) < s);
     const int o = (i / (2 * s)) * 2 * s;
     if (in21) {  // Tm = L21 X11
-      df acc{0.f, 0.f};
-      for (int t = 0; t < s; ++t) acc = df_add(acc, df_mul(L[i][o + t], X[o + t][j]));
-      Tm[i][j] = acc;
+      dot2 acc;
+      for (int t = 0; t < s; ++t) dot2_add(acc, L[i][o + t], X[o + t][j]);
+      Tm[i][j] = dot2_df(acc);
     }
     __syncthreads();
     if (in21) {  // X21 = -X22 Tm
-      df acc{0.f, 0.f};
-      for (int t = s; t < 2 * s; ++t) acc = df_add(acc, df_mul(X[i][o + t], Tm[o + t][j]));
-      X[i][j] = df_neg(acc);
+      dot2 acc;
+      for (int t = s; t < 2 * s; ++t) dot2_add(acc, X[i][o + t], Tm[o + t][j]);
+      X[i][j] = df_neg(dot2_df(acc));
     }
     __syncthreads();
   }

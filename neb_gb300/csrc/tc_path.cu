@@ -572,21 +572,41 @@ __global__ void split_gram_adjoint(const double* __restrict__ GM, const double* 
 }
 
 // wHT[pl][ci][f][p] = split(w_p * (XT_L[c = ci + 1][f][p])) for the three field
-// channels; w_p = 0 for padded points.
+// channels; w_p = 0 for padded points.  Eight points (16 bytes per plane) per
+// thread step; n_pad is a multiple of 128.
 __global__ void weighted_fields_t(const __nv_bfloat16* __restrict__ XT, const float* __restrict__ qw,
                                   int n, int n_pad, int H, __nv_bfloat16* __restrict__ out) {
-  const size_t total = (size_t)3 * H * n_pad;
+  const size_t total = (size_t)3 * H * n_pad, total8 = total / 8;
   const size_t src_plane = (size_t)C * H * n_pad;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-       i += (size_t)gridDim.x * blockDim.x) {
-    int p = (int)(i % n_pad);
-    size_t src = (size_t)H * n_pad + i;  // channel ci + 1
-    float v = __bfloat162float(XT[src]) + __bfloat162float(XT[src_plane + src]);
-    v *= p < n ? qw[p] : 0.f;
-    __nv_bfloat16 h, l;
-    tc::split_bf16(v, h, l);
-    out[i] = h;
-    out[total + i] = l;
+  for (size_t v8 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v8 < total8;
+       v8 += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = v8 * 8;
+    const int p0 = (int)(i % n_pad);
+    const size_t src = (size_t)H * n_pad + i;  // channel ci + 1
+    const uint4 ah = *reinterpret_cast<const uint4*>(XT + src);
+    const uint4 al = *reinterpret_cast<const uint4*>(XT + src_plane + src);
+    const __nv_bfloat16* hh = reinterpret_cast<const __nv_bfloat16*>(&ah);
+    const __nv_bfloat16* ll = reinterpret_cast<const __nv_bfloat16*>(&al);
+    float w[8];
+    if (p0 + 8 <= n && (reinterpret_cast<uintptr_t>(qw) & 15) == 0) {
+      const float4 w0 = *reinterpret_cast<const float4*>(qw + p0);
+      const float4 w1 = *reinterpret_cast<const float4*>(qw + p0 + 4);
+      w[0] = w0.x; w[1] = w0.y; w[2] = w0.z; w[3] = w0.w;
+      w[4] = w1.x; w[5] = w1.y; w[6] = w1.z; w[7] = w1.w;
+    } else {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) w[t] = p0 + t < n ? qw[p0 + t] : 0.f;
+    }
+    uint4 oh, ol;
+    __nv_bfloat16* h8 = reinterpret_cast<__nv_bfloat16*>(&oh);
+    __nv_bfloat16* l8 = reinterpret_cast<__nv_bfloat16*>(&ol);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const float v = (__bfloat162float(hh[t]) + __bfloat162float(ll[t])) * w[t];
+      tc::split_bf16(v, h8[t], l8[t]);
+    }
+    *reinterpret_cast<uint4*>(out + i) = oh;
+    *reinterpret_cast<uint4*>(out + total + i) = ol;
   }
 }
 
@@ -891,8 +911,8 @@ int tc_hidden_gram(const neb_net* net, const float* qw, int64_t n, const void* h
   __nv_bfloat16* wht = (__nv_bfloat16*)(ws + t.wht);
   {
     KernelScope ks("tc_weighted_fields", s, 0, 3.0 * H * d.n_pad * 8);
-    size_t total = (size_t)3 * H * d.n_pad;
-    int blocks = (int)std::min<size_t>((total + 255) / 256, 8192);
+    size_t total8 = (size_t)3 * H * d.n_pad / 8;
+    int blocks = (int)std::min<size_t>((total8 + 255) / 256, 8192);
     weighted_fields_t<<<blocks, 256, 0, s>>>((const __nv_bfloat16*)XT, qw, (int)n, (int)d.n_pad,
                                              H, wht);
     NEB_LAUNCH_CHECK();
