@@ -421,10 +421,11 @@ __global__ void __launch_bounds__(kMaxM) df_solve_rl(const df* __restrict__ F,
 //   alpha, tau;
 //   one pass over the own rows applies the pending rank-2 update of column
 //   k-1 (A -= v p^T + w v^T, w = p - K2 v) and forms p_i = tau A_i v;
-//   every row owner pushes p_i and A_{i,k+1} (column k+1 before update k,
-//   = row k+1 by symmetry) to every CTA, plus one warp partial of p.v, by
-//   st.async, which completes on the receiver's mbarrier (no cluster
-//   barrier): the receivers wait for the byte count of the column;
+//   every CTA stages (p_i, A_{i,k+1}) of its rows (column k+1 before
+//   update k, = row k+1 by symmetry) and its warp partials of p.v in one
+//   288-byte message and bulk-copies it into every CTA of the cluster
+//   (sixteen copies, one per issuing thread), completing on the receiver's
+//   mbarrier (no cluster barrier): the receivers wait for the byte count;
 //   K2 = tau p.v; the next pivot row, row k+1 after update k, is formed by
 //   every CTA from the pushed column; one __syncthreads.
 // The update is lazy by one column, so each element of the trailing matrix
@@ -436,8 +437,8 @@ __global__ void __launch_bounds__(kMaxM) df_solve_rl(const df* __restrict__ F,
 constexpr int kTriCluster = 16;
 constexpr int kTriThreads = 8 * kMaxM / kTriCluster;  // 8 threads per row
 constexpr int kTriWarps = kTriThreads / 32;
-constexpr int kTriSlots = kTriCluster * kTriWarps;    // p.v partials per column
-constexpr int kTriPush = kTriCluster / 8;              // CTAs each thread pushes to
+constexpr int kTriRows = kMaxM / kTriCluster;          // rows per CTA at m = 512
+constexpr int kTriMsg = 2 * kTriRows + kTriWarps;      // floats per CTA message
 constexpr int kTriChunks = kMaxM / 32;                 // float4 per thread
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -453,11 +454,23 @@ __device__ __forceinline__ uint32_t cluster_map(uint32_t a, int rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
   return r;
 }
-// 4-byte store into another CTA's shared memory that completes (complete_tx,
-// release at cluster scope) on that CTA's mbarrier
-__device__ __forceinline__ void st_async_f32(uint32_t raddr, float v, uint32_t rbar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];"
-               ::"r"(raddr), "r"(__float_as_uint(v)), "r"(rbar) : "memory");
+// Bulk copy of `bytes` (a multiple of 16) from this CTA's shared memory to
+// another CTA's, completing (complete_tx) on that CTA's mbarrier; the
+// issuing thread tracks the reads of its source through bulk async-groups.
+__device__ __forceinline__ void bulk_to_cluster(uint32_t dst, uint32_t src, uint32_t bytes,
+                                                uint32_t rbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+      "[%3];" ::"r"(dst),
+      "r"(src), "r"(bytes), "r"(rbar)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
 }
 // Bounded wait (acquire at cluster scope) for the phase of parity `parity`;
 // the thread sleeps in the hardware up to 20 us per try; false after ~2^32
@@ -485,11 +498,11 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
   const int rank = (int)cluster.block_rank();
   const int rb = m / kTriCluster;
   extern __shared__ __align__(16) float sm[];
-  float* vrow = sm;                 // [2][m] pivot rows k (parity k & 1), zero at j <= k
-  float* pbuf = vrow + 2 * m;       // [2][m] p of column k, pushed
-  float* nrow = pbuf + 2 * m;       // [2][m] column k+1 before update k, pushed
-  float* kps = nrow + 2 * m;        // [2][kTriSlots] warp partials of p.v, pushed
-  float* red = kps + 2 * kTriSlots; // [2][kTriWarps] partials of sigma
+  float* vrow = sm;                        // [2][m] pivot rows k (parity k & 1), zero at j <= k
+  float* pnat = vrow + 2 * m;              // [2][m] p of column k, natural order
+  float* recv = pnat + 2 * m;              // [2][kTriCluster][kTriMsg] received messages
+  float* stage = recv + 2 * kTriCluster * kTriMsg;  // [2][kTriMsg] this CTA's message
+  float* red = stage + 2 * kTriMsg;        // [2][kTriWarps] partials of sigma
   __shared__ __align__(8) unsigned long long bars[2];
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
@@ -519,8 +532,8 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
       const float x = j > 0 ? x0 : 0.f;
       vrow[j] = x;
       vrow[m + j] = 0.f;
-      pbuf[j] = 0.f;
-      pbuf[m + j] = 0.f;
+      pnat[j] = 0.f;
+      pnat[m + j] = 0.f;
       part += x * x;
     }
     part = warp_sum(part);
@@ -532,10 +545,8 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   const uint32_t base = smem_addr(sm);
-  uint32_t rsub[kTriPush];  // shared window of CTAs sub + 8 d
-#pragma unroll
-  for (int d = 0; d < kTriPush; ++d) rsub[d] = cluster_map(base, sub + 8 * d);
-  const uint32_t rlane = cluster_map(base, lane % kTriCluster);
+  // threads tid < kTriCluster each copy the message to CTA tid
+  const uint32_t rdst = cluster_map(base, tid % kTriCluster);
   const uint32_t bar_off = smem_addr(&bars[0]) - base;  // the same in every CTA
   bool failed = false;
   cluster.sync();  // barriers initialised and every CTA running before the first push
@@ -545,10 +556,7 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
     const int par = k & 1, npar = par ^ 1;
     const float* vcur = vrow + par * m;
     float* vprv = vrow + npar * m;
-    const float* pb = pbuf + par * m;
-    const float* pbp = pbuf + npar * m;
-    const float* nr = nrow + par * m;
-    const float* kp = kps + par * kTriSlots;
+    const float* pbp = pnat + npar * m;
     float sigma = 0.f;
     {
       const float4* r4 = reinterpret_cast<const float4*>(red + par * kTriWarps);
@@ -566,7 +574,7 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
     if (tid == 0)
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
                        smem_addr(&bars[par])),
-                   "r"(8u * (m - k - 1) + 4u * kTriSlots)
+                   "r"(4u * kTriCluster * kTriMsg)
                    : "memory");
     if (rank == 0 && tid == 0) {
       e_out[k] = alpha;
@@ -589,7 +597,7 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
       const float4* vc4 = reinterpret_cast<const float4*>(vcur);
       const float4* vp4 = reinterpret_cast<const float4*>(vprv);
       const float4* pp4 = reinterpret_cast<const float4*>(pbp);
-      float s0 = 0.f, s1 = 0.f;
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
 #pragma unroll
       for (int t = 0; t < kTriChunks; ++t) {
         if ((t > 0 || sub >= sk) && t + T < nsub) {
@@ -601,11 +609,11 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
           a[t].w = fmaf(-wprev, vp.w, fmaf(-vprev, pp.w, a[t].w));
           s0 = fmaf(a[t].x, vc.x, s0);
           s1 = fmaf(a[t].y, vc.y, s1);
-          s0 = fmaf(a[t].z, vc.z, s0);
-          s1 = fmaf(a[t].w, vc.w, s1);
+          s2 = fmaf(a[t].z, vc.z, s2);
+          s3 = fmaf(a[t].w, vc.w, s3);
         }
       }
-      sacc = s0 + s1;
+      sacc = (s0 + s1) + (s2 + s3);
     }
     sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
     sacc += __shfl_xor_sync(0xffffffffu, sacc, 2);
@@ -616,36 +624,48 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
     if (active) {
       pi = tau * (sacc - alpha * aik1);
       vi = gi == k + 1 ? v1 : vcur[gi];
-#pragma unroll
-      for (int d = 0; d < kTriPush; ++d) {
-        const uint32_t rbar = rsub[d] + bar_off + 8u * par;
-        st_async_f32(rsub[d] + 4u * (uint32_t)(pb + gi - sm), pi, rbar);
-        st_async_f32(rsub[d] + 4u * (uint32_t)(nr + gi - sm), aik1, rbar);
+    }
+    // every lane of a row holds its p_i v_i: two levels sum the warp's four rows
+    float part = pi * vi;
+    part += __shfl_xor_sync(0xffffffffu, part, 8);
+    part += __shfl_xor_sync(0xffffffffu, part, 16);
+    {
+      float* stg = stage + par * kTriMsg;  // (p_i, A_{i,k+1}) by local row, then partials
+      if (has_row && sub == 0) {
+        stg[2 * li] = pi;
+        stg[2 * li + 1] = aik1;
+      }
+      if (lane == 0) stg[2 * kTriRows + warp] = part;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid < kTriCluster) {
+        bulk_to_cluster(rdst + 4u * (uint32_t)(recv + (par * kTriCluster + rank) * kTriMsg - sm),
+                        smem_addr(stg), 4u * kTriMsg, rdst + bar_off + 8u * par);
+        bulk_commit();
       }
     }
-    {  // every lane of a row holds its p_i v_i: two levels sum the warp's four rows
-      float part = pi * vi;
-      part += __shfl_xor_sync(0xffffffffu, part, 8);
-      part += __shfl_xor_sync(0xffffffffu, part, 16);
-      if (lane < kTriCluster)
-        st_async_f32(rlane + 4u * (uint32_t)(kp + rank * kTriWarps + warp - sm), part,
-                     rlane + bar_off + 8u * par);
-    }
     failed = !cluster_bar_wait(smem_addr(&bars[par]), (uint32_t)(k >> 1) & 1u);
+    const float* rv = recv + par * kTriCluster * kTriMsg;  // message of CTA r at rv + r kTriMsg
     float pv;
     {
-      static_assert(kTriSlots == 128, "one float4 of p.v partials per lane");
-      const float4 q = reinterpret_cast<const float4*>(kp)[lane];
+      static_assert(kTriCluster == 16 && kTriWarps == 8, "two float4 of p.v partials per CTA");
+      const float4 q =
+          reinterpret_cast<const float4*>(rv + (lane >> 1) * kTriMsg + 2 * kTriRows)[lane & 1];
       pv = warp_sum((q.x + q.y) + (q.z + q.w));
     }
     const float K2 = tau * pv;
-    // pivot row k+1 after update k, from column k+1 as it stood before it
-    const float w1 = pb[k + 1] - K2 * v1;
-    float part = 0.f;
+    // pivot row k+1 after update k, from column k+1 as it stood before it;
+    // row j travels in the message of CTA j % 16 at local row j / 16
+    const int k1 = k + 1;
+    const float w1 = rv[(k1 % kTriCluster) * kTriMsg + 2 * (k1 / kTriCluster)] - K2 * v1;
+    part = 0.f;
     for (int j = tid; j < m; j += kTriThreads) {
+      const float2 pc = *reinterpret_cast<const float2*>(rv + (j % kTriCluster) * kTriMsg +
+                                                         2 * (j / kTriCluster));
+      pnat[par * m + j] = pc.x;
       float nv = 0.f;
       if (j > k) {
-        nv = nr[j] - (v1 * pb[j] + w1 * vcur[j]);
+        nv = pc.y - (v1 * pc.x + w1 * vcur[j]);
         if (j == k + 1) {
           if (rank == 0) d_out[k + 1] = nv + w1 * alpha;
           nv = 0.f;
@@ -656,14 +676,16 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
     }
     part = warp_sum(part);
     if (lane == 0) red[npar * kTriWarps + warp] = part;
+    if (tid < kTriCluster) bulk_wait_read<1>();  // column k-1's copies have read their stage
     pprev = pi;
     vprev = vi;
     K2prev = K2;
     failed = __syncthreads_or(failed);
     if (failed) break;
   }
+  if (tid < kTriCluster) bulk_wait_read<0>();
   if (failed) {
-    // a stalled exchange: report it, and let pushes still in flight land
+    // a stalled exchange: report it, and let copies still in flight land
     // before any CTA of the cluster exits
     if (tid == 0) atomicExch(info, -2);
     __nanosleep(50000);
@@ -680,7 +702,7 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
   // d_{m-1}: row m-1 (a[0].w of its last thread) with the pending update
   if (has_row && gi == m - 1 && sub == 7) {
     const float w = pprev - K2prev * vprev;
-    d_out[m - 1] = a[0].w - (vprev * pbuf[pl * m + m - 1] + w * vrow[pl * m + m - 1]);
+    d_out[m - 1] = a[0].w - (vprev * pnat[pl * m + m - 1] + w * vrow[pl * m + m - 1]);
   }
   cluster.sync();
 }
@@ -1156,7 +1178,8 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(kTriCluster);
     cfg.blockDim = dim3(kTriThreads);
-    cfg.dynamicSmemBytes = ((size_t)6 * m + 2 * kTriSlots + 2 * kTriWarps) * sizeof(float);
+    cfg.dynamicSmemBytes =
+        ((size_t)4 * m + 2 * kTriCluster * kTriMsg + 2 * kTriMsg + 2 * kTriWarps) * sizeof(float);
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
