@@ -99,21 +99,6 @@ __device__ __forceinline__ df df_from(double v) {
   return {h, (float)(v - (double)h)};
 }
 __device__ __forceinline__ double df_to(df x) { return (double)x.h + (double)x.l; }
-// 1 / x with one Newton step: r + r (1 - x r)
-__device__ __forceinline__ df df_recip(df x) {
-  float r = 1.0f / x.h;
-  df xr = df_mul(x, df{r, 0.f});
-  df res = df_add(df{1.f, 0.f}, df_neg(xr));
-  return df_add(df{r, 0.f}, df_mul(df{r, 0.f}, res));
-}
-// sqrt(x) with one Newton correction
-__device__ __forceinline__ df df_sqrt(df x) {
-  float s = sqrtf(x.h);
-  float p = s * s;
-  float pe = fmaf(s, s, -p);
-  float r = ((x.h - p) - pe) + x.l;
-  return df_quick(s, r / (2.f * s));
-}
 // Compensated dot product (the Dot2 scheme of Ogita, Rump and Oishi): a
 // running FP32 sum s with TwoSum error terms and the TwoProd / cross-term
 // product errors collected in c, about 11 FP32 operations per term against
@@ -157,11 +142,27 @@ __global__ void to_df(const double* __restrict__ a, df* __restrict__ b, size_t n
 // and invert it for the next panel.  A keeps only trailing updates; the
 // factor lives in Lw (lower tiles), the inverse diagonal tiles in linv_pp.
 
+// 1 / sqrt(v): rsqrtf, then one Newton step r + r (1 - v r^2) / 2 with the
+// residual 1 - v r^2 formed in compensated arithmetic (error ~ (2^-22)^2).
+__device__ __forceinline__ df df_rsqrt(df v) {
+  const float r0 = rsqrtf(v.h);
+  const float q = r0 * r0;
+  const df e = df_add(df{1.f, 0.f}, df_neg(df_mul(v, df{q, fmaf(r0, r0, -q)})));
+  return df_quick(r0, 0.5f * r0 * e.h);
+}
+
+__device__ __forceinline__ void bar_named(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
 // Factor the SPD tile a (shared, 1024 threads: thread (i, j) = (ty, tx))
-// into L and its inverse X = L^-1 (both lower).  One barrier per column: every
-// thread forms r = 1 / sqrt(a_kk) itself, column k of L is a_ik r, and the
-// trailing entries take a_ij -= (a_ik r)(a_jk r).  The inverse is built by
-// doubling: [[X11, 0], [X21, X22]] with X21 = -X22 L21 X11, on blocks of
+// into L and its inverse X = L^-1 (both lower).  One barrier per column:
+// every thread forms l_ik = a_ik r with r = 1 / sqrt(a_kk), and the trailing
+// entries take a_ij -= l_ik (a_jk r).  Column k concerns rows i >= k only, so
+// warp i leaves the loop after its column and the barrier of column k counts
+// warps k+1..31 (named barrier 1).  The reciprocal square root of the next
+// pivot is taken once, by the thread that finished it.  The inverse is built
+// by doubling: [[X11, 0], [X21, X22]] with X21 = -X22 L21 X11, on blocks of
 // 1, 2, 4, 8, 16.  Returns (through *bad) the first failing pivot + 1.
 __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1],
                             df (*Tm)[kCB + 1], df* rinv, int* bad) {
@@ -174,15 +175,13 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
       if (*bad == 0) *bad = 1;
       a00 = df{1.f, 0.f};
     }
-    rinv[0] = df_recip(df_sqrt(a00));
+    rinv[0] = df_rsqrt(a00);
   }
   __syncthreads();
-  // step k: r = 1 / l_kk comes from the thread that finalised a_kk in step
-  // k - 1, so the reciprocal square root is taken once per column
-  for (int k = 0; k < kCB; ++k) {
+  for (int k = 0; k <= i; ++k) {
     const df r = rinv[k];
     const df lik = df_mul(a[i][k], r);
-    if (j == k && i >= k) L[i][k] = lik;
+    if (j == k) L[i][k] = lik;
     if (j > k && i >= j) {
       df v = df_add(a[i][j], df_neg(df_mul(lik, df_mul(a[j][k], r))));
       a[i][j] = v;
@@ -191,11 +190,12 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
           if (*bad == 0) *bad = k + 2;
           v = df{1.f, 0.f};
         }
-        rinv[k + 1] = df_recip(df_sqrt(v));
+        rinv[k + 1] = df_rsqrt(v);
       }
     }
-    __syncthreads();
+    if (k < i) bar_named(1, (kCB - 1 - k) * 32);  // exactly warps k+1..31 arrive
   }
+  __syncthreads();
   if (i == j) X[i][i] = rinv[i];
   __syncthreads();
   for (int s = 1; s < kCB; s <<= 1) {
