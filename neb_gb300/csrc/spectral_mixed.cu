@@ -1197,40 +1197,52 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
                                       info));
     NEB_LAUNCH_CHECK();
   }
+  // The compact-WY factors depend only on the reflectors: wy_factor runs on
+  // a side stream (one per host thread and device) while the tridiagonal
+  // eigenproblem is solved, and wy_apply waits for both.
   {
-    KernelScope ks("spec_tridiag_eig", s, 0, 16.0 * m, 2);
-    {
-      KernelScope k1("tri_eigvals", s, 0, 0, 0);
-      tri_eigvals<<<(m * 32 + 255) / 256, 256, (size_t)2 * m * 4, s>>>(d, e, m, lam);
-      NEB_LAUNCH_CHECK();
+    int dev = 0;
+    NEB_CUDA_CHECK(cudaGetDevice(&dev));
+    NEB_REQUIRE(dev >= 0 && dev < 64, "neb_spectral_mixed: device index %d", dev);
+    static thread_local cudaStream_t side[64] = {};
+    static thread_local cudaEvent_t ev_fork[64] = {}, ev_join[64] = {};
+    if (!side[dev]) {
+      NEB_CUDA_CHECK(cudaStreamCreateWithFlags(&side[dev], cudaStreamNonBlocking));
+      NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork[dev], cudaEventDisableTiming));
+      NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_join[dev], cudaEventDisableTiming));
     }
-    static bool vec_configured = false;
-    if (!vec_configured) {
-      NEB_CUDA_CHECK(cudaFuncSetAttribute(tri_eigvecs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (2 * kMaxM * 32 + 2 * kMaxM) * (int)sizeof(float)));
-      vec_configured = true;
-    }
-    tri_eigvecs<<<(m + 31) / 32, 32, ((size_t)2 * m * 32 + 2 * m) * sizeof(float), s>>>(d, e, m,
-                                                                                        lam, Z);
-    NEB_LAUNCH_CHECK();
-  }
-  {
-    KernelScope ks("spec_backtransform_fp32", s, 4.0 * m * mm, 4.0 * mm * (m / kSolveCols), 2);
     static bool wy_configured = false;
     if (!wy_configured) {
       NEB_CUDA_CHECK(cudaFuncSetAttribute(wy_factor, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           kWY * (kMaxM + 1) * (int)sizeof(float)));
-      wy_configured = true;
-    }
-    const int nblk = (m - 2 + kWY - 1) / kWY;
-    wy_factor<<<nblk, 1024, (size_t)kWY * (m + 1) * sizeof(float), s>>>(Vh, tau, m, Tw);
-    NEB_LAUNCH_CHECK();
-    static bool wya_configured = false;
-    if (!wya_configured) {
       NEB_CUDA_CHECK(cudaFuncSetAttribute(wy_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (kSolveCols + kWY) * kMaxM * (int)sizeof(float)));
-      wya_configured = true;
+      NEB_CUDA_CHECK(cudaFuncSetAttribute(tri_eigvecs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (2 * kMaxM * 32 + 2 * kMaxM) * (int)sizeof(float)));
+      wy_configured = true;
     }
+    NEB_CUDA_CHECK(cudaEventRecord(ev_fork[dev], s));
+    NEB_CUDA_CHECK(cudaStreamWaitEvent(side[dev], ev_fork[dev], 0));
+    {
+      KernelScope ks("wy_factor", side[dev], 2.0 * m * mm, 4.0 * mm, 1);
+      const int nblk = (m - 2 + kWY - 1) / kWY;
+      wy_factor<<<nblk, 1024, (size_t)kWY * (m + 1) * sizeof(float), side[dev]>>>(Vh, tau, m, Tw);
+      NEB_LAUNCH_CHECK();
+    }
+    NEB_CUDA_CHECK(cudaEventRecord(ev_join[dev], side[dev]));
+    {
+      KernelScope ks("spec_tridiag_eig", s, 0, 16.0 * m, 2);
+      {
+        KernelScope k1("tri_eigvals", s, 0, 0, 0);
+        tri_eigvals<<<(m * 32 + 255) / 256, 256, (size_t)2 * m * 4, s>>>(d, e, m, lam);
+        NEB_LAUNCH_CHECK();
+      }
+      tri_eigvecs<<<(m + 31) / 32, 32, ((size_t)2 * m * 32 + 2 * m) * sizeof(float), s>>>(
+          d, e, m, lam, Z);
+      NEB_LAUNCH_CHECK();
+    }
+    NEB_CUDA_CHECK(cudaStreamWaitEvent(s, ev_join[dev], 0));
+    KernelScope ks("spec_backtransform_fp32", s, 2.0 * m * mm, 4.0 * mm * (m / kSolveCols), 1);
     wy_apply<<<m / kSolveCols, 256, (size_t)(kSolveCols + kWY) * m * sizeof(float), s>>>(
         Vh, Tw, m, Z, X);
     NEB_LAUNCH_CHECK();
