@@ -966,27 +966,52 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
                             2.0 * 3 * n * (double)H * H, (double)d.n_pad * C * H * 12)))
       return st;
   }
+  // The parameter gradients of layer l (weight-gradient GEMM, its reduction,
+  // the bias sums) run on a side stream, concurrently with the data gradient
+  // of layer l on the main stream: both only read Zbar_l, so the side work
+  // fills the SMs the data-gradient GEMM leaves idle in its last wave.  The
+  // main stream waits for the side work of layer l before the data gradient
+  // of layer l-1 overwrites that Zbar buffer, and before returning.
+  int dev = 0;
+  NEB_CUDA_CHECK(cudaGetDevice(&dev));
+  NEB_REQUIRE(dev >= 0 && dev < 64, "tensor-core backward: device index %d", dev);
+  static thread_local cudaStream_t side[64] = {};
+  static thread_local cudaEvent_t ev_z[64] = {}, ev_w[64][2] = {};
+  if (!side[dev]) {
+    NEB_CUDA_CHECK(cudaStreamCreateWithFlags(&side[dev], cudaStreamNonBlocking));
+    NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_z[dev], cudaEventDisableTiming));
+    for (int q = 0; q < 2; ++q)
+      NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_w[dev][q], cudaEventDisableTiming));
+  }
+  cudaStream_t s2 = side[dev];
   int cur = 0;
   for (int l = L; l >= 1; --l) {
     const int out = d.w[l], in = d.w[l - 1], inp = d.wp[l - 1];
+    NEB_CUDA_CHECK(cudaEventRecord(ev_z[dev], s));  // Zbar_l is complete
+    NEB_CUDA_CHECK(cudaStreamWaitEvent(s2, ev_z[dev], 0));
     // weight gradient: gW_l[o][i] = sum_c sum_p Zbar_l[c][o][p] X_{l-1}[c][i][p]
     const char* x_prev = (const char*)tape.x[l - 1];
     int splits = 0;
     if ((st = launch_rowsum(zb[cur], C, 0, x_prev, C, 0, C, out, inp, d.n_pad, (float*)part,
-                            status, s, "tc_weight_grad", 2.0 * C * n * (double)out * in,
+                            status, s2, "tc_weight_grad", 2.0 * C * n * (double)out * in,
                             &splits)))
       return st;
-    if ((st = reduce((float*)part, splits, out, inp, in, in, false, gW[l - 1], nullptr, s)))
+    if ((st = reduce((float*)part, splits, out, inp, in, in, false, gW[l - 1], nullptr, s2)))
       return st;
     {
-      {
-        KernelScope ks("bias_grad", s, 0, (double)d.n_pad * out * 4);
-        bias_rows_tc<<<(out + 1) / 2, 256, 0, s>>>((const __nv_bfloat16*)zb[cur], (int)d.n_pad,
-                                                   out, gb[l - 1]);
-        NEB_LAUNCH_CHECK();
-      }
+      KernelScope ks("bias_grad", s2, 0, (double)d.n_pad * out * 4);
+      bias_rows_tc<<<(out + 1) / 2, 256, 0, s2>>>((const __nv_bfloat16*)zb[cur], (int)d.n_pad,
+                                                  out, gb[l - 1]);
+      NEB_LAUNCH_CHECK();
     }
-    if (l == 1) break;
+    NEB_CUDA_CHECK(cudaEventRecord(ev_w[dev][l & 1], s2));  // side work of layer l issued
+    if (l == 1) {
+      NEB_CUDA_CHECK(cudaStreamWaitEvent(s, ev_w[dev][1], 0));
+      break;
+    }
+    // the data gradient of layer l overwrites the Zbar buffer the side work
+    // of layer l+1 read
+    if (l < L) NEB_CUDA_CHECK(cudaStreamWaitEvent(s, ev_w[dev][(l + 1) & 1], 0));
     // data gradient through W_l and the tanh transpose of layer l-1
     CUtensorMap ma, mb;
     if ((st = make_map(&ma, zb[cur], (int64_t)2 * C * out, d.n_pad, 64))) return st;
