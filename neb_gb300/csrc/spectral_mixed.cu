@@ -780,24 +780,31 @@ __global__ void __launch_bounds__(256) tri_eigvals(const double* __restrict__ d,
   if (lane == 0) lam[k] = 0.5 * ((double)a + (double)b);
 }
 
-// Thread per eigenvector: twisted factorisation of T - lam I in FP32 (forward
-// and backward pivots, twist at the smallest |gamma|); the eigenvalue is then
-// refined to the Rayleigh quotient z^T T z / z^T z, accumulated in
-// compensated FP32 (T is FP32, so every product is exact as a float pair),
-// with an error below (eps_32 |T|)^2 / gap.  Z[i][k] (column k) FP32.  T is
-// staged in shared memory as floats; the pivots of the 32 threads of a block
-// live there too, [i][thread].
+// Two threads per eigenvector: twisted factorisation of T - lam I in FP32.
+// Warp 0 of a 64-thread block runs the forward pivots of 32 eigenvectors
+// and warp 1 the backward pivots, at the same time; the twist index r is the
+// smallest |gamma| (each warp scans half of the rows); then warp 0 solves
+// z upwards from r and warp 1 downwards.  The eigenvalue is refined to the
+// Rayleigh quotient z^T T z / z^T z, accumulated in compensated FP32 (T is
+// FP32, so every product is exact as a float pair) with an error below
+// (eps_32 |T|)^2 / gap, each warp summing half of the rows.  Z[i][k] (column
+// k) FP32.  T and the pivots ([i][eigenvector]) live in shared memory.
 __device__ __forceinline__ df two_prod(float a, float b) {
   const float p = a * b;
   return {p, fmaf(a, b, -p)};
 }
 
-__global__ void __launch_bounds__(32) tri_eigvecs(const double* __restrict__ d,
+__global__ void __launch_bounds__(64) tri_eigvecs(const double* __restrict__ d,
                                                   const double* __restrict__ e, int m,
                                                   double* __restrict__ lam, float* __restrict__ Z) {
   extern __shared__ float piv[];  // dp [m][32], dm [m][32], dd [m], ee [m]
-  float* dp = piv + threadIdx.x;                   // dp[i * 32]
-  float* dm = piv + (size_t)m * 32 + threadIdx.x;  // dm[i * 32]
+  __shared__ float best_g[2][32];
+  __shared__ int best_i[2][32];
+  __shared__ df part_n[2][32], part_q[2][32];
+  __shared__ float scale[32];
+  const int v = threadIdx.x & 31, half = threadIdx.x >> 5;
+  float* dp = piv + v;                       // dp[i * 32]
+  float* dm = piv + (size_t)m * 32 + v;      // dm[i * 32]
   float* dd = piv + (size_t)m * 64;
   float* ee = dd + m;
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
@@ -805,68 +812,102 @@ __global__ void __launch_bounds__(32) tri_eigvecs(const double* __restrict__ d,
     ee[i] = i + 1 < m ? (float)e[i] : 0.f;
   }
   __syncthreads();
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= m) return;
-  const float l = (float)lam[k];
+  const int k = blockIdx.x * 32 + v;
+  const bool has = k < m;
+  const float l = has ? (float)lam[k] : 0.f;
   const float tiny = 1e-30f;
-  float q = dd[0] - l;
-  if (fabsf(q) < tiny) q = tiny;
-  dp[0] = q;
-  for (int i = 1; i < m; ++i) {
-    const float ei = ee[i - 1];
-    q = (dd[i] - l) - __fdividef(ei * ei, q);
-    if (fabsf(q) < tiny) q = tiny;
-    dp[i * 32] = q;
-  }
-  q = dd[m - 1] - l;
-  if (fabsf(q) < tiny) q = tiny;
-  dm[(m - 1) * 32] = q;
-  float best = fabsf(dp[(m - 1) * 32] + q - (dd[m - 1] - l));
-  int r = m - 1;
-  for (int i = m - 2; i >= 0; --i) {
-    const float ei = ee[i];
-    q = (dd[i] - l) - __fdividef(ei * ei, q);
-    if (fabsf(q) < tiny) q = tiny;
-    dm[i * 32] = q;
-    const float g = fabsf(dp[i * 32] + q - (dd[i] - l));
-    if (g < best) {
-      best = g;
-      r = i;
+  if (has) {
+    if (half == 0) {  // forward pivots
+      float q = dd[0] - l;
+      if (fabsf(q) < tiny) q = tiny;
+      dp[0] = q;
+      for (int i = 1; i < m; ++i) {
+        const float ei = ee[i - 1];
+        q = (dd[i] - l) - __fdividef(ei * ei, q);
+        if (fabsf(q) < tiny) q = tiny;
+        dp[i * 32] = q;
+      }
+    } else {  // backward pivots
+      float q = dd[m - 1] - l;
+      if (fabsf(q) < tiny) q = tiny;
+      dm[(m - 1) * 32] = q;
+      for (int i = m - 2; i >= 0; --i) {
+        const float ei = ee[i];
+        q = (dd[i] - l) - __fdividef(ei * ei, q);
+        if (fabsf(q) < tiny) q = tiny;
+        dm[i * 32] = q;
+      }
     }
   }
-  float z = 1.f;
-  Z[(size_t)r * m + k] = 1.f;
-  for (int i = r - 1; i >= 0; --i) {
-    z = -__fdividef(ee[i], dp[i * 32]) * z;
-    if (fabsf(z) < 1e-30f) z = 0.f;
-    Z[(size_t)i * m + k] = z;
+  __syncthreads();
+  // twist: smallest |gamma_i| = |dp_i + dm_i - (d_i - lam)|, ties to the higher i
+  const int hm = m / 2;
+  if (has) {
+    const int i0 = half ? hm : 0, i1 = half ? m : hm;
+    float best = 3e38f;
+    int r = i1 - 1;
+    for (int i = i1 - 1; i >= i0; --i) {
+      const float g = fabsf(dp[i * 32] + dm[i * 32] - (dd[i] - l));
+      if (g < best) {
+        best = g;
+        r = i;
+      }
+    }
+    best_g[half][v] = best;
+    best_i[half][v] = r;
   }
-  z = 1.f;
-  for (int i = r + 1; i < m; ++i) {
-    z = -__fdividef(ee[i - 1], dm[i * 32]) * z;
-    if (fabsf(z) < 1e-30f) z = 0.f;
-    Z[(size_t)i * m + k] = z;
-  }
-  // Rayleigh quotient and norm in compensated FP32, two chains each
-  df n0{0.f, 0.f}, n1{0.f, 0.f}, q0{0.f, 0.f}, q1{0.f, 0.f};
-  float zp = 0.f;
-  for (int i = 0; i < m; ++i) {
-    const float zi = Z[(size_t)i * m + k];
-    df t = df_mul(two_prod(dd[i], zi), df{zi, 0.f});
-    if (i > 0) t = df_add(t, df_mul(two_prod(2.f * ee[i - 1], zp), df{zi, 0.f}));
-    if (i & 1) {
-      n1 = df_add(n1, two_prod(zi, zi));
-      q1 = df_add(q1, t);
+  __syncthreads();
+  const int r = best_g[1][v] <= best_g[0][v] ? best_i[1][v] : best_i[0][v];
+  if (has) {
+    float z = 1.f;
+    if (half == 0) {
+      Z[(size_t)r * m + k] = 1.f;
+      for (int i = r - 1; i >= 0; --i) {
+        z = -__fdividef(ee[i], dp[i * 32]) * z;
+        if (fabsf(z) < 1e-30f) z = 0.f;
+        Z[(size_t)i * m + k] = z;
+      }
     } else {
-      n0 = df_add(n0, two_prod(zi, zi));
-      q0 = df_add(q0, t);
+      for (int i = r + 1; i < m; ++i) {
+        z = -__fdividef(ee[i - 1], dm[i * 32]) * z;
+        if (fabsf(z) < 1e-30f) z = 0.f;
+        Z[(size_t)i * m + k] = z;
+      }
     }
-    zp = zi;
   }
-  const double nrm = df_to(df_add(n0, n1));
-  lam[k] = df_to(df_add(q0, q1)) / nrm;
-  const float sc = (float)(1.0 / sqrt(nrm));
-  for (int i = 0; i < m; ++i) Z[(size_t)i * m + k] *= sc;
+  __syncthreads();
+  // Rayleigh quotient and norm in compensated FP32, two chains per half
+  const int i0 = half ? hm : 0, i1 = half ? m : hm;
+  if (has) {
+    df n0{0.f, 0.f}, n1{0.f, 0.f}, q0{0.f, 0.f}, q1{0.f, 0.f};
+    float zp = i0 > 0 ? Z[(size_t)(i0 - 1) * m + k] : 0.f;
+    for (int i = i0; i < i1; ++i) {
+      const float zi = Z[(size_t)i * m + k];
+      df t = df_mul(two_prod(dd[i], zi), df{zi, 0.f});
+      if (i > 0) t = df_add(t, df_mul(two_prod(2.f * ee[i - 1], zp), df{zi, 0.f}));
+      if (i & 1) {
+        n1 = df_add(n1, two_prod(zi, zi));
+        q1 = df_add(q1, t);
+      } else {
+        n0 = df_add(n0, two_prod(zi, zi));
+        q0 = df_add(q0, t);
+      }
+      zp = zi;
+    }
+    part_n[half][v] = df_add(n0, n1);
+    part_q[half][v] = df_add(q0, q1);
+  }
+  __syncthreads();
+  if (has && half == 0) {
+    const double nrm = df_to(df_add(part_n[0][v], part_n[1][v]));
+    lam[k] = df_to(df_add(part_q[0][v], part_q[1][v])) / nrm;
+    scale[v] = (float)(1.0 / sqrt(nrm));
+  }
+  __syncthreads();
+  if (has) {
+    const float sc = scale[v];
+    for (int i = i0; i < i1; ++i) Z[(size_t)i * m + k] *= sc;
+  }
 }
 
 // Back-transformation x_k = H_0 H_1 ... H_{m-3} z_k in blocks of 32
@@ -1237,7 +1278,7 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
         tri_eigvals<<<(m * 32 + 255) / 256, 256, (size_t)2 * m * 4, s>>>(d, e, m, lam);
         NEB_LAUNCH_CHECK();
       }
-      tri_eigvecs<<<(m + 31) / 32, 32, ((size_t)2 * m * 32 + 2 * m) * sizeof(float), s>>>(
+      tri_eigvecs<<<(m + 31) / 32, 64, ((size_t)2 * m * 32 + 2 * m) * sizeof(float), s>>>(
           d, e, m, lam, Z);
       NEB_LAUNCH_CHECK();
     }
