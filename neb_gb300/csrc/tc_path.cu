@@ -106,12 +106,11 @@ template <int EPI> struct JetCfg {
   // accumulator buffers in the 512 TMEM columns (double-buffered when they fit)
   static constexpr int NBUF = 2 * NCH * BN <= 512 ? 2 : 1;
   static constexpr int TBUF = 512 / NBUF;        // TMEM columns per accumulator buffer
-  static constexpr int A_ST = 3;
+  static constexpr int A_ST = 5;
   static constexpr int B_ST = 2;
   static constexpr int B_TILE = BN * 128;        // BN rows x 64 bf16
   static constexpr int B_BYTES = 2 * NB * B_TILE;
-  static constexpr int STAGE = 8 * 8192;         // epilogue transpose staging, 8 warps
-  static constexpr int SMEM = 1024 + A_ST * 2 * kTileBytes + B_ST * B_BYTES + STAGE + 256;
+  static constexpr int SMEM = 1024 + A_ST * 2 * kTileBytes + B_ST * B_BYTES + 256;
 };
 
 
@@ -133,8 +132,7 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   uint8_t* smem = align1024(smem_raw);
   uint8_t* a_smem = smem;
   uint8_t* b_smem = smem + A_ST * 2 * kTileBytes;
-  uint8_t* st_smem = b_smem + B_ST * Cfg::B_BYTES;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(st_smem + Cfg::STAGE);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(b_smem + B_ST * Cfg::B_BYTES);
   uint64_t* a_full = bars;
   uint64_t* a_empty = bars + A_ST;
   uint64_t* b_full = bars + 2 * A_ST;
@@ -243,8 +241,6 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     const int q = warp & 3, half = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     const size_t plane = (size_t)C * g.n_pad * g.N;  // elements of one hi or lo plane
-    // transposed outputs are staged per warp: [C][2 planes][16 columns][32 points]
-    __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(st_smem) + (size_t)(warp - 2) * 4096;
     int it = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
       const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
@@ -332,30 +328,19 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             for (int c = 0; c < C; ++c) out[c][j] = v[c];
           }
         }
-        // split outputs [2][C][N][n_pad] (points contiguous), staged through
-        // shared memory into 16-byte vectors of 8 points
+        // split outputs [2][C][N][n_pad] (points contiguous): each store of a
+        // warp writes 32 consecutive points (64 bytes)
 #pragma unroll
         for (int c = 0; c < C; ++c) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             __nv_bfloat16 h, l;
             tc::split_bf16(out[c][j], h, l);
-            stage[((c * 2 + 0) * 16 + j) * 32 + lane] = h;
-            stage[((c * 2 + 1) * 16 + j) * 32 + lane] = l;
+            const size_t gi = ((size_t)c * g.N + col + j) * g.n_pad + p;
+            g.yt_out[gi] = h;
+            g.yt_out[plane + gi] = l;
           }
         }
-        __syncwarp();
-        const uint4* st4 = reinterpret_cast<const uint4*>(stage);
-#pragma unroll
-        for (int u8 = 0; u8 < 16; ++u8) {
-          const int u = lane + 32 * u8;        // 512 vectors of 8 points
-          const int r = u >> 2, quad = u & 3;  // r = (c * 2 + plane) * 16 + j
-          const int c = r >> 5, pl = (r >> 4) & 1, j = r & 15;
-          const size_t gi = (size_t)pl * plane + ((size_t)c * g.N + col + j) * g.n_pad + p0 +
-                            q * 32 + quad * 8;
-          *reinterpret_cast<uint4*>(g.yt_out + gi) = st4[u];
-        }
-        __syncwarp();
       }
     }
   }
