@@ -95,6 +95,12 @@ struct JetGemmArgs {
   int* status;
 };
 
+// epilogue warps of the jet GEMM (four per TMEM lane quarter) and the
+// accumulator columns each reads per TMEM load
+constexpr int kJetEpiWarps = 16;
+constexpr int kJetEpiCols = 8;
+constexpr int kJetThreads = 64 + 32 * kJetEpiWarps;
+
 template <int EPI> struct JetCfg {
   // output columns per tile: 128 for the layer GEMMs (single accumulator
   // buffer, wider MMAs); 64 for the Gram adjoint (three channels, so two
@@ -119,10 +125,10 @@ template <int EPI> struct JetCfg {
 // keeps loading operand stages across tile boundaries; the accumulators are
 // double-buffered in tensor memory when 2 x NCH x BN columns fit in 512, so
 // the epilogue of one tile can overlap the MMAs of the next.  Roles: warp 0 lane 0 issues TMA
-// loads, warp 1 lane 0 issues MMAs, warps 2-9 run the epilogue (lane quarter
-// w % 4, column half (w - 2) / 4).
+// loads, warp 1 lane 0 issues MMAs, warps 2-17 run the epilogue (lane quarter
+// w % 4, column quarter (w - 2) / 4 of the tile, in chunks of kJetEpiCols).
 template <int EPI>
-__global__ void __launch_bounds__(320, 1)
+__global__ void __launch_bounds__(kJetThreads, 1)
 tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             JetGemmArgs g) {
   using Cfg = JetCfg<EPI>;
@@ -157,7 +163,7 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     }
     for (int i = 0; i < 2; ++i) {
       tc::mbar_init(&acc_full[i], 1);
-      tc::mbar_init(&acc_empty[i], 8);  // one arrival per epilogue warp
+      tc::mbar_init(&acc_empty[i], kJetEpiWarps);  // one arrival per epilogue warp
     }
     tc::fence_mbar_init();
   }
@@ -237,8 +243,9 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       tc::mma_commit(&acc_full[buf]);
     }
   } else if (warp >= 2) {
-    // ---------------- epilogue: eight warps, one thread per point (TMEM lane)
-    const int q = warp & 3, half = (warp - 2) >> 2;
+    // ---------------- epilogue: kJetEpiWarps warps, one thread per point
+    // (TMEM lane): warp w reads lane quarter w % 4, column slice (w - 2) / 4
+    const int q = warp & 3, slice = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     const size_t plane = (size_t)C * g.n_pad * g.N;  // elements of one hi or lo plane
     int it = 0;
@@ -248,40 +255,42 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       const int buf = it % Cfg::NBUF, use = it / Cfg::NBUF;
       float w2 = 0.f;
       if constexpr (EPI == 2) w2 = p < g.n_points ? 2.f * g.qw[p] : 0.f;
-      constexpr int kChunks = BN / 32;  // 16-column chunks of this warp's half
+      constexpr int kW = kJetEpiCols;                  // columns per TMEM load
+      constexpr int kSlice = BN / (kJetEpiWarps / 4);  // columns of this warp
+      constexpr int kChunks = kSlice / kW;
       for (int jc = 0; jc < kChunks; ++jc) {
-        const int j0 = half * (BN / 2) + jc * 16;
+        const int j0 = slice * kSlice + jc * kW;
         const int col = n0 + j0;
         // global operands first (bias, or the pre-activations of the target
         // layer), so their latency overlaps the accumulator wait and loads
-        float out[C][16];
-        float bias16[16];
+        float out[C][kW];
+        float bias_c[kW];
         if constexpr (EPI == 0) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) bias16[j] = __ldg(g.bias + col + j);
+          for (int j = 0; j < kW; ++j) bias_c[j] = __ldg(g.bias + col + j);
         } else {
 #pragma unroll
           for (int c = 0; c < C; ++c)
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
+            for (int j = 0; j < kW; ++j)
               out[c][j] = __ldg(g.zprev + ((size_t)c * g.N + col + j) * g.n_pad + p);
         }
         if (jc == 0) {
           tc::mbar_wait(&acc_full[buf], use & 1, g.status);
           tc::tc_fence_after();
         }
-        uint32_t raw[NCH][16];
+        uint32_t raw[NCH][kW];
 #pragma unroll
         for (int ci = 0; ci < NCH; ++ci)
-          tc::tmem_ld16_issue(tmem + ((uint32_t)(q * 32) << 16) + buf * Cfg::TBUF + ci * BN + j0,
+          tc::tmem_ld_issue<kW>(tmem + ((uint32_t)(q * 32) << 16) + buf * Cfg::TBUF + ci * BN + j0,
                               raw[ci]);
         tc::tmem_ld_wait();
-        float acc[NCH][16];
+        float acc[NCH][kW];
 #pragma unroll
         for (int ci = 0; ci < NCH; ++ci) {
           tc::tmem_ld_fence(raw[ci]);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) acc[ci][j] = __uint_as_float(raw[ci][j]);
+          for (int j = 0; j < kW; ++j) acc[ci][j] = __uint_as_float(raw[ci][j]);
         }
         if (jc == kChunks - 1) {  // this warp's columns of the buffer are drained
           tc::tc_fence_before();
@@ -290,18 +299,18 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
         }
         if constexpr (EPI == 0) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < kW; ++j) {
 #pragma unroll
             for (int c = 0; c < C; ++c) out[c][j] = acc[c][j];
-            out[0][j] += bias16[j];
+            out[0][j] += bias_c[j];
           }
 #pragma unroll
           for (int c = 0; c < C; ++c)
 #pragma unroll
-            for (int j = 0; j < 16; ++j)  // [C][N][n_pad]: a warp stores 32 points
+            for (int j = 0; j < kW; ++j)  // [C][N][n_pad]: a warp stores 32 points
               g.z_out[((size_t)c * g.N + col + j) * g.n_pad + p] = out[c][j];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < kW; ++j) {
             float v[C];
 #pragma unroll
             for (int c = 0; c < C; ++c) v[c] = out[c][j];
@@ -311,7 +320,7 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < kW; ++j) {
             float z[C], v[C];
 #pragma unroll
             for (int c = 0; c < C; ++c) z[c] = out[c][j];
@@ -333,7 +342,7 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 #pragma unroll
         for (int c = 0; c < C; ++c) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < kW; ++j) {
             __nv_bfloat16 h, l;
             tc::split_bf16(out[c][j], h, l);
             const size_t gi = ((size_t)c * g.N + col + j) * g.n_pad + p;
@@ -751,7 +760,7 @@ int launch_jet(const CUtensorMap& A, const CUtensorMap& B, const JetGemmArgs& ar
               JetCfg<EPI>::BN);
   const int tiles = (args.N / JetCfg<EPI>::BN) * p_tiles;
   KernelScope ks(name, s, flops, bytes);
-  tc_jet_gemm<EPI><<<std::min(tiles, sms), 320, JetCfg<EPI>::SMEM, s>>>(A, B, args);
+  tc_jet_gemm<EPI><<<std::min(tiles, sms), kJetThreads, JetCfg<EPI>::SMEM, s>>>(A, B, args);
   NEB_LAUNCH_CHECK();
   return NEB_OK;
 }
