@@ -1041,6 +1041,13 @@ __global__ void scale_rows(const float* __restrict__ E, const double* __restrict
   }
 }
 
+__global__ void fill_identity(float* __restrict__ I, int m) {
+  const size_t n = (size_t)m * m;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    I[i] = (i / m == i % m) ? 1.f : 0.f;
+}
+
 __global__ void f32_to_f64(const float* __restrict__ a, double* __restrict__ b, size_t n,
                            double scale) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -1238,9 +1245,10 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
                                       info));
     NEB_LAUNCH_CHECK();
   }
-  // The compact-WY factors depend only on the reflectors: wy_factor runs on
-  // a side stream (one per host thread and device) while the tridiagonal
-  // eigenproblem is solved, and wy_apply waits for both.
+  // The back-transformation depends only on the reflectors: on a side stream
+  // (one per host thread and device) wy_factor forms the compact-WY factors
+  // and wy_apply applies Q to the identity (G = Q^T) while the tridiagonal
+  // eigenproblem is solved on the main stream; X = Z^T Q^T is then one SGEMM.
   {
     int dev = 0;
     NEB_CUDA_CHECK(cudaGetDevice(&dev));
@@ -1270,6 +1278,15 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
       wy_factor<<<nblk, 1024, (size_t)kWY * (m + 1) * sizeof(float), side[dev]>>>(Vh, tau, m, Tw);
       NEB_LAUNCH_CHECK();
     }
+    {
+      KernelScope ks("wy_form_q", side[dev], 2.0 * m * mm, 4.0 * mm * (m / kSolveCols), 2);
+      const int blocks = (int)std::min<size_t>((mm + 255) / 256, 2048);
+      fill_identity<<<blocks, 256, 0, side[dev]>>>(Es, m);
+      NEB_LAUNCH_CHECK();
+      wy_apply<<<m / kSolveCols, 256, (size_t)(kSolveCols + kWY) * m * sizeof(float), side[dev]>>>(
+          Vh, Tw, m, Es, G);
+      NEB_LAUNCH_CHECK();
+    }
     NEB_CUDA_CHECK(cudaEventRecord(ev_join[dev], side[dev]));
     {
       KernelScope ks("spec_tridiag_eig", s, 0, 16.0 * m, 2);
@@ -1283,10 +1300,8 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
       NEB_LAUNCH_CHECK();
     }
     NEB_CUDA_CHECK(cudaStreamWaitEvent(s, ev_join[dev], 0));
-    KernelScope ks("spec_backtransform_fp32", s, 2.0 * m * mm, 4.0 * mm * (m / kSolveCols), 1);
-    wy_apply<<<m / kSolveCols, 256, (size_t)(kSolveCols + kWY) * m * sizeof(float), s>>>(
-        Vh, Tw, m, Z, X);
-    NEB_LAUNCH_CHECK();
+    KernelScope ks("spec_backtransform_fp32", s, 2.0 * m * mm, 12.0 * mm, 1);
+    if ((st = sgemm_rm(h, true, false, m, m, m, 1.f, Z, m, G, m, 0.f, X, m))) return st;
   }
   {
     KernelScope ks("spec_adjoints_fp32", s, 6.0 * m * mm, 24.0 * mm, 9);
