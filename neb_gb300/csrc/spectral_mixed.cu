@@ -155,6 +155,17 @@ __device__ __forceinline__ void bar_named(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
+// Programmatic dependent launch: a kernel launched with the
+// programmatic-stream-serialization attribute may start while the previous
+// kernel of the stream runs; it waits here until that kernel has completed
+// and its writes are visible.  The previous kernel lets it start early.
+__device__ __forceinline__ void pdl_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_allow_next() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Factor the SPD tile a (shared, 1024 threads: thread (i, j) = (ty, tx))
 // into L and its inverse X = L^-1 (both lower).  One barrier per column:
 // every thread forms l_ik = a_ik r with r = 1 / sqrt(a_kk), and the trailing
@@ -223,6 +234,7 @@ __global__ void __launch_bounds__(1024) chol_first(const df* __restrict__ A, int
   __shared__ df a[kCB][kCB + 1], L[kCB][kCB + 1], X[kCB][kCB + 1], Tm[kCB][kCB + 1];
   __shared__ df rinv[kCB];
   __shared__ int bad;
+  pdl_allow_next();  // the first panel launch may take its SMs now
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   a[ty][tx] = A[(size_t)ty * m + tx];
   if (threadIdx.x == 0) bad = 0;
@@ -242,6 +254,8 @@ __global__ void __launch_bounds__(1024) chol_step(df* __restrict__ A, int m, int
   __shared__ df tl[kCB][kCB + 1];  // the updated tile
   __shared__ df rinv[kCB];
   __shared__ int bad;
+  pdl_allow_next();
+  pdl_wait();  // the previous panel (or chol_first) has finished
   int t = blockIdx.x, bi = p + 1;
   while (t >= bi - p) {  // tile index -> (bi, bj) with p < bj <= bi
     t -= bi - p;
@@ -1187,9 +1201,19 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     NEB_LAUNCH_CHECK();
     chol_first<<<1, 1024, 0, s>>>(Mw, m, Lw, linv_pp, info);
     NEB_LAUNCH_CHECK();
+    // the panel launches start while their predecessor finishes (programmatic
+    // dependent launch): the launch latency leaves the panel-to-panel chain
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
     for (int p = 0; p + 1 < nb; ++p) {
-      const int tiles = (nb - p - 1) * (nb - p) / 2;
-      chol_step<<<tiles, 1024, 0, s>>>(Mw, m, p, Lw, linv_pp, info);
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((nb - p - 1) * (nb - p) / 2);
+      cfg.blockDim = dim3(1024);
+      cfg.stream = s;
+      cfg.attrs = pdl;
+      cfg.numAttrs = 1;
+      NEB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, chol_step, Mw, m, p, Lw, linv_pp, info));
       NEB_LAUNCH_CHECK();
     }
   }
