@@ -138,6 +138,19 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // KernelScope, which counts it and, while timing is enabled
 // (neb_timing_begin / neb_timing_end), brackets it with CUDA events on the
 // launching stream and records its algorithmic flops and bytes.
+// Joins a side stream back into the main stream when it leaves scope, so an
+// early error return still leaves the side work ordered before whatever the
+// caller enqueues next on the main stream.  Disarmed once the normal path
+// has joined explicitly.
+struct SideStreamJoin {
+  cudaStream_t main, side;
+  cudaEvent_t ev;
+  bool armed;
+  ~SideStreamJoin() {
+    if (armed && cudaEventRecord(ev, side) == cudaSuccess) cudaStreamWaitEvent(main, ev, 0);
+  }
+};
+
 void timing_record(const char* name, cudaStream_t s, double flops, double bytes, bool begin);
 void count_launch(int n = 1);
 

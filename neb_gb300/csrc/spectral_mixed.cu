@@ -1296,6 +1296,7 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     }
     NEB_CUDA_CHECK(cudaEventRecord(ev_fork[dev], s));
     NEB_CUDA_CHECK(cudaStreamWaitEvent(side[dev], ev_fork[dev], 0));
+    SideStreamJoin join{s, side[dev], ev_join[dev], true};
     {
       KernelScope ks("wy_factor", side[dev], 2.0 * m * mm, 4.0 * mm, 1);
       const int nblk = (m - 2 + kWY - 1) / kWY;
@@ -1324,6 +1325,7 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
       NEB_LAUNCH_CHECK();
     }
     NEB_CUDA_CHECK(cudaStreamWaitEvent(s, ev_join[dev], 0));
+    join.armed = false;
     KernelScope ks("spec_backtransform_fp32", s, 2.0 * m * mm, 12.0 * mm, 1);
     if ((st = sgemm_rm(h, true, false, m, m, m, 1.f, Z, m, G, m, 0.f, X, m))) return st;
   }

@@ -970,14 +970,16 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
   NEB_CUDA_CHECK(cudaGetDevice(&dev));
   NEB_REQUIRE(dev >= 0 && dev < 64, "tensor-core backward: device index %d", dev);
   static thread_local cudaStream_t side[64] = {};
-  static thread_local cudaEvent_t ev_z[64] = {}, ev_w[64][2] = {};
+  static thread_local cudaEvent_t ev_z[64] = {}, ev_w[64][2] = {}, ev_j[64] = {};
   if (!side[dev]) {
     NEB_CUDA_CHECK(cudaStreamCreateWithFlags(&side[dev], cudaStreamNonBlocking));
     NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_z[dev], cudaEventDisableTiming));
     for (int q = 0; q < 2; ++q)
       NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_w[dev][q], cudaEventDisableTiming));
+    NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_j[dev], cudaEventDisableTiming));
   }
   cudaStream_t s2 = side[dev];
+  SideStreamJoin join{s, s2, ev_j[dev], true};
   int cur = 0;
   for (int l = L; l >= 1; --l) {
     const int out = d.w[l], in = d.w[l - 1], inp = d.wp[l - 1];
@@ -1001,6 +1003,7 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
     NEB_CUDA_CHECK(cudaEventRecord(ev_w[dev][l & 1], s2));  // side work of layer l issued
     if (l == 1) {
       NEB_CUDA_CHECK(cudaStreamWaitEvent(s, ev_w[dev][1], 0));
+      join.armed = false;
       break;
     }
     // the data gradient of layer l overwrites the Zbar buffer the side work
