@@ -17,22 +17,28 @@
 // the objective adjoints G_S = V diag(c) V^T, G_M = -V diag(c lam) V^T run in
 // FP32 (they only feed the reverse pass).
 //
-// Pipeline (one stream, no host synchronisation):
+// Pipeline (no host synchronisation; the caller's stream plus one side
+// stream that forks after the tridiagonalisation and joins before the
+// back-transformation):
 //   chol_first / chol_step                 blocked Cholesky, 32-column panels,
-//                                          compensated FP32 (FP64-class)
+//                                          compensated FP32 (FP64-class); the
+//                                          panel launches overlap their
+//                                          predecessor (programmatic dependent
+//                                          launch)
 //   2 x df_solve_rl                        C = L^-1 S L^-T by two right-looking
 //                                          blocked triangular solves with inverse
 //                                          diagonal blocks, compensated FP32
 //   tridiag_cluster                        FP32 Householder tridiagonalisation in
 //                                          one 16-CTA cluster, the rows held in
-//                                          registers, per-column exchange by
-//                                          st.async into mbarrier-guarded
-//                                          shared memory
+//                                          registers, per-column exchange by bulk
+//                                          copies into mbarrier-guarded shared
+//                                          memory
 //   tri_eigvals                            eigenvalue brackets of T, warp per eigenvalue
 //   tri_eigvecs                            eigenvectors of T by twisted factorisations,
 //                                          eigenvalues refined to FP64 Rayleigh quotients
-//   wy_factor / wy_apply                   x_k = Q z_k (FP32), 32 reflectors per
-//                                          block in compact WY form
+//   side: wy_factor / wy_apply on I        Q^T (FP32), 32 reflectors per block in
+//                                          compact WY form, during the two above
+//   SGEMM                                  X = Z^T Q^T (rows x_k = Q z_k)
 //   df_solve_rl, SGEMMs                    V rows = (L^-T x_k)^T, G_S, G_M
 #include <cooperative_groups.h>
 #include <cublas_v2.h>
