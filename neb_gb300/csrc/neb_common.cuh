@@ -138,6 +138,21 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // KernelScope, which counts it and, while timing is enabled
 // (neb_timing_begin / neb_timing_end), brackets it with CUDA events on the
 // launching stream and records its algorithmic flops and bytes.
+// Per-device caches (function attributes set, SM counts, side streams) are
+// arrays indexed by the device ordinal.
+constexpr int kMaxDevices = 64;
+
+// The current device and its SM count (cached per device).
+inline int device_sms(int* dev, int* sms) {
+  static int count[kMaxDevices] = {};
+  NEB_CUDA_CHECK(cudaGetDevice(dev));
+  NEB_REQUIRE(*dev >= 0 && *dev < kMaxDevices, "device index %d", *dev);
+  if (!count[*dev])
+    NEB_CUDA_CHECK(cudaDeviceGetAttribute(&count[*dev], cudaDevAttrMultiProcessorCount, *dev));
+  *sms = count[*dev];
+  return NEB_OK;
+}
+
 // Joins a side stream back into the main stream when it leaves scope, so an
 // early error return still leaves the side work ordered before whatever the
 // caller enqueues next on the main stream.  Disarmed once the normal path

@@ -1261,13 +1261,17 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    static int clusters = -1;  // co-resident 16-CTA clusters (non-portable size)
-    if (clusters < 0) {
+    int dev = 0, sms = 0;
+    if ((st = device_sms(&dev, &sms))) return st;
+    static int clusters[kMaxDevices];  // co-resident 16-CTA clusters (non-portable size)
+    static bool probed[kMaxDevices] = {};
+    if (!probed[dev]) {
       NEB_CUDA_CHECK(cudaFuncSetAttribute(tridiag_cluster,
                                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      NEB_CUDA_CHECK(cudaOccupancyMaxActiveClusters(&clusters, tridiag_cluster, &cfg));
+      NEB_CUDA_CHECK(cudaOccupancyMaxActiveClusters(&clusters[dev], tridiag_cluster, &cfg));
+      probed[dev] = true;
     }
-    NEB_REQUIRE(clusters >= 1,
+    NEB_REQUIRE(clusters[dev] >= 1,
                 "neb_spectral_mixed: the GPU cannot co-schedule a %d-CTA thread-block cluster",
                 kTriCluster);
     KernelScope ks("spec_tridiag_cluster_fp32", s, 4.0 / 3.0 * m * mm, 8.0 * mm);
@@ -1280,25 +1284,24 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   // and wy_apply applies Q to the identity (G = Q^T) while the tridiagonal
   // eigenproblem is solved on the main stream; X = Z^T Q^T is then one SGEMM.
   {
-    int dev = 0;
-    NEB_CUDA_CHECK(cudaGetDevice(&dev));
-    NEB_REQUIRE(dev >= 0 && dev < 64, "neb_spectral_mixed: device index %d", dev);
-    static thread_local cudaStream_t side[64] = {};
-    static thread_local cudaEvent_t ev_fork[64] = {}, ev_join[64] = {};
+    int dev = 0, sms = 0;
+    if ((st = device_sms(&dev, &sms))) return st;
+    static thread_local cudaStream_t side[kMaxDevices] = {};
+    static thread_local cudaEvent_t ev_fork[kMaxDevices] = {}, ev_join[kMaxDevices] = {};
     if (!side[dev]) {
       NEB_CUDA_CHECK(cudaStreamCreateWithFlags(&side[dev], cudaStreamNonBlocking));
       NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork[dev], cudaEventDisableTiming));
       NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_join[dev], cudaEventDisableTiming));
     }
-    static bool wy_configured = false;
-    if (!wy_configured) {
+    static bool wy_configured[kMaxDevices] = {};
+    if (!wy_configured[dev]) {
       NEB_CUDA_CHECK(cudaFuncSetAttribute(wy_factor, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           kWY * (kMaxM + 1) * (int)sizeof(float)));
       NEB_CUDA_CHECK(cudaFuncSetAttribute(wy_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (kSolveCols + kWY) * kMaxM * (int)sizeof(float)));
       NEB_CUDA_CHECK(cudaFuncSetAttribute(tri_eigvecs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (2 * kMaxM * 32 + 2 * kMaxM) * (int)sizeof(float)));
-      wy_configured = true;
+      wy_configured[dev] = true;
     }
     NEB_CUDA_CHECK(cudaEventRecord(ev_fork[dev], s));
     NEB_CUDA_CHECK(cudaStreamWaitEvent(side[dev], ev_fork[dev], 0));

@@ -742,18 +742,14 @@ TcWs tc_ws(const Dims& d) {
 template <int EPI>
 int launch_jet(const CUtensorMap& A, const CUtensorMap& B, const JetGemmArgs& args, int n_tiles,
                int p_tiles, cudaStream_t s, const char* name, double flops, double bytes) {
-  static bool configured = false;
-  if (!configured) {
+  int dev = 0, sms = 0;
+  if (int st = device_sms(&dev, &sms)) return st;
+  static bool configured[kMaxDevices] = {};
+  if (!configured[dev]) {
     NEB_CUDA_CHECK(cudaFuncSetAttribute(tc_jet_gemm<EPI>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         JetCfg<EPI>::SMEM));
-    configured = true;
-  }
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    NEB_CUDA_CHECK(cudaGetDevice(&dev));
-    NEB_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    configured[dev] = true;
   }
   (void)n_tiles;
   NEB_REQUIRE(args.N % JetCfg<EPI>::BN == 0, "jet GEMM: N = %d must be a multiple of %d", args.N,
@@ -770,11 +766,13 @@ int launch_jet(const CUtensorMap& A, const CUtensorMap& B, const JetGemmArgs& ar
 template <int BN>
 int launch_rowsum_bn(const CUtensorMap& A, const CUtensorMap& B, RowsumArgs g, cudaStream_t s,
                      const char* name, double flops, double bytes) {
-  static bool configured = false;
-  if (!configured) {
+  int dev = 0, sms = 0;
+  if (int st = device_sms(&dev, &sms)) return st;
+  static bool configured[kMaxDevices] = {};
+  if (!configured[dev]) {
     NEB_CUDA_CHECK(cudaFuncSetAttribute(tc_rowsum<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         RowCfg<BN>::SMEM));
-    configured = true;
+    configured[dev] = true;
   }
   KernelScope ks(name, s, flops, bytes);
   dim3 grid((g.M / 128) * (g.N / BN), g.splits);
@@ -792,7 +790,9 @@ int launch_rowsum(const void* a_base, int aC, int a_ch0, const void* b_base, int
   NEB_REQUIRE(BN, "tensor-core rowsum: N = %d must be a multiple of 64", N);
   int tiles = (M / 128) * (N / BN);
   int total = n_ch * (int)(n_pad / 64);
-  int splits = (int)std::max(1, std::min(kMaxSplits, (2 * 148 + tiles - 1) / tiles));
+  int dev = 0, sms = 0;
+  if (int st = device_sms(&dev, &sms)) return st;
+  int splits = (int)std::max(1, std::min(kMaxSplits, (2 * sms + tiles - 1) / tiles));
   splits = std::min(splits, total);
   CUtensorMap ma, mb;
   int st = make_map(&ma, a_base, (int64_t)2 * aC * M, n_pad, 128);
@@ -968,9 +968,10 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
   // of layer l-1 overwrites that Zbar buffer, and before returning.
   int dev = 0;
   NEB_CUDA_CHECK(cudaGetDevice(&dev));
-  NEB_REQUIRE(dev >= 0 && dev < 64, "tensor-core backward: device index %d", dev);
-  static thread_local cudaStream_t side[64] = {};
-  static thread_local cudaEvent_t ev_z[64] = {}, ev_w[64][2] = {}, ev_j[64] = {};
+  NEB_REQUIRE(dev >= 0 && dev < kMaxDevices, "tensor-core backward: device index %d", dev);
+  static thread_local cudaStream_t side[kMaxDevices] = {};
+  static thread_local cudaEvent_t ev_z[kMaxDevices] = {}, ev_w[kMaxDevices][2] = {},
+                                  ev_j[kMaxDevices] = {};
   if (!side[dev]) {
     NEB_CUDA_CHECK(cudaStreamCreateWithFlags(&side[dev], cudaStreamNonBlocking));
     NEB_CUDA_CHECK(cudaEventCreateWithFlags(&ev_z[dev], cudaEventDisableTiming));
