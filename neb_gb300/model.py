@@ -283,6 +283,18 @@ class SpectralState:
     def __init__(self, model: Model):
         self.model = model
         self.buf = _Buffers(model.device)
+        self._weights = {}
+
+    def objective_weights(self, kind: str, m: int):
+        """c_k on the device, copied from the host once per (objective, m): a
+        per-step copy from pageable host memory would make the host wait for
+        the stream to drain, leaving the GPU idle while the rest of the step
+        is enqueued."""
+        key = (kind, m)
+        if key not in self._weights:
+            self._weights[key] = torch.as_tensor(objective_weights(kind, m), dtype=torch.float64,
+                                                 device=self.model.device)
+        return self._weights[key]
 
 
 def _f64(shape, device):
@@ -296,7 +308,7 @@ def _solve(model: Model, m: int, PM, PS, kind: str):
     dev = model.device
     st = getattr(model, "_spectral", None) or SpectralState(model)
     model._spectral = st
-    c = torch.as_tensor(objective_weights(kind, m), dtype=torch.float64, device=dev)
+    c = st.objective_weights(kind, m)
     lam, V, GM, GS = _f64((m,), dev), _f64((m, m), dev), _f64((m, m), dev), _f64((m, m), dev)
     loss = _f64((), dev)
     info = torch.zeros((), dtype=torch.int32, device=dev)
@@ -320,7 +332,7 @@ def _solve_range(model: Model, m: int, PM, PS, kind: str, rank_rtol: float = RAN
     dev = model.device
     st = getattr(model, "_spectral", None) or SpectralState(model)
     model._spectral = st
-    c = torch.as_tensor(objective_weights(kind, m), dtype=torch.float64, device=dev)
+    c = st.objective_weights(kind, m)
     lam, V, GM, GS = _f64((m,), dev), _f64((m, m), dev), _f64((m, m), dev), _f64((m, m), dev)
     loss = _f64((), dev)
     info = torch.zeros((), dtype=torch.int32, device=dev)
