@@ -496,8 +496,12 @@ def main():
         return model, res, ms, kernels, launches
 
     pk = peaks()
+    # the headline runs without the library's per-kernel timers (their CUDA
+    # events sit between kernels); a second pass over the same steps fills
+    # the kernel table and the roofline
     with ClockSampler(local) as clocks:
-        model, res, ms, kernels, launches = device_timed(args.precision, timing=True)
+        model, res, ms, _, launches = device_timed(args.precision, timing=False)
+    _, _, _, kernels, _ = device_timed(args.precision, timing=True)
     ms_max = max_ms(ms)
     value = whole_job_steps_per_s(world, K, ms_max)
     clk = clocks.summary()
