@@ -132,7 +132,7 @@ class Model:
 
     def features(self, points) -> torch.Tensor:
         """Input feature jets [n, C, F] (device, master dtype) of points [n, dim]."""
-        pts = torch.as_tensor(points, dtype=torch.float64, device=self.device).contiguous()
+        pts = _to_device(points, torch.float64, self.device).contiguous()
         if pts.ndim != 2 or pts.shape[1] != self.c.dim:
             raise ValueError(f"points must be [n, {self.c.dim}]")
         n = pts.shape[0]
@@ -297,6 +297,14 @@ class SpectralState:
         return self._weights[key]
 
 
+def _to_device(x, dtype, device) -> torch.Tensor:
+    """Host arrays and tensors to the device; a pinned host tensor is copied
+    asynchronously on the current stream (the host does not wait for it)."""
+    if isinstance(x, torch.Tensor) and x.device.type == "cpu" and x.is_pinned():
+        return x.to(device=device, dtype=dtype, non_blocking=True)
+    return torch.as_tensor(x, dtype=dtype, device=device)
+
+
 def _f64(shape, device):
     return torch.empty(shape, dtype=torch.float64, device=device)
 
@@ -391,7 +399,7 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
     kind = objective or cfg.objective
     dev = model.device
     feats = model.features(points) if features is None else features
-    qw = torch.as_tensor(weights, device=dev).to(model.dtype).contiguous()
+    qw = _to_device(weights, model.dtype, dev).contiguous()
     n = feats.shape[0]
     if qw.shape != (n,):
         raise ValueError("weights must be [n]")
@@ -460,7 +468,7 @@ def _spectral_step_direct(model: Model, points, weights, training, objective, re
     kind = objective or cfg.objective
     dev = model.device
     n = int(features.shape[0]) if features is not None else len(points)
-    qw = torch.as_tensor(weights, device=dev).to(model.dtype).contiguous()
+    qw = _to_device(weights, model.dtype, dev).contiguous()
     if qw.shape != (n,):
         raise ValueError("weights must be [n]")
     chunk = int(chunk_points or DEFAULT_CHUNK_POINTS)
