@@ -172,6 +172,24 @@ __device__ __forceinline__ void pdl_allow_next() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Launch with the programmatic-stream-serialization attribute (the kernel
+// calls pdl_wait before touching what its predecessor wrote).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, Args... args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Factor the SPD tile a (shared, 1024 threads: thread (i, j) = (ty, tx))
 // into L and its inverse X = L^-1 (both lower).  One barrier per column:
 // every thread forms l_ik = a_ik r with r = 1 / sqrt(a_kk), and the trailing
@@ -1209,17 +1227,9 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     NEB_LAUNCH_CHECK();
     // the panel launches start while their predecessor finishes (programmatic
     // dependent launch): the launch latency leaves the panel-to-panel chain
-    cudaLaunchAttribute pdl[1];
-    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    pdl[0].val.programmaticStreamSerializationAllowed = 1;
     for (int p = 0; p + 1 < nb; ++p) {
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3((nb - p - 1) * (nb - p) / 2);
-      cfg.blockDim = dim3(1024);
-      cfg.stream = s;
-      cfg.attrs = pdl;
-      cfg.numAttrs = 1;
-      NEB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, chol_step, Mw, m, p, Lw, linv_pp, info));
+      NEB_CUDA_CHECK(launch_pdl(chol_step, dim3((nb - p - 1) * (nb - p) / 2), dim3(1024), 0, s,
+                                Mw, m, p, Lw, linv_pp, info));
       NEB_LAUNCH_CHECK();
     }
   }
