@@ -5,10 +5,14 @@
 // accumulated in FP32 tensor memory as A_hi B_hi + A_lo B_hi + A_hi B_lo
 // (+ A_lo B_lo for the Grams, where the dropped term would bias every
 // diagonal the same way).
-// Operands arrive by TMA (128-byte swizzle, K-major) through an mbarrier ring;
-// one thread issues the MMAs, eight warps run the epilogue from TMEM.  The
-// jet GEMM is persistent (one CTA per SM, 128 x 64 tiles round-robin) with
-// its accumulators double-buffered in TMEM, so epilogue and MMAs overlap.
+// Operands arrive by TMA (128-byte swizzle) through an mbarrier ring; one
+// thread issues the MMAs, and the epilogue reads the accumulators from TMEM
+// (sixteen warps in the jet GEMM, eight in the row sums).  The jet GEMM is
+// persistent (one CTA per SM, tiles dealt round-robin): 128 points x 128
+// outputs for the layer GEMMs (4 channels fill all 512 TMEM columns, so the
+// epilogue of a tile and the MMAs of the next take turns), 128 x 64 with
+// double-buffered accumulators for the Gram adjoint (epilogue and MMAs
+// overlap).
 //
 // Device layouts (n_pad = n rounded up to 128 points; "planar" = one matrix
 // per jet channel c in 0..3 = value, d/dx, d/dy, Laplacian), points
@@ -24,7 +28,8 @@
 //   tc_jet_gemm<1>  reverse data:   Zbar' = tanh-jet^T(Z', Zbar W)
 //   tc_jet_gemm<2>  Gram adjoint:   Zbar_L = tanh-jet^T(Z_L, 2 w [0, h_x G_M, h_y G_M, h_lap G_S])
 //   tc_rowsum       sum over points of A[m][p] B[n][p] (Grams, weight gradients),
-//                   split over point ranges, FP64 partials reduced afterwards.
+//                   split over point ranges, FP32 chunk partials reduced
+//                   afterwards with compensation (reduce_parts).
 #include <cudaTypedefs.h>
 #include "tc_path.cuh"
 #include "tc_ptx.cuh"
