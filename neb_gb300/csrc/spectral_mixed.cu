@@ -126,10 +126,6 @@ __device__ __forceinline__ df dot2_sum(dot2 a, dot2 b) {
   return df_add(dot2_df(a), dot2_df(b));
 }
 
-__device__ __forceinline__ df df_shfl_xor(df x, int o) {
-  return {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
-}
-
 // FP64 -> float pairs (the Cholesky works on float pairs in memory, so its
 // per-panel kernels do no FP64 conversions).
 __global__ void to_df(const double* __restrict__ a, df* __restrict__ b, size_t n) {
