@@ -73,6 +73,23 @@ def test_mixed_spectral_matches_fp64(m, kind):
     assert np.abs(R).max() <= 1e-4 * np.abs(S).max()
 
 
+@pytest.mark.parametrize("m", [128, 192, 320, 384, 448])
+def test_mixed_spectral_every_supported_size(m):
+    """The remaining multiples of 64: the 16-CTA tridiagonalisation holds m/16
+    rows per CTA and m/32 four-column chunks per thread, and its register
+    array shifts every 32 columns, so every size takes a different path."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    M, S = _pencil(m, 7 * m)
+    ref = O.spectral_objective(M, S, "ordering")
+    info, lam, V, GM, GS, loss = _run("neb_spectral_mixed", M, S,
+                                      O.objective_weights("ordering", m))
+    assert info == 0
+    np.testing.assert_allclose(lam, ref["lam"], rtol=1e-5)
+    for g, r in ((GM, ref["GM"]), (GS, ref["GS"])):
+        assert np.linalg.norm(g - r) <= 5e-4 * np.linalg.norm(r)
+
+
 def test_mixed_spectral_on_periodic_hidden_pencil():
     """The K = 1024 periodic training pencil (cond(A_M) ~ 1.5e4)."""
     if not torch.cuda.is_available():
