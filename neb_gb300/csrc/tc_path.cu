@@ -710,7 +710,7 @@ size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr int kMaxSplits = 32;
 struct TcWs {
   size_t status, w[NEB_MAX_HIDDEN + 1], wt[NEB_MAX_HIDDEN + 1], gsplit, wht, zb0, zb1, part,
-      partb, total;
+      total;
 };
 
 TcWs tc_ws(const Dims& d) {
@@ -738,8 +738,6 @@ TcWs tc_ws(const Dims& d) {
   int mx = mw > d.wp[0] ? mw : d.wp[0];
   t.part = off;
   off += a256((size_t)kMaxSplits * mx * mx * 8);
-  t.partb = off;
-  off += a256((size_t)mw * 8);
   t.total = off;
   return t;
 }
