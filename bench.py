@@ -282,6 +282,20 @@ def _kernel_table(N, step, K):
     return {k: round(v[1] / K, 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][1])[:12]}
 
 
+def gram_rate(gram_ms_per_step: float, rows, K: int) -> dict:
+    """Gram throughput in the symmetric-count convention: sum over the Grams
+    of R * K * (K + 1) flops, R = rows of the field matrix (points x field
+    components), K = its columns."""
+    flops = float(sum(r * K * (K + 1) for r in rows))
+    return {"tflops": flops / (gram_ms_per_step / 1e3) / 1e12 if gram_ms_per_step > 0 else None,
+            "ms_per_step": gram_ms_per_step, "flops_per_step": flops,
+            "convention": "sum over Grams of R*K*(K+1), R = field rows"}
+
+
+def _gram_ms(kern_ms: dict) -> float:
+    return sum(v for k, v in kern_ms.items() if k in ("tc_gram", "simt_gram"))
+
+
 def run_workload(args, world, rank, local):
     """One line per configuration other than the headline: device-timed
     steps, the plain FP32 form where the configuration asks for it, and the
@@ -361,7 +375,12 @@ def run_workload(args, world, rank, local):
                     "gram_S_rel_err": _rel_max(r.S.cpu().numpy(), ref.S),
                     "n_eigenvalues": int(r.rank)}
         ms = arms["bf16x3"]["ms_per_step"]
+        H = cfg.widths[-2]  # hidden Grams (factored route)
+        for prec in arms:
+            arms[prec]["gram"] = gram_rate(_gram_ms(arms[prec]["kernels_ms_per_step"]),
+                                           (2 * n, n), H)
         line.update({
+            "gram": arms["bf16x3"]["gram"],
             "metric": "forward + Gram + eigensolve steps/s, K=1024, 256^2 grid",
             "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "bf16x3",
             "point_mode_evals_per_s": n * cfg.K / (ms / 1e3),
@@ -390,7 +409,12 @@ def run_workload(args, world, rank, local):
                 r = spectral_step(m0, dp, dw, training=True, return_grams=True)
                 acc[f"{prec}_rank_rtol_{rt:g}"] = _pencil_errors(r, ref[rt])
         ms = arms["bf16x3"]["ms_per_step"]
+        H, n = cfg.widths[-2], len(w)  # hidden Grams (factored route)
+        for prec in arms:
+            arms[prec]["gram"] = gram_rate(_gram_ms(arms[prec]["kernels_ms_per_step"]),
+                                           (2 * n, n), H)
         line.update({
+            "gram": arms["bf16x3"]["gram"],
             "metric": "objective+grad steps/s, K=1024, multiply connected domain, 200k points",
             "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "bf16x3",
             "fp32_plain": arms["fp32"], "split_bf16": arms["bf16x3"],
@@ -433,6 +457,7 @@ def run_workload(args, world, rank, local):
             "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "f32",
             "points": n, "chunk_points": 1 << 17, "rank_at_init": int(r_full.rank),
             "kernels_ms_per_step": kern, "accuracy_subsample_8192": acc,
+            "gram": gram_rate(_gram_ms(kern), (3 * n, 3 * n), cfg.K),
             "note": "FP32 SIMT kernels with point-chunked recompute; at Glorot init the "
                     "curl fields are nearly dependent, so M is numerically singular and the "
                     "pencil is solved on range(M) in FP64"})
@@ -606,6 +631,8 @@ def main():
               sorted(kernels.items(), key=lambda kv: -kv[1][1])}
     spectral_ms = sum(v[1] for k, v in kernels.items()
                       if k.startswith(("spec_", "cusolver", "cublas", "scale_", "weighted_sum"))) / K
+    gram = gram_rate(sum(v[1] for k, v in kernels.items() if k in ("tc_gram", "simt_gram")) / K,
+                     (2 * n, n), cfg.widths[-2])
 
     # accuracy of this step against the FP64 oracle (same parameters, points)
     accuracy = None
@@ -655,6 +682,7 @@ def main():
         "accuracy": accuracy,
         "solver_ok": info_ok,
         "spectral_stage_ms_per_step": spectral_ms,
+        "gram": gram,
         "kernels_ms_per_step": stages,
     }
     print(json.dumps(line), flush=True)
