@@ -260,7 +260,8 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       const int buf = it % Cfg::NBUF, use = it / Cfg::NBUF;
       float w2 = 0.f;
       if constexpr (EPI == 2) w2 = p < g.n_points ? 2.f * g.qw[p] : 0.f;
-      constexpr int kW = kJetEpiCols;                  // columns per TMEM load
+      // columns per TMEM load: the reverse transposes hold more live values
+      constexpr int kW = EPI == 0 ? kJetEpiCols : kJetEpiCols / 2;
       constexpr int kSlice = BN / (kJetEpiWarps / 4);  // columns of this warp
       constexpr int kChunks = kSlice / kW;
       for (int jc = 0; jc < kChunks; ++jc) {

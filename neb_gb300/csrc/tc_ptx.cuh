@@ -124,11 +124,17 @@ __device__ __forceinline__ void tmem_ld8_issue(uint32_t taddr, uint32_t* r) {
         "=r"(r[7])
       : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_ld4_issue(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+}
 template <int W>
 __device__ __forceinline__ void tmem_ld_issue(uint32_t taddr, uint32_t* r) {
-  static_assert(W == 8 || W == 16, "TMEM load width");
+  static_assert(W == 4 || W == 8 || W == 16, "TMEM load width");
   if constexpr (W == 16) tmem_ld16_issue(taddr, r);
-  else tmem_ld8_issue(taddr, r);
+  else if constexpr (W == 8) tmem_ld8_issue(taddr, r);
+  else tmem_ld4_issue(taddr, r);
 }
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
