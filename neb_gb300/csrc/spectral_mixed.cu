@@ -32,7 +32,8 @@
 //                                          one 16-CTA cluster, the rows held in
 //                                          registers, per-column exchange by bulk
 //                                          copies into mbarrier-guarded shared
-//                                          memory
+//                                          memory; the last 64 columns by one
+//                                          CTA with the block in shared memory
 //   tri_eigvals                            eigenvalue brackets of T, warp per eigenvalue
 //   tri_eigvecs                            eigenvectors of T by twisted factorisations,
 //                                          eigenvalues refined to FP64 Rayleigh quotients
@@ -468,12 +469,22 @@ __global__ void __launch_bounds__(kMaxM) df_solve_rl(const df* __restrict__ F,
 // holding column k+1 is always a[0] of thread (k+1)/4 % 8 (no dynamic
 // register indexing).  v_{k+1} = x1 - alpha is applied through scalar
 // corrections, so the replica holds the raw row.
+// Near the end a column costs the cluster mostly exchange latency, so at
+// column k0 = m - min(m, kTriTail) every CTA applies the pending update to its
+// rows and stores the trailing block into CTA 0's shared memory
+// (distributed shared memory), and CTA 0 finishes the columns alone with
+// __syncthreads in place of the exchange; the other CTAs exit.
 constexpr int kTriCluster = 16;
 constexpr int kTriThreads = 8 * kMaxM / kTriCluster;  // 8 threads per row
 constexpr int kTriWarps = kTriThreads / 32;
 constexpr int kTriRows = kMaxM / kTriCluster;          // rows per CTA at m = 512
 constexpr int kTriMsg = 2 * kTriRows + kTriWarps;      // floats per CTA message
 constexpr int kTriChunks = kMaxM / 32;                 // float4 per thread
+constexpr int kTriTail = 64;  // trailing block finished by one CTA in shared memory
+constexpr int kTriTailRows = kTriTail / 32;  // rows per eight-thread group in the tail
+// the handoff column k0 = m - min(m, kTriTail) must be a multiple of 32 (a
+// whole number of register-array shifts); m is a multiple of 64
+static_assert(kTriTail % 32 == 0 && kTriTail >= 32 && kTriTail <= kMaxM, "tail size");
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -525,7 +536,7 @@ __device__ __forceinline__ bool cluster_bar_wait(uint32_t bar, uint32_t parity) 
 }
 
 __global__ void __launch_bounds__(kTriThreads, 1)
-tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
+tridiag_cluster(const float* __restrict__ C, int m, int k0, double* __restrict__ d_out,
                 double* __restrict__ e_out, float* __restrict__ Vh, float* __restrict__ tau_out,
                 int* __restrict__ info) {
   cg::cluster_group cluster = cg::this_cluster();
@@ -537,7 +548,9 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
   float* recv = pnat + 2 * m;              // [2][kTriCluster][kTriMsg] received messages
   float* stage = recv + 2 * kTriCluster * kTriMsg;  // [2][kTriMsg] this CTA's message
   float* red = stage + 2 * kTriMsg;        // [2][kTriWarps] partials of sigma
+  float* T = red + 2 * kTriWarps;           // [R][R] trailing block (CTA 0), R = m - k0
   __shared__ __align__(8) unsigned long long bars[2];
+  __shared__ int tail_abort;               // CTA 0: some CTA's exchange stalled
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int li = tid >> 3, sub = tid & 7;
@@ -574,6 +587,7 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
     if (lane == 0) red[warp] = part;
   }
   if (tid == 0) {
+    tail_abort = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[0])) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[1])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -586,7 +600,7 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
   cluster.sync();  // barriers initialised and every CTA running before the first push
   float pprev = 0.f, vprev = 0.f, K2prev = 0.f;  // this row's p, v and K2 of column k-1
 
-  for (int k = 0; k + 2 < m; ++k) {
+  for (int k = 0; k < k0; ++k) {
     const int par = k & 1, npar = par ^ 1;
     const float* vcur = vrow + par * m;
     float* vprv = vrow + npar * m;
@@ -718,27 +732,185 @@ tridiag_cluster(const float* __restrict__ C, int m, double* __restrict__ d_out,
     if (failed) break;
   }
   if (tid < kTriCluster) bulk_wait_read<0>();
+  const int R = m - k0, R4 = R >> 2;
   if (failed) {
     // a stalled exchange: report it, and let copies still in flight land
     // before any CTA of the cluster exits
-    if (tid == 0) atomicExch(info, -2);
+    if (tid == 0) {
+      atomicExch(info, -2);
+      *cluster.map_shared_rank(&tail_abort, 0) = 1;
+    }
     __nanosleep(50000);
+  } else {
+    // hand the trailing block (rows and columns k0.., update of column k0-1
+    // applied) to CTA 0; after k0 / 32 shifts a[t] holds chunk sub + 8 (t + S)
+    const int par = k0 & 1, npar = par ^ 1;
+    const float4* vp4 = reinterpret_cast<const float4*>(vrow + npar * m);
+    const float4* pp4 = reinterpret_cast<const float4*>(pnat + npar * m);
+    const float wprev = pprev - K2prev * vprev;
+    const int S = k0 >> 5;
+    float4* T0 = reinterpret_cast<float4*>(cluster.map_shared_rank(T, 0));
+    if (has_row && gi >= k0) {
+#pragma unroll
+      for (int t = 0; t < kTriChunks; ++t) {
+        if (t + S < nsub) {
+          const int q = sub + 8 * (t + S);
+          const float4 pp = pp4[q], vp = vp4[q];
+          float4 x = a[t];
+          x.x = fmaf(-wprev, vp.x, fmaf(-vprev, pp.x, x.x));
+          x.y = fmaf(-wprev, vp.y, fmaf(-vprev, pp.y, x.y));
+          x.z = fmaf(-wprev, vp.z, fmaf(-vprev, pp.z, x.z));
+          x.w = fmaf(-wprev, vp.w, fmaf(-vprev, pp.w, x.w));
+          T0[(size_t)(gi - k0) * R4 + q - (k0 >> 2)] = x;
+        }
+      }
+    }
+    // reflector rows k0.. are zero left of column k0
+    for (int idx = rank * kTriThreads + tid; idx < R * k0; idx += kTriCluster * kTriThreads)
+      Vh[(size_t)(k0 + idx / k0) * m + idx % k0] = 0.f;
   }
-  const int pl = (m - 3) & 1;  // parity of the last column
-  if (tid == 0 && rank == 0) {
-    e_out[m - 2] = vrow[(pl ^ 1) * m + m - 1];
+  cluster.sync();  // the trailing block is in CTA 0; the other CTAs are done
+  if (rank != 0 || tail_abort) return;
+
+  // ---- tail: columns k0 .. m-3 by this CTA alone, the block in shared
+  // memory (local indices r = global - k0).  The same lazy scheme as above:
+  // per column one pass over rows c+1.. applies the update of column c-1 and
+  // forms p = tau T v; the pivot row c+1 after update c is formed from the
+  // updated row; two __syncthreads per column.  xr[2][.] holds pivot rows
+  // (raw, zero at j <= c), pn[2][.] p of the last two columns.
+  float* xr = vrow;
+  float* pn = pnat;
+  float* pvred = stage;  // [kTriWarps] partials of p.v
+  {
+    float part = 0.f;
+    for (int j = tid; j < R; j += kTriThreads) {
+      const float x = j > 0 ? T[j] : 0.f;
+      xr[j] = x;
+      xr[m + j] = 0.f;
+      pn[j] = 0.f;
+      pn[m + j] = 0.f;
+      part += x * x;
+    }
+    part = warp_sum(part);
+    if (lane == 0) red[warp] = part;
+  }
+  __syncthreads();
+  const float4* T4 = reinterpret_cast<const float4*>(T);
+  float K2p = 0.f;  // K2 of column c-1 (no pending update before column 0)
+  for (int c = 0; c + 2 < R; ++c) {
+    const int k = k0 + c;
+    const int par = c & 1, npar = par ^ 1;
+    const float* xc = xr + par * m;  // raw pivot row c
+    float* xp = xr + npar * m;       // raw pivot row c-1; becomes row c+1
+    float* pc = pn + par * m;
+    const float* pp = pn + npar * m;
+    float sigma = 0.f;
+#pragma unroll
+    for (int w = 0; w < kTriWarps; ++w) sigma += red[par * kTriWarps + w];
+    const float x1 = xc[c + 1];
+    const float alpha = sigma > 0.f ? -copysignf(sigma * rsqrtf(sigma), x1) : 0.f;
+    const float v1 = x1 - alpha;
+    const float vv = sigma - x1 * x1 + v1 * v1;
+    const float tau = vv > 0.f ? __fdividef(2.f, vv) : 0.f;
+    if (tid == 0) {
+      e_out[k] = alpha;
+      tau_out[k] = tau;
+    }
+    for (int j = tid; j < R; j += kTriThreads)
+      Vh[(size_t)k * m + k0 + j] = j == c + 1 ? v1 : xc[j];
+    // rows c+1+li+32u: pending update of column c-1, then T_i . x
+    const int q0 = (c + 1) >> 2;
+    float vpi[kTriTailRows], wpi[kTriTailRows], acc[kTriTailRows];
+#pragma unroll
+    for (int u = 0; u < kTriTailRows; ++u) {
+      const int i = c + 1 + li + 32 * u;
+      vpi[u] = i < R ? xp[i] : 0.f;
+      wpi[u] = i < R ? pp[i] - K2p * vpi[u] : 0.f;
+      acc[u] = 0.f;
+    }
+    const float4* pp4 = reinterpret_cast<const float4*>(pp);
+    const float4* xp4 = reinterpret_cast<const float4*>(xp);
+    const float4* xc4 = reinterpret_cast<const float4*>(xc);
+    float4* Tw4 = reinterpret_cast<float4*>(T);
+    // two chunks per trip keep twice the shared-memory loads in flight
+    for (int q = q0 + sub; q < R4; q += 16) {
+      const bool two = q + 8 < R4;
+      const int q2 = two ? q + 8 : q;
+      const float4 pq = pp4[q], vq = xp4[q], xq = xc4[q];
+      const float4 pq2 = pp4[q2], vq2 = xp4[q2], xq2 = xc4[q2];
+#pragma unroll
+      for (int u = 0; u < kTriTailRows; ++u) {
+        const int i = c + 1 + li + 32 * u;
+        if (i < R) {
+          float4* row = Tw4 + (size_t)i * R4;
+          float4 x = T4[(size_t)i * R4 + q];
+          float4 y = T4[(size_t)i * R4 + q2];
+          x.x = fmaf(-wpi[u], vq.x, fmaf(-vpi[u], pq.x, x.x));
+          x.y = fmaf(-wpi[u], vq.y, fmaf(-vpi[u], pq.y, x.y));
+          x.z = fmaf(-wpi[u], vq.z, fmaf(-vpi[u], pq.z, x.z));
+          x.w = fmaf(-wpi[u], vq.w, fmaf(-vpi[u], pq.w, x.w));
+          row[q] = x;
+          acc[u] = fmaf(x.x, xq.x, fmaf(x.y, xq.y, fmaf(x.z, xq.z, fmaf(x.w, xq.w, acc[u]))));
+          if (two) {
+            y.x = fmaf(-wpi[u], vq2.x, fmaf(-vpi[u], pq2.x, y.x));
+            y.y = fmaf(-wpi[u], vq2.y, fmaf(-vpi[u], pq2.y, y.y));
+            y.z = fmaf(-wpi[u], vq2.z, fmaf(-vpi[u], pq2.z, y.z));
+            y.w = fmaf(-wpi[u], vq2.w, fmaf(-vpi[u], pq2.w, y.w));
+            row[q2] = y;
+            acc[u] = fmaf(y.x, xq2.x, fmaf(y.y, xq2.y, fmaf(y.z, xq2.z, fmaf(y.w, xq2.w, acc[u]))));
+          }
+        }
+      }
+    }
+    __syncwarp();  // the group's chunk holding column c+1 is stored
+    float part = 0.f;
+#pragma unroll
+    for (int u = 0; u < kTriTailRows; ++u) {
+      float sacc = acc[u];
+      sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
+      sacc += __shfl_xor_sync(0xffffffffu, sacc, 2);
+      sacc += __shfl_xor_sync(0xffffffffu, sacc, 4);
+      const int i = c + 1 + li + 32 * u;
+      if (i < R && sub == 0) {
+        const float pi = tau * (sacc - alpha * T[(size_t)i * R + c + 1]);
+        pc[i] = pi;
+        part += pi * (i == c + 1 ? v1 : xc[i]);
+      }
+    }
+    part = warp_sum(part);
+    if (lane == 0) pvred[warp] = part;
+    __syncthreads();
+    float pv = 0.f;
+#pragma unroll
+    for (int w = 0; w < kTriWarps; ++w) pv += pvred[w];
+    const float K2 = tau * pv;
+    const float w1 = pc[c + 1] - K2 * v1;
+    // pivot row c+1 after update c
+    part = 0.f;
+    for (int j = tid; j < R; j += kTriThreads) {
+      float nv = 0.f;
+      if (j > c + 1) nv = T[(size_t)(c + 1) * R + j] - (v1 * pc[j] + w1 * xc[j]);
+      if (j == c + 1) d_out[k + 1] = T[(size_t)(c + 1) * R + j] - (v1 * pc[j] + w1 * v1);
+      xp[j] = nv;
+      part += nv * nv;
+    }
+    part = warp_sum(part);
+    if (lane == 0) red[npar * kTriWarps + warp] = part;
+    K2p = K2;
+    __syncthreads();
+  }
+  const int pl = (R - 3) & 1;  // parity of the last column
+  if (tid == 0) {
+    e_out[m - 2] = xr[(pl ^ 1) * m + R - 1];
     tau_out[m - 2] = 0.f;
     tau_out[m - 1] = 0.f;
+    // d_{m-1}: the last element with the pending update of column m-3
+    const float vl = xr[pl * m + R - 1], pl_ = pn[pl * m + R - 1];
+    const float w = pl_ - K2p * vl;
+    d_out[m - 1] = T[(size_t)(R - 1) * R + R - 1] - (vl * pl_ + w * vl);
   }
-  if (rank == 0)
-    for (int k = m - 2; k < m; ++k)
-      for (int i = tid; i < m; i += kTriThreads) Vh[(size_t)k * m + i] = 0.f;
-  // d_{m-1}: row m-1 (a[0].w of its last thread) with the pending update
-  if (has_row && gi == m - 1 && sub == 7) {
-    const float w = pprev - K2prev * vprev;
-    d_out[m - 1] = a[0].w - (vprev * pnat[pl * m + m - 1] + w * vrow[pl * m + m - 1]);
-  }
-  cluster.sync();
+  for (int k = m - 2; k < m; ++k)
+    for (int j = tid; j < R; j += kTriThreads) Vh[(size_t)k * m + k0 + j] = 0.f;
 }
 
 // ------------------------------------------------------- tridiagonal eigen
@@ -1262,8 +1434,14 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(kTriCluster);
     cfg.blockDim = dim3(kTriThreads);
-    cfg.dynamicSmemBytes =
-        ((size_t)4 * m + 2 * kTriCluster * kTriMsg + 2 * kTriMsg + 2 * kTriWarps) * sizeof(float);
+    // columns 0 .. k0-1 by the cluster, the trailing R x R block by CTA 0
+    const int R = std::min(m, kTriTail), k0 = m - R;
+    auto tri_smem = [](int m_, int r_) {
+      return ((size_t)4 * m_ + 2 * kTriCluster * kTriMsg + 2 * kTriMsg + 2 * kTriWarps +
+              (size_t)r_ * r_) *
+             sizeof(float);
+    };
+    cfg.dynamicSmemBytes = tri_smem(m, R);
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
@@ -1274,15 +1452,20 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     if (!probed[dev]) {
       NEB_CUDA_CHECK(cudaFuncSetAttribute(tridiag_cluster,
                                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      NEB_CUDA_CHECK(cudaOccupancyMaxActiveClusters(&clusters[dev], tridiag_cluster, &cfg));
+      NEB_CUDA_CHECK(cudaFuncSetAttribute(tridiag_cluster,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)tri_smem(kMaxM, kTriTail)));
+      cudaLaunchConfig_t probe = cfg;  // the largest block
+      probe.dynamicSmemBytes = tri_smem(kMaxM, kTriTail);
+      NEB_CUDA_CHECK(cudaOccupancyMaxActiveClusters(&clusters[dev], tridiag_cluster, &probe));
       probed[dev] = true;
     }
     NEB_REQUIRE(clusters[dev] >= 1,
                 "neb_spectral_mixed: the GPU cannot co-schedule a %d-CTA thread-block cluster",
                 kTriCluster);
     KernelScope ks("spec_tridiag_cluster_fp32", s, 4.0 / 3.0 * m * mm, 8.0 * mm);
-    NEB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, tridiag_cluster, (const float*)C, m, d, e, Vh, tau,
-                                      info));
+    NEB_CUDA_CHECK(cudaLaunchKernelEx(&cfg, tridiag_cluster, (const float*)C, m, k0, d, e, Vh,
+                                      tau, info));
     NEB_LAUNCH_CHECK();
   }
   // The back-transformation depends only on the reflectors: on a side stream
