@@ -64,9 +64,6 @@ __device__ __forceinline__ uint32_t sh_u32(const void* p) {
 __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sh_u32(dst)), "l"(src) : "memory");
 }
-__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sh_u32(dst)), "l"(src) : "memory");
-}
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sh_u32(dst)), "l"(src)
                : "memory");
@@ -1259,12 +1256,6 @@ __global__ void f32_to_f64(const float* __restrict__ a, double* __restrict__ b, 
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
     b[i] = scale * (double)a[i];
-}
-
-__global__ void f64_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
 }
 
 __global__ void mixed_loss(const double* __restrict__ c, const double* __restrict__ lam, int m,
