@@ -190,14 +190,20 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
 // entries take a_ij -= l_ik (a_jk r).  Column k concerns rows i >= k only, so
 // warp i leaves the loop after its column and the barrier of column k counts
 // warps k+1..31 (named barrier 1).  The reciprocal square root of the next
-// pivot is taken once, by the thread that finished it.  The inverse is built
-// by doubling: [[X11, 0], [X21, X22]] with X21 = -X22 L21 X11, on blocks of
-// 1, 2, 4, 8, 16.  Returns (through *bad) the first failing pivot + 1.
+// pivot is taken once, by the thread that finished it.  The inverse comes
+// out of the same loop (forward substitution on the identity, right-looking):
+// B = I, and at column k the lanes j <= k of row i > k take
+// B_ij -= l_ik (B_kj r); row k of B is final after column k-1, so row k of X
+// is B_kj r, formed by warp k in its last column.  No barrier is added: rows
+// of B are written only by their own warp, and row k is read after the
+// barrier of column k-1.  Tm holds B.  Returns (through *bad) the first
+// failing pivot + 1.
 __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1],
                             df (*Tm)[kCB + 1], df* rinv, int* bad) {
   const int j = threadIdx.x & 31, i = threadIdx.x >> 5;
   L[i][j] = df{0.f, 0.f};
   X[i][j] = df{0.f, 0.f};
+  Tm[i][j] = df{i == j ? 1.f : 0.f, 0.f};
   if (threadIdx.x == 0) {
     df a00 = a[0][0];
     if (!(a00.h > 0.f)) {  // not positive definite (or NaN)
@@ -211,6 +217,10 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
     const df r = rinv[k];
     const df lik = df_mul(a[i][k], r);
     if (j == k) L[i][k] = lik;
+    if (k == i) {  // this row's last column: its row of the inverse
+      if (j <= i) X[i][j] = df_mul(Tm[i][j], r);
+      break;
+    }
     if (j > k && i >= j) {
       df v = df_add(a[i][j], df_neg(df_mul(lik, df_mul(a[j][k], r))));
       a[i][j] = v;
@@ -221,29 +231,12 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
         }
         rinv[k + 1] = df_rsqrt(v);
       }
+    } else if (j <= k) {
+      Tm[i][j] = df_add(Tm[i][j], df_neg(df_mul(lik, df_mul(Tm[k][j], r))));
     }
-    if (k < i) bar_named(1, (kCB - 1 - k) * 32);  // exactly warps k+1..31 arrive
+    bar_named(1, (kCB - 1 - k) * 32);  // exactly warps k+1..31 arrive
   }
   __syncthreads();
-  if (i == j) X[i][i] = rinv[i];
-  __syncthreads();
-  for (int s = 1; s < kCB; s <<= 1) {
-    // block pair starting at o = 2 s q: rows o+s..o+2s-1, columns o..o+s-1
-    const bool in21 = (i / (2 * s) == j / (2 * s)) && (i % (2 * s) >= s) && (j % (2 * s) < s);
-    const int o = (i / (2 * s)) * 2 * s;
-    if (in21) {  // Tm = L21 X11
-      dot2 acc;
-      for (int t = 0; t < s; ++t) dot2_add(acc, L[i][o + t], X[o + t][j]);
-      Tm[i][j] = dot2_df(acc);
-    }
-    __syncthreads();
-    if (in21) {  // X21 = -X22 Tm
-      dot2 acc;
-      for (int t = s; t < 2 * s; ++t) dot2_add(acc, X[i][o + t], Tm[o + t][j]);
-      X[i][j] = df_neg(dot2_df(acc));
-    }
-    __syncthreads();
-  }
 }
 
 __global__ void __launch_bounds__(1024) chol_first(const df* __restrict__ A, int m,
