@@ -221,9 +221,13 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
       if (j <= i) X[i][j] = df_mul(Tm[i][j], r);
       break;
     }
-    if (j > k && i >= j) {
-      df v = df_add(a[i][j], df_neg(df_mul(lik, df_mul(a[j][k], r))));
-      a[i][j] = v;
+    if (j <= i) {
+      // one update form for both lane groups (no divergent second path):
+      // j > k: a_ij -= l_ik (a_jk r);  j <= k: B_ij -= l_ik (B_kj r)
+      df* x = j > k ? &a[i][j] : &Tm[i][j];
+      const df* y = j > k ? &a[j][k] : &Tm[k][j];
+      df v = df_add(*x, df_neg(df_mul(lik, df_mul(*y, r))));
+      *x = v;
       if (i == k + 1 && j == k + 1) {
         if (!(v.h > 0.f)) {
           if (*bad == 0) *bad = k + 2;
@@ -231,8 +235,6 @@ __device__ void tile_factor(df (*a)[kCB + 1], df (*L)[kCB + 1], df (*X)[kCB + 1]
         }
         rinv[k + 1] = df_rsqrt(v);
       }
-    } else if (j <= k) {
-      Tm[i][j] = df_add(Tm[i][j], df_neg(df_mul(lik, df_mul(Tm[k][j], r))));
     }
     bar_named(1, (kCB - 1 - k) * 32);  // exactly warps k+1..31 arrive
   }
