@@ -76,8 +76,9 @@ def test_mixed_spectral_matches_fp64(m, kind):
 @pytest.mark.parametrize("m", [128, 192, 320, 384, 448])
 def test_mixed_spectral_every_supported_size(m):
     """The remaining multiples of 64: the 16-CTA tridiagonalisation holds m/16
-    rows per CTA and m/32 four-column chunks per thread, and its register
-    array shifts every 32 columns, so every size takes a different path."""
+    rows per CTA and m/32 four-column chunks per thread, its register array
+    shifts every 32 columns, and it hands the last 64 columns to one CTA
+    after (m - 64)/32 shifts, so every size takes a different path."""
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     M, S = _pencil(m, 7 * m)
