@@ -43,6 +43,23 @@ WORKLOAD = ("periodic_train: 2D periodic potential, 64 Fourier features (value, 
             "per step, ordering objective sum lam_k/k, FP64 eigensolve, Adam lr 1e-3")
 
 
+# precision of each part of the headline step's spectral stage (the mixed
+# stage of the split-BF16 and plain FP32 forms)
+SPECTRAL_STAGES = {
+    "hidden_grams": "split-BF16 products, FP32 tensor-memory sums drained every 64 points, "
+                    "compensated FP32 cross-CTA reduction, FP64 result",
+    "cholesky_of_M": "compensated FP32 (float pairs, ~2^-44 relative)",
+    "reduction_L^-1 S L^-T": "compensated FP32 right-looking triangular solves",
+    "tridiagonalisation": "FP32 Householder (one 16-CTA cluster)",
+    "tridiagonal_eigenpairs": "FP32 Sturm multisection + twisted factorisations, eigenvalues "
+                              "refined to compensated Rayleigh quotients",
+    "back_transform_and_adjoints": "FP32 (WY back-transform, V = L^-T X by compensated solve, "
+                                   "FP32 Gram-adjoint products)",
+    "gram_adjoint_operand": "G_M, G_S split three ways (24 significant bits) for the "
+                            "tensor-core Gram-adjoint GEMM",
+}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -165,7 +182,7 @@ def cpu_threads():
     return os.cpu_count() or 1
 
 
-def oracle_step_time(n_points: int, seed: int = 0):
+def oracle_step_time(n_points: int, seed: int = 0, step: int = 0):
     """Seconds of one FP64 oracle training step (factored route + Adam) on
     n_points of the periodic workload."""
     sys.path.insert(0, str(ROOT))
@@ -174,7 +191,7 @@ def oracle_step_time(n_points: int, seed: int = 0):
     cfg = CF.CONFIGS["periodic_train"]
     params = O.glorot_init(list(cfg.widths), seed)
     mom = O.zero_moments(params)
-    pts, w = CF.periodic_uniform(n_points, seed, 0)
+    pts, w = CF.periodic_uniform(n_points, seed, step)
     t0 = time.perf_counter()
     X0 = O.features_periodic(pts, cfg.n_freq)
     r = O.objective_and_grad_factored(params, X0, w[0], cfg.objective)
@@ -183,27 +200,29 @@ def oracle_step_time(n_points: int, seed: int = 0):
 
 
 def run_reference(args, world, rank):
+    """The reference algorithm on the host cores: full training steps (all
+    16,384 points, K = 1024, FP64 eigensolve, Adam) of the FP64 NumPy
+    restatement, one warm-up step, then the timed steps."""
     if rank != 0:
         return
-    sample = 2048
     full = 16384
     for _ in range(min(args.warmup, 1)):
-        oracle_step_time(sample)
-    times = [oracle_step_time(sample, seed=i) for i in range(args.steps)]
-    per_full = float(np.mean(times)) * full / sample
-    value = 1.0 / per_full
+        oracle_step_time(full)
+    times = [oracle_step_time(full, seed=0, step=i) for i in range(args.steps)]
+    per_step = float(np.mean(times))
+    value = 1.0 / per_step
     cores = cpu_threads()
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_full * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded uniform random points, Glorot-normal init (seed 0)",
         "config": {"workload": WORKLOAD, "K": 1024, "points_per_step": full},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} steps of {sample} of the {full} points each "
-                                   f"(FP64 NumPy restatement, {cores} BLAS threads), time "
-                                   "scaled by the point fraction to a full step"},
+                         "sample": f"{args.steps} full training steps ({full} points each, "
+                                   f"FP64 NumPy restatement, {cores} BLAS threads), "
+                                   "no extrapolation"},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -240,10 +259,6 @@ def _eig_rel(lam, ref_lam) -> float:
     return float(np.max(np.abs(lam - ref_lam) / np.abs(ref_lam)))
 
 
-# rank tolerances of the finite pencil reported for the configurations
-# whose mass matrix is numerically singular at init: the FP64 rule, and one
-# above the FP32 noise floor of the Grams
-RTOLS = (1e-10, 1e-6)
 
 
 def _pencil_errors(r, ref) -> dict:
@@ -390,24 +405,25 @@ def run_workload(args, world, rank, local):
         pts, w = CF.sample(cfg)
         dp, dw = dev_inputs(pts, w)
         X0 = O.features_multihole(pts, np.asarray(cfg.centres))
-        arms, acc, ref = {}, {}, None
-        for prec in ("bf16x3", "fp32"):
+        arms, acc, ref, t_cpu = {}, {}, {}, None
+        # errors at each form's own rank tolerance (model.RANK_RTOL), the
+        # oracle solving the same pencil at the same tolerance
+        for prec in ("bf16x3", "fp32", "fp64"):
             model = Model(cfg, precision=prec, seed=0, device=dev)
-            step = (lambda i, m=model: train_step(m, dp, dw, check=False))
-            ms = _timed(step, W, K)
-            arms[prec] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms,
-                          "kernels_ms_per_step": _kernel_table(N, step, 2)}
-            if ref is None:
-                m0 = Model(cfg, precision=prec, seed=0, device=dev)
+            if prec != "fp64":
+                step = (lambda i, m=model: train_step(m, dp, dw, check=False))
+                ms = _timed(step, W, K)
+                arms[prec] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms, "gram": model.gram,
+                              "kernels_ms_per_step": _kernel_table(N, step, 2)}
+            m0 = Model(cfg, precision=prec, seed=0, device=dev)
+            rt = m0.rank_rtol
+            if rt not in ref:
                 t0 = time.perf_counter()
-                ref = {rt: O.objective_and_grad_factored(_params64(m0), X0, w, cfg.objective,
-                                                         rank_rtol=rt) for rt in RTOLS}
-                t_cpu = (time.perf_counter() - t0) / len(RTOLS)
-            for rt in RTOLS:
-                m0 = Model(cfg, precision=prec, seed=0, device=dev)
-                m0.rank_rtol = rt
-                r = spectral_step(m0, dp, dw, training=True, return_grams=True)
-                acc[f"{prec}_rank_rtol_{rt:g}"] = _pencil_errors(r, ref[rt])
+                ref[rt] = O.objective_and_grad_factored(_params64(m0), X0, w, cfg.objective,
+                                                        rank_rtol=rt)
+                t_cpu = time.perf_counter() - t0
+            r = spectral_step(m0, dp, dw, training=True, return_grams=True)
+            acc[f"{prec}_rank_rtol_{rt:g}"] = _pencil_errors(r, ref[rt])
         ms = arms["bf16x3"]["ms_per_step"]
         H, n = cfg.widths[-2], len(w)  # hidden Grams (factored route)
         for prec in arms:
@@ -442,25 +458,23 @@ def run_workload(args, world, rank, local):
         ps, ws_ = pts[sub], w[sub] * (n / len(sub))
         X0 = O.features_raw3d(ps)
         acc = {}
-        m0 = Model(cfg, precision="fp64", seed=0, device=dev)
-        ref = {rt: O.objective_and_grad(_params64(m0), X0, ws_, 3, cfg.objective, rank_rtol=rt)
-               for rt in RTOLS}
         for prec in ("fp32", "fp64"):
-            for rt in RTOLS:
-                m0 = Model(cfg, precision=prec, seed=0, device=dev)
-                m0.rank_rtol = rt
-                r = spectral_step(m0, torch.tensor(ps, device=dev),
-                                  torch.tensor(ws_, device=dev), training=True)
-                acc[f"{prec}_rank_rtol_{rt:g}"] = _pencil_errors(r, ref[rt])
+            m0 = Model(cfg, precision=prec, seed=0, device=dev)
+            rt = m0.rank_rtol
+            ref = O.objective_and_grad(_params64(m0), X0, ws_, 3, cfg.objective, rank_rtol=rt)
+            r = spectral_step(m0, torch.tensor(ps, device=dev), torch.tensor(ws_, device=dev),
+                              training=True)
+            acc[f"{prec}_rank_rtol_{rt:g}"] = _pencil_errors(r, ref)
         line.update({
             "metric": "objective+grad steps/s, 3D curl basis K=512, 1,599,754 points",
             "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "f32",
             "points": n, "chunk_points": 1 << 17, "rank_at_init": int(r_full.rank),
             "kernels_ms_per_step": kern, "accuracy_subsample_8192": acc,
             "gram": gram_rate(_gram_ms(kern), (3 * n, 3 * n), cfg.K),
-            "note": "FP32 SIMT kernels with point-chunked recompute; at Glorot init the "
-                    "curl fields are nearly dependent, so M is numerically singular and the "
-                    "pencil is solved on range(M) in FP64"})
+            "note": "FP32 SIMT kernels with point-chunked recompute and compensated Grams; at "
+                    "Glorot init the curl fields are nearly dependent, so M is numerically "
+                    "singular and the pencil is solved on range(M) in FP64 at the form's rank "
+                    "tolerance"})
     print(json.dumps(line), flush=True)
 
 
@@ -499,10 +513,11 @@ def main():
     dev_batches = [(torch.tensor(p, device=dev), torch.tensor(w, device=dev, dtype=torch.float32))
                    for p, w in batches]
 
-    def device_timed(precision, timing=False):
-        model = Model(cfg, precision=precision, seed=0, device=dev)
+    def device_timed(precision, timing=False, spectral=None, config=None, batches=None):
+        model = Model(config or cfg, precision=precision, seed=0, device=dev, spectral=spectral)
+        batches = batches or dev_batches
         for s in range(W):
-            train_step(model, *dev_batches[s], check=False)
+            train_step(model, *batches[s % len(batches)], check=False)
         torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
@@ -512,7 +527,7 @@ def main():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for s in range(W, W + K):
-            res = train_step(model, *dev_batches[s], check=False)
+            res = train_step(model, *batches[s % len(batches)], check=False)
         e1.record()
         torch.cuda.synchronize()
         kernels = N.timing_end() if timing else None
@@ -539,6 +554,35 @@ def main():
         _, _, ms32, _, _ = device_timed("fp32")
         ms32 = max_ms(ms32)
         fp32 = {"value": world * K / (ms32 / 1e3), "ms_per_step": ms32 / K}
+
+    # both forms again with the strict FP64 spectral stage (cuSOLVER Dsygvd
+    # and FP64 adjoint products) in place of the mixed one, so the cost of an
+    # FP64-datatype eigensolve is visible beside the headline ratio
+    strict = None
+    if not args.no_fp32_plain and args.precision != "fp32":
+        _, _, ms_s, _, _ = device_timed(args.precision, spectral="fp64")
+        _, _, ms_s32, _, _ = device_timed("fp32", spectral="fp64")
+        ms_s, ms_s32 = max_ms(ms_s), max_ms(ms_s32)
+        strict = {"spectral": "fp64 (cuSOLVER Dsygvd, cuBLAS FP64 adjoints)",
+                  args.precision: {"value": world * K / (ms_s / 1e3), "ms_per_step": ms_s / K},
+                  "fp32": {"value": world * K / (ms_s32 / 1e3), "ms_per_step": ms_s32 / K},
+                  "speedup_vs_fp32_plain": ms_s32 / ms_s}
+
+    # objective + gradient + Adam on the 256^2 periodic grid (65,536 points,
+    # the grid of the evaluation configuration), both forms
+    grid256 = None
+    if not args.no_fp32_plain and args.precision != "fp32":
+        gcfg = CONFIGS["periodic_eval"]
+        gp, gw = CF.sample(gcfg)
+        gb = [(torch.tensor(gp, device=dev), torch.tensor(gw, device=dev, dtype=torch.float32))]
+        _, _, ms_g, _, _ = device_timed(args.precision, config=gcfg, batches=gb)
+        _, _, ms_g32, _, _ = device_timed("fp32", config=gcfg, batches=gb)
+        ms_g, ms_g32 = max_ms(ms_g), max_ms(ms_g32)
+        grid256 = {"workload": "periodic 256^2 grid (65,536 points), 4x512 tanh, K=1024, "
+                               "ordering objective, reverse pass and Adam per step",
+                   "value": world * K / (ms_g / 1e3), "unit": "steps/s", "ms_per_step": ms_g / K,
+                   "fp32_plain": {"value": world * K / (ms_g32 / 1e3), "ms_per_step": ms_g32 / K},
+                   "speedup_vs_fp32_plain": ms_g32 / ms_g}
 
     # end to end through the public API: host (pinned) points and weights in
     # (asynchronous H2D inside the timed region), loss and solver status of
@@ -629,6 +673,18 @@ def main():
                 "tensor_frac": tensor_frac, "hbm_frac": hbm_frac}
     stages = {k: {"launches_per_step": v[0] / K, "ms_per_step": v[1] / K} for k, v in
               sorted(kernels.items(), key=lambda kv: -kv[1][1])}
+    # the same roofline arithmetic for every tensor-core kernel of the step,
+    # largest first (concurrent ones marked: their event durations include
+    # the kernel they share the GPU with)
+    tc_roofline = {}
+    for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][1]):
+        if not k.startswith("tc_") or v[0] == 0 or v[1] <= 0:
+            continue
+        per = v[1] / v[0] / 1e3
+        tc_roofline[k] = {"per_launch_ms": per * 1e3,
+                          "tensor_frac": v[2] / v[0] / per / 1e12 / pk["bf16"],
+                          "hbm_frac": v[3] / v[0] / per / 1e9 / pk["hbm"],
+                          "concurrent": k in concurrent}
     spectral_ms = sum(v[1] for k, v in kernels.items()
                       if k.startswith(("spec_", "cusolver", "cublas", "scale_", "weighted_sum"))) / K
     gram = gram_rate(sum(v[1] for k, v in kernels.items() if k in ("tc_gram", "simt_gram")) / K,
@@ -671,8 +727,12 @@ def main():
         "data": "synthetic: seeded uniform random points per step, Glorot-normal init (seed 0)",
         "config": {"workload": WORKLOAD, "K": 1024, "hidden": [512] * 4, "points_per_step": n,
                    "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "no flush: each step rewrites ~1.1 GB of activation tape (> 129 MB L2)"},
+                   "l2": "no flush: each step rewrites ~1.1 GB of activation tape (> 129 MB L2)",
+                   "spectral": SPECTRAL_STAGES},
         "roofline": roofline,
+        "tc_kernels_roofline": tc_roofline,
+        "strict_fp64_spectral": strict,
+        "grid256": grid256,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),

@@ -48,6 +48,13 @@ enum {
 };
 
 enum { NEB_PREC_FP32 = 0, NEB_PREC_FP64 = 1, NEB_PREC_BF16X3 = 2 };
+/* Accumulation of the FP32 Grams (FP64 always sums in FP64; split-BF16 sums
+ * in tensor memory, drained every 64 points): PLAIN sums the products in
+ * FP32; COMPENSATED forms every product exactly (FMA) and keeps each chunk
+ * sum as a TwoSum pair, for bases whose mass matrix is nearly singular,
+ * where the ~1e-7 relative error a plain FP32 sum leaves in every entry
+ * moves the small eigenvalues of the pencil. */
+enum { NEB_GRAM_PLAIN = 0, NEB_GRAM_COMPENSATED = 1 };
 enum { NEB_FEAT_PERIODIC = 0, NEB_FEAT_MULTIHOLE = 1, NEB_FEAT_RAW3D = 2 };
 
 #define NEB_MAX_HIDDEN 8
@@ -59,6 +66,7 @@ typedef struct neb_net {
   int32_t n_hidden;   /* 1..NEB_MAX_HIDDEN */
   int32_t widths[NEB_MAX_HIDDEN + 2];
   int32_t precision;  /* NEB_PREC_* */
+  int32_t gram;       /* NEB_GRAM_* (0 = plain) */
 } neb_net;
 
 /* Thread-local message of the last failing call. */
@@ -127,7 +135,10 @@ int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n_points,
  * partials live in a fixed 8 MiB device array: chunks x H x H doubles must
  * fit (H <= 128 at any n_points), else NEB_ERR_ARG.  The first call on each
  * device sets up the array's address and should come before any stream
- * capture; calls overlapping in time on one device race on the array. */
+ * capture; calls overlapping in time on one device race on the array.  The
+ * address is cached per device for the life of the process: after
+ * cudaDeviceReset on a device the cached address is stale, so a process
+ * that resets a device must not call this entry point on it again. */
 int neb_hidden_gram_static(const neb_net* net, const void* qw, int64_t n_points,
                            const void* tape, double* A_M, double* A_S, neb_stream_t stream);
 
@@ -241,15 +252,31 @@ int neb_check_status(const neb_net* net, int64_t n_points, void* workspace,
 /* One Adam transaction over n_tensors parameter tensors (float when dtype
  * is 0, double when 1): global gradient norm, clip scale min(1, clip/norm),
  * commit only when every gradient is finite and the norm positive (device
- * flag; nothing changes otherwise), bias-corrected moments with step + 1.
- * Replaces NCC:156-171 Model.adam and HB:2184-2277 adam_step_jet1_device.
- * norm_out, committed_out: device pointers (double, int). */
+ * flag; nothing changes otherwise), bias-corrected moments with t = number
+ * of committed steps + 1.  The committed-step count is *step_counter (a
+ * device int, read on the device and advanced there only when the update
+ * commits, so a rejected step leaves it unchanged without a host
+ * synchronisation) or, when step_counter is NULL, the host argument `step`.
+ * Replaces NCC:156-171 Model.adam (epoch advanced only after a committed
+ * update, NCC:157-158, 170) and HB:2184-2277 adam_step_jet1_device.
+ * norm_out, committed_out: device pointers (double, int).  One shared
+ * network has one parameter vector, so the clip norm is global: norm_out is
+ * the single entry of what NCC returns per mode. */
 size_t neb_adam_workspace_bytes(void);
 int neb_adam(int dtype, int n_tensors, void* const* params, void* const* exp_avg,
              void* const* exp_avg_sq, const void* const* grads, const int64_t* sizes,
-             int step, double lr, double clip, double beta1, double beta2, double eps,
-             double* norm_out, int* committed_out, void* workspace,
+             int step, int* step_counter, double lr, double clip, double beta1, double beta2,
+             double eps, double* norm_out, int* committed_out, void* workspace,
              size_t workspace_bytes, neb_stream_t stream);
+
+/* Self-test of the bounded device-side wait that every tensor-core pipeline
+ * uses (no counterpart in the reference, whose CuPy kernels never wait on
+ * the device): one CTA waits on an mbarrier phase that completes only when
+ * `arrive` is non-zero; without the arrival the wait gives up after
+ * spin_limit polls (1024 .. 2^24), records the give-up in *status (device
+ * int) and the call returns NEB_ERR_TIMEOUT, leaving the context usable.
+ * No copy or MMA is in flight during the wait.  Synchronises the stream. */
+int neb_wait_selftest(int arrive, uint32_t spin_limit, int* status, neb_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -26,18 +26,24 @@ FEAT = {"periodic": 0, "multihole": 1, "raw3d": 2}
 MAX_HIDDEN = 8
 
 
+GRAM = {"plain": 0, "compensated": 1}
+
+
 class NebNet(ctypes.Structure):
     _fields_ = [("dim", c_int32), ("n_hidden", c_int32),
-                ("widths", c_int32 * (MAX_HIDDEN + 2)), ("precision", c_int32)]
+                ("widths", c_int32 * (MAX_HIDDEN + 2)), ("precision", c_int32),
+                ("gram", c_int32)]
 
     @classmethod
-    def make(cls, dim: int, widths, precision: str) -> "NebNet":
+    def make(cls, dim: int, widths, precision: str, gram: str = "plain") -> "NebNet":
         widths = list(widths)
         n_hidden = len(widths) - 2
         if not 1 <= n_hidden <= MAX_HIDDEN:
             raise ValueError(f"need 1..{MAX_HIDDEN} hidden layers, got widths={widths}")
+        if gram not in GRAM:
+            raise ValueError(f"gram must be one of {tuple(GRAM)}")
         arr = (c_int32 * (MAX_HIDDEN + 2))(*(widths + [0] * (MAX_HIDDEN + 2 - len(widths))))
-        return cls(dim, n_hidden, arr, PREC[precision])
+        return cls(dim, n_hidden, arr, PREC[precision], GRAM[gram])
 
 
 # name -> (restype, argtypes)
@@ -89,8 +95,10 @@ _SIGNATURES = {
     "neb_check_status": (c_int, [POINTER(NebNet), c_int64, c_void_p, c_size_t, c_void_p]),
     "neb_adam_workspace_bytes": (c_size_t, []),
     "neb_adam": (c_int, [c_int, c_int, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p),
-                         POINTER(c_void_p), POINTER(c_int64), c_int, c_double, c_double, c_double,
-                         c_double, c_double, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+                         POINTER(c_void_p), POINTER(c_int64), c_int, c_void_p, c_double, c_double,
+                         c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_size_t,
+                         c_void_p]),
+    "neb_wait_selftest": (c_int, [c_int, ctypes.c_uint32, c_void_p, c_void_p]),
 }
 
 EXPORTED = tuple(_SIGNATURES)

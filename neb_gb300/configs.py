@@ -51,6 +51,10 @@ class NebConfig:
     # periodic Fourier-feature bases), "range" (FP64, rank-revealing) where
     # raw-coordinate inputs make the fields nearly dependent at init
     spectral: str = "mixed"
+    # Gram accumulation of the FP32 / split-BF16 forms: "plain" FP32 sums, or
+    # "compensated" (exact products, TwoSum chunk sums) for the bases whose
+    # mass matrix is nearly singular at init
+    gram: str = "plain"
 
     @property
     def K(self) -> int:
@@ -89,9 +93,10 @@ CONFIGS = {
                                 steps=25, lr=1e-3),
     "multihole": NebConfig("multihole", 2, "multihole", (5, 256, 256, 256, 256, 1024), "ordering",
                            centres=MULTIHOLE_CENTRES, sampler="multihole", n_points=200_000,
-                           spectral="range"),
+                           spectral="range", gram="compensated"),
     "metaball3d": NebConfig("metaball3d", 3, "raw3d", (3, 512, 512, 512, 512, 1536), "ordering",
-                            sampler="metaball", n_points=1_599_754, spectral="range"),
+                            sampler="metaball", n_points=1_599_754, spectral="range",
+                            gram="compensated"),
 }
 
 

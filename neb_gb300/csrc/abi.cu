@@ -83,6 +83,8 @@ int check_net(const neb_net* net) {
   NEB_REQUIRE(net->precision == NEB_PREC_FP32 || net->precision == NEB_PREC_FP64 ||
                   net->precision == NEB_PREC_BF16X3,
               "unknown precision %d", net->precision);
+  NEB_REQUIRE(net->gram == NEB_GRAM_PLAIN || net->gram == NEB_GRAM_COMPENSATED,
+              "unknown Gram accumulation %d", net->gram);
   if (net->dim == 3) NEB_REQUIRE(net->widths[net->n_hidden + 1] % 3 == 0,
                                  "3D output width must be 3 K");
   return NEB_OK;
@@ -211,7 +213,7 @@ int launch_bwd(const T* A, const T* B0, const T* B1, const T* rowscale, T scale,
 template <typename T, int C, typename OutT>
 int launch_rowsum(const T* P, int ldp, const T* Q, int ldq, const T* w, simt::ChanSet chans,
                   int64_t n, int M, int N, bool sym, double scale, double* part, OutT* out,
-                  cudaStream_t s, int accumulate = 0) {
+                  cudaStream_t s, int accumulate = 0, bool comp = false) {
   const int64_t cp = chunk_points(n);
   const int chunks = (int)ceil_div(n, cp);
   const int mt = (int)ceil_div(M, 128), nt = (int)ceil_div(N, simt::kBN);
@@ -219,11 +221,18 @@ int launch_rowsum(const T* P, int ldp, const T* Q, int ldq, const T* w, simt::Ch
   if (sym) NEB_REQUIRE(M == N, "symmetric rowsum needs M == N");
   dim3 grid(tiles, chunks);
   {
-    KernelScope ks(sym ? "simt_gram" : "simt_weight_grad", s,
+    const bool c32 = comp && sizeof(T) == 4;
+    KernelScope ks(sym ? (c32 ? "simt_gram_compensated" : "simt_gram") : "simt_weight_grad", s,
                    (sym ? 1.0 : 2.0) * n * chans.n * (double)M * N,
                    (double)n * chans.n * (M + N) * sizeof(T));
-    simt::rowsum_gemm<T, C><<<grid, simt::kThreads, 0, s>>>(P, ldp, Q, ldq, w, chans, n, cp, M, N,
-                                                            sym ? 1 : 0, part);
+    if constexpr (sizeof(T) == 4) {
+      if (c32)
+        simt::rowsum_gemm<T, C, true><<<grid, simt::kThreads, 0, s>>>(
+            P, ldp, Q, ldq, w, chans, n, cp, M, N, sym ? 1 : 0, part);
+    }
+    if (!c32)
+      simt::rowsum_gemm<T, C><<<grid, simt::kThreads, 0, s>>>(P, ldp, Q, ldq, w, chans, n, cp, M,
+                                                              N, sym ? 1 : 0, part);
     NEB_LAUNCH_CHECK();
   }
   int64_t total = (int64_t)M * N;
@@ -381,11 +390,12 @@ int hidden_gram_simt(const neb_net* net, const void* qw, int64_t n, const void* 
   double* part = (double*)((char*)ws + wl.part);
   simt::ChanSet grad{2, {1, 2}};
   simt::ChanSet lap{1, {3}};
+  const bool comp = net->gram == NEB_GRAM_COMPENSATED;
   int st = launch_rowsum<T, C, double>(HL, H, HL, H, (const T*)qw, grad, n, H, H, true, 1.0, part,
-                                       AM, s);
+                                       AM, s, 0, comp);
   if (st) return st;
   return launch_rowsum<T, C, double>(HL, H, HL, H, (const T*)qw, lap, n, H, H, true, 1.0, part, AS,
-                                     s);
+                                     s, 0, comp);
 }
 
 // ------------------------------------------------------ direct route
@@ -423,11 +433,12 @@ int fields_gram_simt(const neb_net* net, const void* Wout, const void* qw, int64
   if (st) return st;
   simt::ChanSet vel = C == 4 ? simt::ChanSet{2, {1, 2}} : simt::ChanSet{3, {1, 2, 3}};
   simt::ChanSet vor = C == 4 ? simt::ChanSet{1, {3}} : simt::ChanSet{3, {4, 5, 6}};
+  const bool comp = net->gram == NEB_GRAM_COMPENSATED;
   st = launch_rowsum<T, C, double>(F, K, F, K, (const T*)qw, vel, n, K, K, true, 1.0, part, M, s,
-                                   accumulate);
+                                   accumulate, comp);
   if (st) return st;
   return launch_rowsum<T, C, double>(F, K, F, K, (const T*)qw, vor, n, K, K, true, 1.0, part, S,
-                                     s, accumulate);
+                                     s, accumulate, comp);
 }
 
 // Reverse of fields_gram + objective adjoints G_M, G_S: field adjoints
@@ -779,11 +790,27 @@ extern "C" int neb_check_status(const neb_net* net, int64_t n, void* ws, size_t 
   return NEB_OK;
 }
 
+extern "C" int neb_wait_selftest(int arrive, uint32_t spin_limit, int* status,
+                                 neb_stream_t stream) {
+  NEB_REQUIRE(status != nullptr, "neb_wait_selftest: null status");
+  NEB_REQUIRE(spin_limit >= 1024 && spin_limit <= (1u << 24),
+              "neb_wait_selftest: spin_limit must be in [1024, 2^24]");
+  int code = 0;
+  int st = tc_wait_selftest(arrive, spin_limit, status, (cudaStream_t)stream, &code);
+  if (st) return st;
+  if (code) {
+    set_error("a bounded device-side wait gave up (status %d)", code);
+    return NEB_ERR_TIMEOUT;
+  }
+  return NEB_OK;
+}
+
 extern "C" size_t neb_adam_workspace_bytes(void) { return 256; }
 
 extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* const* m,
                         void* const* v, const void* const* grads, const int64_t* sizes, int step,
-                        double lr, double clip, double beta1, double beta2, double eps,
+                        int* step_counter, double lr, double clip, double beta1, double beta2,
+                        double eps,
                         double* norm_out, int* committed_out, void* ws, size_t ws_bytes,
                         neb_stream_t stream) {
   NEB_REQUIRE(dtype == 0 || dtype == 1, "neb_adam: dtype must be 0 (float) or 1 (double)");
@@ -822,16 +849,13 @@ extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* con
   double* scal = (double*)((char*)ws + 128);
   {
     KernelScope ks("adam_update", s, 0, total * es * 7, 2);
-    adam_finalize<<<1, 1, 0, s>>>(acc, flag, clip, norm_out, committed_out, scal);
+    adam_finalize<<<1, 1, 0, s>>>(acc, flag, clip, step, step_counter, lr, beta1, beta2,
+                                  norm_out, committed_out, scal);
     NEB_LAUNCH_CHECK();
-    const double step1 = (double)step + 1;
-    const double lr_c1 = lr / (1.0 - std::pow(beta1, step1));
-    const double inv_c2 = 1.0 / (1.0 - std::pow(beta2, step1));
     if (dtype == 0)
-      adam_update<float><<<blocks, 256, 0, s>>>(t, scal, (float)lr_c1, (float)inv_c2,
-                                                (float)beta1, (float)beta2, (float)eps);
+      adam_update<float><<<blocks, 256, 0, s>>>(t, scal, (float)beta1, (float)beta2, (float)eps);
     else
-      adam_update<double><<<blocks, 256, 0, s>>>(t, scal, lr_c1, inv_c2, beta1, beta2, eps);
+      adam_update<double><<<blocks, 256, 0, s>>>(t, scal, beta1, beta2, eps);
     NEB_LAUNCH_CHECK();
   }
   return NEB_OK;

@@ -126,27 +126,38 @@ __global__ void adam_norm(AdamTable t, double* __restrict__ acc, int* __restrict
 }
 
 // The transaction's scalars, once: global norm, commit decision (finite
-// gradients and a positive norm, hardcoded_backend.py:2184-2277) and the clip
-// scale min(1, clip / norm); scal[0] = 0 means "do not commit".
+// gradients and a positive norm, hardcoded_backend.py:2184-2277), the clip
+// scale min(1, clip / norm) (scal[0] = 0 means "do not commit") and the bias
+// corrections of step t = committed steps + 1 (scal[1] = lr / (1 - beta1^t),
+// scal[2] = 1 / (1 - beta2^t)).  The committed-step count comes from the
+// device counter *steps when given (advanced here only on commit, as the
+// reference advances its epoch only after a committed update,
+// native_cupy_core.py:157-170), else from the host argument.
 static __global__ void adam_finalize(const double* __restrict__ acc, const int* __restrict__ flag,
-                              double clip, double* __restrict__ norm_out,
-                              int* __restrict__ committed_out, double* __restrict__ scal) {
+                                     double clip, int host_steps, int* __restrict__ steps,
+                                     double lr, double beta1, double beta2,
+                                     double* __restrict__ norm_out,
+                                     int* __restrict__ committed_out, double* __restrict__ scal) {
   const double norm = sqrt(acc[0]);
   const bool ok = (flag[0] == 0) && isfinite(norm) && norm > 0.0;
   if (norm_out) *norm_out = norm;
   if (committed_out) *committed_out = ok ? 1 : 0;
+  const double t = (double)(steps ? *steps : host_steps) + 1.0;
   scal[0] = ok ? fmin(1.0, clip / fmax(norm, 1e-30)) : 0.0;
+  scal[1] = lr / (1.0 - pow(beta1, t));
+  scal[2] = 1.0 / (1.0 - pow(beta2, t));
+  if (steps && ok) *steps += 1;
 }
 
-// Masked Adam update with the scalars of adam_finalize; lr_c1 = lr / (1 -
-// beta1^step), inv_c2 = 1 / (1 - beta2^step) come from the host, so no
-// per-element double-precision work remains for the FP32 form.
+// Masked Adam update with the scalars of adam_finalize (the bias
+// corrections are formed once there, so no per-element double-precision
+// work remains for the FP32 form).
 template <typename T>
-__global__ void adam_update(AdamTable t, const double* __restrict__ scal, T lr_c1, T inv_c2,
-                            T b1, T b2, T eps) {
+__global__ void adam_update(AdamTable t, const double* __restrict__ scal, T b1, T b2, T eps) {
   const double sc = scal[0];
   if (sc == 0.0) return;
-  const T scale = (T)sc, ob1 = T(1) - b1, ob2 = T(1) - b2;
+  const T scale = (T)sc, lr_c1 = (T)scal[1], inv_c2 = (T)scal[2];
+  const T ob1 = T(1) - b1, ob2 = T(1) - b2;
   const int64_t total = t.off[t.n];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {

@@ -308,17 +308,47 @@ jet_gemm_bwd(const T* __restrict__ A, const T* __restrict__ B0, const T* __restr
 // P[p*C + c][m] Q[p*C + c][n].  P: [n*C][ldp], Q: [n*C][ldq].  Tiles (mt, nt)
 // with blockIdx.x enumerating the tile pairs (upper triangle only when sym);
 // blockIdx.y is the point chunk.  part: [chunks][M][N] double.
+//
+// COMP (FP32 only): every product is split exactly into p + e (e = fma(a, b,
+// -p)) and the running sum is kept as an unevaluated pair hi + lo updated
+// by TwoSum, so a chunk sum is accurate to about eps_32^2 relative to its
+// terms instead of eps_32 times the number of terms.  The Grams of a nearly
+// dependent basis need this: a plain FP32 sum perturbs every entry by ~1e-7
+// of the largest, independently, which moves the small eigenvalues of the
+// mass matrix by that much.
 // ---------------------------------------------------------------------------
 struct ChanSet {
   int n;
   int c[10];
 };
 
-template <typename T, int C>
+template <typename T, bool COMP> struct RowAcc;
+template <typename T> struct RowAcc<T, false> {
+  T s;
+  __device__ __forceinline__ void zero() { s = T(0); }
+  __device__ __forceinline__ void add(T a, T b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return (double)s; }
+};
+template <> struct RowAcc<float, true> {
+  float hi, lo;
+  __device__ __forceinline__ void zero() { hi = lo = 0.f; }
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);  // a * b = p + e exactly
+    const float s = hi + p;
+    const float bb = s - hi;
+    lo += ((hi - (s - bb)) + (p - bb)) + e;
+    hi = s;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <typename T, int C, bool COMP = false>
 __global__ void __launch_bounds__(kThreads)
 rowsum_gemm(const T* __restrict__ Pm, int ldp, const T* __restrict__ Qm, int ldq,
             const T* __restrict__ wts, ChanSet chans, int64_t n_points, int64_t chunk_pts,
             int M, int N, int sym, double* __restrict__ part) {
+  static_assert(!COMP || sizeof(T) == 4, "compensated sums are the FP32 form");
   constexpr int BMr = 128;
   __shared__ __align__(16) T Ps[kBK][BMr + 4];
   __shared__ __align__(16) T Qs[kBK][kBN + 4];
@@ -340,11 +370,11 @@ rowsum_gemm(const T* __restrict__ Pm, int ldp, const T* __restrict__ Qm, int ldq
   if (p_end > n_points) p_end = n_points;
   const int64_t klen = (p_end - p_begin) * chans.n;
 
-  T acc[8][8];
+  RowAcc<T, COMP> acc[8][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+    for (int j = 0; j < 8; ++j) acc[i][j].zero();
 
   // each thread loads 4 P and 4 Q elements per k tile: k = e / 128, m = e % 128
   T rp[4], rq[4];
@@ -389,7 +419,7 @@ rowsum_gemm(const T* __restrict__ Pm, int ldp, const T* __restrict__ Qm, int ldq
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 8; ++j) acc[i][j].add(a[i], b[j]);
     }
     __syncthreads();
   }
@@ -401,7 +431,7 @@ rowsum_gemm(const T* __restrict__ Pm, int ldp, const T* __restrict__ Qm, int ldq
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       int n = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
-      if (n < N) out[(int64_t)m * N + n] = (double)acc[i][j];
+      if (n < N) out[(int64_t)m * N + n] = acc[i][j].value();
     }
   }
 }

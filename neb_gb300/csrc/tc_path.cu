@@ -117,10 +117,15 @@ template <int EPI> struct JetCfg {
   // accumulator buffers in the 512 TMEM columns (double-buffered when they fit)
   static constexpr int NBUF = 2 * NCH * BN <= 512 ? 2 : 1;
   static constexpr int TBUF = 512 / NBUF;        // TMEM columns per accumulator buffer
-  static constexpr int A_ST = 5;
+  // planes of B: the weights are split in two (hi, lo); the Gram adjoints
+  // G_M, G_S in three (24 significant bits), because h G cancels in the
+  // directions where G is large, so an independent rounding of G's entries
+  // to 16 bits would show up in the gradient amplified by that cancellation
+  static constexpr int NPL = EPI == 2 ? 3 : 2;
+  static constexpr int A_ST = EPI == 2 ? 4 : 5;  // shared memory holds 4 A stages with 3 B planes
   static constexpr int B_ST = 2;
   static constexpr int B_TILE = BN * 128;        // BN rows x 64 bf16
-  static constexpr int B_BYTES = 2 * NB * B_TILE;
+  static constexpr int B_BYTES = NPL * NB * B_TILE;
   static constexpr int SMEM = 1024 + A_ST * 2 * kTileBytes + B_ST * B_BYTES + 256;
 };
 
@@ -138,7 +143,8 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             JetGemmArgs g) {
   using Cfg = JetCfg<EPI>;
   constexpr int BN = Cfg::BN, NB = Cfg::NB, NCH = Cfg::NCH, CH0 = Cfg::CH0, A_ST = Cfg::A_ST,
-                B_ST = Cfg::B_ST;
+                B_ST = Cfg::B_ST, NPL = Cfg::NPL;
+  static_assert(Cfg::SMEM <= 232448, "jet GEMM shared memory above the 227 KB per block");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* a_smem = smem;
@@ -150,7 +156,8 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   uint64_t* b_empty = bars + 2 * A_ST + B_ST;
   uint64_t* acc_full = bars + 2 * A_ST + 2 * B_ST;   // [2]
   uint64_t* acc_empty = acc_full + 2;                // [2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  uint64_t* mma_done = acc_empty + 2;                // every MMA of this CTA completed
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int KC = g.K / 64;
@@ -170,6 +177,7 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       tc::mbar_init(&acc_full[i], 1);
       tc::mbar_init(&acc_empty[i], kJetEpiWarps);  // one arrival per epilogue warp
     }
+    tc::mbar_init(mma_done, 1);
     tc::fence_mbar_init();
   }
   if (warp == 1) {
@@ -182,21 +190,31 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer
+    // ---------------- TMA producer.  A wait that gives up ends the issue
+    // before the stage's expect_tx, so every stage is either fully issued or
+    // untouched; the copies already issued are drained before the CTA exits.
     int ai = 0, bi = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    bool ok = true;
+    for (int t = blockIdx.x; ok && t < total; t += gridDim.x) {
       const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
-      for (int kc = 0; kc < KC; ++kc, ++bi) {
+      for (int kc = 0; ok && kc < KC; ++kc) {
         const int bs = bi % B_ST;
-        tc::mbar_wait(&b_empty[bs], ((bi / B_ST) & 1) ^ 1, g.status);
+        if (!tc::mbar_wait(&b_empty[bs], ((bi / B_ST) & 1) ^ 1, g.status)) {
+          ok = false;
+          break;
+        }
         tc::mbar_expect_tx(&b_full[bs], Cfg::B_BYTES);
         for (int b = 0; b < NB; ++b)
-          for (int pl = 0; pl < 2; ++pl)
-            tc::tma_load_2d(b_smem + bs * Cfg::B_BYTES + (b * 2 + pl) * Cfg::B_TILE, &tmB,
+          for (int pl = 0; pl < NPL; ++pl)
+            tc::tma_load_2d(b_smem + bs * Cfg::B_BYTES + (b * NPL + pl) * Cfg::B_TILE, &tmB,
                             &b_full[bs], kc * 64, (pl * NB + b) * g.N + n0);
-        for (int ci = 0; ci < NCH; ++ci, ++ai) {
+        ++bi;
+        for (int ci = 0; ci < NCH; ++ci) {
           const int as = ai % A_ST, c = CH0 + ci;
-          tc::mbar_wait(&a_empty[as], ((ai / A_ST) & 1) ^ 1, g.status);
+          if (!tc::mbar_wait(&a_empty[as], ((ai / A_ST) & 1) ^ 1, g.status)) {
+            ok = false;
+            break;
+          }
           tc::mbar_expect_tx(&a_full[as], 2 * kTileBytes);
           // A is MN-major: [plane][channel][k][point]; a tile is two boxes of
           // 64 points x 64 k rows
@@ -204,30 +222,40 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             for (int hb = 0; hb < 2; ++hb)
               tc::tma_load_2d(a_smem + (as * 2 + pl) * kTileBytes + hb * (kTileBytes / 2), &tmA,
                               &a_full[as], p0 + hb * 64, (pl * C + c) * g.K + kc * 64);
+          ++ai;
         }
       }
     }
+    tc::drain_ring(b_full, B_ST, bi, g.status);
+    tc::drain_ring(a_full, A_ST, ai, g.status);
   } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer
+    // ---------------- MMA issuer (stops at the first wait that gives up)
     constexpr uint32_t idesc = tc::idesc_bf16(128, BN, true);
     int ai = 0, bi = 0, it = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
+    bool ok = true;
+    for (int t = blockIdx.x; ok && t < total; t += gridDim.x, ++it) {
       const int buf = it % Cfg::NBUF, use = it / Cfg::NBUF;
-      tc::mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status);
+      if (!tc::mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status)) break;
       tc::tc_fence_after();
-      for (int kc = 0; kc < KC; ++kc, ++bi) {
+      for (int kc = 0; ok && kc < KC; ++kc) {
         const int bs = bi % B_ST;
-        tc::mbar_wait(&b_full[bs], (bi / B_ST) & 1, g.status);
+        if (!tc::mbar_wait(&b_full[bs], (bi / B_ST) & 1, g.status)) {
+          ok = false;
+          break;
+        }
         tc::tc_fence_after();
-        for (int ci = 0; ci < NCH; ++ci, ++ai) {
+        for (int ci = 0; ci < NCH; ++ci) {
           const int as = ai % A_ST, c = CH0 + ci;
-          tc::mbar_wait(&a_full[as], (ai / A_ST) & 1, g.status);
+          if (!tc::mbar_wait(&a_full[as], (ai / A_ST) & 1, g.status)) {
+            ok = false;
+            break;
+          }
           tc::tc_fence_after();
           const int bsel = (EPI == 2 && c == 3) ? 1 : 0;
           const uint32_t a_hi = tc::smem_u32(a_smem + (as * 2) * kTileBytes);
           const uint32_t a_lo = a_hi + kTileBytes;
           const uint32_t b_hi =
-              tc::smem_u32(b_smem + bs * Cfg::B_BYTES + (bsel * 2) * Cfg::B_TILE);
+              tc::smem_u32(b_smem + bs * Cfg::B_BYTES + (bsel * NPL) * Cfg::B_TILE);
           const uint32_t b_lo = b_hi + Cfg::B_TILE;
           const uint32_t d = tmem + buf * Cfg::TBUF + ci * BN;
 #pragma unroll
@@ -240,13 +268,25 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
             tc::mma_bf16(d, dah, dbh, idesc, (kc | kk) != 0);
             tc::mma_bf16(d, dal, dbh, idesc, 1);
             tc::mma_bf16(d, dah, dbl, idesc, 1);
+            if constexpr (NPL == 3) {  // B = b1 + b2 + b3: add lo.b2 and hi.b3
+              const uint64_t db3 = tc::desc_sw128(b_hi + 2 * Cfg::B_TILE + boff);
+              tc::mma_bf16(d, dal, dbl, idesc, 1);
+              tc::mma_bf16(d, dah, db3, idesc, 1);
+            }
           }
           tc::mma_commit(&a_empty[as]);
+          ++ai;
         }
+        if (!ok) break;
         tc::mma_commit(&b_empty[bs]);
+        ++bi;
       }
+      if (!ok) break;
       tc::mma_commit(&acc_full[buf]);
     }
+    // the MMAs issued so far must complete before the tensor memory is freed
+    tc::mma_commit(mma_done);
+    tc::mbar_wait_drain(mma_done, 0, g.status);
   } else if (warp >= 2) {
     // ---------------- epilogue: kJetEpiWarps warps, one thread per point
     // (TMEM lane): warp w reads lane quarter w % 4, column slice (w - 2) / 4
@@ -254,7 +294,8 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     const int row = q * 32 + lane;
     const size_t plane = (size_t)C * g.n_pad * g.N;  // elements of one hi or lo plane
     int it = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++it) {
+    bool ok = true;
+    for (int t = blockIdx.x; ok && t < total; t += gridDim.x, ++it) {
       const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
       const int p = p0 + row;
       const int buf = it % Cfg::NBUF, use = it / Cfg::NBUF;
@@ -282,7 +323,10 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
               out[c][j] = __ldg(g.zprev + ((size_t)c * g.N + col + j) * g.n_pad + p);
         }
         if (jc == 0) {
-          tc::mbar_wait(&acc_full[buf], use & 1, g.status);
+          // the TMEM loads below are warp-collective: the whole warp goes on
+          // only when every lane saw the accumulators complete
+          ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[buf], use & 1, g.status));
+          if (!ok) break;
           tc::tc_fence_after();
         }
         uint32_t raw[NCH][kW];
@@ -408,7 +452,8 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
   uint64_t* empty = bars + ST;
   uint64_t* acc_ready = bars + 2 * ST;      // [2]
   uint64_t* acc_free = bars + 2 * ST + 2;   // [2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * ST + 4);
+  uint64_t* mma_done = bars + 2 * ST + 4;   // every MMA of this CTA completed
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * ST + 5);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = g.N / BN;
@@ -429,6 +474,7 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
       tc::mbar_init(&acc_ready[i], 1);
       tc::mbar_init(&acc_free[i], 256);
     }
+    tc::mbar_init(mma_done, 1);
     tc::fence_mbar_init();
   }
   if (warp == 1) {
@@ -441,10 +487,13 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
+    // producer: stops at the first wait that gives up, then drains the
+    // copies it issued before the CTA exits
+    int issued = 0;
     for (int it = 0; it < n_it; ++it) {
       const int kq = k_begin + it, s = it % ST;
       const int ci = kq / pblocks, pb = kq % pblocks;
-      tc::mbar_wait(&empty[s], ((it / ST) & 1) ^ 1, g.status);
+      if (!tc::mbar_wait(&empty[s], ((it / ST) & 1) ^ 1, g.status)) break;
       tc::mbar_expect_tx(&full[s], Cfg::A_BYTES + Cfg::B_BYTES);
       for (int pl = 0; pl < 2; ++pl) {
         tc::tma_load_2d(a_smem + s * Cfg::A_BYTES + pl * kTileBytes, &tmA, &full[s], pb * 64,
@@ -452,13 +501,15 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
         tc::tma_load_2d(b_smem + s * Cfg::B_BYTES + pl * (BN * 128), &tmB, &full[s], pb * 64,
                         (pl * g.bC + g.b_ch0 + ci) * g.N + n0);
       }
+      ++issued;
     }
+    tc::drain_ring(full, ST, issued, g.status);
   } else if (warp == 1 && lane == 0) {
     constexpr uint32_t idesc = tc::idesc_bf16(128, BN);
     for (int it = 0; it < n_it; ++it) {
       const int s = it % ST, buf = it & 1;
-      if (it >= 2) tc::mbar_wait(&acc_free[buf], ((it >> 1) & 1) ^ 1, g.status);
-      tc::mbar_wait(&full[s], (it / ST) & 1, g.status);
+      if (it >= 2 && !tc::mbar_wait(&acc_free[buf], ((it >> 1) & 1) ^ 1, g.status)) break;
+      if (!tc::mbar_wait(&full[s], (it / ST) & 1, g.status)) break;
       tc::tc_fence_after();
       const uint32_t d = tmem + buf * BN;
       const uint32_t a_hi = tc::smem_u32(a_smem + s * Cfg::A_BYTES), a_lo = a_hi + kTileBytes;
@@ -476,6 +527,9 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
       tc::mma_commit(&empty[s]);
       tc::mma_commit(&acc_ready[buf]);
     }
+    // the MMAs issued so far must complete before the tensor memory is freed
+    tc::mma_commit(mma_done);
+    tc::mbar_wait_drain(mma_done, 0, g.status);
   } else if (warp >= 2) {
     // eight drain warps: lane quarter q = warp % 4, column half h
     constexpr int HB = BN / 2;
@@ -486,7 +540,9 @@ tc_rowsum(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
     for (int j = 0; j < HB; ++j) sum[j] = 0.f;
     for (int it = 0; it < n_it; ++it) {
       const int buf = it & 1;
-      tc::mbar_wait(&acc_ready[buf], (it >> 1) & 1, g.status);
+      // warp-uniform: the TMEM loads below are warp-collective
+      if (!__all_sync(0xffffffffu, tc::mbar_wait(&acc_ready[buf], (it >> 1) & 1, g.status)))
+        break;
       tc::tc_fence_after();
       uint32_t raw[HB / 16][16];
 #pragma unroll
@@ -557,17 +613,21 @@ __global__ void split_weight(const float* __restrict__ W, int out, int in, int i
   }
 }
 
-// G_M, G_S (double [H][H]) -> [2 planes][2 (M, S)][H][H] bf16.
+// G_M, G_S (double [H][H]) -> [3 planes][2 (M, S)][H][H] bf16 with
+// G = b1 + b2 + b3 to 24 significant bits (the residuals are formed in FP64).
 __global__ void split_gram_adjoint(const double* __restrict__ GM, const double* __restrict__ GS,
                                    int H, __nv_bfloat16* __restrict__ out) {
   const size_t hh = (size_t)H * H;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 2 * hh;
        i += (size_t)gridDim.x * blockDim.x) {
-    float v = (float)(i < hh ? GM[i] : GS[i - hh]);
-    __nv_bfloat16 h, l;
-    tc::split_bf16(v, h, l);
-    out[i] = h;
-    out[2 * hh + i] = l;
+    const double v = i < hh ? GM[i] : GS[i - hh];
+    const __nv_bfloat16 b1 = __double2bfloat16(v);
+    const double r1 = v - (double)__bfloat162float(b1);
+    const __nv_bfloat16 b2 = __double2bfloat16(r1);
+    const double r2 = r1 - (double)__bfloat162float(b2);
+    out[i] = b1;
+    out[2 * hh + i] = b2;
+    out[4 * hh + i] = __double2bfloat16(r2);
   }
 }
 
@@ -728,7 +788,7 @@ TcWs tc_ws(const Dims& d) {
     mw = mw > d.w[l] ? mw : d.w[l];
   }
   t.gsplit = off;
-  off += a256((size_t)4 * d.H * d.H * 2);
+  off += a256((size_t)6 * d.H * d.H * 2);
   t.wht = off;
   off += a256((size_t)2 * 3 * d.H * d.n_pad * 2);
   size_t zb = a256((size_t)2 * C * d.n_pad * mw * 2);
@@ -939,7 +999,7 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
   const int L = d.L, H = d.H;
   __nv_bfloat16* gs = (__nv_bfloat16*)(ws + t.gsplit);
   {
-    KernelScope ks("tc_split_gram_adjoint", s, 0, (double)H * H * 2 * 12);
+    KernelScope ks("tc_split_gram_adjoint", s, 0, (double)H * H * 2 * 14);
     split_gram_adjoint<<<(int)std::min<size_t>((2ull * H * H + 255) / 256, 4096), 256, 0, s>>>(
         GMh, GSh, H, gs);
     NEB_LAUNCH_CHECK();
@@ -950,7 +1010,7 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
   {
     CUtensorMap ma, mb;
     if ((st = make_map(&ma, tape.x[L], (int64_t)2 * C * H, d.n_pad, 64))) return st;
-    if ((st = make_map(&mb, gs, (int64_t)4 * H, H, JetCfg<2>::BN))) return st;
+    if ((st = make_map(&mb, gs, (int64_t)JetCfg<2>::NPL * 2 * H, H, JetCfg<2>::BN))) return st;
     JetGemmArgs g{};
     g.n_points = (int)n;
     g.n_pad = (int)d.n_pad;
@@ -1039,6 +1099,33 @@ int tc_output(const neb_net*, const float*, const float*, int, int, int64_t, con
               cudaStream_t) {
   set_error("NEB_PREC_BF16X3 stores no output-layer jets; evaluate them with NEB_PREC_FP32");
   return NEB_ERR_UNSUPPORTED;
+}
+
+// One CTA waits, with the same bounded mbarrier wait every tensor-core
+// pipeline uses, for a phase that completes only if `arrive` is set (thread
+// 1 arrives); no copy or MMA is involved.  Without the arrival the wait runs
+// out after `limit` polls and records bit 0 in *status.
+__global__ void wait_selftest_kernel(int arrive, uint32_t limit, int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (arrive && threadIdx.x == 1) tc::mbar_arrive(&bar);
+  if (threadIdx.x == 0) tc::mbar_wait(&bar, 0, status, limit);
+}
+
+int tc_wait_selftest(int arrive, uint32_t limit, int* status, cudaStream_t s, int* out) {
+  NEB_CUDA_CHECK(cudaMemsetAsync(status, 0, sizeof(int), s));
+  {
+    KernelScope ks("wait_selftest", s, 0, 0);
+    wait_selftest_kernel<<<1, 32, 0, s>>>(arrive, limit, status);
+    NEB_LAUNCH_CHECK();
+  }
+  NEB_CUDA_CHECK(cudaMemcpyAsync(out, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NEB_CUDA_CHECK(cudaStreamSynchronize(s));
+  return NEB_OK;
 }
 
 int tc_read_status(const neb_net* net, int64_t n, char* ws, cudaStream_t s, int* out) {

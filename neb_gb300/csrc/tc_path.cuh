@@ -15,6 +15,8 @@ size_t tc_workspace_bytes(const neb_net* net, int64_t n);
 size_t tc_tape_bytes(const neb_net* net, int64_t n, size_t* x_off, size_t* z_off);
 // Synchronises the stream and reads the bounded-wait status word (0 = ok).
 int tc_read_status(const neb_net* net, int64_t n, char* ws, cudaStream_t s, int* out);
+// Runs the bounded-wait self-test kernel, synchronises and returns its status word.
+int tc_wait_selftest(int arrive, uint32_t limit, int* status, cudaStream_t s, int* out);
 int tc_forward(const neb_net* net, const float* const* W, const float* const* b, const float* feats,
                int64_t n, const TcTape& tape, char* ws, cudaStream_t s);
 int tc_output(const neb_net* net, const float* Wout, const float* bout, int start, int stop,

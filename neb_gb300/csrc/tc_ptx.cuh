@@ -43,18 +43,39 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: returns false (and sets bit 0 of *status) after kMaxSpins
+// Bounded wait: returns false (and sets bit 0 of *status) after `limit`
 // polls, or soon after another wait of this launch has already given up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
+// A caller that gets false issues no further copies or MMAs.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status,
+                                          uint32_t limit = kMaxSpins) {
   uint32_t spins = 0;
   while (!mbar_try_wait(bar, parity)) {
     if ((++spins & 1023u) == 0u &&
-        (spins >= kMaxSpins || *reinterpret_cast<volatile int*>(status) != 0)) {
+        (spins >= limit || *reinterpret_cast<volatile int*>(status) != 0)) {
       atomicOr(status, 1);
       return false;
     }
   }
   return true;
+}
+// The same wait for the shutdown of a CTA that gave up: it is not cut short
+// by the status word (copies or MMAs this CTA issued must land before it
+// exits), still bounded by kMaxSpins; a wait that runs out sets bit 1.
+__device__ __forceinline__ void mbar_wait_drain(uint64_t* bar, uint32_t parity, int* status) {
+  uint32_t spins = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++spins >= kMaxSpins) {
+      atomicOr(status, 2);
+      return;
+    }
+  }
+}
+// Waits until the last copy issued into each of the `stages` stages of a
+// ring (issue count `issued`, stage = issue % stages, phase = issue /
+// stages) has completed on its `full` barrier.
+__device__ __forceinline__ void drain_ring(uint64_t* full, int stages, int issued, int* status) {
+  for (int j = issued > stages ? issued - stages : 0; j < issued; ++j)
+    mbar_wait_drain(&full[j % stages], (uint32_t)((j / stages) & 1), status);
 }
 
 // ------------------------------------------------------------------ TMA

@@ -63,7 +63,7 @@ class Model:
 
     def __init__(self, cfg: NebConfig, K: int | None = None, seed: int = 0,
                  precision: str | None = None, device: str | torch.device = "cuda",
-                 spectral: str | None = None):
+                 spectral: str | None = None, gram: str | None = None):
         # split-BF16 tensor cores for the 2D hidden-layer route; the 3D curl
         # fields take the direct route, which runs the FP32 kernels
         precision = precision or ("bf16x3" if cfg.dim == 2 else "fp32")
@@ -81,8 +81,10 @@ class Model:
         if spectral not in ("mixed", "fp64", "range"):
             raise ValueError("spectral must be 'mixed', 'fp64' or 'range'")
         self.spectral = spectral
-        # range solves keep the eigen-directions of M above rank_rtol * max
-        self.rank_rtol = RANK_RTOL
+        # range solves keep the eigen-directions of M above rank_rtol * max:
+        # the tolerance at which the finite pencil is determined by the
+        # fields to the working precision (RANK_RTOL)
+        self.rank_rtol = RANK_RTOL[precision]
         if K is not None:
             cfg = cfg.scaled(outputs=K * (3 if cfg.dim == 3 else 1))
         self.c = cfg
@@ -90,7 +92,10 @@ class Model:
         self.precision = precision
         self.device = torch.device(device)
         self.dtype = torch.float64 if precision == "fp64" else torch.float32
-        self.epoch = 0
+        # committed Adam steps, kept on the device: the update advances it
+        # only when it commits, so a rejected step on the asynchronous path
+        # leaves the bias correction of every later step unchanged
+        self._steps = torch.zeros((), dtype=torch.int32, device=self.device)
         self.W, self.b = [], []
         for W, b in glorot_params(cfg.widths, seed):
             self.W.append(torch.tensor(W, dtype=self.dtype, device=self.device))
@@ -99,15 +104,27 @@ class Model:
         self.vW = [torch.zeros_like(w) for w in self.W]
         self.mb = [torch.zeros_like(b) for b in self.b]
         self.vb = [torch.zeros_like(b) for b in self.b]
-        self.net = N.NebNet.make(cfg.dim, cfg.widths, precision)
+        # Gram accumulation of the FP32 form (FP64 sums in FP64, split-BF16
+        # in tensor memory)
+        self.gram = gram or (cfg.gram if precision == "fp32" else "plain")
+        self.net = N.NebNet.make(cfg.dim, cfg.widths, precision, self.gram)
         # the reference-API forward/backward evaluate output-layer jets, which
         # the tensor-core path does not store: they run the FP32 kernels
         self.net_eval = self.net if precision != "bf16x3" else \
-            N.NebNet.make(cfg.dim, cfg.widths, "fp32")
+            N.NebNet.make(cfg.dim, cfg.widths, "fp32", self.gram)
         self._buf = _Buffers(self.device)
         N.load()
 
     # ------------------------------------------------------------ helpers
+    @property
+    def epoch(self) -> int:
+        """Committed optimizer steps (reads the device counter)."""
+        return int(self._steps.item())
+
+    @epoch.setter
+    def epoch(self, value: int) -> None:
+        self._steps.fill_(int(value))
+
     @property
     def channels(self) -> int:
         return 4 if self.c.dim == 2 else 10
@@ -215,7 +232,8 @@ class Model:
 
     def adam_async(self, gW, gb, lr, clip=8.0, beta1=0.9, beta2=0.999, eps=1e-8):
         """Adam without a host synchronisation: returns device (norm,
-        committed) tensors; the epoch advances (the caller checks commit)."""
+        committed) tensors.  The step counter on the device advances only
+        when the update commits (the caller checks ``committed``)."""
         params = [*self.W, *self.b]
         grads = [g.to(self.dtype).contiguous() for g in [*gW, *gb]]
         for p, g in zip(params, grads):
@@ -227,10 +245,9 @@ class Model:
         ws = self._buf.get("adam", N.load().neb_adam_workspace_bytes())
         N.call("neb_adam", 1 if self.dtype == torch.float64 else 0, len(params),
                N.ptr_array(params), N.ptr_array([*self.mW, *self.mb]),
-               N.ptr_array([*self.vW, *self.vb]), N.ptr_array(grads), sizes, self.epoch, lr, clip,
-               beta1, beta2, eps, norm.data_ptr(), committed.data_ptr(), ws.data_ptr(), ws.numel(),
-               _stream())
-        self.epoch += 1
+               N.ptr_array([*self.vW, *self.vb]), N.ptr_array(grads), sizes, 0,
+               self._steps.data_ptr(), lr, clip, beta1, beta2, eps, norm.data_ptr(),
+               committed.data_ptr(), ws.data_ptr(), ws.numel(), _stream())
         return norm, committed
 
     def save(self, path, configuration=None) -> None:
@@ -329,10 +346,21 @@ def _solve(model: Model, m: int, PM, PS, kind: str):
     return loss, lam, V, GM, GS, info
 
 
-RANK_RTOL = 1e-10
+# Rank tolerance of the range solve (the eigenvalue-ratio test of
+# experiments/periodic/paper_rollout.py:180-186) per working precision.  The
+# raw-coordinate bases are nearly dependent at init: the mass Gram's
+# eigenvalues fall smoothly over ten decades, and a direction with e / e_max
+# = tau carries its eigenvalue and its share of the gradient with a condition
+# number growing like tau^-1/2 and faster.  Below a precision's tolerance the
+# finite pencil is set by rounding rather than by the fields: FP64 resolves
+# 1e-10; the FP32 form (compensated Grams, FP32 activations, FP32 Gram
+# adjoints) 1e-5; split-BF16 (16-bit activations, FP32 accumulation in
+# tensor memory) 1e-4.  The FP64 oracle solves the same pencil at the same
+# tolerance, and the ranks agree.
+RANK_RTOL = {"fp64": 1e-10, "fp32": 1e-5, "bf16x3": 1e-4}
 
 
-def _solve_range(model: Model, m: int, PM, PS, kind: str, rank_rtol: float = RANK_RTOL):
+def _solve_range(model: Model, m: int, PM, PS, kind: str, rank_rtol: float = 1e-10):
     """FP64 finite pencil of a possibly singular M (rank from the eigenvalue
     ratio test); returns the r finite pairs.  Reads the rank back (one
     stream synchronisation)."""
@@ -381,7 +409,7 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
     chunks of ``chunk_points``; the reverse pass recomputes each chunk's
     activations instead of keeping them (velocity/core.py:88-99).  The
     pencil is solved in FP64 on range(M) (rank from the eigenvalue ratio
-    test, RANK_RTOL), so a mass matrix whose fields are nearly dependent
+    test, ``model.rank_rtol``), so a mass matrix whose fields are nearly dependent
     gives the r finite eigenvalues rather than noise; ``rank`` reports r.
 
     ``check`` reads the solver status back (one 4-byte D2H) and raises

@@ -1,7 +1,7 @@
 """Times the reference's own 3D velocity training step on the host CPU.
 
 Test infrastructure, development container only: it imports the reference
-checkout (default ``/root/reference``, or ``$NEB_REFERENCE``), which the GPU
+checkout named by ``$NEB_REFERENCE`` (required), which the GPU
 machines do not have, and runs its CuPy code on NumPy through the stand-in
 module of ``tests/golden/make_golden.py`` (the pattern of the reference's
 tests/test_finite_gauge.py:10-16).  The step is
@@ -27,7 +27,12 @@ from pathlib import Path
 from types import SimpleNamespace
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("NEB_REFERENCE", "/root/reference"))
+def reference_root() -> Path:
+    """The reference checkout, named by $NEB_REFERENCE (required)."""
+    root = os.environ.get("NEB_REFERENCE")
+    if not root:
+        raise SystemExit("set NEB_REFERENCE to the reference checkout (baiming-zhang/NEB)")
+    return Path(root)
 
 
 def main(points: int | None = None) -> dict:
@@ -36,14 +41,14 @@ def main(points: int | None = None) -> dict:
     import make_golden as MG
     MG.install_shim()
     import numpy as np
-    vendor = REF / "experiments/metaball/_backend"
+    vendor = reference_root() / "experiments/metaball/_backend"
     case = vendor / "flow/cases/metaball"
     sys.path[:0] = [str(vendor), str(case), str(case / "velocity")]
     spec = importlib.util.spec_from_file_location("reference_train",
-                                                  REF / "experiments/metaball/train.py")
+                                                  reference_root() / "experiments/metaball/train.py")
     train = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(train)
-    cfg_path = REF / "experiments/metaball/configs/metaball-velocity-k32-seed0.json"
+    cfg_path = reference_root() / "experiments/metaball/configs/metaball-velocity-k32-seed0.json"
     config = train.runtime_configuration(json.loads(cfg_path.read_text()))
     c = SimpleNamespace(**config)
     core = MG.load(case / "velocity/core.py", "reference_velocity_core")

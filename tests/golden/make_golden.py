@@ -4,7 +4,7 @@ Runs the reference's own (CuPy) functions on the CPU by installing a NumPy
 stand-in for ``cupy`` / ``cupyx`` (the pattern of the reference's
 tests/test_finite_gauge.py:10-16) and records small seeded input/output
 vectors in ``tests/golden/reference_vectors.npz``.  It needs the reference
-checkout (default ``/root/reference``, or ``$NEB_REFERENCE``), which exists only
+checkout named by ``$NEB_REFERENCE`` (required), which exists only
 where the fixtures are made; the tests read the committed ``.npz`` alone.
 
 Reference functions exercised (paths relative to the reference project):
@@ -22,7 +22,7 @@ Reference functions exercised (paths relative to the reference project):
 * experiments/periodic/paper_rollout.py:178-187 recipe (Grams, then
   ``scipy.linalg.eigh(S, M)``).
 
-Usage:  python tests/golden/make_golden.py
+Usage:  NEB_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -37,7 +37,12 @@ from types import SimpleNamespace
 import numpy as np
 import scipy.linalg as sla
 
-REF = Path(os.environ.get("NEB_REFERENCE", "/root/reference"))
+def reference_root() -> Path:
+    """The reference checkout, named by $NEB_REFERENCE (required)."""
+    root = os.environ.get("NEB_REFERENCE")
+    if not root:
+        raise SystemExit("set NEB_REFERENCE to the reference checkout (baiming-zhang/NEB)")
+    return Path(root)
 OUT = Path(__file__).resolve().parent / "reference_vectors.npz"
 
 
@@ -87,11 +92,11 @@ def load(path, name):
 
 def main():
     install_shim()
-    hb_src = REF / "experiments/2d/_backend/periodic_core/vortex_merger/src"
+    hb_src = reference_root() / "experiments/2d/_backend/periodic_core/vortex_merger/src"
     sys.path.insert(0, str(hb_src))
     from eigenfluid.gen.vortex_merger2d import hardcoded_backend as HB
     HB.F32 = np.float64  # run the reference's FP32-typed GEMMs in FP64
-    vendor = REF / "experiments/metaball/_backend"
+    vendor = reference_root() / "experiments/metaball/_backend"
     metaball = vendor / "flow/cases/metaball"
     sys.path[:0] = [str(vendor), str(metaball)]
     ncc = load(metaball / "native_cupy_core.py", "native_cupy_core")
