@@ -278,6 +278,112 @@ int neb_adam(int dtype, int n_tensors, void* const* params, void* const* exp_avg
  * No copy or MMA is in flight during the wait.  Synchronises the stream. */
 int neb_wait_selftest(int arrive, uint32_t spin_limit, int* status, neb_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Mode-stacked SIREN networks: the reference's own per-mode architecture.
+ * K independent networks (one per mode) with weights stacked [K][out][in]
+ * and biases [K][out]; hidden layers y = sin(omega (W x + b)) (omega_first on
+ * the first layer, omega_hidden after), a linear output layer, the output jet
+ * multiplied by an envelope jet.  Jets: order 1 = value and gradient
+ * (C = 1 + dim), order 2 adds the compact Hessian (2D xx, xy, yy; 3D xx, xy,
+ * xz, yy, yz, zz).  Layout per mode [n][C][width]; a block of B modes
+ * [B][n][C][width]; features [n][C][widths[0]] and the envelope [n][C]
+ * (one column; NULL = the identity envelope) are shared by all modes.
+ * NCC:111-154 (Model, order 1, 3D) and VTJ2:26-82 (order 2, 3D). */
+typedef struct neb_modes {
+  int32_t dim;        /* 2 or 3 */
+  int32_t order;      /* 1 or 2 */
+  int32_t n_layers;   /* linear layers including the output layer, 1..NEB_MAX_HIDDEN+1 */
+  int32_t widths[NEB_MAX_HIDDEN + 2]; /* widths[0] inputs .. widths[n_layers] outputs per mode */
+  int32_t n_modes;    /* K: modes stacked in every parameter array */
+  int32_t precision;  /* NEB_PREC_FP32 or NEB_PREC_FP64 */
+  double omega_first;
+  double omega_hidden;
+} neb_modes;
+
+/* Bytes of the activation tape of a block of n_block modes (scaled
+ * pre-activations and outputs of every hidden layer) and of the reverse
+ * pass's workspace. */
+size_t neb_modes_tape_bytes(const neb_modes* net, int n_block, int64_t n_points);
+size_t neb_modes_workspace_bytes(const neb_modes* net, int n_block, int64_t n_points);
+
+/* Output jets of modes [start, stop) into out ([stop-start][n][C][widths[L]],
+ * envelope applied), keeping the tape.  W, b: host arrays of n_layers device
+ * pointers to the FULL stacked parameters (the call offsets to `start`).
+ * Replaces NCC:130-140 Model.forward and VTJ2:65-76 forward. */
+int neb_modes_forward(const neb_modes* net, int start, int stop, const void* const* W,
+                      const void* const* b, const void* features, const void* envelope,
+                      int64_t n_points, void* tape, size_t tape_bytes, void* out,
+                      neb_stream_t stream);
+
+/* Parameter gradients of <adjoint, output> for modes [start, stop) from the
+ * tape of the matching neb_modes_forward: gW, gb are n_layers device
+ * pointers to BLOCK arrays [stop-start][out][in], [stop-start][out],
+ * overwritten (accumulate = 0) or added to.  NCC:142-154 Model.backward,
+ * VTJ2:77-82 backward. */
+int neb_modes_backward(const neb_modes* net, int start, int stop, const void* const* W,
+                       const void* features, const void* envelope, int64_t n_points,
+                       const void* tape, const void* adjoint, void* const* gW, void* const* gb,
+                       int accumulate, void* workspace, size_t workspace_bytes,
+                       neb_stream_t stream);
+
+/* Velocity u = curl A and its gradient d_j u_a of 3D second-order vector
+ * potentials (3 outputs per mode) for modes [start, stop): writes columns
+ * start..stop-1 of U [3n][n_modes] (rows p*3 + a) and D [9n][n_modes] (rows
+ * p*9 + a*3 + j).  VTJ2:93-101 velocity / velocity_grad; and the adjoint
+ * (VC:32-38 lift): GU, GD in the same layouts -> output-jet adjoints
+ * [stop-start][n][10][3]. */
+int neb_velocity_fields(int precision, const void* out, int start, int stop, int64_t n_points,
+                        int n_modes, void* U, void* D, neb_stream_t stream);
+int neb_velocity_lift(int precision, const void* GU, const void* GD, int start, int stop,
+                      int64_t n_points, int n_modes, void* adjoint, neb_stream_t stream);
+
+/* Per-mode Adam (NCC:156-171): the clip norm of mode k runs over mode k's
+ * slice of every tensor (tensors stacked [n_modes][...], sizes[i] elements
+ * in total); nothing changes unless every mode's norm is finite and
+ * positive; beta1 0.9, beta2 0.999, eps 1e-8 as the reference.
+ * *step_counter (device int): committed steps, advanced on commit.
+ * norms_out [n_modes] (device double, may be NULL), committed_out (device
+ * int, may be NULL). */
+size_t neb_modes_adam_workspace_bytes(int n_modes);
+int neb_modes_adam(int dtype, int n_modes, int n_tensors, void* const* params,
+                   void* const* exp_avg, void* const* exp_avg_sq, const void* const* grads,
+                   const int64_t* sizes, int* step_counter, double lr, double clip,
+                   double* norms_out, int* committed_out, void* workspace,
+                   size_t workspace_bytes, neb_stream_t stream);
+
+/* G = scale A^T A (FP64, K x K) of the columns of A [rows][K] (FP32 or
+ * FP64, row-major), per-chunk partials reduced in FP64; compensated != 0
+ * sums FP32 products exactly paired (see NEB_GRAM_COMPENSATED).  The Grams
+ * of VC:40-46 (M = U^T U / n, S = D^T D / n). */
+size_t neb_column_gram_workspace_bytes(int64_t rows, int K);
+int neb_column_gram(int precision, int64_t rows, int K, const void* A, double scale,
+                    int compensated, double* G, void* workspace, size_t workspace_bytes,
+                    neb_stream_t stream);
+
+/* out = scale A C for A [rows][K] (FP32 or FP64) and C [K][K] FP64, both
+ * row-major, computed in FP64; out in A's type.  The field adjoints
+ * U Cu / n, D Cd / n of VC:94-95. */
+size_t neb_column_apply_workspace_bytes(int64_t rows, int K);
+int neb_column_apply(int precision, int64_t rows, int K, const void* A, const double* C,
+                     double scale, void* out, void* workspace, size_t workspace_bytes,
+                     neb_stream_t stream);
+
+/* Causal Rayleigh peel in Gram form, FP64 (VC:48-69 coefficient_peel):
+ * order = stable ascending sort of S_kk / M_kk; the sorted M orthonormalised
+ * by a scaled Cholesky factor applied twice (T with T^T M_sorted T = I);
+ * losses[r] = (T^T S_sorted T)_rr in causal order; T_out [K][K] row-major
+ * with rows in mode order; Cu, Cd [K][K] with dL/dU = U Cu / n and
+ * dL/dD = D Cd / n for L = sum(losses); relative_mass[r] and ortho_error
+ * (device, may be NULL).  info (device int): 0 ok, 1 a Cholesky factor
+ * failed (rank), 2 the reference's gate failed (a non-finite or
+ * non-positive loss, relative mass below 1e-4, orthogonality error above
+ * 1e-5).  No host synchronisation. */
+size_t neb_peel_workspace_bytes(int K);
+int neb_coefficient_peel(int K, const double* M, const double* S, double* losses, int* order,
+                         double* T_out, double* Cu, double* Cd, double* relative_mass,
+                         double* ortho_error, int* info, void* workspace,
+                         size_t workspace_bytes, neb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,6 +8,8 @@ hand-written reverse pass -- CUDA kernels behind a C ABI
 from .configs import CONFIGS, NebConfig, sample, objective_weights
 from .jets import Jet, pack, unpack
 from .model import Model, SpectralObjective, SpectralResult, spectral_step, train_step
+from .modes import ModeModel, coefficient_peel, velocity_step
 
 __all__ = ["CONFIGS", "NebConfig", "sample", "objective_weights", "Jet", "pack", "unpack",
-           "Model", "SpectralObjective", "SpectralResult", "spectral_step", "train_step"]
+           "Model", "SpectralObjective", "SpectralResult", "spectral_step", "train_step",
+           "ModeModel", "coefficient_peel", "velocity_step"]

@@ -46,6 +46,16 @@ class NebNet(ctypes.Structure):
         return cls(dim, n_hidden, arr, PREC[precision], GRAM[gram])
 
 
+class ModeNet(ctypes.Structure):
+    """neb_modes: shape of a mode-stacked SIREN network."""
+    _fields_ = [("dim", c_int32), ("order", c_int32), ("n_layers", c_int32),
+                ("widths", c_int32 * (MAX_HIDDEN + 2)), ("n_modes", c_int32),
+                ("precision", c_int32), ("omega_first", c_double), ("omega_hidden", c_double)]
+
+
+_P = c_void_p
+_PP = POINTER(c_void_p)
+
 # name -> (restype, argtypes)
 _SIGNATURES = {
     "neb_last_error": (ctypes.c_char_p, []),
@@ -99,6 +109,25 @@ _SIGNATURES = {
                          c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_size_t,
                          c_void_p]),
     "neb_wait_selftest": (c_int, [c_int, ctypes.c_uint32, c_void_p, c_void_p]),
+    "neb_modes_tape_bytes": (c_size_t, [POINTER(ModeNet), c_int, c_int64]),
+    "neb_modes_workspace_bytes": (c_size_t, [POINTER(ModeNet), c_int, c_int64]),
+    "neb_modes_forward": (c_int, [POINTER(ModeNet), c_int, c_int, _PP, _PP, _P, _P, c_int64, _P,
+                                  c_size_t, _P, _P]),
+    "neb_modes_backward": (c_int, [POINTER(ModeNet), c_int, c_int, _PP, _P, _P, c_int64, _P, _P,
+                                   _PP, _PP, c_int, _P, c_size_t, _P]),
+    "neb_velocity_fields": (c_int, [c_int, _P, c_int, c_int, c_int64, c_int, _P, _P, _P]),
+    "neb_velocity_lift": (c_int, [c_int, _P, _P, c_int, c_int, c_int64, c_int, _P, _P]),
+    "neb_modes_adam_workspace_bytes": (c_size_t, [c_int]),
+    "neb_modes_adam": (c_int, [c_int, c_int, c_int, _PP, _PP, _PP, _PP, POINTER(c_int64), _P,
+                               c_double, c_double, _P, _P, _P, c_size_t, _P]),
+    "neb_column_gram_workspace_bytes": (c_size_t, [c_int64, c_int]),
+    "neb_column_gram": (c_int, [c_int, c_int64, c_int, _P, c_double, c_int, _P, _P, c_size_t,
+                                _P]),
+    "neb_column_apply_workspace_bytes": (c_size_t, [c_int64, c_int]),
+    "neb_column_apply": (c_int, [c_int, c_int64, c_int, _P, _P, c_double, _P, _P, c_size_t, _P]),
+    "neb_peel_workspace_bytes": (c_size_t, [c_int]),
+    "neb_coefficient_peel": (c_int, [c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, c_size_t,
+                                     _P]),
 }
 
 EXPORTED = tuple(_SIGNATURES)

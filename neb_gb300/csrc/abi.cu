@@ -790,6 +790,31 @@ extern "C" int neb_check_status(const neb_net* net, int64_t n, void* ws, size_t 
   return NEB_OK;
 }
 
+extern "C" size_t neb_column_gram_workspace_bytes(int64_t rows, int K) {
+  if (rows <= 0 || K <= 0) return 0;
+  return a256((size_t)ceil_div(rows, chunk_points(rows)) * K * K * sizeof(double));
+}
+
+extern "C" int neb_column_gram(int precision, int64_t rows, int K, const void* A, double scale,
+                               int compensated, double* G, void* ws, size_t ws_bytes,
+                               neb_stream_t stream) {
+  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64,
+              "neb_column_gram: FP32 or FP64");
+  NEB_REQUIRE(rows > 0 && K > 0 && A && G, "neb_column_gram: bad arguments");
+  if (!ws || ws_bytes < neb_column_gram_workspace_bytes(rows, K)) {
+    set_error("neb_column_gram: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  simt::ChanSet one{1, {0}};
+  cudaStream_t s = (cudaStream_t)stream;
+  if (precision == NEB_PREC_FP64)
+    return launch_rowsum<double, 1, double>((const double*)A, K, (const double*)A, K, nullptr,
+                                            one, rows, K, K, true, scale, (double*)ws, G, s);
+  return launch_rowsum<float, 1, double>((const float*)A, K, (const float*)A, K, nullptr, one,
+                                         rows, K, K, true, scale, (double*)ws, G, s, 0,
+                                         compensated != 0);
+}
+
 extern "C" int neb_wait_selftest(int arrive, uint32_t spin_limit, int* status,
                                  neb_stream_t stream) {
   NEB_REQUIRE(status != nullptr, "neb_wait_selftest: null status");

@@ -1,0 +1,837 @@
+// Mode-stacked SIREN networks: the reference's own per-mode architecture.
+//
+// K independent networks, one per mode, with weights stacked [K][out][in]
+// and biases [K][out]: hidden layers y = sin(omega (W x + b)) (omega_first on
+// the first layer, omega_hidden after), a linear output layer, and the output
+// jet multiplied by an envelope jet (the reference's Model of
+// experiments/metaball/_backend/flow/cases/metaball/native_cupy_core.py:
+// 111-154 for first-order jets, velocity_trace_jet2.py:26-82 for second-order
+// jets).  Jets carry C = 1 + dim (+ dim (dim + 1) / 2 Hessian entries for
+// order 2) channels per point, laid out [n][C][width] per mode, modes
+// outermost: [B][n][C][width] for a block of B modes.  The input features
+// [n][C][F] are shared by every mode.
+//
+// Kernels (SIMT, FP32 or FP64 as the parameters):
+//   mode_gemm<EPI>   per-mode jet GEMM over all channels, tiles of 8 points
+//                    x 32 columns, the reduction staged through shared memory;
+//                    epilogues: output layer (+ bias, x envelope), hidden
+//                    layer (+ bias, x omega, sine jet, pre-activation kept),
+//                    reverse data (sine-jet transpose of the layer below).
+//   mode_wgrad       gW[k] = sum over points and channels of Abar (x) X,
+//                    split over point ranges, FP64-free deterministic sum.
+//   mode_bias        gb[k] = sum over points of the value-channel adjoint.
+//   mode_envelope_reverse, velocity_fields, velocity_lift (3D curl fields of
+//   a vector potential), and the per-mode Adam transaction.
+#include <algorithm>
+#include "neb_common.cuh"
+#include "elementwise.cuh"
+
+namespace neb {
+namespace {
+
+// Compact Hessian pairs: 2D (xx, xy, yy), 3D (xx, xy, xz, yy, yz, zz).
+__host__ __device__ constexpr int pair_i(int dim, int k) {
+  return dim == 2 ? (k < 2 ? 0 : 1) : (k < 3 ? 0 : (k < 5 ? 1 : 2));
+}
+__host__ __device__ constexpr int pair_j(int dim, int k) {
+  return dim == 2 ? (k == 0 ? 0 : 1) : (k < 3 ? k : (k == 3 ? 1 : 2));
+}
+
+template <int DIM, int ORD> struct Jet {
+  static constexpr int NH = ORD == 2 ? DIM * (DIM + 1) / 2 : 0;
+  static constexpr int C = 1 + DIM + NH;
+};
+
+// y = sin z, grad y = cos z grad z, H y = cos z H z - sin z grad z grad z^T
+template <int DIM, int ORD, typename T>
+__device__ __forceinline__ void sine_jet(const T* z, T* y) {
+  T s, c;
+  if constexpr (sizeof(T) == 8) sincos(z[0], &s, &c); else sincosf(z[0], &s, &c);
+  y[0] = s;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) y[1 + a] = c * z[1 + a];
+#pragma unroll
+  for (int k = 0; k < Jet<DIM, ORD>::NH; ++k)
+    y[1 + DIM + k] = c * z[1 + DIM + k] - s * z[1 + pair_i(DIM, k)] * z[1 + pair_j(DIM, k)];
+}
+
+// Transpose of sine_jet at z: adjoint a of y -> adjoint b of z.
+template <int DIM, int ORD, typename T>
+__device__ __forceinline__ void sine_jet_reverse(const T* z, const T* a, T* b) {
+  T s, c;
+  if constexpr (sizeof(T) == 8) sincos(z[0], &s, &c); else sincosf(z[0], &s, &c);
+  T zb = c * a[0];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    zb -= s * a[1 + d] * z[1 + d];
+    b[1 + d] = c * a[1 + d];
+  }
+#pragma unroll
+  for (int k = 0; k < Jet<DIM, ORD>::NH; ++k) {
+    const int i = pair_i(DIM, k), j = pair_j(DIM, k), q = 1 + DIM + k;
+    const T ah = a[q];
+    zb += ah * (-s * z[q] - c * z[1 + i] * z[1 + j]);
+    b[1 + i] -= s * ah * z[1 + j];
+    b[1 + j] -= s * ah * z[1 + i];
+    b[q] = c * ah;
+  }
+  b[0] = zb;
+}
+
+// Product of the envelope e with x (Leibniz rule on every channel).
+template <int DIM, int ORD, typename T>
+__device__ __forceinline__ void envelope_mul(const T* e, const T* x, T* y) {
+  y[0] = e[0] * x[0];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) y[1 + a] = e[0] * x[1 + a] + e[1 + a] * x[0];
+#pragma unroll
+  for (int k = 0; k < Jet<DIM, ORD>::NH; ++k) {
+    const int i = pair_i(DIM, k), j = pair_j(DIM, k), q = 1 + DIM + k;
+    y[q] = e[0] * x[q] + e[q] * x[0] + e[1 + i] * x[1 + j] + e[1 + j] * x[1 + i];
+  }
+}
+
+// Adjoint of x in envelope_mul: a (adjoint of y) -> b.
+template <int DIM, int ORD, typename T>
+__device__ __forceinline__ void envelope_mul_reverse(const T* e, const T* a, T* b) {
+  T xb = e[0] * a[0];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    xb += e[1 + d] * a[1 + d];
+    b[1 + d] = e[0] * a[1 + d];
+  }
+#pragma unroll
+  for (int k = 0; k < Jet<DIM, ORD>::NH; ++k) {
+    const int i = pair_i(DIM, k), j = pair_j(DIM, k), q = 1 + DIM + k;
+    xb += e[q] * a[q];
+    b[1 + i] += e[1 + j] * a[q];
+    b[1 + j] += e[1 + i] * a[q];
+    b[q] = e[0] * a[q];
+  }
+  b[0] = xb;
+}
+
+constexpr int kTilePts = 8;    // points per block (two per warp)
+constexpr int kTileCols = 32;  // output columns per block (one per lane)
+constexpr int kTileK = 32;     // reduction chunk staged in shared memory
+
+enum { EPI_OUTPUT = 0, EPI_HIDDEN = 1, EPI_REVERSE = 2 };
+
+// Per-mode jet GEMM.  blockIdx.x = tile of 8 points, blockIdx.y = tile of 32
+// columns, blockIdx.z = mode b of the block; every pointer is
+// already offset to the block's first mode and advanced by its *_mode stride.
+//   EPI_OUTPUT : out = env * (A W^T + b on the value channel), W [N][Kd]
+//   EPI_HIDDEN : pre = omega (A W^T + b), out = sine_jet(pre),   W [N][Kd]
+//   EPI_REVERSE: out = omega sine_jet^T(pre_in, A W),            W [Kd][N]
+// A: [n][C][Kd] (a_mode = 0 for the shared features); out, pre: [n][C][N].
+template <typename T, int DIM, int ORD, int EPI>
+__global__ void __launch_bounds__(128)
+mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int64_t w_mode,
+          const T* __restrict__ bias, int64_t b_mode, const T* __restrict__ env,
+          const T* __restrict__ pre_in, T* __restrict__ pre_out, T* __restrict__ out,
+          int64_t o_mode, int n, int Kd, int N, T omega) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  __shared__ T Bs[kTileK][kTileCols + 1];
+  __shared__ T As[kTilePts * C][kTileK];
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const int mb = blockIdx.z;
+  const int col0 = blockIdx.y * kTileCols, p0 = blockIdx.x * kTilePts;
+  A += mb * a_mode;
+  W += mb * w_mode;
+  T acc[2][C];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int c = 0; c < C; ++c) acc[q][c] = T(0);
+  for (int j0 = 0; j0 < Kd; j0 += kTileK) {
+    for (int e = tid; e < kTileK * kTileCols; e += 128) {
+      int jj, col;
+      if constexpr (EPI == EPI_REVERSE) {
+        jj = e / kTileCols;
+        col = e % kTileCols;
+      } else {
+        col = e / kTileK;
+        jj = e % kTileK;
+      }
+      const int j = j0 + jj, o = col0 + col;
+      T v = T(0);
+      if (j < Kd && o < N) v = EPI == EPI_REVERSE ? W[(int64_t)j * N + o] : W[(int64_t)o * Kd + j];
+      Bs[jj][col] = v;
+    }
+    for (int e = tid; e < kTilePts * C * kTileK; e += 128) {
+      const int jj = e % kTileK, rc = e / kTileK;
+      const int p = p0 + rc / C, c = rc % C, j = j0 + jj;
+      As[rc][jj] = (p < n && j < Kd) ? A[((int64_t)p * C + c) * Kd + j] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int jj = 0; jj < kTileK; ++jj) {
+      const T bv = Bs[jj][tx];
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[q][c] += As[(ty * 2 + q) * C + c][jj] * bv;
+    }
+    __syncthreads();
+  }
+  const int o = col0 + tx;
+  if (o >= N) return;
+  out += mb * o_mode;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int p = p0 + ty * 2 + q;
+    if (p >= n) continue;
+    T z[C], y[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) z[c] = acc[q][c];
+    const int64_t base = (int64_t)p * C * N + o;
+    if constexpr (EPI == EPI_OUTPUT) {
+      z[0] += bias[mb * b_mode + o];
+      if (env) {
+        T e[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) e[c] = env[(int64_t)p * C + c];
+        envelope_mul<DIM, ORD>(e, z, y);
+      } else {
+#pragma unroll
+        for (int c = 0; c < C; ++c) y[c] = z[c];
+      }
+    } else if constexpr (EPI == EPI_HIDDEN) {
+      z[0] += bias[mb * b_mode + o];
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        z[c] *= omega;
+        pre_out[mb * o_mode + base + (int64_t)c * N] = z[c];
+      }
+      sine_jet<DIM, ORD>(z, y);
+    } else {
+      T pz[C];
+#pragma unroll
+      for (int c = 0; c < C; ++c) pz[c] = pre_in[mb * o_mode + base + (int64_t)c * N];
+      sine_jet_reverse<DIM, ORD>(pz, z, y);
+#pragma unroll
+      for (int c = 0; c < C; ++c) y[c] *= omega;
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) out[base + (int64_t)c * N] = y[c];
+  }
+}
+
+// part[s][b][o][i] = sum over rows r in split s of Abar[b][r][o] X[b][r][i],
+// rows r = (point, channel).  grid = (tiles of 32 x 32, B, splits), 256
+// threads, 2 x 2 outputs each.
+template <typename T>
+__global__ void __launch_bounds__(256)
+mode_wgrad(const T* __restrict__ Abar, const T* __restrict__ X, int64_t x_mode, int64_t rows,
+           int N, int Kin, int64_t rows_per_split, T* __restrict__ part) {
+  __shared__ T As[16][33];
+  __shared__ T Xs[16][33];
+  const int tiles_i = (Kin + 31) / 32;
+  const int o0 = (blockIdx.x / tiles_i) * 32, i0 = (blockIdx.x % tiles_i) * 32;
+  const int mb = blockIdx.y, s = blockIdx.z;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  Abar += (int64_t)mb * rows * N;
+  X += mb * x_mode;
+  const int64_t r0 = (int64_t)s * rows_per_split;
+  const int64_t r1 = r0 + rows_per_split < rows ? r0 + rows_per_split : rows;
+  T acc[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
+  for (int64_t rb = r0; rb < r1; rb += 16) {
+    for (int e = tid; e < 512; e += 256) {
+      const int rr = e >> 5, cc = e & 31;
+      const int64_t r = rb + rr;
+      const bool ok = r < r1;
+      As[rr][cc] = (ok && o0 + cc < N) ? Abar[r * N + o0 + cc] : T(0);
+      Xs[rr][cc] = (ok && i0 + cc < Kin) ? X[r * Kin + i0 + cc] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int rr = 0; rr < 16; ++rr) {
+      const T a0 = As[rr][ty * 2], a1 = As[rr][ty * 2 + 1];
+      const T x0 = Xs[rr][tx * 2], x1 = Xs[rr][tx * 2 + 1];
+      acc[0][0] += a0 * x0;
+      acc[0][1] += a0 * x1;
+      acc[1][0] += a1 * x0;
+      acc[1][1] += a1 * x1;
+    }
+    __syncthreads();
+  }
+  T* dst = part + ((int64_t)s * gridDim.y + mb) * N * Kin;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int o = o0 + ty * 2 + a, i = i0 + tx * 2 + c;
+      if (o < N && i < Kin) dst[(int64_t)o * Kin + i] = acc[a][c];
+    }
+}
+
+// gW[b][o][i] (+)= sum_s part[s][b][o][i]
+template <typename T>
+__global__ void mode_wgrad_reduce(const T* __restrict__ part, int splits, int64_t per_split,
+                                  int accumulate, T* __restrict__ gW) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < per_split;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    T s = T(0);
+    for (int z = 0; z < splits; ++z) s += part[z * per_split + i];
+    gW[i] = accumulate ? gW[i] + s : s;
+  }
+}
+
+// gb[b][o] (+)= sum_p Abar[b][p][0][o]; one warp per (b, o), lanes over points.
+template <typename T, int C>
+__global__ void mode_bias(const T* __restrict__ Abar, int n, int N, int B, int accumulate,
+                          T* __restrict__ gb) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= B * N) return;
+  const int mb = w / N, o = w % N;
+  const T* a = Abar + (int64_t)mb * n * C * N + o;
+  T s = T(0);
+  for (int p = lane; p < n; p += 32) s += a[(int64_t)p * C * N];
+#pragma unroll
+  for (int sh = 16; sh > 0; sh >>= 1) s += __shfl_xor_sync(0xffffffffu, s, sh);
+  if (lane == 0) gb[w] = accumulate ? gb[w] + s : s;
+}
+
+// adjoint of the raw output: b = envelope_mul_reverse(env, a), [B][n][C][N]
+template <typename T, int DIM, int ORD>
+__global__ void mode_envelope_reverse(const T* __restrict__ env, const T* __restrict__ a,
+                                      int64_t total_pn, int n, int N, T* __restrict__ b) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total_pn;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = i / N;  // (mode, point)
+    const int o = (int)(i % N), p = (int)(row % n);
+    const int64_t base = row * C * N + o;
+    T e[C], av[C], bv[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      e[c] = env ? env[(int64_t)p * C + c] : (c == 0 ? T(1) : T(0));
+      av[c] = a[base + (int64_t)c * N];
+    }
+    envelope_mul_reverse<DIM, ORD>(e, av, bv);
+#pragma unroll
+    for (int c = 0; c < C; ++c) b[base + (int64_t)c * N] = bv[c];
+  }
+}
+
+// 3D second-order vector potential A (3 outputs per mode) -> velocity
+// u = curl A into U[(p*3 + a)][col] and its gradient d_j u_a into
+// D[(p*9 + a*3 + j)][col], col = mode0 + b (velocity_trace_jet2.py:93-101).
+template <typename T>
+__global__ void velocity_fields(const T* __restrict__ out, int B, int n, int K, int mode0,
+                                T* __restrict__ U, T* __restrict__ D) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)B * n) return;
+  const int mb = (int)(i / n), p = (int)(i % n);
+  const T* o = out + ((int64_t)mb * n + p) * 10 * 3;  // [10][3] of this point
+  auto g = [&](int comp, int axis) { return o[(1 + axis) * 3 + comp]; };
+  auto h = [&](int comp, int a, int b) { return o[(4 + hess_slot(a < b ? a : b, a < b ? b : a)) * 3 + comp]; };
+  const int col = mode0 + mb;
+  U[((int64_t)p * 3 + 0) * K + col] = g(2, 1) - g(1, 2);
+  U[((int64_t)p * 3 + 1) * K + col] = g(0, 2) - g(2, 0);
+  U[((int64_t)p * 3 + 2) * K + col] = g(1, 0) - g(0, 1);
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      D[((int64_t)p * 9 + a * 3 + j) * K + col] =
+          h((a + 2) % 3, j, (a + 1) % 3) - h((a + 1) % 3, j, (a + 2) % 3);
+}
+
+// Adjoint of velocity_fields: GU, GD (layouts of U, D) -> output adjoint
+// [B][n][10][3] (velocity/core.py:32-38 lift).
+template <typename T>
+__global__ void velocity_lift(const T* __restrict__ GU, const T* __restrict__ GD, int B, int n,
+                              int K, int mode0, T* __restrict__ adj) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)B * n) return;
+  const int mb = (int)(i / n), p = (int)(i % n), col = mode0 + mb;
+  T a[10][3];
+#pragma unroll
+  for (int c = 0; c < 10; ++c)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) a[c][k] = T(0);
+  const T u0 = GU[((int64_t)p * 3 + 0) * K + col], u1 = GU[((int64_t)p * 3 + 1) * K + col],
+          u2 = GU[((int64_t)p * 3 + 2) * K + col];
+  a[1 + 1][2] += u0; a[1 + 2][1] -= u0;
+  a[1 + 2][0] += u1; a[1 + 0][2] -= u1;
+  a[1 + 0][1] += u2; a[1 + 1][0] -= u2;
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const T gd = GD[((int64_t)p * 9 + ax * 3 + j) * K + col];
+      const int b1 = (ax + 1) % 3, b2 = (ax + 2) % 3;
+      a[4 + hess_slot(j < b1 ? j : b1, j < b1 ? b1 : j)][b2] += gd;
+      a[4 + hess_slot(j < b2 ? j : b2, j < b2 ? b2 : j)][b1] -= gd;
+    }
+  T* dst = adj + ((int64_t)mb * n + p) * 30;
+#pragma unroll
+  for (int c = 0; c < 10; ++c)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dst[c * 3 + k] = a[c][k];
+}
+
+// ------------------------------------------------------- per-mode Adam
+// Tensors are stacked [K][...]; per_mode[t] elements of tensor t per mode.
+struct ModeAdamTable {
+  AdamTable t;
+  int64_t per_mode[kMaxAdamTensors];
+};
+
+// norm2[k] = sum over tensors of |g_k|^2 (one block per mode), bad |= non-finite
+template <typename T>
+__global__ void mode_adam_norms(ModeAdamTable mt, double* __restrict__ norm2, int* __restrict__ bad) {
+  __shared__ double red[32];
+  const int k = blockIdx.x;
+  double s = 0.0;
+  int nf = 0;
+  for (int ti = 0; ti < mt.t.n; ++ti) {
+    const T* g = static_cast<const T*>(mt.t.g[ti]) + (int64_t)k * mt.per_mode[ti];
+    for (int64_t i = threadIdx.x; i < mt.per_mode[ti]; i += blockDim.x) {
+      const double v = (double)g[i];
+      if (!isfinite(v)) nf = 1;
+      s += v * v;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  nf = __any_sync(0xffffffffu, nf);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  if (nf && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) norm2[k] = v;
+  }
+}
+
+// Commit decision (every mode's norm finite and positive, native_cupy_core.py:
+// 157-158), norms out, per-mode clip scales, bias corrections of step
+// *steps + 1, and the step counter advanced on commit.
+__global__ void mode_adam_finalize(const double* __restrict__ norm2, const int* __restrict__ bad,
+                                   int K, double clip, double lr, int* __restrict__ steps,
+                                   double* __restrict__ norms_out, int* __restrict__ committed,
+                                   double* __restrict__ scal, double* __restrict__ scales) {
+  __shared__ int ok_all;
+  if (threadIdx.x == 0) ok_all = bad[0] == 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    const double nm = sqrt(norm2[k]);
+    if (norms_out) norms_out[k] = nm;
+    if (!(isfinite(nm) && nm > 0.0)) atomicAnd(&ok_all, 0);
+    scales[k] = fmin(1.0, clip / fmax(nm, 1e-30));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double t = (double)(*steps) + 1.0;
+    scal[0] = ok_all ? 1.0 : 0.0;
+    scal[1] = lr / (1.0 - pow(0.9, t));
+    scal[2] = 1.0 / (1.0 - pow(0.999, t));
+    if (committed) *committed = ok_all;
+    if (ok_all) *steps += 1;
+  }
+}
+
+template <typename T>
+__global__ void mode_adam_update(ModeAdamTable mt, const double* __restrict__ scal,
+                                 const double* __restrict__ scales) {
+  if (scal[0] == 0.0) return;
+  const T lr_c1 = (T)scal[1], inv_c2 = (T)scal[2];
+  const int64_t total = mt.t.off[mt.t.n];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int ti = adam_find(mt.t, i);
+    const int64_t j = i - mt.t.off[ti];
+    const int k = (int)(j / mt.per_mode[ti]);
+    T* p = static_cast<T*>(mt.t.p[ti]);
+    T* m = static_cast<T*>(mt.t.m[ti]);
+    T* v = static_cast<T*>(mt.t.v[ti]);
+    const T g = static_cast<const T*>(mt.t.g[ti])[j] * (T)scales[k];
+    const T mn = T(0.9) * m[j] + T(0.1) * g;
+    const T vn = T(0.999) * v[j] + T(0.001) * g * g;
+    m[j] = mn;
+    v[j] = vn;
+    p[j] -= lr_c1 * mn / (sqrt(vn * inv_c2) + T(1e-8));
+  }
+}
+
+// ------------------------------------------------------------- host side
+size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int mode_channels(const neb_modes* m) {
+  return 1 + m->dim + (m->order == 2 ? m->dim * (m->dim + 1) / 2 : 0);
+}
+
+int check_modes(const neb_modes* m) {
+  NEB_REQUIRE(m != nullptr, "null neb_modes");
+  NEB_REQUIRE(m->dim == 2 || m->dim == 3, "neb_modes.dim must be 2 or 3");
+  NEB_REQUIRE(m->order == 1 || m->order == 2, "neb_modes.order must be 1 or 2");
+  NEB_REQUIRE(m->n_layers >= 1 && m->n_layers <= NEB_MAX_HIDDEN + 1,
+              "neb_modes.n_layers must be in [1, %d]", NEB_MAX_HIDDEN + 1);
+  for (int l = 0; l <= m->n_layers; ++l)
+    NEB_REQUIRE(m->widths[l] > 0 && m->widths[l] <= 65536, "neb_modes.widths[%d] invalid", l);
+  NEB_REQUIRE(m->precision == NEB_PREC_FP32 || m->precision == NEB_PREC_FP64,
+              "neb_modes: FP32 or FP64 parameters");
+  NEB_REQUIRE(m->n_modes > 0, "neb_modes.n_modes must be positive");
+  return NEB_OK;
+}
+
+size_t esize(const neb_modes* m) { return m->precision == NEB_PREC_FP64 ? 8 : 4; }
+
+// Tape of a block of B modes: for hidden layer j (0..n_layers-2) the scaled
+// pre-activation P_j and the output X_{j+1}, each [B][n][C][w_{j+1}].
+struct ModeTape {
+  size_t pre[NEB_MAX_HIDDEN + 1], x[NEB_MAX_HIDDEN + 2], total;
+};
+
+ModeTape mode_tape(const neb_modes* m, int B, int64_t n) {
+  ModeTape t{};
+  const size_t C = mode_channels(m), es = esize(m);
+  size_t off = 0;
+  for (int j = 0; j + 1 < m->n_layers; ++j) {
+    const size_t sz = a256((size_t)B * n * C * m->widths[j + 1] * es);
+    t.pre[j] = off;
+    off += sz;
+    t.x[j + 1] = off;
+    off += sz;
+  }
+  t.total = off;
+  return t;
+}
+
+int max_width(const neb_modes* m) {
+  int w = 0;
+  for (int l = 0; l <= m->n_layers; ++l) w = std::max(w, m->widths[l]);
+  return w;
+}
+
+constexpr int kMaxWgradSplits = 32;
+
+// Workspace of the reverse pass: two adjoint buffers [B][n][C][max w] and
+// the weight-gradient split partials.
+struct ModeWs {
+  size_t a0, a1, part, total;
+};
+
+ModeWs mode_ws(const neb_modes* m, int B, int64_t n) {
+  ModeWs w{};
+  const size_t C = mode_channels(m), es = esize(m), mw = max_width(m);
+  const size_t adj = a256((size_t)B * n * C * mw * es);
+  w.a0 = 0;
+  w.a1 = adj;
+  w.part = 2 * adj;
+  w.total = w.part + a256((size_t)kMaxWgradSplits * B * mw * mw * es);
+  return w;
+}
+
+template <typename T, int DIM, int ORD, int EPI>
+int launch_mode_gemm(const T* A, int64_t a_mode, const T* W, int64_t w_mode, const T* bias,
+                     int64_t b_mode, const T* env, const T* pre_in, T* pre_out, T* out,
+                     int64_t o_mode, int B, int n, int Kd, int N, double omega, cudaStream_t s,
+                     const char* name) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  NEB_REQUIRE(ceil_div(N, kTileCols) <= 65535, "mode GEMM: width %d too large", N);
+  dim3 grid((unsigned)ceil_div(n, kTilePts), (unsigned)ceil_div(N, kTileCols), (unsigned)B);
+  KernelScope ks(name, s, 2.0 * B * n * C * (double)Kd * N,
+                 (double)B * n * C * (Kd + N * (EPI == EPI_OUTPUT ? 1 : 2)) * sizeof(T));
+  mode_gemm<T, DIM, ORD, EPI><<<grid, 128, 0, s>>>(A, a_mode, W, w_mode, bias, b_mode, env, pre_in,
+                                                   pre_out, out, o_mode, n, Kd, N, (T)omega);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+template <typename T, int DIM, int ORD>
+int modes_forward_t(const neb_modes* m, int start, int B, const void* const* Wv,
+                    const void* const* bv, const T* feats, const T* env, int64_t n, char* tape,
+                    T* out, cudaStream_t s) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  ModeTape tl = mode_tape(m, B, n);
+  const T* x = feats;
+  int64_t x_mode = 0;
+  for (int j = 0; j < m->n_layers; ++j) {
+    const int in = m->widths[j], o = m->widths[j + 1];
+    const T* W = (const T*)Wv[j] + (int64_t)start * o * in;
+    const T* b = (const T*)bv[j] + (int64_t)start * o;
+    const int64_t o_mode = (int64_t)n * C * o;
+    int st;
+    if (j + 1 < m->n_layers) {
+      T* pre = (T*)(tape + tl.pre[j]);
+      T* y = (T*)(tape + tl.x[j + 1]);
+      const double om = j == 0 ? m->omega_first : m->omega_hidden;
+      st = launch_mode_gemm<T, DIM, ORD, EPI_HIDDEN>(x, x_mode, W, (int64_t)o * in, b, o, nullptr,
+                                                     nullptr, pre, y, o_mode, B, (int)n, in, o, om,
+                                                     s, "mode_layer_fwd");
+      x = y;
+      x_mode = o_mode;
+    } else {
+      st = launch_mode_gemm<T, DIM, ORD, EPI_OUTPUT>(x, x_mode, W, (int64_t)o * in, b, o, env,
+                                                     nullptr, nullptr, out, o_mode, B, (int)n, in,
+                                                     o, 1.0, s, "mode_output_fwd");
+    }
+    if (st) return st;
+  }
+  return NEB_OK;
+}
+
+template <typename T, int DIM, int ORD>
+int modes_backward_t(const neb_modes* m, int start, int B, const void* const* Wv, const T* feats,
+                     const T* env, int64_t n, const char* tape, const T* adjoint,
+                     void* const* gW, void* const* gb, int accumulate, char* ws, cudaStream_t s) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  ModeTape tl = mode_tape(m, B, n);
+  ModeWs wl = mode_ws(m, B, n);
+  T* buf[2] = {(T*)(ws + wl.a0), (T*)(ws + wl.a1)};
+  T* part = (T*)(ws + wl.part);
+  const int L = m->n_layers;
+  int dev = 0, sms = 0;
+  if (int st = device_sms(&dev, &sms)) return st;
+  {  // adjoint of the raw output
+    const int No = m->widths[L];
+    const int64_t total = (int64_t)B * n * No;
+    KernelScope ks("mode_envelope_reverse", s, 0, 2.0 * total * C * sizeof(T));
+    mode_envelope_reverse<T, DIM, ORD><<<(int)std::min<int64_t>(ceil_div(total, 256), 8192), 256, 0,
+                                         s>>>(env, adjoint, total, (int)n, No, buf[0]);
+    NEB_LAUNCH_CHECK();
+  }
+  int cur = 0;
+  for (int j = L - 1; j >= 0; --j) {
+    const int in = m->widths[j], o = m->widths[j + 1];
+    const T* X = j == 0 ? feats : (const T*)(tape + tl.x[j]);
+    const int64_t x_mode = j == 0 ? 0 : (int64_t)n * C * in;
+    const int64_t rows = n * C;
+    // weight gradient, split over row ranges so that B x tiles x splits
+    // covers the SMs about twice
+    const int tiles = (int)(ceil_div(o, 32) * ceil_div(in, 32));
+    int splits = (int)std::max<int64_t>(1, std::min<int64_t>(kMaxWgradSplits,
+                                                             ceil_div(2 * sms, (int64_t)tiles * B)));
+    splits = (int)std::min<int64_t>(splits, ceil_div(rows, 16));
+    const int64_t per = ceil_div(ceil_div(rows, splits), 16) * 16;
+    splits = (int)ceil_div(rows, per);
+    {
+      KernelScope ks("mode_weight_grad", s, 2.0 * B * rows * (double)o * in,
+                     (double)B * rows * (o + in) * sizeof(T));
+      mode_wgrad<T><<<dim3(tiles, B, splits), 256, 0, s>>>(buf[cur], X, x_mode, rows, o, in, per,
+                                                           part);
+      NEB_LAUNCH_CHECK();
+    }
+    {
+      const int64_t per_split = (int64_t)B * o * in;
+      KernelScope ks("mode_weight_grad_reduce", s, 0, (double)splits * per_split * sizeof(T));
+      mode_wgrad_reduce<T><<<(int)std::min<int64_t>(ceil_div(per_split, 256), 4096), 256, 0, s>>>(
+          part, splits, per_split, accumulate, (T*)gW[j]);
+      NEB_LAUNCH_CHECK();
+    }
+    {
+      KernelScope ks("mode_bias_grad", s, 0, (double)B * n * o * sizeof(T));
+      mode_bias<T, C><<<(int)ceil_div((int64_t)B * o * 32, 256), 256, 0, s>>>(
+          buf[cur], (int)n, o, B, accumulate, (T*)gb[j]);
+      NEB_LAUNCH_CHECK();
+    }
+    if (j == 0) break;
+    // data gradient through W_j and the sine-jet transpose of layer j - 1
+    const T* W = (const T*)Wv[j] + (int64_t)start * o * in;
+    const T* pre = (const T*)(tape + tl.pre[j - 1]);
+    const double om = j - 1 == 0 ? m->omega_first : m->omega_hidden;
+    int st = launch_mode_gemm<T, DIM, ORD, EPI_REVERSE>(
+        buf[cur], (int64_t)n * C * o, W, (int64_t)o * in, nullptr, 0, nullptr, pre, nullptr,
+        buf[cur ^ 1], (int64_t)n * C * in, B, (int)n, o, in, om, s, "mode_layer_bwd_data");
+    if (st) return st;
+    cur ^= 1;
+  }
+  return NEB_OK;
+}
+
+#define NEB_MODES_DISPATCH(m, FN, ...)                                                  \
+  ((m)->precision == NEB_PREC_FP64                                                     \
+       ? ((m)->dim == 2 ? ((m)->order == 1 ? FN<double, 2, 1>(__VA_ARGS__)             \
+                                           : FN<double, 2, 2>(__VA_ARGS__))            \
+                        : ((m)->order == 1 ? FN<double, 3, 1>(__VA_ARGS__)             \
+                                           : FN<double, 3, 2>(__VA_ARGS__)))           \
+       : ((m)->dim == 2 ? ((m)->order == 1 ? FN<float, 2, 1>(__VA_ARGS__)              \
+                                           : FN<float, 2, 2>(__VA_ARGS__))             \
+                        : ((m)->order == 1 ? FN<float, 3, 1>(__VA_ARGS__)              \
+                                           : FN<float, 3, 2>(__VA_ARGS__))))
+
+template <typename T, int DIM, int ORD>
+int modes_forward_d(const neb_modes* m, int start, int B, const void* const* W,
+                    const void* const* b, const void* feats, const void* env, int64_t n,
+                    void* tape, void* out, cudaStream_t s) {
+  return modes_forward_t<T, DIM, ORD>(m, start, B, W, b, (const T*)feats, (const T*)env, n,
+                                      (char*)tape, (T*)out, s);
+}
+
+template <typename T, int DIM, int ORD>
+int modes_backward_d(const neb_modes* m, int start, int B, const void* const* W, const void* feats,
+                     const void* env, int64_t n, const void* tape, const void* adjoint,
+                     void* const* gW, void* const* gb, int accumulate, void* ws, cudaStream_t s) {
+  return modes_backward_t<T, DIM, ORD>(m, start, B, W, (const T*)feats, (const T*)env, n,
+                                       (const char*)tape, (const T*)adjoint, gW, gb, accumulate,
+                                       (char*)ws, s);
+}
+
+}  // namespace
+}  // namespace neb
+
+using namespace neb;
+
+extern "C" size_t neb_modes_tape_bytes(const neb_modes* m, int n_block, int64_t n_points) {
+  if (check_modes(m) || n_block <= 0 || n_points <= 0) return 0;
+  return mode_tape(m, n_block, n_points).total;
+}
+
+extern "C" size_t neb_modes_workspace_bytes(const neb_modes* m, int n_block, int64_t n_points) {
+  if (check_modes(m) || n_block <= 0 || n_points <= 0) return 0;
+  return mode_ws(m, n_block, n_points).total;
+}
+
+extern "C" int neb_modes_forward(const neb_modes* m, int start, int stop, const void* const* W,
+                                 const void* const* b, const void* features,
+                                 const void* envelope, int64_t n_points, void* tape,
+                                 size_t tape_bytes, void* out, neb_stream_t stream) {
+  int st = check_modes(m);
+  if (st) return st;
+  NEB_REQUIRE(0 <= start && start < stop && stop <= m->n_modes,
+              "neb_modes_forward: modes [%d, %d) outside [0, %d)", start, stop, m->n_modes);
+  NEB_REQUIRE(n_points > 0 && n_points <= (1 << 30) && W && b && features && out,
+              "neb_modes_forward: bad arguments");
+  for (int j = 0; j < m->n_layers; ++j)
+    NEB_REQUIRE(W[j] && b[j], "neb_modes_forward: null parameters of layer %d", j);
+  const int B = stop - start;
+  NEB_REQUIRE(B <= 65535, "neb_modes_forward: at most 65535 modes per call");
+  if (mode_tape(m, B, n_points).total > 0 && (!tape || tape_bytes < mode_tape(m, B, n_points).total)) {
+    set_error("neb_modes_forward: tape smaller than neb_modes_tape_bytes");
+    return NEB_ERR_WORKSPACE;
+  }
+  return NEB_MODES_DISPATCH(m, modes_forward_d, m, start, B, W, b, features, envelope, n_points,
+                            tape, out, (cudaStream_t)stream);
+}
+
+extern "C" int neb_modes_backward(const neb_modes* m, int start, int stop, const void* const* W,
+                                  const void* features, const void* envelope, int64_t n_points,
+                                  const void* tape, const void* adjoint, void* const* gW,
+                                  void* const* gb, int accumulate, void* workspace,
+                                  size_t workspace_bytes, neb_stream_t stream) {
+  int st = check_modes(m);
+  if (st) return st;
+  NEB_REQUIRE(0 <= start && start < stop && stop <= m->n_modes,
+              "neb_modes_backward: modes [%d, %d) outside [0, %d)", start, stop, m->n_modes);
+  NEB_REQUIRE(n_points > 0 && n_points <= (1 << 30) && W && features && adjoint && gW && gb,
+              "neb_modes_backward: bad arguments");
+  NEB_REQUIRE(m->n_layers == 1 || tape, "neb_modes_backward: null tape");
+  for (int j = 0; j < m->n_layers; ++j)
+    NEB_REQUIRE(W[j] && gW[j] && gb[j], "neb_modes_backward: null pointer at layer %d", j);
+  const int B = stop - start;
+  NEB_REQUIRE(B <= 65535, "neb_modes_backward: at most 65535 modes per call");
+  if (!workspace || workspace_bytes < mode_ws(m, B, n_points).total) {
+    set_error("neb_modes_backward: workspace smaller than neb_modes_workspace_bytes");
+    return NEB_ERR_WORKSPACE;
+  }
+  return NEB_MODES_DISPATCH(m, modes_backward_d, m, start, B, W, features, envelope, n_points,
+                            tape, adjoint, gW, gb, accumulate, workspace, (cudaStream_t)stream);
+}
+
+extern "C" int neb_velocity_fields(int precision, const void* out, int start, int stop,
+                                   int64_t n_points, int n_modes, void* U, void* D,
+                                   neb_stream_t stream) {
+  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64,
+              "neb_velocity_fields: FP32 or FP64");
+  NEB_REQUIRE(out && U && D && n_points > 0 && 0 <= start && start < stop && stop <= n_modes,
+              "neb_velocity_fields: bad arguments");
+  const int B = stop - start;
+  const int64_t total = (int64_t)B * n_points;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t es = precision == NEB_PREC_FP64 ? 8 : 4;
+  KernelScope ks("velocity_fields", s, 0, (double)total * (30 + 12) * es);
+  if (precision == NEB_PREC_FP64)
+    velocity_fields<double><<<(int)ceil_div(total, 256), 256, 0, s>>>(
+        (const double*)out, B, (int)n_points, n_modes, start, (double*)U, (double*)D);
+  else
+    velocity_fields<float><<<(int)ceil_div(total, 256), 256, 0, s>>>(
+        (const float*)out, B, (int)n_points, n_modes, start, (float*)U, (float*)D);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+extern "C" int neb_velocity_lift(int precision, const void* GU, const void* GD, int start,
+                                 int stop, int64_t n_points, int n_modes, void* adjoint,
+                                 neb_stream_t stream) {
+  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64,
+              "neb_velocity_lift: FP32 or FP64");
+  NEB_REQUIRE(GU && GD && adjoint && n_points > 0 && 0 <= start && start < stop &&
+                  stop <= n_modes,
+              "neb_velocity_lift: bad arguments");
+  const int B = stop - start;
+  const int64_t total = (int64_t)B * n_points;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t es = precision == NEB_PREC_FP64 ? 8 : 4;
+  KernelScope ks("velocity_lift", s, 0, (double)total * (30 + 12) * es);
+  if (precision == NEB_PREC_FP64)
+    velocity_lift<double><<<(int)ceil_div(total, 256), 256, 0, s>>>(
+        (const double*)GU, (const double*)GD, B, (int)n_points, n_modes, start, (double*)adjoint);
+  else
+    velocity_lift<float><<<(int)ceil_div(total, 256), 256, 0, s>>>(
+        (const float*)GU, (const float*)GD, B, (int)n_points, n_modes, start, (float*)adjoint);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+extern "C" size_t neb_modes_adam_workspace_bytes(int n_modes) {
+  return n_modes <= 0 ? 0 : 512 + 2 * a256((size_t)n_modes * sizeof(double));
+}
+
+extern "C" int neb_modes_adam(int dtype, int n_modes, int n_tensors, void* const* params,
+                              void* const* exp_avg, void* const* exp_avg_sq,
+                              const void* const* grads, const int64_t* sizes, int* step_counter,
+                              double lr, double clip, double* norms_out, int* committed_out,
+                              void* workspace, size_t workspace_bytes, neb_stream_t stream) {
+  NEB_REQUIRE(dtype == 0 || dtype == 1, "neb_modes_adam: dtype must be 0 (float) or 1 (double)");
+  NEB_REQUIRE(n_modes > 0 && n_tensors > 0 && n_tensors <= kMaxAdamTensors,
+              "neb_modes_adam: 1..%d tensors of at least one mode", kMaxAdamTensors);
+  NEB_REQUIRE(params && exp_avg && exp_avg_sq && grads && sizes && step_counter,
+              "neb_modes_adam: bad arguments");
+  if (!workspace || workspace_bytes < neb_modes_adam_workspace_bytes(n_modes)) {
+    set_error("neb_modes_adam: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  ModeAdamTable mt{};
+  mt.t.n = n_tensors;
+  mt.t.off[0] = 0;
+  for (int i = 0; i < n_tensors; ++i) {
+    NEB_REQUIRE(params[i] && exp_avg[i] && exp_avg_sq[i] && grads[i] && sizes[i] > 0 &&
+                    sizes[i] % n_modes == 0,
+                "neb_modes_adam: tensor %d must hold a whole number of modes", i);
+    mt.t.p[i] = params[i];
+    mt.t.m[i] = exp_avg[i];
+    mt.t.v[i] = exp_avg_sq[i];
+    mt.t.g[i] = grads[i];
+    mt.t.off[i + 1] = mt.t.off[i] + sizes[i];
+    mt.per_mode[i] = sizes[i] / n_modes;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  char* ws = (char*)workspace;
+  int* bad = (int*)ws;
+  double* scal = (double*)(ws + 256);
+  double* norm2 = (double*)(ws + 512);
+  double* scales = (double*)(ws + 512 + a256((size_t)n_modes * sizeof(double)));
+  NEB_CUDA_CHECK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  const int64_t total = mt.t.off[n_tensors];
+  const double es = dtype == 0 ? 4.0 : 8.0;
+  {
+    KernelScope ks("mode_adam_norms", s, 0, total * es);
+    if (dtype == 0) mode_adam_norms<float><<<n_modes, 256, 0, s>>>(mt, norm2, bad);
+    else mode_adam_norms<double><<<n_modes, 256, 0, s>>>(mt, norm2, bad);
+    NEB_LAUNCH_CHECK();
+  }
+  {
+    KernelScope ks("mode_adam_update", s, 0, total * es * 7, 2);
+    mode_adam_finalize<<<1, 256, 0, s>>>(norm2, bad, n_modes, clip, lr, step_counter, norms_out,
+                                         committed_out, scal, scales);
+    NEB_LAUNCH_CHECK();
+    const int blocks = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(total, 256), 1), 2048);
+    if (dtype == 0) mode_adam_update<float><<<blocks, 256, 0, s>>>(mt, scal, scales);
+    else mode_adam_update<double><<<blocks, 256, 0, s>>>(mt, scal, scales);
+    NEB_LAUNCH_CHECK();
+  }
+  return NEB_OK;
+}

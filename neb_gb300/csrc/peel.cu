@@ -1,0 +1,381 @@
+// Causal Rayleigh peel in Gram form, FP64 on the device, and the FP64
+// products of field columns with K x K coefficient matrices.
+//
+// The peel (experiments/metaball/_backend/flow/cases/metaball/velocity/
+// core.py:48-69 coefficient_peel): modes sorted by their raw quotients
+// S_kk / M_kk (stable), the sorted mass matrix orthonormalised by a scaled
+// Cholesky factor applied twice (the Gram form of two-pass modified
+// Gram-Schmidt in the mass metric), losses = diag(T^T S T), and the
+// coefficient adjoints Cu, Cd with dL/dU = U Cu / n, dL/dD = D Cd / n for
+// L = sum(losses).  The order is a rank computation on the device (no host
+// round trip); the factorisations are cuSOLVER potrf and cuBLAS trsm / gemm.
+// Matrices are symmetric at the boundary (row- and column-major coincide);
+// T and the adjoints are returned row-major.
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+#include <algorithm>
+#include "neb_common.cuh"
+
+namespace neb {
+namespace {
+
+struct PeelHandles {
+  cusolverDnHandle_t solver = nullptr;
+  cublasHandle_t blas = nullptr;
+  ~PeelHandles() {
+    if (solver) cusolverDnDestroy(solver);
+    if (blas) cublasDestroy(blas);
+  }
+};
+thread_local PeelHandles g_peel;
+
+int peel_handles(cudaStream_t s) {
+  if (!g_peel.solver && cusolverDnCreate(&g_peel.solver) != CUSOLVER_STATUS_SUCCESS) {
+    set_error("cusolverDnCreate failed");
+    return NEB_ERR_CUDA;
+  }
+  if (!g_peel.blas && cublasCreate(&g_peel.blas) != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasCreate failed");
+    return NEB_ERR_CUDA;
+  }
+  cusolverDnSetStream(g_peel.solver, s);
+  cublasSetStream(g_peel.blas, s);
+  cublasSetPointerMode(g_peel.blas, CUBLAS_POINTER_MODE_HOST);
+  return NEB_OK;
+}
+
+size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+#define NEB_BLAS(expr, what)                                                   \
+  do {                                                                         \
+    if ((expr) != CUBLAS_STATUS_SUCCESS) {                                     \
+      set_error("%s failed", what);                                            \
+      return NEB_ERR_CUDA;                                                     \
+    }                                                                          \
+  } while (0)
+
+// raw_i = S_ii / M_ii (a non-finite quotient sorts last); stable ascending
+// ranks; order[rank] = i.
+__global__ void peel_order(const double* __restrict__ M, const double* __restrict__ S, int K,
+                           int* __restrict__ order, double* __restrict__ raw) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
+    double r = S[(size_t)i * K + i] / M[(size_t)i * K + i];
+    raw[i] = r;
+  }
+}
+__global__ void peel_rank(const double* __restrict__ raw, int K, int* __restrict__ order) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
+    const double ri = raw[i];
+    const bool fi = isfinite(ri);
+    int rank = 0;
+    for (int j = 0; j < K; ++j) {
+      const double rj = raw[j];
+      const bool fj = isfinite(rj);
+      const bool before = fi ? (fj && (rj < ri || (rj == ri && j < i))) : (fj || j < i);
+      rank += before;
+    }
+    order[rank] = i;
+  }
+}
+
+// ms = M[order][order], ss = S[order][order], scale = sqrt(diag ms),
+// H = ms / (scale_i scale_j) (column-major, symmetric).
+__global__ void peel_gather(const double* __restrict__ M, const double* __restrict__ S,
+                            const int* __restrict__ order, int K, double* __restrict__ ms,
+                            double* __restrict__ ss, double* __restrict__ H,
+                            double* __restrict__ scale) {
+  const int64_t total = (int64_t)K * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % K), j = (int)(e / K);
+    const int oi = order[i], oj = order[j];
+    const double m = M[(size_t)oi * K + oj];
+    ms[e] = m;
+    ss[e] = S[(size_t)oi * K + oj];
+    const double si = sqrt(M[(size_t)oi * K + oi]), sj = sqrt(M[(size_t)oj * K + oj]);
+    H[e] = m / si / sj;
+    if (i == j) scale[i] = si;
+  }
+}
+
+// T (column-major) rows divided by scale; also the identity for the next solve.
+__global__ void scale_rows(double* __restrict__ T, const double* __restrict__ scale, int K) {
+  const int64_t total = (int64_t)K * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    T[e] /= scale[e % K];
+}
+
+__global__ void set_identity(double* __restrict__ X, int K) {
+  const int64_t total = (int64_t)K * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    X[e] = (e % K) == (e / K) ? 1.0 : 0.0;
+}
+
+__global__ void symmetrize(double* __restrict__ X, int K) {
+  const int64_t total = (int64_t)K * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % K), j = (int)(e / K);
+    if (i < j) {
+      const double v = 0.5 * (X[e] + X[(int64_t)i * K + j]);
+      X[e] = v;
+      X[(int64_t)i * K + j] = v;
+    }
+  }
+}
+
+// Gate of core.py:60-62 and the per-rank scalars: losses = diag F,
+// norm = 1 / diag T, relative = norm^2 / diag ms, error = max |O - I|;
+// Fu = strict upper triangle of F (in place).  info: 0 ok, 2 gate failed.
+__global__ void peel_gate(const double* __restrict__ T, const double* __restrict__ ms,
+                          const double* __restrict__ O, double* __restrict__ F, int K,
+                          double* __restrict__ loss, double* __restrict__ norm,
+                          double* __restrict__ relative, double* __restrict__ error,
+                          int* __restrict__ info) {
+  __shared__ double emax[32];
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  double e = 0.0;
+  for (int64_t x = threadIdx.x; x < (int64_t)K * K; x += blockDim.x) {
+    const int i = (int)(x % K), j = (int)(x / K);
+    e = fmax(e, fabs(O[x] - (i == j ? 1.0 : 0.0)));
+  }
+  for (int i = threadIdx.x; i < K; i += blockDim.x) {
+    const double l = F[(int64_t)i * K + i];
+    const double nm = 1.0 / T[(int64_t)i * K + i];
+    const double rel = nm * nm / ms[(int64_t)i * K + i];
+    loss[i] = l;
+    norm[i] = nm;
+    relative[i] = rel;
+    if (!(isfinite(l) && l > 0.0 && rel >= 1e-4)) atomicOr(&bad, 1);
+  }
+  for (int o = 16; o > 0; o >>= 1) e = fmax(e, __shfl_down_sync(0xffffffffu, e, o));
+  if ((threadIdx.x & 31) == 0) emax[threadIdx.x >> 5] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, emax[w]);
+    *error = m;
+    if ((!(m <= 1e-5) || bad) && *info == 0) *info = 2;
+  }
+  __syncthreads();
+  // strict upper triangle of F for C = T diag(loss) + T triu(F, 1)
+  for (int64_t x = threadIdx.x; x < (int64_t)K * K; x += blockDim.x) {
+    const int i = (int)(x % K), j = (int)(x / K);
+    if (i >= j) F[x] = 0.0;
+  }
+}
+
+// C = -2 (T diag(loss) + TF) / norm_j, B = 2 T / norm_j (sorted order,
+// column-major), scattered to mode order: Cu[order_i][order_j] = C_ij,
+// Cd[order_i][order_j] = B_ij, T_out[order_i][j] = T_ij (row-major).
+__global__ void peel_adjoints(const double* __restrict__ T, const double* __restrict__ TF,
+                              const double* __restrict__ loss, const double* __restrict__ norm,
+                              const int* __restrict__ order, int K, double* __restrict__ Cu,
+                              double* __restrict__ Cd, double* __restrict__ T_out) {
+  const int64_t total = (int64_t)K * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % K), j = (int)(e / K);
+    const double t = T[e];
+    const double c = -2.0 * (t * loss[j] + TF[e]) / norm[j];
+    const double b = 2.0 * t / norm[j];
+    const int oi = order[i], oj = order[j];
+    Cu[(size_t)oi * K + oj] = c;
+    Cd[(size_t)oi * K + oj] = b;
+    T_out[(size_t)oi * K + j] = t;
+  }
+}
+
+__global__ void potrf_gate(const int* __restrict__ dev_info, int* __restrict__ info) {
+  if (*dev_info != 0 && *info == 0) *info = 1;
+}
+
+template <typename S, typename D>
+__global__ void convert(const S* __restrict__ src, D* __restrict__ dst, int64_t n, double scale) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (D)((double)src[i] * scale);
+}
+
+int grid_for(int64_t n) { return (int)std::min<int64_t>(std::max<int64_t>(ceil_div(n, 256), 1), 4096); }
+
+}  // namespace
+}  // namespace neb
+
+using namespace neb;
+
+extern "C" size_t neb_peel_workspace_bytes(int K) {
+  if (K <= 0 || peel_handles(nullptr)) return 0;
+  int lwork = 0;
+  if (cusolverDnDpotrf_bufferSize(g_peel.solver, CUBLAS_FILL_MODE_LOWER, K, nullptr, K, &lwork) !=
+      CUSOLVER_STATUS_SUCCESS)
+    return 0;
+  const size_t kk = a256((size_t)K * K * sizeof(double)), k1 = a256((size_t)K * sizeof(double));
+  return 8 * kk + 5 * k1 + a256(sizeof(int) * 2) + a256((size_t)lwork * sizeof(double));
+}
+
+extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, double* losses,
+                                    int* order, double* T_out, double* Cu, double* Cd,
+                                    double* relative_mass, double* ortho_error, int* info,
+                                    void* workspace, size_t workspace_bytes,
+                                    neb_stream_t stream) {
+  NEB_REQUIRE(K > 0 && M && S && losses && order && T_out && Cu && Cd && info,
+              "neb_coefficient_peel: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  int st = peel_handles(s);
+  if (st) return st;
+  int lwork = 0;
+  if (cusolverDnDpotrf_bufferSize(g_peel.solver, CUBLAS_FILL_MODE_LOWER, K, nullptr, K, &lwork) !=
+      CUSOLVER_STATUS_SUCCESS) {
+    set_error("cusolverDnDpotrf_bufferSize failed");
+    return NEB_ERR_CUDA;
+  }
+  const size_t kk = a256((size_t)K * K * sizeof(double)), k1 = a256((size_t)K * sizeof(double));
+  const size_t need = 8 * kk + 5 * k1 + a256(sizeof(int) * 2) + a256((size_t)lwork * sizeof(double));
+  if (!workspace || workspace_bytes < need) {
+    set_error("neb_coefficient_peel: workspace %zu < %zu bytes", workspace_bytes, need);
+    return NEB_ERR_WORKSPACE;
+  }
+  char* w = (char*)workspace;
+  double* ms = (double*)w;
+  double* ss = (double*)(w + kk);
+  double* L = (double*)(w + 2 * kk);
+  double* T = (double*)(w + 3 * kk);
+  double* W1 = (double*)(w + 4 * kk);
+  double* L2 = (double*)(w + 5 * kk);
+  double* F = (double*)(w + 6 * kk);
+  double* TF = (double*)(w + 7 * kk);
+  double* raw = (double*)(w + 8 * kk);
+  double* scale = (double*)(w + 8 * kk + k1);
+  double* norm = (double*)(w + 8 * kk + 2 * k1);
+  double* rel_tmp = (double*)(w + 8 * kk + 3 * k1);
+  double* err_tmp = (double*)(w + 8 * kk + 4 * k1);
+  int* dinfo = (int*)(w + 8 * kk + 5 * k1);
+  double* work = (double*)(w + 8 * kk + 5 * k1 + a256(sizeof(int) * 2));
+  double* rel = relative_mass ? relative_mass : rel_tmp;
+  double* err = ortho_error ? ortho_error : err_tmp;
+  const int64_t kk_n = (int64_t)K * K;
+  cublasHandle_t h = g_peel.blas;
+  const double one = 1.0, zero = 0.0;
+  NEB_CUDA_CHECK(cudaMemsetAsync(info, 0, sizeof(int), s));
+  {
+    KernelScope ks("peel_order", s, 0, 8.0 * K * K);
+    peel_order<<<grid_for(K), 256, 0, s>>>(M, S, K, order, raw);
+    NEB_LAUNCH_CHECK();
+    peel_rank<<<grid_for(K), 256, 0, s>>>(raw, K, order);
+    NEB_LAUNCH_CHECK();
+    peel_gather<<<grid_for(kk_n), 256, 0, s>>>(M, S, order, K, ms, ss, L, scale);
+    NEB_LAUNCH_CHECK();
+  }
+  // first pass: H = L L^T, T = L^-T / scale (rows)
+  {
+    KernelScope ks("peel_cholesky", s, 2.0 * K * (double)K * K, 0);
+    if (cusolverDnDpotrf(g_peel.solver, CUBLAS_FILL_MODE_LOWER, K, L, K, work, lwork, dinfo) !=
+        CUSOLVER_STATUS_SUCCESS) {
+      set_error("cusolverDnDpotrf failed");
+      return NEB_ERR_SOLVER;
+    }
+    potrf_gate<<<1, 1, 0, s>>>(dinfo, info);
+    NEB_LAUNCH_CHECK();
+    set_identity<<<grid_for(kk_n), 256, 0, s>>>(T, K);
+    NEB_LAUNCH_CHECK();
+    NEB_BLAS(cublasDtrsm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, L, K, T, K),
+             "cublasDtrsm (L^-T)");
+    scale_rows<<<grid_for(kk_n), 256, 0, s>>>(T, scale, K);
+    NEB_LAUNCH_CHECK();
+    // second pass: H2 = T^T ms T = L2 L2^T, T <- T L2^-T
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, ms, K, T, K, &zero, W1, K),
+             "cublasDgemm (ms T)");
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, K, K, K, &one, T, K, W1, K, &zero, L2, K),
+             "cublasDgemm (T^T ms T)");
+    symmetrize<<<grid_for(kk_n), 256, 0, s>>>(L2, K);
+    NEB_LAUNCH_CHECK();
+    if (cusolverDnDpotrf(g_peel.solver, CUBLAS_FILL_MODE_LOWER, K, L2, K, work, lwork, dinfo) !=
+        CUSOLVER_STATUS_SUCCESS) {
+      set_error("cusolverDnDpotrf failed");
+      return NEB_ERR_SOLVER;
+    }
+    potrf_gate<<<1, 1, 0, s>>>(dinfo, info);
+    NEB_LAUNCH_CHECK();
+    NEB_BLAS(cublasDtrsm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, L2, K, T, K),
+             "cublasDtrsm (T L2^-T)");
+  }
+  {
+    KernelScope ks("peel_objective", s, 8.0 * K * (double)K * K, 0);
+    // O = T^T ms T (orthogonality), F = T^T ss T
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, ms, K, T, K, &zero, W1, K),
+             "cublasDgemm (ms T)");
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, K, K, K, &one, T, K, W1, K, &zero, L, K),
+             "cublasDgemm (T^T ms T)");
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, ss, K, T, K, &zero, W1, K),
+             "cublasDgemm (ss T)");
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, K, K, K, &one, T, K, W1, K, &zero, F, K),
+             "cublasDgemm (T^T ss T)");
+    peel_gate<<<1, 1024, 0, s>>>(T, ms, L, F, K, losses, norm, rel, err, info);
+    NEB_LAUNCH_CHECK();
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, T, K, F, K, &zero, TF, K),
+             "cublasDgemm (T triu(F))");
+    peel_adjoints<<<grid_for(kk_n), 256, 0, s>>>(T, TF, losses, norm, order, K, Cu, Cd, T_out);
+    NEB_LAUNCH_CHECK();
+  }
+  return NEB_OK;
+}
+
+extern "C" size_t neb_column_apply_workspace_bytes(int64_t rows, int K) {
+  if (rows <= 0 || K <= 0) return 0;
+  return 2 * a256((size_t)rows * K * sizeof(double));
+}
+
+// out = scale * A C, A [rows][K] (FP32 or FP64, row-major), C [K][K] FP64
+// row-major, computed in FP64 (cuBLAS DGEMM), out in A's type.
+extern "C" int neb_column_apply(int precision, int64_t rows, int K, const void* A,
+                                const double* Cm, double scale, void* out, void* workspace,
+                                size_t workspace_bytes, neb_stream_t stream) {
+  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64,
+              "neb_column_apply: FP32 or FP64");
+  NEB_REQUIRE(rows > 0 && rows <= (int64_t)1 << 31 && K > 0 && A && Cm && out,
+              "neb_column_apply: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  int st = peel_handles(s);
+  if (st) return st;
+  const int64_t total = rows * K;
+  cublasHandle_t h = g_peel.blas;
+  const double zero = 0.0;
+  if (precision == NEB_PREC_FP64) {
+    KernelScope ks("cublas_dgemm", s, 2.0 * rows * (double)K * K, 0);
+    // row-major out = A C  <=>  column-major out^T = C^T A^T
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, (int)rows, K, &scale, Cm, K,
+                         (const double*)A, K, &zero, (double*)out, K),
+             "cublasDgemm (columns)");
+    return NEB_OK;
+  }
+  if (!workspace || workspace_bytes < neb_column_apply_workspace_bytes(rows, K)) {
+    set_error("neb_column_apply: workspace too small");
+    return NEB_ERR_WORKSPACE;
+  }
+  double* A64 = (double*)workspace;
+  double* O64 = (double*)((char*)workspace + a256((size_t)rows * K * sizeof(double)));
+  {
+    KernelScope ks("convert", s, 0, 12.0 * total);
+    convert<float, double><<<grid_for(total), 256, 0, s>>>((const float*)A, A64, total, 1.0);
+    NEB_LAUNCH_CHECK();
+  }
+  {
+    KernelScope ks("cublas_dgemm", s, 2.0 * rows * (double)K * K, 0);
+    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, (int)rows, K, &scale, Cm, K, A64, K,
+                         &zero, O64, K),
+             "cublasDgemm (columns)");
+  }
+  {
+    KernelScope ks("convert", s, 0, 12.0 * total);
+    convert<double, float><<<grid_for(total), 256, 0, s>>>(O64, (float*)out, total, 1.0);
+    NEB_LAUNCH_CHECK();
+  }
+  return NEB_OK;
+}

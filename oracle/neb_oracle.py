@@ -559,3 +559,255 @@ def scaled_widths(widths, hidden=None, outputs=None):
     if outputs is not None:
         w[-1] = outputs
     return w
+
+
+# ==========================================================================
+# Mode-stacked SIREN networks: the reference's own per-mode architecture
+# ==========================================================================
+# K independent networks, one per mode, with weights stacked [K, out, in]:
+# hidden layers y = sin(omega (W x + b)) (omega_first on layer 0,
+# omega_hidden after), a linear output layer, and the output multiplied by an
+# envelope jet (native_cupy_core.py:111-154 for first-order jets,
+# velocity_trace_jet2.py:26-82 for second-order jets in 3D).  Jets here are
+# channel-first arrays [C, n, F]: value, the dim gradient channels, and for
+# order 2 the compact Hessian (2D: xx, xy, yy; 3D: xx, xy, xz, yy, yz, zz).
+PAIRS_2D = [(0, 0), (0, 1), (1, 1)]
+
+
+def jet_pairs(dim):
+    return PAIRS_2D if dim == 2 else PAIRS
+
+
+def jet_channels_of(dim, order):
+    return 1 + dim + (len(jet_pairs(dim)) if order == 2 else 0)
+
+
+def sine_jet_forward(Z, dim, order):
+    """y = sin z, grad y = cos z grad z, H y = cos z H z - sin z grad z grad z^T
+    (velocity_trace_jet2.py:31-34; hardcoded_backend.py sine_forward_jet1)."""
+    s, c = np.sin(Z[0]), np.cos(Z[0])
+    Y = np.empty_like(Z)
+    Y[0] = s
+    for a in range(dim):
+        Y[1 + a] = c * Z[1 + a]
+    if order == 2:
+        for k, (i, j) in enumerate(jet_pairs(dim)):
+            Y[1 + dim + k] = c * Z[1 + dim + k] - s * Z[1 + i] * Z[1 + j]
+    return Y
+
+
+def sine_jet_backward(Z, A, dim, order):
+    """Transpose of :func:`sine_jet_forward` (velocity_trace_jet2.py:35-41,
+    sine_backward_jet1 of the analytic-jets backend)."""
+    s, c = np.sin(Z[0]), np.cos(Z[0])
+    B = np.empty_like(Z)
+    zb = c * A[0]
+    for a in range(dim):
+        zb = zb - s * A[1 + a] * Z[1 + a]
+        B[1 + a] = c * A[1 + a]
+    if order == 2:
+        for k, (i, j) in enumerate(jet_pairs(dim)):
+            ah = A[1 + dim + k]
+            zb = zb + ah * (-s * Z[1 + dim + k] - c * Z[1 + i] * Z[1 + j])
+            B[1 + i] -= s * ah * Z[1 + j]
+            B[1 + j] -= s * ah * Z[1 + i]
+            B[1 + dim + k] = c * ah
+    B[0] = zb
+    return B
+
+
+def envelope_product(E, X, dim, order):
+    """Product of the envelope jet E [C, n, 1] with X [C, n, F]
+    (native_cupy_core.py product1, velocity_trace_jet2.py product)."""
+    Y = np.empty_like(X)
+    Y[0] = E[0] * X[0]
+    for a in range(dim):
+        Y[1 + a] = E[0] * X[1 + a] + E[1 + a] * X[0]
+    if order == 2:
+        for k, (i, j) in enumerate(jet_pairs(dim)):
+            q = 1 + dim + k
+            Y[q] = E[0] * X[q] + E[q] * X[0] + E[1 + i] * X[1 + j] + E[1 + j] * X[1 + i]
+    return Y
+
+
+def envelope_product_backward(E, A, dim, order):
+    """Adjoint of X in :func:`envelope_product` (envelope_product_backward_jet1,
+    velocity_trace_jet2.py product_reverse)."""
+    B = np.empty_like(A)
+    xb = E[0] * A[0]
+    for a in range(dim):
+        xb = xb + E[1 + a] * A[1 + a]
+        B[1 + a] = E[0] * A[1 + a]
+    if order == 2:
+        for k, (i, j) in enumerate(jet_pairs(dim)):
+            q = 1 + dim + k
+            xb = xb + E[q] * A[q]
+            B[1 + i] += E[1 + j] * A[q]
+            B[1 + j] += E[1 + i] * A[q]
+            B[q] = E[0] * A[q]
+    B[0] = xb
+    return B
+
+
+def mode_omegas(n_layers, omega_first, omega_hidden):
+    """omega of every hidden layer (the output layer has none)."""
+    return [omega_first if j == 0 else omega_hidden for j in range(n_layers - 1)]
+
+
+def mode_forward(W, b, X0, E, dim, order, omegas):
+    """One mode: W, b lists of [out, in], [out]; X0 the shared feature jet.
+    Returns (layer inputs, scaled pre-activations, envelope * output)."""
+    X, xs, pres = X0, [], []
+    for j in range(len(W) - 1):
+        xs.append(X)
+        P = omegas[j] * linear_forward(X, W[j], b[j])
+        pres.append(P)
+        X = sine_jet_forward(P, dim, order)
+    xs.append(X)
+    raw = linear_forward(X, W[-1], b[-1])
+    return xs, pres, envelope_product(E, raw, dim, order)
+
+
+def mode_backward(W, xs, pres, E, A, dim, order, omegas):
+    """Hand-written reverse of :func:`mode_forward` for one mode
+    (native_cupy_core.py:142-154, velocity_trace_jet2.py:77-82)."""
+    a = envelope_product_backward(E, A, dim, order)
+    gW, gb = [None] * len(W), [None] * len(W)
+    a, gW[-1], gb[-1] = linear_backward(xs[-1], a, W[-1])
+    for j in range(len(W) - 2, -1, -1):
+        a = omegas[j] * sine_jet_backward(pres[j], a, dim, order)
+        a, gW[j], gb[j] = linear_backward(xs[j], a, W[j])
+    return gW, gb
+
+
+def mode_adam(W, b, mW, vW, mb, vb, gW, gb, epoch, lr, clip=8.0):
+    """Per-mode Adam (native_cupy_core.py:156-171): the clip norm of mode k
+    runs over that mode's slice of every tensor; any non-finite or zero norm
+    raises with nothing changed.  Arrays are stacked [K, ...].  Returns the
+    new (W, b, mW, vW, mb, vb, epoch) and the per-mode norms."""
+    K = W[0].shape[0]
+    norms = np.sqrt(sum(np.sum(np.asarray(g, dtype=np.float64).reshape(K, -1) ** 2, axis=1)
+                        for g in [*gW, *gb]))
+    if not np.all(np.isfinite(norms) & (norms > 0)):
+        raise FloatingPointError("Invalid parameter gradients; no optimizer update")
+    scales = np.minimum(1.0, clip / np.maximum(norms, 1e-30))
+    t = epoch + 1
+    out = []
+    for pars, ms, vs, gs in ((W, mW, vW, gW), (b, mb, vb, gb)):
+        np_, nm, nv = [], [], []
+        for p, m, v, g in zip(pars, ms, vs, gs):
+            g = g * scales.reshape((K,) + (1,) * (g.ndim - 1))
+            m = 0.9 * m + 0.1 * g
+            v = 0.999 * v + 0.001 * g * g
+            np_.append(p - lr * (m / (1 - 0.9 ** t)) / (np.sqrt(v / (1 - 0.999 ** t)) + 1e-8))
+            nm.append(m)
+            nv.append(v)
+        out.append((np_, nm, nv))
+    (W2, mW2, vW2), (b2, mb2, vb2) = out
+    return (W2, b2, mW2, vW2, mb2, vb2, t), norms
+
+
+def velocity_fields(out):
+    """Velocity u = curl A and its gradient D[a][j] = d_j u_a of a 3D
+    vector potential jet out [10, n, 3] (velocity_trace_jet2.py:93-101):
+    returns U [n, 3], D [n, 3, 3]."""
+    def g(comp, axis):
+        return out[1 + axis][:, comp]
+
+    def h(comp, a, b):
+        return out[4 + hid(a, b)][:, comp]
+
+    U = np.stack([g(2, 1) - g(1, 2), g(0, 2) - g(2, 0), g(1, 0) - g(0, 1)], -1)
+    D = np.stack([np.stack([h((a + 2) % 3, j, (a + 1) % 3) - h((a + 1) % 3, j, (a + 2) % 3)
+                            for j in range(3)], -1) for a in range(3)], -2)
+    return U, D
+
+
+def velocity_lift(GU, GD):
+    """Adjoint of :func:`velocity_fields`: GU [n, 3], GD [n, 3, 3] -> output
+    jet adjoint [10, n, 3] (core.py:32-38 lift)."""
+    n = GU.shape[0]
+    A = np.zeros((10, n, 3))
+    A[1 + 1][:, 2] += GU[:, 0]; A[1 + 2][:, 1] -= GU[:, 0]
+    A[1 + 2][:, 0] += GU[:, 1]; A[1 + 0][:, 2] -= GU[:, 1]
+    A[1 + 0][:, 1] += GU[:, 2]; A[1 + 1][:, 0] -= GU[:, 2]
+    for a in range(3):
+        for j in range(3):
+            A[4 + hid(j, (a + 1) % 3)][:, (a + 2) % 3] += GD[:, a, j]
+            A[4 + hid(j, (a + 2) % 3)][:, (a + 1) % 3] -= GD[:, a, j]
+    return A
+
+
+def coefficient_peel(M, S):
+    """Causal Rayleigh peel in Gram form (core.py:48-69): modes sorted by
+    their raw quotients S_kk / M_kk (stable), the sorted mass matrix
+    orthonormalised by a scaled Cholesky factor applied twice (the Gram form
+    of two-pass modified Gram-Schmidt), losses = diag(T^T S T).  Returns the
+    losses in causal order, the order, the transform T (rows in mode order),
+    and the coefficient adjoints Cu, Cd with dL/dU = U Cu / n and
+    dL/dD = D Cd / n for L = sum(losses).  Raises FloatingPointError where
+    the reference's rank / relative-mass / orthogonality gate fails."""
+    K = len(M)
+    raw = np.diag(S) / np.diag(M)
+    order = np.argsort(raw, kind="stable")
+    ms = M[np.ix_(order, order)]
+    ss = S[np.ix_(order, order)]
+    scale = np.sqrt(np.diag(ms))
+    L = np.linalg.cholesky(ms / scale[:, None] / scale[None, :])
+    T = sla.solve_triangular(L.T, np.eye(K), lower=False) / scale[:, None]
+    H2 = T.T @ ms @ T
+    L2 = np.linalg.cholesky(0.5 * (H2 + H2.T))
+    T = T @ sla.solve_triangular(L2.T, np.eye(K), lower=False)
+    error = float(np.max(np.abs(T.T @ ms @ T - np.eye(K))))
+    norm = 1.0 / np.diag(T)
+    relative = norm * norm / np.diag(ms)
+    F = T.T @ ss @ T
+    loss = np.diag(F).copy()
+    if not (np.all(np.isfinite(loss) & (loss > 0) & (relative >= 1e-4)) and error <= 1e-5):
+        raise FloatingPointError("Velocity rank/relative mass/orthogonality gate failed")
+    C = -2.0 * (T * loss[None, :] + T @ np.triu(F, 1)) / norm[None, :]
+    B = 2.0 * T / norm[None, :]
+    Cu = np.empty_like(C); Cd = np.empty_like(B); Tm = np.empty_like(T)
+    Cu[np.ix_(order, order)] = C
+    Cd[np.ix_(order, order)] = B
+    Tm[order] = T
+    return dict(losses=loss, order=order, T=Tm, Cu=Cu, Cd=Cd, relative_mass=relative,
+                gram_max=error, raw=raw)
+
+
+def velocity_step(W, b, X0, E, omegas, want_grad=True):
+    """The 3D velocity objective of the mode-stacked network (core.py:79-103):
+    every mode's vector potential (3 outputs, second-order jets), U [3n, K]
+    and D [9n, K], M = U^T U / n, S = D^T D / n, the Gram-form peel, and the
+    parameter gradient of sum(losses).  W, b: lists of stacked [K, out, in],
+    [K, out] arrays."""
+    K = W[0].shape[0]
+    n = X0.shape[1]
+    per, Us, Ds = [], [], []
+    for k in range(K):
+        Wk = [w[k] for w in W]
+        bk = [x[k] for x in b]
+        xs, pres, out = mode_forward(Wk, bk, X0, E, 3, 2, omegas)
+        u, d = velocity_fields(out)
+        per.append((Wk, xs, pres))
+        Us.append(u.reshape(-1))
+        Ds.append(d.reshape(-1))
+    U = np.stack(Us, 1)
+    D = np.stack(Ds, 1)
+    M = U.T @ U / n
+    S = D.T @ D / n
+    obj = coefficient_peel(M, S)
+    obj.update(M=M, S=S, U=U, D=D)
+    if want_grad:
+        gu = U @ obj["Cu"] / n
+        gd = D @ obj["Cd"] / n
+        gW = [np.zeros_like(w) for w in W]
+        gb = [np.zeros_like(x) for x in b]
+        for k, (Wk, xs, pres) in enumerate(per):
+            A = velocity_lift(gu[:, k].reshape(n, 3), gd[:, k].reshape(n, 3, 3))
+            gwk, gbk = mode_backward(Wk, xs, pres, E, A, 3, 2, omegas)
+            for j in range(len(W)):
+                gW[j][k] = gwk[j]
+                gb[j][k] = gbk[j]
+        obj["grads"] = (gW, gb)
+    return obj

@@ -16,9 +16,13 @@ Reference functions exercised (paths relative to the reference project):
 * experiments/metaball/_backend/flow/cases/metaball/velocity_trace_jet2.py:
   ``sine`` (:31), ``sine_reverse`` (:35), ``velocity`` (:93), ``vorticity`` (:96),
   ``lift_reverse`` (:102), ``trace_objective`` (:107);
-* experiments/metaball/_backend/flow/cases/metaball/velocity/core.py: ``grams`` (:40);
+* experiments/metaball/_backend/flow/cases/metaball/velocity/core.py: ``grams`` (:40),
+  ``coefficient_peel`` (:48), ``lift`` (:32), composed as ``compute`` (:79) composes them;
 * experiments/metaball/_backend/flow/cases/metaball/native_cupy_core.py:
-  ``Model`` forward / backward / adam (:111-171);
+  ``Model`` forward / backward / adam (:111-171), with one mode and the
+  identity envelope, and with two modes and a random envelope;
+* experiments/metaball/_backend/flow/cases/metaball/velocity_trace_jet2.py:
+  ``forward`` / ``backward`` (:65-82) of a four-mode second-order network;
 * experiments/periodic/paper_rollout.py:178-187 recipe (Grams, then
   ``scipy.linalg.eigh(S, M)``).
 
@@ -194,6 +198,64 @@ def main():
     g.update(ncc_feat=feat, ncc_fgrad=fgrad, ncc_value=val.value[0], ncc_grad=val.grad[0],
              ncc_av=av[0], ncc_ag=agr[0], ncc_omega=np.asarray([2.3, 1.7]),
              ncc_layers=np.asarray(len(W0)))
+    # --- the per-mode network with a non-trivial envelope (the shape of the
+    # reference's backend test, tests/test_network_backends.py:37-98): two
+    # modes, first-order jets, two Adam steps
+    model = ncc.Model(c, K=2, seed=31)
+    n = 5
+    feat = rng.normal(size=(n, 15)); fgrad = rng.normal(size=(n, 15, 3))
+    env_v = rng.uniform(.3, .8, size=(n, 1)); env_g = rng.normal(size=(n, 1, 3))
+    data = SimpleNamespace(features=ncc.Jet1(feat, fgrad), envelope=ncc.Jet1(env_v, env_g))
+    W0 = [w.copy() for w in model.W]; b0 = [bb.copy() for bb in model.b]
+    val, tape = model.forward(data, 0, 2, True)
+    av = rng.normal(size=val.value.shape); agr = rng.normal(size=val.grad.shape)
+    gw, gbias = model.backward(data, 0, 2, tape, ncc.Jet1(av, agr))
+    norms1 = model.adam(gw, gbias, 1e-3, clip=0.5)
+    norms2 = model.adam([2 * x for x in gw], [-x for x in gbias], 1e-3, clip=0.5)
+    for j in range(len(W0)):
+        g[f"env_W{j}"] = W0[j]; g[f"env_b{j}"] = b0[j]
+        g[f"env_gW{j}"] = gw[j]; g[f"env_gb{j}"] = gbias[j]
+        g[f"env_W{j}_after"] = model.W[j]; g[f"env_b{j}_after"] = model.b[j]
+    g.update(env_feat=feat, env_fgrad=fgrad, env_ev=env_v, env_eg=env_g, env_value=val.value,
+             env_grad=val.grad, env_av=av, env_ag=agr, env_norms1=norms1, env_norms2=norms2)
+
+    # --- 3D second-order per-mode network with envelope, velocity fields,
+    # Grams, the Gram-form causal peel and the gradient, composed from the
+    # reference's own functions as velocity/core.py:79-103 composes them
+    K3, n3 = 4, 7
+    c3 = SimpleNamespace(hidden=6, hidden_layers=2, siren_first_omega0=1.9,
+                         siren_hidden_omega0=1.3)
+    m3 = ncc.Model(c3, K=K3, seed=5)
+    f3 = vtj2.J2(rng.normal(size=(n3, 15)) * 0.5, rng.normal(size=(n3, 15, 3)) * 0.5,
+                 rng.normal(size=(n3, 15, 6)) * 0.5)
+    e3 = vtj2.J2(rng.uniform(.3, .8, size=(n3, 1)), rng.normal(size=(n3, 1, 3)) * 0.3,
+                 rng.normal(size=(n3, 1, 6)) * 0.3)
+    d3 = SimpleNamespace(features=f3, envelope=e3, n=n3)
+    out3, hist3 = vtj2.forward(m3, d3, 0, K3, True)
+    U3 = vtj2.velocity(out3).reshape(K3, -1).T
+    D3 = vtj2.velocity_grad(out3).reshape(K3, -1).T
+    M3, S3 = vcore.grams(U3, D3)
+    pk = vcore.coefficient_peel(M3, S3)
+    gu3 = (U3 @ pk["Cu"] / n3).T.reshape(K3, n3, 3)
+    gd3 = (D3 @ pk["Cd"] / n3).T.reshape(K3, n3, 3, 3)
+    gw3, gb3 = vtj2.backward(m3, d3, hist3, vcore.lift(gu3, gd3))
+    for j in range(len(m3.W)):
+        g[f"vel_W{j}"] = m3.W[j]; g[f"vel_b{j}"] = m3.b[j]
+        g[f"vel_gW{j}"] = gw3[j]; g[f"vel_gb{j}"] = gb3[j]
+    g.update(vel_fv=f3.value, vel_fg=f3.grad, vel_fh=f3.hess, vel_ev=e3.value, vel_eg=e3.grad,
+             vel_eh=e3.hess, vel_out_v=out3.value, vel_out_g=out3.grad, vel_out_h=out3.hess,
+             vel_U=U3, vel_D=D3, vel_M=M3, vel_S=S3, vel_losses=pk["losses"],
+             vel_order=pk["order"], vel_T=pk["T"], vel_Cu=pk["Cu"], vel_Cd=pk["Cd"],
+             vel_omega=np.asarray([1.9, 1.3]), vel_layers=np.asarray(len(m3.W)))
+
+    # --- the Gram-form peel alone on a larger, well-conditioned pencil
+    Kp = 12
+    X = rng.normal(size=(60, Kp)); Y = rng.normal(size=(60, Kp)) * np.linspace(0.5, 3, Kp)
+    Mp, Sp = X.T @ X / 20, Y.T @ Y / 20
+    pp = vcore.coefficient_peel(Mp, Sp)
+    g.update(peel_M=Mp, peel_S=Sp, peel_losses=pp["losses"], peel_order=pp["order"],
+             peel_T=pp["T"], peel_Cu=pp["Cu"], peel_Cd=pp["Cd"])
+
     g = {key: np.asarray(v, dtype=np.float64) if np.asarray(v).dtype.kind == "f" else np.asarray(v)
          for key, v in g.items()}
     np.savez_compressed(OUT, **g)

@@ -199,3 +199,83 @@ def test_adam_rejects_invalid_gradients_without_change():
         O.adam_step(params, mom, [(np.full((2, 2), np.nan), np.zeros(2))], 0, 1e-3)
     with pytest.raises(FloatingPointError):
         O.adam_step(params, mom, [(np.zeros((2, 2)), np.zeros(2))], 0, 1e-3)
+
+
+# ------------------------------------------- mode-stacked SIREN networks
+def _jet1(value, grad):
+    """[n, F] value and [n, F, d] gradient -> channel-first [1 + d, n, F]."""
+    return np.concatenate([value[None], np.moveaxis(grad, -1, 0)])
+
+
+def _jet2(value, grad, hess):
+    return np.concatenate([value[None], np.moveaxis(grad, -1, 0), np.moveaxis(hess, -1, 0)])
+
+
+def test_mode_network_with_envelope_matches_reference_model():
+    """Two modes, first-order jets, a random envelope: forward, reverse and
+    two Adam steps with per-mode norms, against native_cupy_core.Model."""
+    layers = 3
+    W = [G[f"env_W{j}"] for j in range(layers)]
+    b = [G[f"env_b{j}"] for j in range(layers)]
+    X0 = _jet1(G["env_feat"], G["env_fgrad"])
+    E = _jet1(G["env_ev"], G["env_eg"])
+    om = O.mode_omegas(layers, 2.3, 1.7)
+    gW = [np.zeros_like(w) for w in W]
+    gb = [np.zeros_like(x) for x in b]
+    for k in range(2):
+        xs, pres, out = O.mode_forward([w[k] for w in W], [x[k] for x in b], X0, E, 3, 1, om)
+        np.testing.assert_allclose(out[0], G["env_value"][k], rtol=1e-6, atol=1e-6)
+        np.testing.assert_allclose(np.moveaxis(out[1:], 0, -1), G["env_grad"][k], rtol=1e-6,
+                                   atol=1e-6)
+        A = _jet1(G["env_av"][k], G["env_ag"][k])
+        gwk, gbk = O.mode_backward([w[k] for w in W], xs, pres, E, A, 3, 1, om)
+        for j in range(layers):
+            gW[j][k], gb[j][k] = gwk[j], gbk[j]
+    for j in range(layers):
+        np.testing.assert_allclose(gW[j], G[f"env_gW{j}"], rtol=1e-6, atol=1e-6)
+        np.testing.assert_allclose(gb[j], G[f"env_gb{j}"], rtol=1e-6, atol=1e-6)
+    zeros = [np.zeros_like(w) for w in W], [np.zeros_like(x) for x in b]
+    st, n1 = O.mode_adam(W, b, zeros[0], zeros[0], zeros[1], zeros[1], gW, gb, 0, 1e-3, 0.5)
+    st, n2 = O.mode_adam(st[0], st[1], st[2], st[3], st[4], st[5], [2 * g for g in gW],
+                         [-g for g in gb], st[6], 1e-3, 0.5)
+    np.testing.assert_allclose(n1, G["env_norms1"], rtol=1e-6)
+    np.testing.assert_allclose(n2, G["env_norms2"], rtol=1e-6)
+    for j in range(layers):
+        np.testing.assert_allclose(st[0][j], G[f"env_W{j}_after"], rtol=1e-6, atol=1e-7)
+        np.testing.assert_allclose(st[1][j], G[f"env_b{j}_after"], rtol=1e-6, atol=1e-7)
+    assert st[6] == 2
+
+
+def test_gram_form_peel_matches_coefficient_peel():
+    p = O.coefficient_peel(G["peel_M"], G["peel_S"])
+    np.testing.assert_array_equal(p["order"], G["peel_order"])
+    np.testing.assert_allclose(p["losses"], G["peel_losses"], rtol=1e-12)
+    for key in ("T", "Cu", "Cd"):
+        np.testing.assert_allclose(p[key], G[f"peel_{key}"], rtol=1e-10,
+                                   atol=1e-12 * np.abs(G[f"peel_{key}"]).max())
+
+
+def test_velocity_step_matches_reference_composition():
+    """Second-order 3D mode network with envelope, velocity and velocity
+    gradient fields, Grams, the Gram-form peel and the parameter gradient,
+    against the reference's velocity_trace_jet2 / velocity/core.py functions
+    composed as core.py compute composes them."""
+    layers = int(G["vel_layers"])
+    W = [G[f"vel_W{j}"] for j in range(layers)]
+    b = [G[f"vel_b{j}"] for j in range(layers)]
+    X0 = _jet2(G["vel_fv"], G["vel_fg"], G["vel_fh"])
+    E = _jet2(G["vel_ev"], G["vel_eg"], G["vel_eh"])
+    om = O.mode_omegas(layers, *G["vel_omega"])
+    r = O.velocity_step(W, b, X0, E, om)
+    np.testing.assert_allclose(r["U"], G["vel_U"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(r["D"], G["vel_D"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(r["M"], G["vel_M"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(r["S"], G["vel_S"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_array_equal(r["order"], G["vel_order"])
+    np.testing.assert_allclose(r["losses"], G["vel_losses"], rtol=1e-9)
+    gW, gb = r["grads"]
+    for j in range(layers):
+        np.testing.assert_allclose(gW[j], G[f"vel_gW{j}"], rtol=1e-8,
+                                   atol=1e-10 * np.abs(G[f"vel_gW{j}"]).max())
+        np.testing.assert_allclose(gb[j], G[f"vel_gb{j}"], rtol=1e-8,
+                                   atol=1e-10 * np.abs(G[f"vel_gb{j}"]).max())
