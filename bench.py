@@ -73,7 +73,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="periodic_train",
                     choices=["periodic_train", "periodic_small", "periodic_eval", "multihole",
-                             "metaball3d"],
+                             "metaball3d", "reference_velocity"],
                     help="periodic_train is the headline line; the others print one line "
                          "each for the remaining configurations (timing and FP64-oracle "
                          "errors), not the headline metric")
@@ -311,6 +311,78 @@ def _gram_ms(kern_ms: dict) -> float:
     return sum(v for k, v in kern_ms.items() if k in ("tc_gram", "simt_gram"))
 
 
+# The reference's own 3D velocity training configuration
+# (experiments/metaball/configs/metaball-velocity-k1024-seed0.json): K
+# per-mode SIRENs of 5 x 128 sine layers (omega 40 / 36) on 15 input
+# features, vector potentials (3 outputs), second-order jets, 6,144 points
+# per step, the Gram-form causal peel, Adam (lr 2.8e-5, clip 8).  Its
+# published per-update stage means at K = 1024 (data/paper/
+# initial_capacity_training.json:83-92, hardware not stated) sum to 11.94 s.
+REF_VELOCITY = dict(hidden=128, hidden_layers=5, siren_first_omega0=40.0,
+                    siren_hidden_omega0=36.0, points=6144, lr=2.8e-5, clip=8.0,
+                    published_s_per_update_k1024=2.698278 + 8.952445 + 0.265934 + 0.018048)
+
+
+def velocity_inputs(n: int, seed: int = 0):
+    """Synthetic inputs with the configuration's shapes: points uniform in
+    the unit cube; features (2x - 1 for the coordinates, 12 constant
+    geometry codes in [-1, 1]) with their jets; a smooth bubble envelope
+    prod_a 4 x_a (1 - x_a) with analytic gradient and Hessian.  Channel-
+    first [10, n, F] arrays."""
+    rng = np.random.default_rng(seed)
+    x = rng.random((n, 3))
+    X0 = np.zeros((10, n, 15))
+    X0[0, :, :3] = 2 * x - 1
+    X0[0, :, 3:] = rng.uniform(-1, 1, 12)[None]
+    for a in range(3):
+        X0[1 + a, :, a] = 2.0
+    f = 4 * x * (1 - x)
+    df = 4 - 8 * x
+    E = np.zeros((10, n, 1))
+    E[0, :, 0] = f.prod(1)
+    for a in range(3):
+        E[1 + a, :, 0] = df[:, a] * np.prod(np.delete(f, a, 1), 1)
+    pairs = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+    for k, (i, j) in enumerate(pairs):
+        if i == j:
+            E[4 + k, :, 0] = -8 * np.prod(np.delete(f, i, 1), 1)
+        else:
+            E[4 + k, :, 0] = df[:, i] * df[:, j] * f[:, 3 - i - j]
+    return X0, E
+
+
+def time_velocity(K: int, steps: int, warmup: int, dev, block: int = 256):
+    """ms per training step (velocity objective + gradient + Adam) of the
+    reference's velocity configuration at K modes, CUDA events."""
+    import torch
+    from types import SimpleNamespace
+    from neb_gb300 import ModeModel, velocity_step
+    c = SimpleNamespace(**{k: REF_VELOCITY[k] for k in ("hidden", "hidden_layers",
+                                                       "siren_first_omega0",
+                                                       "siren_hidden_omega0")})
+    model = ModeModel(c, K=K, seed=0, inputs=15, outputs=3, dim=3, order=2, device=dev)
+    X0, E = velocity_inputs(REF_VELOCITY["points"])
+    feats = torch.tensor(np.moveaxis(X0, 0, 1), dtype=torch.float32, device=dev).contiguous()
+    env = torch.tensor(np.moveaxis(E, 0, 1), dtype=torch.float32, device=dev).contiguous()
+    data = SimpleNamespace(features=feats, envelope=env)
+
+    def step():
+        r = velocity_step(model, data, block=block, check=False)
+        model.adam_async(*r["grads"], lr=REF_VELOCITY["lr"], clip=REF_VELOCITY["clip"])
+        return r
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        r = step()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, int(r["info"].item())
+
+
 def run_workload(args, world, rank, local):
     """One line per configuration other than the headline: device-timed
     steps, the plain FP32 form where the configuration asks for it, and the
@@ -328,16 +400,50 @@ def run_workload(args, world, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     name = args.workload
-    cfg = CONFIGS[name]
     W, K = max(args.warmup, 1), args.steps
-    line = {"workload": name, "n_gpus": 1, "steps": K, "warmup": W,
-            "data": "synthetic: seeded samples of the configuration, Glorot-normal init",
-            "widths": list(cfg.widths), "objective": cfg.objective}
+    line = {"workload": name, "n_gpus": 1, "steps": K, "warmup": W}
+    if name in CONFIGS:
+        cfg = CONFIGS[name]
+        line.update({"data": "synthetic: seeded samples of the configuration, Glorot-normal "
+                             "init", "widths": list(cfg.widths), "objective": cfg.objective})
 
     def dev_inputs(pts, w):
         return torch.tensor(pts, device=dev), torch.tensor(w, device=dev)
 
-    if name == "periodic_small":
+    if name == "reference_velocity":
+        # the reference's own architecture and objective: GPU steps at K = 32
+        # and K = 1024, and the FP64 oracle's step at K = 32 on the host
+        out = {}
+        vsteps = max(1, min(args.steps, 5))
+        for K in (32, 1024):
+            ms, info = time_velocity(K, vsteps, 1, dev)
+            out[f"K{K}"] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms, "steps": vsteps,
+                            "peel_info": info}
+        from types import SimpleNamespace
+        from neb_gb300.modes import siren_init
+        c = SimpleNamespace(**{k: REF_VELOCITY[k] for k in ("hidden", "hidden_layers",
+                                                           "siren_first_omega0",
+                                                           "siren_hidden_omega0")})
+        Wn, bn = siren_init(c, 32, 0, 15, 3)
+        X0, E = velocity_inputs(REF_VELOCITY["points"])
+        t0 = time.perf_counter()
+        O.velocity_step([w.astype(np.float64) for w in Wn], [x.astype(np.float64) for x in bn],
+                        X0, E, O.mode_omegas(6, 40.0, 36.0))
+        t_cpu = time.perf_counter() - t0
+        line.update({
+            "metric": "velocity objective+grad+Adam steps/s, the reference's per-mode SIREN "
+                      "(5x128 sine, omega 40/36), 6144 points, causal peel",
+            "value": out["K1024"]["steps_per_s"], "unit": "steps/s",
+            "ms_per_step": out["K1024"]["ms_per_step"], "dtype": "f32", "modes": out,
+            "published_reference_s_per_update_k1024": REF_VELOCITY["published_s_per_update_k1024"],
+            "speedup_vs_published_k1024": REF_VELOCITY["published_s_per_update_k1024"]
+            / (out["K1024"]["ms_per_step"] / 1e3),
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": cpu_threads(),
+                             "kind": "port", "sample": "1 objective+gradient step at K=32 of "
+                             "the FP64 NumPy restatement (velocity_step)"},
+            "data": "synthetic: uniform points in the unit cube, coordinate features with 12 "
+                    "constant geometry codes, bubble envelope; reference initialisation"})
+    elif name == "periodic_small":
         pts, w = CF.sample(cfg)
         dp, dw = dev_inputs(pts, w)
         model = Model(cfg, precision="fp64", seed=0, device=dev)
@@ -568,6 +674,20 @@ def main():
                   "fp32": {"value": world * K / (ms_s32 / 1e3), "ms_per_step": ms_s32 / K},
                   "speedup_vs_fp32_plain": ms_s32 / ms_s}
 
+    # the reference's own per-mode architecture and causal peel at its K =
+    # 1024 velocity configuration (beside its published per-update time)
+    ref_arch = None
+    if not args.no_fp32_plain and world == 1:
+        ms_v, info_v = time_velocity(1024, 2, 1, dev)
+        ref_arch = {"workload": "reference velocity configuration: K=1024 per-mode SIRENs "
+                                "(5x128 sine, omega 40/36), 6144 points, second-order jets, "
+                                "Gram-form causal peel, Adam; FP32 SIMT mode kernels",
+                    "value": 1e3 / ms_v, "unit": "steps/s", "ms_per_step": ms_v,
+                    "peel_info": info_v,
+                    "published_reference_s_per_update": REF_VELOCITY[
+                        "published_s_per_update_k1024"],
+                    "published_hardware": "not stated (16 GB-class GPU guard)"}
+
     # objective + gradient + Adam on the 256^2 periodic grid (65,536 points,
     # the grid of the evaluation configuration), both forms
     grid256 = None
@@ -733,6 +853,7 @@ def main():
         "tc_kernels_roofline": tc_roofline,
         "strict_fp64_spectral": strict,
         "grid256": grid256,
+        "reference_architecture": ref_arch,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),
