@@ -13,7 +13,9 @@
 //
 // Kernels (SIMT, FP32 or FP64 as the parameters):
 //   mode_gemm<EPI>   per-mode jet GEMM over all channels, tiles of 8 points
-//                    x 32 columns, the reduction staged through shared memory;
+//                    x 128 (FP32) or 64 (FP64) columns, the reduction staged
+//                    through double-buffered shared memory by cp.async;
+//   mode_output_narrow the output layer when it has at most 4 columns;
 //                    epilogues: output layer (+ bias, x envelope), hidden
 //                    layer (+ bias, x omega, sine jet, pre-activation kept),
 //                    reverse data (sine-jet transpose of the layer below).
@@ -111,19 +113,57 @@ __device__ __forceinline__ void envelope_mul_reverse(const T* e, const T* a, T* 
   b[0] = xb;
 }
 
-constexpr int kTilePts = 8;    // points per block (two per warp)
-constexpr int kTileCols = 32;  // output columns per block (one per lane)
-constexpr int kTileK = 32;     // reduction chunk staged in shared memory
+constexpr int kTilePts = 8;  // points per block (two per warp)
+constexpr int kTileK = 32;   // reduction chunk staged in shared memory
+// output columns per thread (one per lane and step of 32): four in FP32,
+// two in FP64, so a block covers 128 or 64 columns
+template <typename T> constexpr int cols_per_thread() { return sizeof(T) == 4 ? 4 : 2; }
+template <typename T> constexpr int tile_cols() { return 32 * cols_per_thread<T>(); }
 
 enum { EPI_OUTPUT = 0, EPI_HIDDEN = 1, EPI_REVERSE = 2 };
 
-// Per-mode jet GEMM.  blockIdx.x = tile of 8 points, blockIdx.y = tile of 32
-// columns, blockIdx.z = mode b of the block; every pointer is
+// Asynchronous global -> shared copy of one element (4 or 8 bytes); a copy
+// with valid == false fills the destination with zeros and reads nothing.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src, bool valid) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src),
+                 "r"(valid ? 4 : 0)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src),
+                 "r"(valid ? 8 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Shared memory of one pipeline stage of mode_gemm: B tile [kTileK][TC + 1]
+// then A tile [8 C][kTileK]; two stages.
+template <typename T, int C> constexpr int mode_stage_elems() {
+  return kTileK * (tile_cols<T>() + 1) + kTilePts * C * kTileK;
+}
+template <typename T, int C> constexpr int mode_gemm_smem() {
+  return 2 * mode_stage_elems<T, C>() * (int)sizeof(T);
+}
+
+// Per-mode jet GEMM.  blockIdx.x = tile of 8 points, blockIdx.y = tile of
+// tile_cols<T>() columns, blockIdx.z = mode b of the block; every pointer is
 // already offset to the block's first mode and advanced by its *_mode stride.
 //   EPI_OUTPUT : out = env * (A W^T + b on the value channel), W [N][Kd]
 //   EPI_HIDDEN : pre = omega (A W^T + b), out = sine_jet(pre),   W [N][Kd]
 //   EPI_REVERSE: out = omega sine_jet^T(pre_in, A W),            W [Kd][N]
 // A: [n][C][Kd] (a_mode = 0 for the shared features); out, pre: [n][C][N].
+// A thread holds 2 points x C channels x cols_per_thread columns: each
+// shared-memory value it reads feeds cols_per_thread (A) or 2 C (B) FMAs.
+// The next reduction chunk is copied into the other shared-memory stage by
+// cp.async while the current one is consumed.
 template <typename T, int DIM, int ORD, int EPI>
 __global__ void __launch_bounds__(128)
 mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int64_t w_mode,
@@ -131,137 +171,230 @@ mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int6
           const T* __restrict__ pre_in, T* __restrict__ pre_out, T* __restrict__ out,
           int64_t o_mode, int n, int Kd, int N, T omega) {
   constexpr int C = Jet<DIM, ORD>::C;
-  __shared__ T Bs[kTileK][kTileCols + 1];
-  __shared__ T As[kTilePts * C][kTileK];
+  constexpr int CPT = cols_per_thread<T>(), TC = tile_cols<T>();
+  constexpr int STAGE = mode_stage_elems<T, C>();
+  extern __shared__ __align__(16) unsigned char mode_smem[];
+  T* smem = reinterpret_cast<T*>(mode_smem);
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   const int mb = blockIdx.z;
-  const int col0 = blockIdx.y * kTileCols, p0 = blockIdx.x * kTilePts;
+  const int col0 = blockIdx.y * TC, p0 = blockIdx.x * kTilePts;
   A += mb * a_mode;
   W += mb * w_mode;
-  T acc[2][C];
-#pragma unroll
-  for (int q = 0; q < 2; ++q)
-#pragma unroll
-    for (int c = 0; c < C; ++c) acc[q][c] = T(0);
-  for (int j0 = 0; j0 < Kd; j0 += kTileK) {
-    for (int e = tid; e < kTileK * kTileCols; e += 128) {
+  // issue the copies of reduction chunk j0 into stage st
+  auto stage_copy = [&](int j0, int st) {
+    T* Bs = smem + st * STAGE;                 // [kTileK][TC + 1]
+    T* As = Bs + kTileK * (TC + 1);            // [8 C][kTileK]
+    for (int e = tid; e < kTileK * TC; e += 128) {
       int jj, col;
       if constexpr (EPI == EPI_REVERSE) {
-        jj = e / kTileCols;
-        col = e % kTileCols;
+        jj = e / TC;
+        col = e % TC;
       } else {
         col = e / kTileK;
         jj = e % kTileK;
       }
       const int j = j0 + jj, o = col0 + col;
-      T v = T(0);
-      if (j < Kd && o < N) v = EPI == EPI_REVERSE ? W[(int64_t)j * N + o] : W[(int64_t)o * Kd + j];
-      Bs[jj][col] = v;
+      const bool ok = j < Kd && o < N;
+      const T* src = ok ? (EPI == EPI_REVERSE ? W + (int64_t)j * N + o : W + (int64_t)o * Kd + j) : W;
+      cp_async_elem(&Bs[jj * (TC + 1) + col], src, ok);
     }
     for (int e = tid; e < kTilePts * C * kTileK; e += 128) {
       const int jj = e % kTileK, rc = e / kTileK;
       const int p = p0 + rc / C, c = rc % C, j = j0 + jj;
-      As[rc][jj] = (p < n && j < Kd) ? A[((int64_t)p * C + c) * Kd + j] : T(0);
+      const bool ok = p < n && j < Kd;
+      cp_async_elem(&As[rc * kTileK + jj], ok ? A + ((int64_t)p * C + c) * Kd + j : A, ok);
+    }
+    cp_async_commit();
+  };
+  T acc[2][C][CPT];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+#pragma unroll
+      for (int u = 0; u < CPT; ++u) acc[q][c][u] = T(0);
+  const int chunks = (Kd + kTileK - 1) / kTileK;
+  stage_copy(0, 0);
+  for (int ch = 0; ch < chunks; ++ch) {
+    if (ch + 1 < chunks) {
+      stage_copy((ch + 1) * kTileK, (ch + 1) & 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
-#pragma unroll 8
+    const T* Bs = smem + (ch & 1) * STAGE;
+    const T* As = Bs + kTileK * (TC + 1);
+#pragma unroll 4
     for (int jj = 0; jj < kTileK; ++jj) {
-      const T bv = Bs[jj][tx];
+      T bv[CPT];
+#pragma unroll
+      for (int u = 0; u < CPT; ++u) bv[u] = Bs[jj * (TC + 1) + tx + 32 * u];
 #pragma unroll
       for (int q = 0; q < 2; ++q)
 #pragma unroll
-        for (int c = 0; c < C; ++c) acc[q][c] += As[(ty * 2 + q) * C + c][jj] * bv;
+        for (int c = 0; c < C; ++c) {
+          const T av = As[((ty * 2 + q) * C + c) * kTileK + jj];
+#pragma unroll
+          for (int u = 0; u < CPT; ++u) acc[q][c][u] += av * bv[u];
+        }
     }
-    __syncthreads();
+    __syncthreads();  // the stage is refilled by the copies issued next
   }
-  const int o = col0 + tx;
-  if (o >= N) return;
   out += mb * o_mode;
 #pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    const int p = p0 + ty * 2 + q;
-    if (p >= n) continue;
+  for (int u = 0; u < CPT; ++u) {
+    const int o = col0 + tx + 32 * u;
+    if (o >= N) continue;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int p = p0 + ty * 2 + q;
+      if (p >= n) continue;
+      T z[C], y[C];
+#pragma unroll
+      for (int c = 0; c < C; ++c) z[c] = acc[q][c][u];
+      const int64_t base = (int64_t)p * C * N + o;
+      if constexpr (EPI == EPI_OUTPUT) {
+        z[0] += bias[mb * b_mode + o];
+        if (env) {
+          T e[C];
+#pragma unroll
+          for (int c = 0; c < C; ++c) e[c] = env[(int64_t)p * C + c];
+          envelope_mul<DIM, ORD>(e, z, y);
+        } else {
+#pragma unroll
+          for (int c = 0; c < C; ++c) y[c] = z[c];
+        }
+      } else if constexpr (EPI == EPI_HIDDEN) {
+        z[0] += bias[mb * b_mode + o];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          z[c] *= omega;
+          pre_out[mb * o_mode + base + (int64_t)c * N] = z[c];
+        }
+        sine_jet<DIM, ORD>(z, y);
+      } else {
+        T pz[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) pz[c] = pre_in[mb * o_mode + base + (int64_t)c * N];
+        sine_jet_reverse<DIM, ORD>(pz, z, y);
+#pragma unroll
+        for (int c = 0; c < C; ++c) y[c] *= omega;
+      }
+#pragma unroll
+      for (int c = 0; c < C; ++c) out[base + (int64_t)c * N] = y[c];
+    }
+  }
+}
+
+// Output layer with few columns (N <= kNarrowCols, a vector potential's 3):
+// one thread per (point, mode) holds all N columns x C channels, reads its
+// point's input row directly and W_k (N x Kd) from shared memory; + bias on
+// the value channel, x envelope.  grid = (ceil(n / 128), B).
+constexpr int kNarrowCols = 4;
+template <typename T, int DIM, int ORD>
+__global__ void __launch_bounds__(128)
+mode_output_narrow(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W,
+                   int64_t w_mode, const T* __restrict__ bias, int64_t b_mode,
+                   const T* __restrict__ env, T* __restrict__ out, int64_t o_mode, int n, int Kd,
+                   int N) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  extern __shared__ __align__(16) unsigned char narrow_smem[];
+  T* Ws = reinterpret_cast<T*>(narrow_smem);  // [N][Kd]
+  const int mb = blockIdx.y;
+  W += mb * w_mode;
+  for (int e = threadIdx.x; e < N * Kd; e += blockDim.x) Ws[e] = W[e];
+  __syncthreads();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const T* a = A + mb * a_mode + (int64_t)p * C * Kd;
+  T acc[C][kNarrowCols];
+#pragma unroll
+  for (int c = 0; c < C; ++c)
+#pragma unroll
+    for (int u = 0; u < kNarrowCols; ++u) acc[c][u] = T(0);
+  for (int j = 0; j < Kd; ++j) {
+    T w[kNarrowCols];
+#pragma unroll
+    for (int u = 0; u < kNarrowCols; ++u) w[u] = u < N ? Ws[u * Kd + j] : T(0);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const T av = __ldg(a + (int64_t)c * Kd + j);
+#pragma unroll
+      for (int u = 0; u < kNarrowCols; ++u) acc[c][u] += av * w[u];
+    }
+  }
+  T e[C];
+#pragma unroll
+  for (int c = 0; c < C; ++c) e[c] = env ? env[(int64_t)p * C + c] : (c == 0 ? T(1) : T(0));
+  T* o = out + mb * o_mode + (int64_t)p * C * N;
+#pragma unroll
+  for (int u = 0; u < kNarrowCols; ++u) {
+    if (u >= N) break;
     T z[C], y[C];
 #pragma unroll
-    for (int c = 0; c < C; ++c) z[c] = acc[q][c];
-    const int64_t base = (int64_t)p * C * N + o;
-    if constexpr (EPI == EPI_OUTPUT) {
-      z[0] += bias[mb * b_mode + o];
-      if (env) {
-        T e[C];
+    for (int c = 0; c < C; ++c) z[c] = acc[c][u];
+    z[0] += bias[mb * b_mode + u];
+    envelope_mul<DIM, ORD>(e, z, y);
 #pragma unroll
-        for (int c = 0; c < C; ++c) e[c] = env[(int64_t)p * C + c];
-        envelope_mul<DIM, ORD>(e, z, y);
-      } else {
-#pragma unroll
-        for (int c = 0; c < C; ++c) y[c] = z[c];
-      }
-    } else if constexpr (EPI == EPI_HIDDEN) {
-      z[0] += bias[mb * b_mode + o];
-#pragma unroll
-      for (int c = 0; c < C; ++c) {
-        z[c] *= omega;
-        pre_out[mb * o_mode + base + (int64_t)c * N] = z[c];
-      }
-      sine_jet<DIM, ORD>(z, y);
-    } else {
-      T pz[C];
-#pragma unroll
-      for (int c = 0; c < C; ++c) pz[c] = pre_in[mb * o_mode + base + (int64_t)c * N];
-      sine_jet_reverse<DIM, ORD>(pz, z, y);
-#pragma unroll
-      for (int c = 0; c < C; ++c) y[c] *= omega;
-    }
-#pragma unroll
-    for (int c = 0; c < C; ++c) out[base + (int64_t)c * N] = y[c];
+    for (int c = 0; c < C; ++c) o[(int64_t)c * N + u] = y[c];
   }
 }
 
 // part[s][b][o][i] = sum over rows r in split s of Abar[b][r][o] X[b][r][i],
-// rows r = (point, channel).  grid = (tiles of 32 x 32, B, splits), 256
-// threads, 2 x 2 outputs each.
+// rows r = (point, channel).  grid = (tiles of 64 x 64, B, splits), 256
+// threads as 16 x 16, 4 x 4 outputs each; rows staged 32 at a time.
+constexpr int kWgTile = 64, kWgRows = 32;
 template <typename T>
 __global__ void __launch_bounds__(256)
 mode_wgrad(const T* __restrict__ Abar, const T* __restrict__ X, int64_t x_mode, int64_t rows,
            int N, int Kin, int64_t rows_per_split, T* __restrict__ part) {
-  __shared__ T As[16][33];
-  __shared__ T Xs[16][33];
-  const int tiles_i = (Kin + 31) / 32;
-  const int o0 = (blockIdx.x / tiles_i) * 32, i0 = (blockIdx.x % tiles_i) * 32;
+  __shared__ __align__(16) T As[kWgRows][kWgTile + 4];
+  __shared__ __align__(16) T Xs[kWgRows][kWgTile + 4];
+  const int tiles_i = (Kin + kWgTile - 1) / kWgTile;
+  const int o0 = (blockIdx.x / tiles_i) * kWgTile, i0 = (blockIdx.x % tiles_i) * kWgTile;
   const int mb = blockIdx.y, s = blockIdx.z;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   Abar += (int64_t)mb * rows * N;
   X += mb * x_mode;
   const int64_t r0 = (int64_t)s * rows_per_split;
   const int64_t r1 = r0 + rows_per_split < rows ? r0 + rows_per_split : rows;
-  T acc[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
-  for (int64_t rb = r0; rb < r1; rb += 16) {
-    for (int e = tid; e < 512; e += 256) {
-      const int rr = e >> 5, cc = e & 31;
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[a][c] = T(0);
+  for (int64_t rb = r0; rb < r1; rb += kWgRows) {
+    for (int e = tid; e < kWgRows * kWgTile; e += 256) {
+      const int rr = e / kWgTile, cc = e % kWgTile;
       const int64_t r = rb + rr;
       const bool ok = r < r1;
       As[rr][cc] = (ok && o0 + cc < N) ? Abar[r * N + o0 + cc] : T(0);
       Xs[rr][cc] = (ok && i0 + cc < Kin) ? X[r * Kin + i0 + cc] : T(0);
     }
     __syncthreads();
+#pragma unroll 8
+    for (int rr = 0; rr < kWgRows; ++rr) {
+      T a[4], x[4];
 #pragma unroll
-    for (int rr = 0; rr < 16; ++rr) {
-      const T a0 = As[rr][ty * 2], a1 = As[rr][ty * 2 + 1];
-      const T x0 = Xs[rr][tx * 2], x1 = Xs[rr][tx * 2 + 1];
-      acc[0][0] += a0 * x0;
-      acc[0][1] += a0 * x1;
-      acc[1][0] += a1 * x0;
-      acc[1][1] += a1 * x1;
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[rr][ty * 4 + u];
+        x[u] = Xs[rr][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * x[v];
     }
     __syncthreads();
   }
   T* dst = part + ((int64_t)s * gridDim.y + mb) * N * Kin;
 #pragma unroll
-  for (int a = 0; a < 2; ++a)
+  for (int u = 0; u < 4; ++u)
 #pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      const int o = o0 + ty * 2 + a, i = i0 + tx * 2 + c;
-      if (o < N && i < Kin) dst[(int64_t)o * Kin + i] = acc[a][c];
+    for (int v = 0; v < 4; ++v) {
+      const int o = o0 + ty * 4 + u, i = i0 + tx * 4 + v;
+      if (o < N && i < Kin) dst[(int64_t)o * Kin + i] = acc[u][v];
     }
 }
 
@@ -531,12 +664,31 @@ int launch_mode_gemm(const T* A, int64_t a_mode, const T* W, int64_t w_mode, con
                      int64_t o_mode, int B, int n, int Kd, int N, double omega, cudaStream_t s,
                      const char* name) {
   constexpr int C = Jet<DIM, ORD>::C;
-  NEB_REQUIRE(ceil_div(N, kTileCols) <= 65535, "mode GEMM: width %d too large", N);
-  dim3 grid((unsigned)ceil_div(n, kTilePts), (unsigned)ceil_div(N, kTileCols), (unsigned)B);
   KernelScope ks(name, s, 2.0 * B * n * C * (double)Kd * N,
                  (double)B * n * C * (Kd + N * (EPI == EPI_OUTPUT ? 1 : 2)) * sizeof(T));
-  mode_gemm<T, DIM, ORD, EPI><<<grid, 128, 0, s>>>(A, a_mode, W, w_mode, bias, b_mode, env, pre_in,
-                                                   pre_out, out, o_mode, n, Kd, N, (T)omega);
+  int dev = 0, sms = 0;
+  if (int st = device_sms(&dev, &sms)) return st;
+  if (EPI == EPI_OUTPUT && N <= kNarrowCols) {
+    const size_t smem = (size_t)N * Kd * sizeof(T);
+    NEB_REQUIRE(smem <= 48 * 1024, "mode output layer: %d inputs too many", Kd);
+    mode_output_narrow<T, DIM, ORD><<<dim3((unsigned)ceil_div(n, 128), (unsigned)B), 128, smem,
+                                      s>>>(A, a_mode, W, w_mode, bias, b_mode, env, out, o_mode,
+                                           n, Kd, N);
+    NEB_LAUNCH_CHECK();
+    return NEB_OK;
+  }
+  static bool configured[kMaxDevices] = {};
+  constexpr int smem = mode_gemm_smem<T, C>();
+  if (!configured[dev]) {
+    NEB_CUDA_CHECK(cudaFuncSetAttribute(mode_gemm<T, DIM, ORD, EPI>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured[dev] = true;
+  }
+  NEB_REQUIRE(ceil_div(N, tile_cols<T>()) <= 65535, "mode GEMM: width %d too large", N);
+  dim3 grid((unsigned)ceil_div(n, kTilePts), (unsigned)ceil_div(N, tile_cols<T>()), (unsigned)B);
+  mode_gemm<T, DIM, ORD, EPI><<<grid, 128, smem, s>>>(A, a_mode, W, w_mode, bias, b_mode, env,
+                                                      pre_in, pre_out, out, o_mode, n, Kd, N,
+                                                      (T)omega);
   NEB_LAUNCH_CHECK();
   return NEB_OK;
 }
@@ -602,11 +754,11 @@ int modes_backward_t(const neb_modes* m, int start, int B, const void* const* Wv
     const int64_t rows = n * C;
     // weight gradient, split over row ranges so that B x tiles x splits
     // covers the SMs about twice
-    const int tiles = (int)(ceil_div(o, 32) * ceil_div(in, 32));
+    const int tiles = (int)(ceil_div(o, kWgTile) * ceil_div(in, kWgTile));
     int splits = (int)std::max<int64_t>(1, std::min<int64_t>(kMaxWgradSplits,
                                                              ceil_div(2 * sms, (int64_t)tiles * B)));
-    splits = (int)std::min<int64_t>(splits, ceil_div(rows, 16));
-    const int64_t per = ceil_div(ceil_div(rows, splits), 16) * 16;
+    splits = (int)std::min<int64_t>(splits, ceil_div(rows, kWgRows));
+    const int64_t per = ceil_div(ceil_div(rows, splits), kWgRows) * kWgRows;
     splits = (int)ceil_div(rows, per);
     {
       KernelScope ks("mode_weight_grad", s, 2.0 * B * rows * (double)o * in,
