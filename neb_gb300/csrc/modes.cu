@@ -288,10 +288,15 @@ mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int6
 }
 
 // Output layer with few columns (N <= kNarrowCols, a vector potential's 3):
-// one thread per (point, mode) holds all N columns x C channels, reads its
-// point's input row directly and W_k (N x Kd) from shared memory; + bias on
-// the value channel, x envelope.  grid = (ceil(n / 128), B).
-constexpr int kNarrowCols = 4;
+// a block takes 32 points of one mode; thread (u, p) = (tid / 32, tid % 32)
+// holds column u of point p over all C channels.  The input rows are staged
+// [C][32 points][33] through shared memory in coalesced 32-wide chunks, W_k
+// (N x Kd) sits in shared memory; + bias on the value channel, x envelope.
+// grid = (ceil(n / 32), B).
+constexpr int kNarrowCols = 4, kNarrowPts = 32;
+template <typename T, int C> constexpr int narrow_smem(int N, int Kd) {
+  return (C * kNarrowPts * (kTileK + 1) + N * Kd) * (int)sizeof(T);
+}
 template <typename T, int DIM, int ORD>
 __global__ void __launch_bounds__(128)
 mode_output_narrow(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W,
@@ -299,58 +304,61 @@ mode_output_narrow(const T* __restrict__ A, int64_t a_mode, const T* __restrict_
                    const T* __restrict__ env, T* __restrict__ out, int64_t o_mode, int n, int Kd,
                    int N) {
   constexpr int C = Jet<DIM, ORD>::C;
-  extern __shared__ __align__(16) unsigned char narrow_smem[];
-  T* Ws = reinterpret_cast<T*>(narrow_smem);  // [N][Kd]
-  const int mb = blockIdx.y;
+  extern __shared__ __align__(16) unsigned char narrow_smem_raw[];
+  T* As = reinterpret_cast<T*>(narrow_smem_raw);        // [C][32][kTileK + 1]
+  T* Ws = As + C * kNarrowPts * (kTileK + 1);           // [N][Kd]
+  const int mb = blockIdx.y, p0 = blockIdx.x * kNarrowPts;
+  const int tid = threadIdx.x, pl = tid % kNarrowPts, u = tid / kNarrowPts;
+  A += mb * a_mode;
   W += mb * w_mode;
-  for (int e = threadIdx.x; e < N * Kd; e += blockDim.x) Ws[e] = W[e];
-  __syncthreads();
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const T* a = A + mb * a_mode + (int64_t)p * C * Kd;
-  T acc[C][kNarrowCols];
+  for (int e = tid; e < N * Kd; e += blockDim.x) Ws[e] = W[e];
+  T acc[C];
 #pragma unroll
-  for (int c = 0; c < C; ++c)
+  for (int c = 0; c < C; ++c) acc[c] = T(0);
+  for (int j0 = 0; j0 < Kd; j0 += kTileK) {
+    __syncthreads();
+    for (int e = tid; e < kNarrowPts * C * kTileK; e += blockDim.x) {
+      const int jj = e % kTileK, rc = e / kTileK;  // rc = point * C + channel
+      const int p = p0 + rc / C, c = rc % C, j = j0 + jj;
+      As[(c * kNarrowPts + rc / C) * (kTileK + 1) + jj] =
+          (p < n && j < Kd) ? A[((int64_t)p * C + c) * Kd + j] : T(0);
+    }
+    __syncthreads();
+    if (u < N) {
+      const int jn = min(kTileK, Kd - j0);
+      for (int jj = 0; jj < jn; ++jj) {
+        const T w = Ws[u * Kd + j0 + jj];
 #pragma unroll
-    for (int u = 0; u < kNarrowCols; ++u) acc[c][u] = T(0);
-  for (int j = 0; j < Kd; ++j) {
-    T w[kNarrowCols];
-#pragma unroll
-    for (int u = 0; u < kNarrowCols; ++u) w[u] = u < N ? Ws[u * Kd + j] : T(0);
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-      const T av = __ldg(a + (int64_t)c * Kd + j);
-#pragma unroll
-      for (int u = 0; u < kNarrowCols; ++u) acc[c][u] += av * w[u];
+        for (int c = 0; c < C; ++c) acc[c] += As[(c * kNarrowPts + pl) * (kTileK + 1) + jj] * w;
+      }
     }
   }
-  T e[C];
+  const int p = p0 + pl;
+  if (u >= N || p >= n) return;
+  T e[C], y[C];
 #pragma unroll
   for (int c = 0; c < C; ++c) e[c] = env ? env[(int64_t)p * C + c] : (c == 0 ? T(1) : T(0));
+  acc[0] += bias[mb * b_mode + u];
+  envelope_mul<DIM, ORD>(e, acc, y);
   T* o = out + mb * o_mode + (int64_t)p * C * N;
 #pragma unroll
-  for (int u = 0; u < kNarrowCols; ++u) {
-    if (u >= N) break;
-    T z[C], y[C];
-#pragma unroll
-    for (int c = 0; c < C; ++c) z[c] = acc[c][u];
-    z[0] += bias[mb * b_mode + u];
-    envelope_mul<DIM, ORD>(e, z, y);
-#pragma unroll
-    for (int c = 0; c < C; ++c) o[(int64_t)c * N + u] = y[c];
-  }
+  for (int c = 0; c < C; ++c) o[(int64_t)c * N + u] = y[c];
 }
 
 // part[s][b][o][i] = sum over rows r in split s of Abar[b][r][o] X[b][r][i],
 // rows r = (point, channel).  grid = (tiles of 64 x 64, B, splits), 256
-// threads as 16 x 16, 4 x 4 outputs each; rows staged 32 at a time.
-constexpr int kWgTile = 64, kWgRows = 32;
+// threads as 16 x 16, 4 x 4 outputs each; rows staged 32 at a time into
+// double-buffered shared memory by cp.async.
+constexpr int kWgTile = 64, kWgRows = 32, kWgLd = kWgTile + 4;
+template <typename T> constexpr int mode_wgrad_smem() {
+  return 2 * 2 * kWgRows * kWgLd * (int)sizeof(T);
+}
 template <typename T>
 __global__ void __launch_bounds__(256)
 mode_wgrad(const T* __restrict__ Abar, const T* __restrict__ X, int64_t x_mode, int64_t rows,
            int N, int Kin, int64_t rows_per_split, T* __restrict__ part) {
-  __shared__ __align__(16) T As[kWgRows][kWgTile + 4];
-  __shared__ __align__(16) T Xs[kWgRows][kWgTile + 4];
+  extern __shared__ __align__(16) unsigned char wg_smem[];
+  T* smem = reinterpret_cast<T*>(wg_smem);  // [stage][A, X][kWgRows][kWgLd]
   const int tiles_i = (Kin + kWgTile - 1) / kWgTile;
   const int o0 = (blockIdx.x / tiles_i) * kWgTile, i0 = (blockIdx.x % tiles_i) * kWgTile;
   const int mb = blockIdx.y, s = blockIdx.z;
@@ -359,27 +367,42 @@ mode_wgrad(const T* __restrict__ Abar, const T* __restrict__ X, int64_t x_mode, 
   X += mb * x_mode;
   const int64_t r0 = (int64_t)s * rows_per_split;
   const int64_t r1 = r0 + rows_per_split < rows ? r0 + rows_per_split : rows;
+  auto stage_copy = [&](int64_t rb, int st) {
+    T* As = smem + st * 2 * kWgRows * kWgLd;
+    T* Xs = As + kWgRows * kWgLd;
+    for (int e = tid; e < kWgRows * kWgTile; e += 256) {
+      const int rr = e / kWgTile, cc = e % kWgTile;
+      const int64_t r = rb + rr;
+      const bool ra = r < r1 && o0 + cc < N, rx = r < r1 && i0 + cc < Kin;
+      cp_async_elem(&As[rr * kWgLd + cc], ra ? Abar + r * N + o0 + cc : Abar, ra);
+      cp_async_elem(&Xs[rr * kWgLd + cc], rx ? X + r * Kin + i0 + cc : X, rx);
+    }
+    cp_async_commit();
+  };
   T acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int c = 0; c < 4; ++c) acc[a][c] = T(0);
-  for (int64_t rb = r0; rb < r1; rb += kWgRows) {
-    for (int e = tid; e < kWgRows * kWgTile; e += 256) {
-      const int rr = e / kWgTile, cc = e % kWgTile;
-      const int64_t r = rb + rr;
-      const bool ok = r < r1;
-      As[rr][cc] = (ok && o0 + cc < N) ? Abar[r * N + o0 + cc] : T(0);
-      Xs[rr][cc] = (ok && i0 + cc < Kin) ? X[r * Kin + i0 + cc] : T(0);
+  const int64_t chunks = r1 > r0 ? (r1 - r0 + kWgRows - 1) / kWgRows : 0;
+  if (chunks > 0) stage_copy(r0, 0);
+  for (int64_t ch = 0; ch < chunks; ++ch) {
+    if (ch + 1 < chunks) {
+      stage_copy(r0 + (ch + 1) * kWgRows, (int)((ch + 1) & 1));
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
+    const T* As = smem + (ch & 1) * 2 * kWgRows * kWgLd;
+    const T* Xs = As + kWgRows * kWgLd;
 #pragma unroll 8
     for (int rr = 0; rr < kWgRows; ++rr) {
       T a[4], x[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        a[u] = As[rr][ty * 4 + u];
-        x[u] = Xs[rr][tx * 4 + u];
+        a[u] = As[rr * kWgLd + ty * 4 + u];
+        x[u] = Xs[rr * kWgLd + tx * 4 + u];
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u)
@@ -669,11 +692,17 @@ int launch_mode_gemm(const T* A, int64_t a_mode, const T* W, int64_t w_mode, con
   int dev = 0, sms = 0;
   if (int st = device_sms(&dev, &sms)) return st;
   if (EPI == EPI_OUTPUT && N <= kNarrowCols) {
-    const size_t smem = (size_t)N * Kd * sizeof(T);
-    NEB_REQUIRE(smem <= 48 * 1024, "mode output layer: %d inputs too many", Kd);
-    mode_output_narrow<T, DIM, ORD><<<dim3((unsigned)ceil_div(n, 128), (unsigned)B), 128, smem,
-                                      s>>>(A, a_mode, W, w_mode, bias, b_mode, env, out, o_mode,
-                                           n, Kd, N);
+    const int smem = narrow_smem<T, C>(N, Kd);
+    NEB_REQUIRE(smem <= 200 * 1024, "mode output layer: %d inputs too many", Kd);
+    static int configured_narrow[kMaxDevices] = {};
+    if (configured_narrow[dev] < smem) {
+      NEB_CUDA_CHECK(cudaFuncSetAttribute(mode_output_narrow<T, DIM, ORD>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      configured_narrow[dev] = smem;
+    }
+    mode_output_narrow<T, DIM, ORD>
+        <<<dim3((unsigned)ceil_div(n, kNarrowPts), (unsigned)B), 128, smem, s>>>(
+            A, a_mode, W, w_mode, bias, b_mode, env, out, o_mode, n, Kd, N);
     NEB_LAUNCH_CHECK();
     return NEB_OK;
   }
@@ -763,8 +792,15 @@ int modes_backward_t(const neb_modes* m, int start, int B, const void* const* Wv
     {
       KernelScope ks("mode_weight_grad", s, 2.0 * B * rows * (double)o * in,
                      (double)B * rows * (o + in) * sizeof(T));
-      mode_wgrad<T><<<dim3(tiles, B, splits), 256, 0, s>>>(buf[cur], X, x_mode, rows, o, in, per,
-                                                           part);
+      static bool configured[kMaxDevices] = {};
+      if (!configured[dev]) {
+        NEB_CUDA_CHECK(cudaFuncSetAttribute(mode_wgrad<T>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            mode_wgrad_smem<T>()));
+        configured[dev] = true;
+      }
+      mode_wgrad<T><<<dim3(tiles, B, splits), 256, mode_wgrad_smem<T>(), s>>>(
+          buf[cur], X, x_mode, rows, o, in, per, part);
       NEB_LAUNCH_CHECK();
     }
     {
