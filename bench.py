@@ -358,7 +358,8 @@ def time_velocity(K: int, steps: int, warmup: int, dev, block: int = 256):
     reference's velocity configuration at K modes, CUDA events."""
     import torch
     from types import SimpleNamespace
-    from neb_gb300 import ModeModel, velocity_step
+    from neb_gb300 import ModeModel
+    from neb_gb300.training import velocity_train_step
     c = SimpleNamespace(**{k: REF_VELOCITY[k] for k in ("hidden", "hidden_layers",
                                                        "siren_first_omega0",
                                                        "siren_hidden_omega0")})
@@ -369,9 +370,8 @@ def time_velocity(K: int, steps: int, warmup: int, dev, block: int = 256):
     data = SimpleNamespace(features=feats, envelope=env)
 
     def step():
-        r = velocity_step(model, data, block=block, check=False)
-        model.adam_async(*r["grads"], lr=REF_VELOCITY["lr"], clip=REF_VELOCITY["clip"])
-        return r
+        return velocity_train_step(model, data, REF_VELOCITY["lr"], REF_VELOCITY["clip"],
+                                   block=block)
 
     for _ in range(warmup):
         step()

@@ -257,6 +257,10 @@ int neb_check_status(const neb_net* net, int64_t n_points, void* workspace,
  * device int, read on the device and advanced there only when the update
  * commits, so a rejected step leaves it unchanged without a host
  * synchronisation) or, when step_counter is NULL, the host argument `step`.
+ * gate (device int, may be NULL): the objective's status word; the update
+ * commits only when it is 0 (the physical-validity gate of the reference's
+ * device Adam transaction, HB:2184-2277 physical_valid, HB:3677-3721), so a
+ * failed eigensolve or peel changes nothing without a host round trip.
  * Replaces NCC:156-171 Model.adam (epoch advanced only after a committed
  * update, NCC:157-158, 170) and HB:2184-2277 adam_step_jet1_device.
  * norm_out, committed_out: device pointers (double, int).  One shared
@@ -265,9 +269,9 @@ int neb_check_status(const neb_net* net, int64_t n_points, void* workspace,
 size_t neb_adam_workspace_bytes(void);
 int neb_adam(int dtype, int n_tensors, void* const* params, void* const* exp_avg,
              void* const* exp_avg_sq, const void* const* grads, const int64_t* sizes,
-             int step, int* step_counter, double lr, double clip, double beta1, double beta2,
-             double eps, double* norm_out, int* committed_out, void* workspace,
-             size_t workspace_bytes, neb_stream_t stream);
+             int step, int* step_counter, const int* gate, double lr, double clip,
+             double beta1, double beta2, double eps, double* norm_out, int* committed_out,
+             void* workspace, size_t workspace_bytes, neb_stream_t stream);
 
 /* Self-test of the bounded device-side wait that every tensor-core pipeline
  * uses (no counterpart in the reference, whose CuPy kernels never wait on
@@ -341,13 +345,14 @@ int neb_velocity_lift(int precision, const void* GU, const void* GD, int start, 
  * slice of every tensor (tensors stacked [n_modes][...], sizes[i] elements
  * in total); nothing changes unless every mode's norm is finite and
  * positive; beta1 0.9, beta2 0.999, eps 1e-8 as the reference.
- * *step_counter (device int): committed steps, advanced on commit.
+ * *step_counter (device int): committed steps, advanced on commit.  gate
+ * (device int, may be NULL): commit only when it holds 0, as for neb_adam.
  * norms_out [n_modes] (device double, may be NULL), committed_out (device
  * int, may be NULL). */
 size_t neb_modes_adam_workspace_bytes(int n_modes);
 int neb_modes_adam(int dtype, int n_modes, int n_tensors, void* const* params,
                    void* const* exp_avg, void* const* exp_avg_sq, const void* const* grads,
-                   const int64_t* sizes, int* step_counter, double lr, double clip,
+                   const int64_t* sizes, int* step_counter, const int* gate, double lr, double clip,
                    double* norms_out, int* committed_out, void* workspace,
                    size_t workspace_bytes, neb_stream_t stream);
 

@@ -9,7 +9,9 @@ from .configs import CONFIGS, NebConfig, sample, objective_weights
 from .jets import Jet, pack, unpack
 from .model import Model, SpectralObjective, SpectralResult, spectral_step, train_step
 from .modes import ModeModel, coefficient_peel, velocity_step
+from .training import cosine_learning_rate, train, velocity_train_step
 
 __all__ = ["CONFIGS", "NebConfig", "sample", "objective_weights", "Jet", "pack", "unpack",
            "Model", "SpectralObjective", "SpectralResult", "spectral_step", "train_step",
-           "ModeModel", "coefficient_peel", "velocity_step"]
+           "ModeModel", "coefficient_peel", "velocity_step", "cosine_learning_rate", "train",
+           "velocity_train_step"]

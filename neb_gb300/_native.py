@@ -105,9 +105,9 @@ _SIGNATURES = {
     "neb_check_status": (c_int, [POINTER(NebNet), c_int64, c_void_p, c_size_t, c_void_p]),
     "neb_adam_workspace_bytes": (c_size_t, []),
     "neb_adam": (c_int, [c_int, c_int, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p),
-                         POINTER(c_void_p), POINTER(c_int64), c_int, c_void_p, c_double, c_double,
-                         c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_size_t,
-                         c_void_p]),
+                         POINTER(c_void_p), POINTER(c_int64), c_int, c_void_p, c_void_p, c_double,
+                         c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p,
+                         c_size_t, c_void_p]),
     "neb_wait_selftest": (c_int, [c_int, ctypes.c_uint32, c_void_p, c_void_p]),
     "neb_modes_tape_bytes": (c_size_t, [POINTER(ModeNet), c_int, c_int64]),
     "neb_modes_workspace_bytes": (c_size_t, [POINTER(ModeNet), c_int, c_int64]),
@@ -119,7 +119,7 @@ _SIGNATURES = {
     "neb_velocity_lift": (c_int, [c_int, _P, _P, c_int, c_int, c_int64, c_int, _P, _P]),
     "neb_modes_adam_workspace_bytes": (c_size_t, [c_int]),
     "neb_modes_adam": (c_int, [c_int, c_int, c_int, _PP, _PP, _PP, _PP, POINTER(c_int64), _P,
-                               c_double, c_double, _P, _P, _P, c_size_t, _P]),
+                               _P, c_double, c_double, _P, _P, _P, c_size_t, _P]),
     "neb_column_gram_workspace_bytes": (c_size_t, [c_int64, c_int]),
     "neb_column_gram": (c_int, [c_int, c_int64, c_int, _P, c_double, c_int, _P, _P, c_size_t,
                                 _P]),

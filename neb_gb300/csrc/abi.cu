@@ -834,7 +834,8 @@ extern "C" size_t neb_adam_workspace_bytes(void) { return 256; }
 
 extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* const* m,
                         void* const* v, const void* const* grads, const int64_t* sizes, int step,
-                        int* step_counter, double lr, double clip, double beta1, double beta2,
+                        int* step_counter, const int* gate, double lr, double clip,
+                        double beta1, double beta2,
                         double eps,
                         double* norm_out, int* committed_out, void* ws, size_t ws_bytes,
                         neb_stream_t stream) {
@@ -874,7 +875,7 @@ extern "C" int neb_adam(int dtype, int n_tensors, void* const* params, void* con
   double* scal = (double*)((char*)ws + 128);
   {
     KernelScope ks("adam_update", s, 0, total * es * 7, 2);
-    adam_finalize<<<1, 1, 0, s>>>(acc, flag, clip, step, step_counter, lr, beta1, beta2,
+    adam_finalize<<<1, 1, 0, s>>>(acc, flag, clip, step, step_counter, gate, lr, beta1, beta2,
                                   norm_out, committed_out, scal);
     NEB_LAUNCH_CHECK();
     if (dtype == 0)

@@ -126,7 +126,9 @@ __global__ void adam_norm(AdamTable t, double* __restrict__ acc, int* __restrict
 }
 
 // The transaction's scalars, once: global norm, commit decision (finite
-// gradients and a positive norm, hardcoded_backend.py:2184-2277), the clip
+// gradients, a positive norm and, when given, a zero status word of the
+// objective -- the physical-validity gate of hardcoded_backend.py:2184-2277,
+// 3677-3721), the clip
 // scale min(1, clip / norm) (scal[0] = 0 means "do not commit") and the bias
 // corrections of step t = committed steps + 1 (scal[1] = lr / (1 - beta1^t),
 // scal[2] = 1 / (1 - beta2^t)).  The committed-step count comes from the
@@ -135,11 +137,11 @@ __global__ void adam_norm(AdamTable t, double* __restrict__ acc, int* __restrict
 // native_cupy_core.py:157-170), else from the host argument.
 static __global__ void adam_finalize(const double* __restrict__ acc, const int* __restrict__ flag,
                                      double clip, int host_steps, int* __restrict__ steps,
-                                     double lr, double beta1, double beta2,
-                                     double* __restrict__ norm_out,
+                                     const int* __restrict__ gate, double lr, double beta1,
+                                     double beta2, double* __restrict__ norm_out,
                                      int* __restrict__ committed_out, double* __restrict__ scal) {
   const double norm = sqrt(acc[0]);
-  const bool ok = (flag[0] == 0) && isfinite(norm) && norm > 0.0;
+  const bool ok = (flag[0] == 0) && isfinite(norm) && norm > 0.0 && (!gate || *gate == 0);
   if (norm_out) *norm_out = norm;
   if (committed_out) *committed_out = ok ? 1 : 0;
   const double t = (double)(steps ? *steps : host_steps) + 1.0;

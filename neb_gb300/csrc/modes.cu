@@ -563,14 +563,16 @@ __global__ void mode_adam_norms(ModeAdamTable mt, double* __restrict__ norm2, in
 }
 
 // Commit decision (every mode's norm finite and positive, native_cupy_core.py:
-// 157-158), norms out, per-mode clip scales, bias corrections of step
+// 157-158, and the objective's status word zero when a gate is given),
+// norms out, per-mode clip scales, bias corrections of step
 // *steps + 1, and the step counter advanced on commit.
 __global__ void mode_adam_finalize(const double* __restrict__ norm2, const int* __restrict__ bad,
-                                   int K, double clip, double lr, int* __restrict__ steps,
+                                   const int* __restrict__ gate, int K, double clip, double lr,
+                                   int* __restrict__ steps,
                                    double* __restrict__ norms_out, int* __restrict__ committed,
                                    double* __restrict__ scal, double* __restrict__ scales) {
   __shared__ int ok_all;
-  if (threadIdx.x == 0) ok_all = bad[0] == 0;
+  if (threadIdx.x == 0) ok_all = bad[0] == 0 && (!gate || *gate == 0);
   __syncthreads();
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     const double nm = sqrt(norm2[k]);
@@ -971,7 +973,7 @@ extern "C" size_t neb_modes_adam_workspace_bytes(int n_modes) {
 extern "C" int neb_modes_adam(int dtype, int n_modes, int n_tensors, void* const* params,
                               void* const* exp_avg, void* const* exp_avg_sq,
                               const void* const* grads, const int64_t* sizes, int* step_counter,
-                              double lr, double clip, double* norms_out, int* committed_out,
+                              const int* gate, double lr, double clip, double* norms_out, int* committed_out,
                               void* workspace, size_t workspace_bytes, neb_stream_t stream) {
   NEB_REQUIRE(dtype == 0 || dtype == 1, "neb_modes_adam: dtype must be 0 (float) or 1 (double)");
   NEB_REQUIRE(n_modes > 0 && n_tensors > 0 && n_tensors <= kMaxAdamTensors,
@@ -1013,7 +1015,7 @@ extern "C" int neb_modes_adam(int dtype, int n_modes, int n_tensors, void* const
   }
   {
     KernelScope ks("mode_adam_update", s, 0, total * es * 7, 2);
-    mode_adam_finalize<<<1, 256, 0, s>>>(norm2, bad, n_modes, clip, lr, step_counter, norms_out,
+    mode_adam_finalize<<<1, 256, 0, s>>>(norm2, bad, gate, n_modes, clip, lr, step_counter, norms_out,
                                          committed_out, scal, scales);
     NEB_LAUNCH_CHECK();
     const int blocks = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(total, 256), 1), 2048);

@@ -230,10 +230,12 @@ class Model:
             raise FloatingPointError("Invalid parameter gradients; no optimizer update")
         return float(norm.item())
 
-    def adam_async(self, gW, gb, lr, clip=8.0, beta1=0.9, beta2=0.999, eps=1e-8):
+    def adam_async(self, gW, gb, lr, clip=8.0, beta1=0.9, beta2=0.999, eps=1e-8, gate=None):
         """Adam without a host synchronisation: returns device (norm,
         committed) tensors.  The step counter on the device advances only
-        when the update commits (the caller checks ``committed``)."""
+        when the update commits (the caller checks ``committed``).  ``gate``:
+        a device int status of the objective (e.g. ``SpectralResult.info``);
+        the update commits only when it is 0."""
         params = [*self.W, *self.b]
         grads = [g.to(self.dtype).contiguous() for g in [*gW, *gb]]
         for p, g in zip(params, grads):
@@ -246,7 +248,8 @@ class Model:
         N.call("neb_adam", 1 if self.dtype == torch.float64 else 0, len(params),
                N.ptr_array(params), N.ptr_array([*self.mW, *self.mb]),
                N.ptr_array([*self.vW, *self.vb]), N.ptr_array(grads), sizes, 0,
-               self._steps.data_ptr(), lr, clip, beta1, beta2, eps, norm.data_ptr(),
+               self._steps.data_ptr(), 0 if gate is None else gate.data_ptr(), lr, clip,
+               beta1, beta2, eps, norm.data_ptr(),
                committed.data_ptr(), ws.data_ptr(), ws.numel(), _stream())
         return norm, committed
 
@@ -547,7 +550,9 @@ def train_step(model: Model, points, weights, lr: float | None = None,
     if check:
         model.adam(gW, gb, lr, clip)
     else:
-        model.adam_async(gW, gb, lr, clip)
+        # the solver status gates the update on the device: a failed
+        # eigensolve commits nothing
+        model.adam_async(gW, gb, lr, clip, gate=res.info)
     return res
 
 

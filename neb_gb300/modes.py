@@ -233,9 +233,11 @@ class ModeModel:
             pack_block(adj, self.dim, self.order, self.dtype, self.device)
         return self.backward_packed(cache, a)
 
-    def adam_async(self, gW, gb, lr: float, clip: float = 8.0):
+    def adam_async(self, gW, gb, lr: float, clip: float = 8.0, gate=None):
         """Per-mode Adam without a host synchronisation: device (norms [K],
-        committed) tensors; the epoch counter advances on commit only."""
+        committed) tensors; the epoch counter advances on commit only.
+        ``gate``: a device int status of the objective (the peel's ``info``);
+        the update commits only when it is 0."""
         params = [*self.W, *self.b]
         grads = [g.to(self.dtype).contiguous() for g in [*gW, *gb]]
         for p, g in zip(params, grads):
@@ -249,7 +251,8 @@ class ModeModel:
         N.call("neb_modes_adam", 1 if self.dtype == torch.float64 else 0, self.K, len(params),
                N.ptr_array(params), N.ptr_array([*self.mW, *self.mb]),
                N.ptr_array([*self.vW, *self.vb]), N.ptr_array(grads), sizes,
-               self._steps.data_ptr(), lr, clip, norms.data_ptr(), committed.data_ptr(),
+               self._steps.data_ptr(), 0 if gate is None else gate.data_ptr(), lr, clip,
+               norms.data_ptr(), committed.data_ptr(),
                ws.data_ptr(), ws.numel(), _stream())
         return norms, committed
 

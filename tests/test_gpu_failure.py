@@ -100,3 +100,33 @@ def test_rejected_adam_step_keeps_epoch(asynchronous):
     for (W, b), (rW, rb) in zip(_params64(model), ref):
         np.testing.assert_allclose(W, rW, rtol=2e-6, atol=2e-7)
         np.testing.assert_allclose(b, rb, rtol=2e-6, atol=2e-7)
+
+
+def test_adam_gate_blocks_commit_on_device():
+    """A non-zero objective status word handed to Adam as its gate commits
+    nothing, for the shared network and the per-mode networks alike."""
+    _needs_gpu()
+    from types import SimpleNamespace
+    from neb_gb300 import ModeModel
+    cfg = CONFIGS["periodic_small"].scaled(hidden=16, outputs=8)
+    model = Model(cfg, precision="fp32", seed=4)
+    p0 = _params64(model)
+    _, gW, gb = _grads(model, 1)
+    bad = torch.ones((), dtype=torch.int32, device="cuda")
+    good = torch.zeros((), dtype=torch.int32, device="cuda")
+    _, committed = model.adam_async(gW, gb, 1e-3, gate=bad)
+    assert int(committed.item()) == 0 and model.epoch == 0
+    for (W, b), (rW, rb) in zip(_params64(model), p0):
+        assert np.array_equal(W, rW) and np.array_equal(b, rb)
+    _, committed = model.adam_async(gW, gb, 1e-3, gate=good)
+    assert int(committed.item()) == 1 and model.epoch == 1
+    c = SimpleNamespace(hidden=8, hidden_layers=2, siren_first_omega0=2.0, siren_hidden_omega0=1.5)
+    mm = ModeModel(c, K=3, seed=1, inputs=5, outputs=3)
+    W0 = [w.clone() for w in mm.W]
+    gw = [torch.ones_like(w) for w in mm.W]
+    gbb = [torch.ones_like(x) for x in mm.b]
+    _, committed = mm.adam_async(gw, gbb, 1e-3, gate=bad)
+    assert int(committed.item()) == 0 and mm.epoch == 0
+    assert all(torch.equal(a, b) for a, b in zip(mm.W, W0))
+    _, committed = mm.adam_async(gw, gbb, 1e-3, gate=good)
+    assert int(committed.item()) == 1 and mm.epoch == 1
