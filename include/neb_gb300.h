@@ -119,6 +119,17 @@ int neb_output(const neb_net* net, const void* W_out, const void* b_out, int sta
                int stop, int64_t n_points, const void* tape, void* psi,
                neb_stream_t stream);
 
+/* Envelope jet times output jets (Leibniz rule on the jet channels):
+ * y = e * x (reverse = 0) or the adjoint of x given the adjoint x of the
+ * product (reverse != 0; y may alias x for neither).  envelope: [n][C] one
+ * scalar jet per point; x, y: [n][C][width], the network's master type (use
+ * the FP32 / FP64 evaluation network).  2D uses the Laplacian channel
+ * (lap(e f) = e lap f + f lap e + 2 grad e . grad f), 3D the Hessian.
+ * Replaces NCC:139 product1 and NCC:144 envelope_product_backward_jet1,
+ * VTJ2 product / product_reverse. */
+int neb_envelope_product(const neb_net* net, const void* envelope, int64_t n_points, int width,
+                         const void* x, void* y, int reverse, neb_stream_t stream);
+
 /* 2D scalar potential: weighted Grams of the last hidden layer's field
  * channels, A_M = sum_p w_p (h_x h_x^T + h_y h_y^T), A_S = sum_p w_p h_lap
  * h_lap^T (FP64, [H][H]); per-CTA partial sums, FP64 cross-CTA reduction.

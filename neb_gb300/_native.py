@@ -109,6 +109,8 @@ _SIGNATURES = {
                          c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p,
                          c_size_t, c_void_p]),
     "neb_wait_selftest": (c_int, [c_int, ctypes.c_uint32, c_void_p, c_void_p]),
+    "neb_envelope_product": (c_int, [POINTER(NebNet), c_void_p, c_int64, c_int, c_void_p, c_void_p,
+                                     c_int, c_void_p]),
     "neb_modes_tape_bytes": (c_size_t, [POINTER(ModeNet), c_int, c_int64]),
     "neb_modes_workspace_bytes": (c_size_t, [POINTER(ModeNet), c_int, c_int64]),
     "neb_modes_forward": (c_int, [POINTER(ModeNet), c_int, c_int, _PP, _PP, _P, _P, c_int64, _P,

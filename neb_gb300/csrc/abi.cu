@@ -660,6 +660,35 @@ extern "C" int neb_output(const neb_net* net, const void* Wout, const void* bout
                       (cudaStream_t)stream);
 }
 
+namespace neb {
+namespace {
+template <typename T, int C>
+int envelope_simt(const void* e, const void* x, void* y, int64_t n, int W, int reverse,
+                  cudaStream_t s) {
+  const int64_t total = n * W;
+  KernelScope ks("envelope_jets", s, 0, 2.0 * total * C * sizeof(T));
+  if (reverse)
+    envelope_jets<T, C, true><<<(unsigned)ceil_div(total, 256), 256, 0, s>>>(
+        (const T*)e, (const T*)x, (T*)y, n, W);
+  else
+    envelope_jets<T, C, false><<<(unsigned)ceil_div(total, 256), 256, 0, s>>>(
+        (const T*)e, (const T*)x, (T*)y, n, W);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+}  // namespace
+}  // namespace neb
+
+extern "C" int neb_envelope_product(const neb_net* net, const void* envelope, int64_t n, int width,
+                                    const void* x, void* y, int reverse, neb_stream_t stream) {
+  int st = check_net(net);
+  if (st) return st;
+  NEB_REQUIRE(envelope && x && y && n > 0 && width > 0, "neb_envelope_product: bad arguments");
+  NEB_REQUIRE(net->precision != NEB_PREC_BF16X3,
+              "neb_envelope_product: output jets are FP32 or FP64 (the evaluation network)");
+  return NEB_DISPATCH(net, envelope_simt, envelope, x, y, n, width, reverse, (cudaStream_t)stream);
+}
+
 extern "C" int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n, const void* tape,
                                double* AM, double* AS, void* ws, size_t ws_bytes,
                                neb_stream_t stream) {

@@ -104,3 +104,75 @@ __global__ void fields_adjoint(const T* __restrict__ Fb, T* __restrict__ Pb, int
 }
 
 }  // namespace neb
+
+namespace neb {
+
+// Envelope product of the output jets of the shared network (Leibniz rule
+// on the jet channels; reference: native_cupy_core.py product1,
+// velocity_trace_jet2.py product).  e: [n][C] one scalar jet per point;
+// x, y: [n][C][W].  2D (C = 4, value / d_x / d_y / Laplacian):
+//   lap(e x) = e lap x + x lap e + 2 grad e . grad x;
+// 3D (C = 10, value / gradient / Hessian xx xy xz yy yz zz):
+//   H(e x) = e H x + x H e + grad e grad x^T + grad x grad e^T.
+// REVERSE: y = adjoint of x given the adjoint x of the product.
+template <typename T, int C, bool REVERSE>
+__global__ void envelope_jets(const T* __restrict__ e, const T* __restrict__ x,
+                              T* __restrict__ y, int64_t n, int W) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n * W) return;
+  const int64_t p = i / W;
+  const int k = (int)(i % W);
+  T ev[C], a[C], b[C];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    ev[c] = e[p * C + c];
+    a[c] = x[(p * C + c) * W + k];
+  }
+  if constexpr (C == 4) {
+    if constexpr (!REVERSE) {
+      b[0] = ev[0] * a[0];
+      b[1] = ev[0] * a[1] + ev[1] * a[0];
+      b[2] = ev[0] * a[2] + ev[2] * a[0];
+      b[3] = ev[0] * a[3] + ev[3] * a[0] + T(2) * (ev[1] * a[1] + ev[2] * a[2]);
+    } else {
+      b[0] = ev[0] * a[0] + ev[1] * a[1] + ev[2] * a[2] + ev[3] * a[3];
+      b[1] = ev[0] * a[1] + T(2) * ev[1] * a[3];
+      b[2] = ev[0] * a[2] + T(2) * ev[2] * a[3];
+      b[3] = ev[0] * a[3];
+    }
+  } else {
+    if constexpr (!REVERSE) {
+      b[0] = ev[0] * a[0];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) b[1 + d] = ev[0] * a[1 + d] + ev[1 + d] * a[0];
+#pragma unroll
+      for (int i2 = 0; i2 < 3; ++i2)
+#pragma unroll
+        for (int j2 = i2; j2 < 3; ++j2) {
+          const int q = 4 + hess_slot(i2, j2);
+          b[q] = ev[0] * a[q] + ev[q] * a[0] + ev[1 + i2] * a[1 + j2] + ev[1 + j2] * a[1 + i2];
+        }
+    } else {
+      b[0] = ev[0] * a[0];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        b[0] += ev[1 + d] * a[1 + d];
+        b[1 + d] = ev[0] * a[1 + d];
+      }
+#pragma unroll
+      for (int i2 = 0; i2 < 3; ++i2)
+#pragma unroll
+        for (int j2 = i2; j2 < 3; ++j2) {
+          const int q = 4 + hess_slot(i2, j2);
+          b[0] += ev[q] * a[q];
+          b[1 + i2] += ev[1 + j2] * a[q];
+          b[1 + j2] += ev[1 + i2] * a[q];
+          b[q] = ev[0] * a[q];
+        }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < C; ++c) y[(p * C + c) * W + k] = b[c];
+}
+
+}  // namespace neb

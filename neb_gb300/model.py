@@ -191,17 +191,34 @@ class Model:
     def forward(self, data, start: int = 0, stop: int | None = None, cache: bool = False):
         """Output jets of outputs [start, stop) at ``data.features``.
 
-        ``data.features``: a :class:`Jet` or a packed [n, C, F] tensor.  An
-        ``envelope`` other than the identity is not supported.  Returns
-        ``(field_jet, tape)``; the tape is None unless ``cache``."""
-        _check_identity_envelope(data)
+        ``data.features``: a :class:`Jet` or a packed [n, C, F] tensor;
+        ``data.envelope`` (optional): a scalar :class:`Jet` per point or a
+        packed [n, C] tensor; the output jets are multiplied by it
+        (native_cupy_core.py:139 product1).  Returns ``(field_jet, tape)``;
+        the tape is None unless ``cache``."""
         feats = data.features
         feats = pack(feats, self.c.dim).to(self.device, self.dtype) if isinstance(feats, Jet) else feats
         tape = self.run_forward(feats, self.net_eval)
         if cache:  # keep this tape: later calls must not overwrite it
             tape = Tape(tape.buffer.clone(), tape.n_points, tape.features)
         psi = self.output(tape, start, stop)
+        env = self._envelope(data, tape.n_points)
+        if env is not None:
+            out = torch.empty_like(psi)
+            N.call("neb_envelope_product", ctypes.byref(self.net_eval), env.data_ptr(),
+                   tape.n_points, psi.shape[2], psi.data_ptr(), out.data_ptr(), 0, _stream())
+            psi = out
         return unpack(psi, self.c.dim), (tape if cache else None)
+
+    def _envelope(self, data, n: int):
+        """The envelope of ``data`` as a packed [n, C] device tensor, or None."""
+        env = getattr(data, "envelope", None)
+        if env is None:
+            return None
+        if isinstance(env, Jet):
+            env = pack(env, self.c.dim)
+        env = torch.as_tensor(env).to(self.device, self.dtype).reshape(n, self.channels)
+        return env.contiguous()
 
     def backward(self, data, start: int, stop: int | None, tape: Tape, adj):
         """Parameter gradients of <adj, forward(data, start, stop)> (lists of
@@ -212,6 +229,12 @@ class Model:
             if isinstance(adj, Jet) else adj.to(self.dtype).contiguous()
         if pb.shape != (tape.n_points, self.channels, stop - start):
             raise ValueError(f"adjoint shape {tuple(pb.shape)} does not match the outputs")
+        env = self._envelope(data, tape.n_points)
+        if env is not None:  # adjoint of the raw outputs (envelope_product_backward_jet1)
+            raw = torch.empty_like(pb)
+            N.call("neb_envelope_product", ctypes.byref(self.net_eval), env.data_ptr(),
+                   tape.n_points, pb.shape[2], pb.data_ptr(), raw.data_ptr(), 1, _stream())
+            pb = raw
         gW = [torch.zeros_like(w) for w in self.W]
         gb = [torch.zeros_like(b) for b in self.b]
         ws = self._ws(tape.n_points, self.net_eval)
@@ -269,17 +292,6 @@ class Model:
             for name in ("W", "b", "mW", "vW", "mb", "vb"):
                 for j, a in enumerate(getattr(self, name)):
                     a.copy_(torch.as_tensor(z[f"{name}_{j}"], dtype=self.dtype))
-
-
-def _check_identity_envelope(data) -> None:
-    env = getattr(data, "envelope", None)
-    if env is None:
-        return
-    v = env.value if isinstance(env, Jet) else torch.as_tensor(env)
-    g = env.grad if isinstance(env, Jet) else None
-    ok = bool(torch.all(torch.as_tensor(v) == 1)) and (g is None or bool(torch.all(torch.as_tensor(g) == 0)))
-    if not ok:
-        raise ValueError("only the identity envelope (periodic / free domains) is supported")
 
 
 # ----------------------------------------------------------------- spectral
