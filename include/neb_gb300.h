@@ -352,20 +352,38 @@ int neb_velocity_fields(int precision, const void* out, int start, int stop, int
 int neb_velocity_lift(int precision, const void* GU, const void* GD, int start, int stop,
                       int64_t n_points, int n_modes, void* adjoint, neb_stream_t stream);
 
-/* Per-mode Adam (NCC:156-171): the clip norm of mode k runs over mode k's
- * slice of every tensor (tensors stacked [n_modes][...], sizes[i] elements
- * in total); nothing changes unless every mode's norm is finite and
- * positive; beta1 0.9, beta2 0.999, eps 1e-8 as the reference.
- * *step_counter (device int): committed steps, advanced on commit.  gate
- * (device int, may be NULL): commit only when it holds 0, as for neb_adam.
- * norms_out [n_modes] (device double, may be NULL), committed_out (device
- * int, may be NULL). */
+/* 2D scalar potential of one output per mode with first-order jets (the
+ * periodic backend's streamfunction, HB:3455-3460): value of modes
+ * [start, stop) into columns of V [n][n_modes], gradient into G [2n][n_modes]
+ * (rows p*2 + a); and the adjoint: dV, dG -> output-jet adjoints
+ * [stop-start][n][3][1].  neb_column_center subtracts each column's mean
+ * over the rows (the mean-zero gauge, HB:3461-3465, and its transpose,
+ * HB:3579-3583), FP64 sums. */
+int neb_potential_fields(int precision, const void* out, int start, int stop, int64_t n_points,
+                         int n_modes, void* V, void* G, neb_stream_t stream);
+int neb_potential_lift(int precision, const void* dV, const void* dG, int start, int stop,
+                       int64_t n_points, int n_modes, void* adjoint, neb_stream_t stream);
+int neb_column_center(int precision, int64_t rows, int K, void* A, neb_stream_t stream);
+
+/* Per-mode Adam (NCC:156-171 Model.adam; HB:2184-2277 adam_step_jet1_device):
+ * the clip norm of mode k runs over mode k's slice of every tensor (tensors
+ * stacked [n_modes][...], sizes[i] elements in total); beta1 0.9, beta2
+ * 0.999, eps 1e-8 as the reference.  The transaction commits only when the
+ * gate (device int, may be NULL: the objective's status word) is 0 and
+ * every active mode's norm is finite and positive; then the active modes
+ * update (active: device int [n_modes], may be NULL = all) and nothing else
+ * changes.  step_counter (device int): the committed steps, one shared count
+ * (steps_per_mode = 0, NCC's epoch) or one per mode ([n_modes],
+ * steps_per_mode = 1, HB's per-mode counts); the updated modes' counts
+ * advance.  norms_out [n_modes] (device double, may be NULL), committed_out
+ * (device int, may be NULL). */
 size_t neb_modes_adam_workspace_bytes(int n_modes);
 int neb_modes_adam(int dtype, int n_modes, int n_tensors, void* const* params,
                    void* const* exp_avg, void* const* exp_avg_sq, const void* const* grads,
-                   const int64_t* sizes, int* step_counter, const int* gate, double lr, double clip,
-                   double* norms_out, int* committed_out, void* workspace,
-                   size_t workspace_bytes, neb_stream_t stream);
+                   const int64_t* sizes, int* step_counter, int steps_per_mode, const int* active,
+                   const int* gate, double lr, double clip, double* norms_out,
+                   int* committed_out, void* workspace, size_t workspace_bytes,
+                   neb_stream_t stream);
 
 /* G = scale A^T A (FP64, K x K) of the columns of A [rows][K] (FP32 or
  * FP64, row-major), per-chunk partials reduced in FP64; compensated != 0
@@ -385,17 +403,22 @@ int neb_column_apply(int precision, int64_t rows, int K, const void* A, const do
                      neb_stream_t stream);
 
 /* Causal Rayleigh peel in Gram form, FP64 (VC:48-69 coefficient_peel):
- * order = stable ascending sort of S_kk / M_kk; the sorted M orthonormalised
+ * order = stable ascending sort of S_kk / M_kk when sort != 0 (the
+ * reference's geometry_rayleigh sorting), the identity when sort == 0 (its
+ * fixed_order, HB:3471-3475); the ordered M orthonormalised
  * by a scaled Cholesky factor applied twice (T with T^T M_sorted T = I);
  * losses[r] = (T^T S_sorted T)_rr in causal order; T_out [K][K] row-major
  * with rows in mode order; Cu, Cd [K][K] with dL/dU = U Cu / n and
  * dL/dD = D Cd / n for L = sum(losses); relative_mass[r] and ortho_error
  * (device, may be NULL).  info (device int): 0 ok, 1 a Cholesky factor
- * failed (rank), 2 the reference's gate failed (a non-finite or
- * non-positive loss, relative mass below 1e-4, orthogonality error above
- * 1e-5).  No host synchronisation. */
+ * failed (rank), 2 the gate failed: with mass_floor <= 0 the gate of VC:60-62
+ * (a non-finite or non-positive loss, relative mass below 1e-4,
+ * orthogonality error above 1e-5), with mass_floor > 0 the gate of the 2D
+ * peel, HB:3555-3567 (a non-finite value, a raw or peeled mass at or below
+ * the floor).  No host synchronisation. */
 size_t neb_peel_workspace_bytes(int K);
-int neb_coefficient_peel(int K, const double* M, const double* S, double* losses, int* order,
+int neb_coefficient_peel(int K, const double* M, const double* S, double mass_floor,
+                         int sort, double* losses, int* order,
                          double* T_out, double* Cu, double* Cd, double* relative_mass,
                          double* ortho_error, int* info, void* workspace,
                          size_t workspace_bytes, neb_stream_t stream);

@@ -9,9 +9,11 @@ from .configs import CONFIGS, NebConfig, sample, objective_weights
 from .jets import Jet, pack, unpack
 from .model import Model, SpectralObjective, SpectralResult, spectral_step, train_step
 from .modes import ModeModel, coefficient_peel, velocity_step
+from .hardcoded import HardcodedModel
+from . import hardcoded
 from .training import cosine_learning_rate, train, velocity_train_step
 
 __all__ = ["CONFIGS", "NebConfig", "sample", "objective_weights", "Jet", "pack", "unpack",
            "Model", "SpectralObjective", "SpectralResult", "spectral_step", "train_step",
            "ModeModel", "coefficient_peel", "velocity_step", "cosine_learning_rate", "train",
-           "velocity_train_step"]
+           "velocity_train_step", "HardcodedModel", "hardcoded"]

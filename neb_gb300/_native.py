@@ -119,17 +119,20 @@ _SIGNATURES = {
                                    _PP, _PP, c_int, _P, c_size_t, _P]),
     "neb_velocity_fields": (c_int, [c_int, _P, c_int, c_int, c_int64, c_int, _P, _P, _P]),
     "neb_velocity_lift": (c_int, [c_int, _P, _P, c_int, c_int, c_int64, c_int, _P, _P]),
+    "neb_potential_fields": (c_int, [c_int, _P, c_int, c_int, c_int64, c_int, _P, _P, _P]),
+    "neb_potential_lift": (c_int, [c_int, _P, _P, c_int, c_int, c_int64, c_int, _P, _P]),
+    "neb_column_center": (c_int, [c_int, c_int64, c_int, _P, _P]),
     "neb_modes_adam_workspace_bytes": (c_size_t, [c_int]),
     "neb_modes_adam": (c_int, [c_int, c_int, c_int, _PP, _PP, _PP, _PP, POINTER(c_int64), _P,
-                               _P, c_double, c_double, _P, _P, _P, c_size_t, _P]),
+                               c_int, _P, _P, c_double, c_double, _P, _P, _P, c_size_t, _P]),
     "neb_column_gram_workspace_bytes": (c_size_t, [c_int64, c_int]),
     "neb_column_gram": (c_int, [c_int, c_int64, c_int, _P, c_double, c_int, _P, _P, c_size_t,
                                 _P]),
     "neb_column_apply_workspace_bytes": (c_size_t, [c_int64, c_int]),
     "neb_column_apply": (c_int, [c_int, c_int64, c_int, _P, _P, c_double, _P, _P, c_size_t, _P]),
     "neb_peel_workspace_bytes": (c_size_t, [c_int]),
-    "neb_coefficient_peel": (c_int, [c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, c_size_t,
-                                     _P]),
+    "neb_coefficient_peel": (c_int, [c_int, _P, _P, c_double, c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                     c_size_t, _P]),
 }
 
 EXPORTED = tuple(_SIGNATURES)

@@ -25,6 +25,7 @@
 //   mode_envelope_reverse, velocity_fields, velocity_lift (3D curl fields of
 //   a vector potential), and the per-mode Adam transaction.
 #include <algorithm>
+#include <math_constants.h>
 #include "neb_common.cuh"
 #include "elementwise.cuh"
 
@@ -528,6 +529,53 @@ __global__ void velocity_lift(const T* __restrict__ GU, const T* __restrict__ GD
     for (int k = 0; k < 3; ++k) dst[c * 3 + k] = a[c][k];
 }
 
+// 2D scalar potential of one output per mode, first-order jets: the value
+// into V[p][col] and the gradient into G[(p*2 + a)][col], col = mode0 + b
+// (hardcoded_backend.py:3455-3460 raw_value / raw_gradient columns).
+template <typename T>
+__global__ void potential_fields(const T* __restrict__ out, int B, int n, int K, int mode0,
+                                 T* __restrict__ V, T* __restrict__ G) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)B * n) return;
+  const int mb = (int)(i / n), p = (int)(i % n), col = mode0 + mb;
+  const T* o = out + ((int64_t)mb * n + p) * 3;  // [3][1] of this point
+  V[(int64_t)p * K + col] = o[0];
+  G[((int64_t)p * 2) * K + col] = o[1];
+  G[((int64_t)p * 2 + 1) * K + col] = o[2];
+}
+
+// Adjoint of potential_fields: dV, dG -> output-jet adjoints [B][n][3][1].
+template <typename T>
+__global__ void potential_lift(const T* __restrict__ dV, const T* __restrict__ dG, int B, int n,
+                               int K, int mode0, T* __restrict__ adj) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)B * n) return;
+  const int mb = (int)(i / n), p = (int)(i % n), col = mode0 + mb;
+  T* a = adj + ((int64_t)mb * n + p) * 3;
+  a[0] = dV[(int64_t)p * K + col];
+  a[1] = dG[((int64_t)p * 2) * K + col];
+  a[2] = dG[((int64_t)p * 2 + 1) * K + col];
+}
+
+// A[r][k] -= mean over rows of column k (one block of 256 threads per
+// column, FP64 sums): the sample-wise mean-zero gauge of the streamfunction
+// (hardcoded_backend.py:3461-3465) and, applied to an adjoint, its transpose
+// (:3579-3583).
+template <typename T>
+__global__ void column_center(T* __restrict__ A, int64_t rows, int K) {
+  __shared__ double red[8];
+  const int k = blockIdx.x;
+  double s = 0.0;
+  for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) s += (double)A[r * K + k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  double tot = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+  const T mean = (T)(tot / (double)rows);
+  for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) A[r * K + k] -= mean;
+}
+
 // ------------------------------------------------------- per-mode Adam
 // Tensors are stacked [K][...]; per_mode[t] elements of tensor t per mode.
 struct ModeAdamTable {
@@ -535,25 +583,25 @@ struct ModeAdamTable {
   int64_t per_mode[kMaxAdamTensors];
 };
 
-// norm2[k] = sum over tensors of |g_k|^2 (one block per mode), bad |= non-finite
+// norm2[k] = sum over tensors of |g_k|^2 (one block per mode); a non-finite
+// gradient makes the mode's norm non-finite.
 template <typename T>
-__global__ void mode_adam_norms(ModeAdamTable mt, double* __restrict__ norm2, int* __restrict__ bad) {
+__global__ void mode_adam_norms(ModeAdamTable mt, double* __restrict__ norm2) {
   __shared__ double red[32];
   const int k = blockIdx.x;
   double s = 0.0;
-  int nf = 0;
+  bool nf = false;
   for (int ti = 0; ti < mt.t.n; ++ti) {
     const T* g = static_cast<const T*>(mt.t.g[ti]) + (int64_t)k * mt.per_mode[ti];
     for (int64_t i = threadIdx.x; i < mt.per_mode[ti]; i += blockDim.x) {
       const double v = (double)g[i];
-      if (!isfinite(v)) nf = 1;
+      if (!isfinite(v)) nf = true;
       s += v * v;
     }
   }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   nf = __any_sync(0xffffffffu, nf);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  if (nf && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nf ? CUDART_NAN : s;
   __syncthreads();
   if (threadIdx.x < 32) {
     double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
@@ -562,50 +610,61 @@ __global__ void mode_adam_norms(ModeAdamTable mt, double* __restrict__ norm2, in
   }
 }
 
-// Commit decision (every mode's norm finite and positive, native_cupy_core.py:
-// 157-158, and the objective's status word zero when a gate is given),
-// norms out, per-mode clip scales, bias corrections of step
-// *steps + 1, and the step counter advanced on commit.
-__global__ void mode_adam_finalize(const double* __restrict__ norm2, const int* __restrict__ bad,
-                                   const int* __restrict__ gate, int K, double clip, double lr,
-                                   int* __restrict__ steps,
-                                   double* __restrict__ norms_out, int* __restrict__ committed,
-                                   double* __restrict__ scal, double* __restrict__ scales) {
+// The transaction: commit when the objective's gate (if any) is 0 and
+// every active mode's norm is finite and positive (native_cupy_core.py:
+// 157-158; hardcoded_backend.py:2204-2212 with its active-mode mask).  Per
+// mode: norms out, the clip scale (0 for a mode left unchanged) and the
+// bias corrections of its step t = steps + 1, where steps is one shared
+// count (per_mode = 0) or one count per mode; the counts of the updated
+// modes advance.  par[k] = (scale, lr / (1 - 0.9^t), 1 / (1 - 0.999^t)).
+__global__ void mode_adam_finalize(const double* __restrict__ norm2,
+                                   const int* __restrict__ gate, const int* __restrict__ active,
+                                   int K, double clip, double lr, int* __restrict__ steps,
+                                   int per_mode, double* __restrict__ norms_out,
+                                   int* __restrict__ committed, double* __restrict__ par) {
   __shared__ int ok_all;
-  if (threadIdx.x == 0) ok_all = bad[0] == 0 && (!gate || *gate == 0);
+  if (threadIdx.x == 0) ok_all = !gate || *gate == 0;
   __syncthreads();
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     const double nm = sqrt(norm2[k]);
     if (norms_out) norms_out[k] = nm;
-    if (!(isfinite(nm) && nm > 0.0)) atomicAnd(&ok_all, 0);
-    scales[k] = fmin(1.0, clip / fmax(nm, 1e-30));
+    const bool act = !active || active[k] != 0;
+    if (act && !(isfinite(nm) && nm > 0.0)) atomicAnd(&ok_all, 0);
   }
   __syncthreads();
+  const bool ok = ok_all != 0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    const double nm = sqrt(norm2[k]);
+    const bool upd = ok && (!active || active[k] != 0);
+    const double t = (double)(per_mode ? steps[k] : steps[0]) + 1.0;
+    par[3 * k] = upd ? fmin(1.0, clip / fmax(nm, 1e-30)) : 0.0;
+    par[3 * k + 1] = lr / (1.0 - pow(0.9, t));
+    par[3 * k + 2] = 1.0 / (1.0 - pow(0.999, t));
+  }
+  __syncthreads();  // every thread has read the step counts
+  for (int k = threadIdx.x; k < K; k += blockDim.x)
+    if (per_mode && ok && (!active || active[k] != 0)) steps[k] += 1;
   if (threadIdx.x == 0) {
-    const double t = (double)(*steps) + 1.0;
-    scal[0] = ok_all ? 1.0 : 0.0;
-    scal[1] = lr / (1.0 - pow(0.9, t));
-    scal[2] = 1.0 / (1.0 - pow(0.999, t));
-    if (committed) *committed = ok_all;
-    if (ok_all) *steps += 1;
+    if (committed) *committed = ok;
+    if (!per_mode && ok) steps[0] += 1;
   }
 }
 
 template <typename T>
-__global__ void mode_adam_update(ModeAdamTable mt, const double* __restrict__ scal,
-                                 const double* __restrict__ scales) {
-  if (scal[0] == 0.0) return;
-  const T lr_c1 = (T)scal[1], inv_c2 = (T)scal[2];
+__global__ void mode_adam_update(ModeAdamTable mt, const double* __restrict__ par) {
   const int64_t total = mt.t.off[mt.t.n];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int ti = adam_find(mt.t, i);
     const int64_t j = i - mt.t.off[ti];
     const int k = (int)(j / mt.per_mode[ti]);
+    const double sc = par[3 * k];
+    if (sc == 0.0) continue;  // mode not updated
+    const T lr_c1 = (T)par[3 * k + 1], inv_c2 = (T)par[3 * k + 2];
     T* p = static_cast<T*>(mt.t.p[ti]);
     T* m = static_cast<T*>(mt.t.m[ti]);
     T* v = static_cast<T*>(mt.t.v[ti]);
-    const T g = static_cast<const T*>(mt.t.g[ti])[j] * (T)scales[k];
+    const T g = static_cast<const T*>(mt.t.g[ti])[j] * (T)sc;
     const T mn = T(0.9) * m[j] + T(0.1) * g;
     const T vn = T(0.999) * v[j] + T(0.001) * g * g;
     m[j] = mn;
@@ -966,15 +1025,75 @@ extern "C" int neb_velocity_lift(int precision, const void* GU, const void* GD, 
   return NEB_OK;
 }
 
+extern "C" int neb_potential_fields(int precision, const void* out, int start, int stop,
+                                    int64_t n_points, int n_modes, void* V, void* G,
+                                    neb_stream_t stream) {
+  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64,
+              "neb_potential_fields: FP32 or FP64");
+  NEB_REQUIRE(out && V && G && n_points > 0 && 0 <= start && start < stop && stop <= n_modes,
+              "neb_potential_fields: bad arguments");
+  const int B = stop - start;
+  const int64_t total = (int64_t)B * n_points;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t es = precision == NEB_PREC_FP64 ? 8 : 4;
+  KernelScope ks("potential_fields", s, 0, (double)total * 6 * es);
+  if (precision == NEB_PREC_FP64)
+    potential_fields<double><<<(int)ceil_div(total, 256), 256, 0, s>>>(
+        (const double*)out, B, (int)n_points, n_modes, start, (double*)V, (double*)G);
+  else
+    potential_fields<float><<<(int)ceil_div(total, 256), 256, 0, s>>>(
+        (const float*)out, B, (int)n_points, n_modes, start, (float*)V, (float*)G);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+extern "C" int neb_potential_lift(int precision, const void* dV, const void* dG, int start,
+                                  int stop, int64_t n_points, int n_modes, void* adjoint,
+                                  neb_stream_t stream) {
+  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64,
+              "neb_potential_lift: FP32 or FP64");
+  NEB_REQUIRE(dV && dG && adjoint && n_points > 0 && 0 <= start && start < stop &&
+                  stop <= n_modes,
+              "neb_potential_lift: bad arguments");
+  const int B = stop - start;
+  const int64_t total = (int64_t)B * n_points;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t es = precision == NEB_PREC_FP64 ? 8 : 4;
+  KernelScope ks("potential_lift", s, 0, (double)total * 6 * es);
+  if (precision == NEB_PREC_FP64)
+    potential_lift<double><<<(int)ceil_div(total, 256), 256, 0, s>>>(
+        (const double*)dV, (const double*)dG, B, (int)n_points, n_modes, start, (double*)adjoint);
+  else
+    potential_lift<float><<<(int)ceil_div(total, 256), 256, 0, s>>>(
+        (const float*)dV, (const float*)dG, B, (int)n_points, n_modes, start, (float*)adjoint);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+extern "C" int neb_column_center(int precision, int64_t rows, int K, void* A,
+                                 neb_stream_t stream) {
+  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64,
+              "neb_column_center: FP32 or FP64");
+  NEB_REQUIRE(A && rows > 0 && K > 0, "neb_column_center: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  KernelScope ks("column_center", s, 0, 2.0 * rows * K * (precision == NEB_PREC_FP64 ? 8 : 4));
+  if (precision == NEB_PREC_FP64) column_center<double><<<K, 256, 0, s>>>((double*)A, rows, K);
+  else column_center<float><<<K, 256, 0, s>>>((float*)A, rows, K);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
 extern "C" size_t neb_modes_adam_workspace_bytes(int n_modes) {
-  return n_modes <= 0 ? 0 : 512 + 2 * a256((size_t)n_modes * sizeof(double));
+  return n_modes <= 0 ? 0 : a256((size_t)n_modes * sizeof(double)) +
+                                a256((size_t)3 * n_modes * sizeof(double));
 }
 
 extern "C" int neb_modes_adam(int dtype, int n_modes, int n_tensors, void* const* params,
                               void* const* exp_avg, void* const* exp_avg_sq,
                               const void* const* grads, const int64_t* sizes, int* step_counter,
-                              const int* gate, double lr, double clip, double* norms_out, int* committed_out,
-                              void* workspace, size_t workspace_bytes, neb_stream_t stream) {
+                              int steps_per_mode, const int* active, const int* gate, double lr,
+                              double clip, double* norms_out, int* committed_out, void* workspace,
+                              size_t workspace_bytes, neb_stream_t stream) {
   NEB_REQUIRE(dtype == 0 || dtype == 1, "neb_modes_adam: dtype must be 0 (float) or 1 (double)");
   NEB_REQUIRE(n_modes > 0 && n_tensors > 0 && n_tensors <= kMaxAdamTensors,
               "neb_modes_adam: 1..%d tensors of at least one mode", kMaxAdamTensors);
@@ -1000,27 +1119,24 @@ extern "C" int neb_modes_adam(int dtype, int n_modes, int n_tensors, void* const
   }
   cudaStream_t s = (cudaStream_t)stream;
   char* ws = (char*)workspace;
-  int* bad = (int*)ws;
-  double* scal = (double*)(ws + 256);
-  double* norm2 = (double*)(ws + 512);
-  double* scales = (double*)(ws + 512 + a256((size_t)n_modes * sizeof(double)));
-  NEB_CUDA_CHECK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  double* norm2 = (double*)ws;
+  double* par = (double*)(ws + a256((size_t)n_modes * sizeof(double)));
   const int64_t total = mt.t.off[n_tensors];
   const double es = dtype == 0 ? 4.0 : 8.0;
   {
     KernelScope ks("mode_adam_norms", s, 0, total * es);
-    if (dtype == 0) mode_adam_norms<float><<<n_modes, 256, 0, s>>>(mt, norm2, bad);
-    else mode_adam_norms<double><<<n_modes, 256, 0, s>>>(mt, norm2, bad);
+    if (dtype == 0) mode_adam_norms<float><<<n_modes, 256, 0, s>>>(mt, norm2);
+    else mode_adam_norms<double><<<n_modes, 256, 0, s>>>(mt, norm2);
     NEB_LAUNCH_CHECK();
   }
   {
     KernelScope ks("mode_adam_update", s, 0, total * es * 7, 2);
-    mode_adam_finalize<<<1, 256, 0, s>>>(norm2, bad, gate, n_modes, clip, lr, step_counter, norms_out,
-                                         committed_out, scal, scales);
+    mode_adam_finalize<<<1, 256, 0, s>>>(norm2, gate, active, n_modes, clip, lr, step_counter,
+                                         steps_per_mode ? 1 : 0, norms_out, committed_out, par);
     NEB_LAUNCH_CHECK();
     const int blocks = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(total, 256), 1), 2048);
-    if (dtype == 0) mode_adam_update<float><<<blocks, 256, 0, s>>>(mt, scal, scales);
-    else mode_adam_update<double><<<blocks, 256, 0, s>>>(mt, scal, scales);
+    if (dtype == 0) mode_adam_update<float><<<blocks, 256, 0, s>>>(mt, par);
+    else mode_adam_update<double><<<blocks, 256, 0, s>>>(mt, par);
     NEB_LAUNCH_CHECK();
   }
   return NEB_OK;

@@ -55,7 +55,7 @@ size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
   } while (0)
 
 // raw_i = S_ii / M_ii (a non-finite quotient sorts last); stable ascending
-// ranks; order[rank] = i.
+// ranks; order[rank] = i (peel_rank).
 __global__ void peel_order(const double* __restrict__ M, const double* __restrict__ S, int K,
                            int* __restrict__ order, double* __restrict__ raw) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
@@ -76,6 +76,11 @@ __global__ void peel_rank(const double* __restrict__ raw, int K, int* __restrict
     }
     order[rank] = i;
   }
+}
+
+__global__ void peel_fixed_order(int K, int* __restrict__ order) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x)
+    order[i] = i;
 }
 
 // ms = M[order][order], ss = S[order][order], scale = sqrt(diag ms),
@@ -126,11 +131,16 @@ __global__ void symmetrize(double* __restrict__ X, int K) {
   }
 }
 
-// Gate of core.py:60-62 and the per-rank scalars: losses = diag F,
-// norm = 1 / diag T, relative = norm^2 / diag ms, error = max |O - I|;
-// Fu = strict upper triangle of F (in place).  info: 0 ok, 2 gate failed.
+// Gate and the per-rank scalars: losses = diag F, norm = 1 / diag T (the
+// peeled mass is norm^2), relative = norm^2 / diag ms, error = max |O - I|;
+// Fu = strict upper triangle of F (in place).  mass_floor <= 0: the gate of
+// velocity/core.py:60-62 (finite positive losses, relative mass >= 1e-4,
+// orthogonality error <= 1e-5); mass_floor > 0: the gate of
+// hardcoded_backend.py:3555-3567 (finite values, raw and peeled masses above
+// the floor).  info: 0 ok, 2 gate failed.
 __global__ void peel_gate(const double* __restrict__ T, const double* __restrict__ ms,
                           const double* __restrict__ O, double* __restrict__ F, int K,
+                          double mass_floor,
                           double* __restrict__ loss, double* __restrict__ norm,
                           double* __restrict__ relative, double* __restrict__ error,
                           int* __restrict__ info) {
@@ -150,7 +160,12 @@ __global__ void peel_gate(const double* __restrict__ T, const double* __restrict
     loss[i] = l;
     norm[i] = nm;
     relative[i] = rel;
-    if (!(isfinite(l) && l > 0.0 && rel >= 1e-4)) atomicOr(&bad, 1);
+    const double m = ms[(int64_t)i * K + i];
+    const bool ok = mass_floor > 0.0
+                        ? (isfinite(l) && isfinite(m) && m > mass_floor && isfinite(nm) &&
+                           nm * nm > mass_floor)
+                        : (isfinite(l) && l > 0.0 && rel >= 1e-4);
+    if (!ok) atomicOr(&bad, 1);
   }
   for (int o = 16; o > 0; o >>= 1) e = fmax(e, __shfl_down_sync(0xffffffffu, e, o));
   if ((threadIdx.x & 31) == 0) emax[threadIdx.x >> 5] = e;
@@ -159,7 +174,8 @@ __global__ void peel_gate(const double* __restrict__ T, const double* __restrict
     double m = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, emax[w]);
     *error = m;
-    if ((!(m <= 1e-5) || bad) && *info == 0) *info = 2;
+    const bool ortho_bad = mass_floor > 0.0 ? !(m == m) : !(m <= 1e-5);
+    if ((ortho_bad || bad) && *info == 0) *info = 2;
   }
   __syncthreads();
   // strict upper triangle of F for C = T diag(loss) + T triu(F, 1)
@@ -218,7 +234,8 @@ extern "C" size_t neb_peel_workspace_bytes(int K) {
   return 8 * kk + 5 * k1 + a256(sizeof(int) * 2) + a256((size_t)lwork * sizeof(double));
 }
 
-extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, double* losses,
+extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, double mass_floor,
+                                    int sort, double* losses,
                                     int* order, double* T_out, double* Cu, double* Cd,
                                     double* relative_mass, double* ortho_error, int* info,
                                     void* workspace, size_t workspace_bytes,
@@ -266,7 +283,8 @@ extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, dou
     KernelScope ks("peel_order", s, 0, 8.0 * K * K);
     peel_order<<<grid_for(K), 256, 0, s>>>(M, S, K, order, raw);
     NEB_LAUNCH_CHECK();
-    peel_rank<<<grid_for(K), 256, 0, s>>>(raw, K, order);
+    if (sort) peel_rank<<<grid_for(K), 256, 0, s>>>(raw, K, order);
+    else peel_fixed_order<<<grid_for(K), 256, 0, s>>>(K, order);
     NEB_LAUNCH_CHECK();
     peel_gather<<<grid_for(kk_n), 256, 0, s>>>(M, S, order, K, ms, ss, L, scale);
     NEB_LAUNCH_CHECK();
@@ -317,7 +335,7 @@ extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, dou
              "cublasDgemm (ss T)");
     NEB_BLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, K, K, K, &one, T, K, W1, K, &zero, F, K),
              "cublasDgemm (T^T ss T)");
-    peel_gate<<<1, 1024, 0, s>>>(T, ms, L, F, K, losses, norm, rel, err, info);
+    peel_gate<<<1, 1024, 0, s>>>(T, ms, L, F, K, mass_floor, losses, norm, rel, err, info);
     NEB_LAUNCH_CHECK();
     NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, T, K, F, K, &zero, TF, K),
              "cublasDgemm (T triu(F))");

@@ -251,7 +251,7 @@ class ModeModel:
         N.call("neb_modes_adam", 1 if self.dtype == torch.float64 else 0, self.K, len(params),
                N.ptr_array(params), N.ptr_array([*self.mW, *self.mb]),
                N.ptr_array([*self.vW, *self.vb]), N.ptr_array(grads), sizes,
-               self._steps.data_ptr(), 0 if gate is None else gate.data_ptr(), lr, clip,
+               self._steps.data_ptr(), 0, 0, 0 if gate is None else gate.data_ptr(), lr, clip,
                norms.data_ptr(), committed.data_ptr(),
                ws.data_ptr(), ws.numel(), _stream())
         return norms, committed
@@ -296,10 +296,14 @@ class PeelResult:
     info: torch.Tensor         # 0 ok, 1 rank (Cholesky), 2 gate
 
 
-def coefficient_peel(M: torch.Tensor, S: torch.Tensor, check: bool = True) -> PeelResult:
+def coefficient_peel(M: torch.Tensor, S: torch.Tensor, check: bool = True,
+                     mass_floor: float = 0.0, sort: bool = True) -> PeelResult:
     """Causal Rayleigh peel in Gram form on the device (velocity/core.py:48-69);
     ``check`` reads the status back and raises FloatingPointError where the
-    reference's gate fails."""
+    reference's gate fails (``mass_floor`` > 0: the 2D peel's gate,
+    hardcoded_backend.py:3555-3567, instead of velocity/core.py:60-62);
+    ``sort`` False keeps the modes in network order (the 2D peel's
+    fixed_order, hardcoded_backend.py:3471-3475)."""
     K = M.shape[0]
     dev = M.device
     M = M.to(torch.float64).contiguous()
@@ -311,7 +315,8 @@ def coefficient_peel(M: torch.Tensor, S: torch.Tensor, check: bool = True) -> Pe
                    torch.zeros((), dtype=torch.int32, device=dev))
     lib = N.load()
     ws = torch.empty(max(lib.neb_peel_workspace_bytes(K), 256), dtype=torch.uint8, device=dev)
-    N.call("neb_coefficient_peel", K, M.data_ptr(), S.data_ptr(), r.losses.data_ptr(),
+    N.call("neb_coefficient_peel", K, M.data_ptr(), S.data_ptr(), float(mass_floor), int(sort),
+           r.losses.data_ptr(),
            r.order.data_ptr(), r.T.data_ptr(), r.Cu.data_ptr(), r.Cd.data_ptr(),
            r.relative_mass.data_ptr(), r.gram_max.data_ptr(), r.info.data_ptr(), ws.data_ptr(),
            ws.numel(), _stream())

@@ -738,9 +738,11 @@ def velocity_lift(GU, GD):
     return A
 
 
-def coefficient_peel(M, S):
+def coefficient_peel(M, S, sort=True):
     """Causal Rayleigh peel in Gram form (core.py:48-69): modes sorted by
-    their raw quotients S_kk / M_kk (stable), the sorted mass matrix
+    their raw quotients S_kk / M_kk (stable; with ``sort`` False the network
+    order, the 2D peel's fixed_order, hardcoded_backend.py:3471-3475), the
+    sorted mass matrix
     orthonormalised by a scaled Cholesky factor applied twice (the Gram form
     of two-pass modified Gram-Schmidt), losses = diag(T^T S T).  Returns the
     losses in causal order, the order, the transform T (rows in mode order),
@@ -749,7 +751,7 @@ def coefficient_peel(M, S):
     the reference's rank / relative-mass / orthogonality gate fails."""
     K = len(M)
     raw = np.diag(S) / np.diag(M)
-    order = np.argsort(raw, kind="stable")
+    order = np.argsort(raw, kind="stable") if sort else np.arange(K)
     ms = M[np.ix_(order, order)]
     ss = S[np.ix_(order, order)]
     scale = np.sqrt(np.diag(ms))
@@ -810,4 +812,57 @@ def velocity_step(W, b, X0, E, omegas, want_grad=True):
                 gW[j][k] = gwk[j]
                 gb[j][k] = gbk[j]
         obj["grads"] = (gW, gb)
+    return obj
+
+
+def potential_peel_step(W, b, X0, weight, omegas, lr=None, clip=8.0, moments=None, epoch=0,
+                        sort=True):
+    """The periodic 2D streamfunction Rayleigh peel (hardcoded_backend.py:
+    3383-3771) on the mode-stacked network with first-order jets and the
+    identity envelope: raw values (mean removed, the constant gauge) and
+    gradients of every mode, M = w V^T V, S = w G^T G (w = area / n), the
+    Gram-form causal peel, the gradient of sum(losses) (detached prefix) and,
+    when ``lr`` is given, the all-mode Adam transaction.  X0: [3, n, F]
+    feature jet.  Returns the peel dict with ``loss`` = mean of the peeled
+    quotients and ``grads``; with ``lr`` also ``state`` (mode_adam's)."""
+    K = W[0].shape[0]
+    n = X0.shape[1]
+    E = np.zeros((3, n, 1))
+    E[0] = 1.0
+    per, vals, grads = [], [], []
+    for k in range(K):
+        Wk = [w[k] for w in W]
+        bk = [x[k] for x in b]
+        xs, pres, out = mode_forward(Wk, bk, X0, E, 2, 1, omegas)
+        per.append((Wk, xs, pres))
+        vals.append(out[0][:, 0])
+        grads.append(np.stack([out[1][:, 0], out[2][:, 0]], -1).reshape(-1))
+    V = np.stack(vals, 1)
+    V = V - V.mean(axis=0, keepdims=True)
+    G = np.stack(grads, 1)
+    M = weight * V.T @ V
+    S = weight * G.T @ G
+    obj = coefficient_peel(M, S, sort)
+    obj.update(M=M, S=S, loss=float(np.mean(obj["losses"])))
+    dV = weight * V @ obj["Cu"]
+    dG = weight * G @ obj["Cd"]
+    dV = dV - dV.mean(axis=0, keepdims=True)
+    gW = [np.zeros_like(w) for w in W]
+    gb = [np.zeros_like(x) for x in b]
+    for k, (Wk, xs, pres) in enumerate(per):
+        A = np.zeros((3, n, 1))
+        A[0, :, 0] = dV[:, k]
+        A[1, :, 0] = dG[0::2, k]
+        A[2, :, 0] = dG[1::2, k]
+        gwk, gbk = mode_backward(Wk, xs, pres, E, A, 2, 1, omegas)
+        for j in range(len(W)):
+            gW[j][k] = gwk[j]
+            gb[j][k] = gbk[j]
+    obj["grads"] = (gW, gb)
+    if lr is not None:
+        if moments is None:
+            moments = ([np.zeros_like(w) for w in W], [np.zeros_like(w) for w in W],
+                       [np.zeros_like(x) for x in b], [np.zeros_like(x) for x in b])
+        mW, vW, mb, vb = moments
+        obj["state"], obj["norms"] = mode_adam(W, b, mW, vW, mb, vb, gW, gb, epoch, lr, clip)
     return obj

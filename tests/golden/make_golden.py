@@ -24,7 +24,10 @@ Reference functions exercised (paths relative to the reference project):
 * experiments/metaball/_backend/flow/cases/metaball/velocity_trace_jet2.py:
   ``forward`` / ``backward`` (:65-82) of a four-mode second-order network;
 * experiments/periodic/paper_rollout.py:178-187 recipe (Grams, then
-  ``scipy.linalg.eigh(S, M)``).
+  ``scipy.linalg.eigh(S, M)``);
+* hardcoded_backend.py ``HardcodedModel`` (:1705) ``forward_stream_jet1``
+  (:1716), ``arrays`` (:1987) and ``peel_step`` (:3774) with the
+  streamfunction Rayleigh peel (:3383) on a four-mode periodic network.
 
 Usage:  NEB_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 """
@@ -255,6 +258,45 @@ def main():
     pp = vcore.coefficient_peel(Mp, Sp)
     g.update(peel_M=Mp, peel_S=Sp, peel_losses=pp["losses"], peel_order=pp["order"],
              peel_T=pp["T"], peel_Cu=pp["Cu"], peel_Cd=pp["Cd"])
+
+    # --- the periodic backend's HardcodedModel: first-order fields of every
+    # mode, then one training step of the streamfunction Rayleigh peel
+    # (hardcoded_backend.py:3383-3771) with its all-mode device Adam
+    hcfg = HB.cfg_namespace(dict(
+        modes=4, hidden=8, hidden_layers=2, frequencies=3, xmin=0.0, xmax=2 * math.pi,
+        ymin=0.0, ymax=2 * math.pi, geometry_mode="periodic_box",
+        envelope_mode="periodic_identity", input_encoding="periodic_sincos_xy",
+        canonical_siren=True, siren_first_omega0=8.0, siren_hidden_omega0=30.0,
+        basis_objective="streamfunction_dirichlet_rayleigh", causal_sorting="geometry_rayleigh",
+        reorthogonalization_passes=2, mass_floor=1e-14, learning_rate=1e-3, grad_clip=5.0,
+        spatial_derivative_order=1, mode_forward_batch=2, mode_backward_batch=2,
+        mlp_compute_dtype="float32", master_weight_dtype="float32"))
+    harr = {}
+    for mode in range(4):
+        for layer, (inside, outside) in enumerate(((12, 8), (8, 8), (8, 1))):
+            label = f"l{layer}" if layer < 2 else "output"
+            for offset, (kind, shape) in enumerate((("weight", (outside, inside)),
+                                                    ("bias", (outside,)))):
+                harr[f"m{mode:03d}.{label}.{kind}"] = rng.normal(0, .15, size=shape)
+                stem = f"m{mode:03d}.adam.p{2 * layer + offset:02d}"
+                harr[stem + ".exp_avg"] = np.zeros(shape)
+                harr[stem + ".exp_avg_sq"] = np.zeros(shape)
+                harr[stem + ".step"] = np.asarray(0, "i8")
+    hmodel = HB.HardcodedModel(hcfg, harr)
+    hpts = rng.uniform(0, 2 * math.pi, size=(48, 2))
+    fields = list(hmodel.forward_stream_jet1(hcfg, hpts, 0.0, 0.0, False))
+    g.update(hb_points=hpts,
+             hb_value=np.stack([np.asarray(f.value[:, 0]) for _, f, _ in fields]),
+             hb_grad=np.stack([np.asarray(f.grad[:, 0]) for _, f, _ in fields]))
+    for key, value in harr.items():
+        g["hb_in." + key] = np.asarray(value)
+    res = HB.peel_step(hcfg, hmodel, hpts, 0.0, 0.0, True)
+    g.update(hb_loss=np.asarray(res["loss"]), hb_energies=np.asarray(res["mode_energies"]),
+             hb_order=np.asarray(res["causal_order"]),
+             hb_norm_min=np.asarray(res["gradient_norm_min"]),
+             hb_norm_max=np.asarray(res["gradient_norm_max"]))
+    for key, value in hmodel.arrays().items():
+        g["hb_out." + key] = np.asarray(value)
 
     g = {key: np.asarray(v, dtype=np.float64) if np.asarray(v).dtype.kind == "f" else np.asarray(v)
          for key, v in g.items()}

@@ -6,6 +6,7 @@ import math
 from types import SimpleNamespace
 
 import numpy as np
+import pytest
 
 from oracle import neb_oracle as O
 from neb_gb300.modes import jet_channels, siren_init
@@ -66,3 +67,45 @@ def test_velocity_step_gradient_matches_central_differences():
         fd = (float(lp["losses"].sum()) - float(lm["losses"].sum())) / (2 * h)
         an = (gW if use_w else gb)[j][idx]
         assert abs(fd - an) <= 1e-6 * max(1.0, abs(an)), (j, use_w, idx, fd, an)
+
+
+# ------------------------------------------- the periodic backend's facade
+def test_hardcoded_trial_spaces_and_dispatch():
+    """Host-side validation of the periodic backend's API: the supported
+    trial spaces, the layer frequencies and the objective dispatch
+    (hardcoded_backend.py:1250-1260, :3401-3427, :3796-3811)."""
+    from types import SimpleNamespace
+    from neb_gb300 import hardcoded as H
+    periodic = SimpleNamespace(geometry_mode="periodic_box", envelope_mode="periodic_identity",
+                               input_encoding="periodic_sincos_xy")
+    assert H._trial_space(periodic) == H.PERIODIC
+    airfoil = SimpleNamespace(geometry_mode="cinf_ellipse", envelope_mode="cinf_localized",
+                              input_encoding="raw_xy")
+    with pytest.raises(NotImplementedError):
+        H._trial_space(airfoil)
+    assert H.siren_layer_omega(SimpleNamespace(), 0) == 1.0
+    c = SimpleNamespace(canonical_siren=True, siren_first_omega0=8.0)
+    assert H.siren_layer_omega(c, 0) == 8.0 and H.siren_layer_omega(c, 1) == 30.0
+    with pytest.raises(ValueError):
+        H.peel_step(SimpleNamespace(basis_objective="nonsense"), None, [])
+    with pytest.raises(ValueError):
+        H.peel_step(SimpleNamespace(basis_objective="potential_rayleigh"), None, [],
+                    reference_model=object())
+    with pytest.raises(NotImplementedError):
+        H.peel_step(SimpleNamespace(basis_objective="velocity_rayleigh"), None, [])
+
+
+def test_fixed_order_peel_oracle():
+    """With fixed_order the peel keeps network order: T orthonormalises M
+    in that order and the losses are the diagonal of T^T S T."""
+    rng = np.random.default_rng(2)
+    X = rng.normal(size=(40, 6))
+    Y = rng.normal(size=(40, 6)) * np.linspace(3, 0.5, 6)
+    M, S = X.T @ X / 40, Y.T @ Y / 40
+    r = O.coefficient_peel(M, S, sort=False)
+    assert list(r["order"]) == list(range(6))
+    T = r["T"]
+    np.testing.assert_allclose(T.T @ M @ T, np.eye(6), atol=1e-10)
+    np.testing.assert_allclose(np.diag(T.T @ S @ T), r["losses"], rtol=1e-10)
+    s = O.coefficient_peel(M, S)
+    assert list(s["order"]) != list(range(6))

@@ -279,3 +279,43 @@ def test_velocity_step_matches_reference_composition():
                                    atol=1e-10 * np.abs(G[f"vel_gW{j}"]).max())
         np.testing.assert_allclose(gb[j], G[f"vel_gb{j}"], rtol=1e-8,
                                    atol=1e-10 * np.abs(G[f"vel_gb{j}"]).max())
+
+
+# ------------------------------------------- the periodic backend's peel step
+def _hb_arrays(prefix):
+    W = [np.stack([G[f"{prefix}.m{k:03d}.{lab}.weight"] for k in range(4)])
+         for lab in ("l0", "l1", "output")]
+    b = [np.stack([G[f"{prefix}.m{k:03d}.{lab}.bias"] for k in range(4)])
+         for lab in ("l0", "l1", "output")]
+    return W, b
+
+
+def test_periodic_fields_match_forward_stream_jet1():
+    W, b = _hb_arrays("hb_in")
+    X0 = O.features_periodic(G["hb_points"], 3)[:3]
+    E = np.zeros((3, 48, 1)); E[0] = 1.0
+    om = O.mode_omegas(3, 8.0, 30.0)
+    for k in range(4):
+        _, _, out = O.mode_forward([w[k] for w in W], [x[k] for x in b], X0, E, 2, 1, om)
+        np.testing.assert_allclose(out[0][:, 0], G["hb_value"][k], rtol=1e-9, atol=1e-10)
+        np.testing.assert_allclose(np.stack([out[1][:, 0], out[2][:, 0]], -1), G["hb_grad"][k],
+                                   rtol=1e-9, atol=1e-9)
+
+
+def test_potential_peel_step_matches_reference_peel_step():
+    """One training step of the reference's streamfunction Rayleigh peel
+    (its loss, per-rank energies, causal order and the parameters after its
+    device Adam) against the oracle's Gram-form restatement."""
+    W, b = _hb_arrays("hb_in")
+    X0 = O.features_periodic(G["hb_points"], 3)[:3]
+    weight = (2 * math.pi) ** 2 / 48
+    r = O.potential_peel_step(W, b, X0, weight, O.mode_omegas(3, 8.0, 30.0), lr=1e-3, clip=5.0)
+    np.testing.assert_array_equal(r["order"], G["hb_order"])
+    np.testing.assert_allclose(r["losses"], G["hb_energies"], rtol=1e-6)
+    np.testing.assert_allclose(r["loss"], G["hb_loss"], rtol=1e-6)
+    np.testing.assert_allclose([r["norms"].min(), r["norms"].max()],
+                               [G["hb_norm_min"], G["hb_norm_max"]], rtol=1e-9)
+    W2, b2 = _hb_arrays("hb_out")
+    for j in range(3):
+        np.testing.assert_allclose(r["state"][0][j], W2[j], rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(r["state"][1][j], b2[j], rtol=1e-9, atol=1e-12)
