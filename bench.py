@@ -75,7 +75,7 @@ def parse():
                     help="mode counts of the reference_velocity workload")
     ap.add_argument("--workload", default="periodic_train",
                     choices=["periodic_train", "periodic_small", "periodic_eval", "multihole",
-                             "metaball3d", "reference_velocity"],
+                             "metaball3d", "reference_velocity", "reference_potential"],
                     help="periodic_train is the headline line; the others print one line "
                          "each for the remaining configurations (timing and FP64-oracle "
                          "errors), not the headline metric")
@@ -325,6 +325,54 @@ REF_VELOCITY = dict(hidden=128, hidden_layers=5, siren_first_omega0=40.0,
                     published_s_per_update_k1024=2.698278 + 8.952445 + 0.265934 + 0.018048)
 
 
+# The reference's periodic vortex-merger Potential training configuration
+# (checkpoints/2d/periodic-potential-k1024-seed0/model.json): K per-mode
+# SIRENs 24 -> 4 x 32 sine (omega 8/30) -> 1, 6 Fourier frequencies, 4096
+# uniform points per update, the streamfunction Rayleigh peel, Adam (clip 5,
+# cosine schedule from 2e-4).  Published: 2,000 updates in 6,228-6,599 s at
+# K = 1024 (data/paper/periodic_merger.json:26,1297,2568; hardware not stated).
+REF_POTENTIAL = dict(modes=1024, hidden=32, hidden_layers=4, frequencies=6, input_features=24,
+                     xmin=0.0, xmax=2 * math.pi, ymin=0.0, ymax=2 * math.pi,
+                     geometry_mode="periodic_box", envelope_mode="periodic_identity",
+                     input_encoding="periodic_sincos_xy", canonical_siren=True,
+                     siren_first_omega0=8.0, siren_hidden_omega0=30.0,
+                     basis_objective="potential_rayleigh", causal_sorting="geometry_rayleigh",
+                     reorthogonalization_passes=2, mass_floor=1e-14, learning_rate=2e-4,
+                     grad_clip=5.0, spatial_derivative_order=1, mode_forward_batch=32,
+                     mode_backward_batch=32, mlp_compute_dtype="float32",
+                     sampling_mode="uniform_random", points_per_step=4096, seed=0)
+PUBLISHED_POTENTIAL_S_PER_UPDATE = (6228.0 / 2000, 6599.0 / 2000)
+
+
+def time_potential(K: int, steps: int, warmup: int, dev):
+    """ms per training update of the reference's Potential configuration at
+    K modes through the periodic backend's API (hardcoded.peel_step): each
+    update samples its points on the host (fluid_points, seed + 1009 epoch,
+    as the trainer does), uploads them, and reads the diagnostics back.
+    Returns (ms per update, last result)."""
+    import torch
+    from types import SimpleNamespace
+    from neb_gb300 import hardcoded as H
+    cfg = SimpleNamespace(**dict(REF_POTENTIAL, modes=K))
+    model = H.HardcodedModel(cfg, H.initial_arrays(cfg), device=dev)
+    n = cfg.points_per_step
+
+    def step(epoch):
+        pts = H.fluid_points(cfg, n, 0.0, 0.0, cfg.seed + epoch * 1009)
+        return H.peel_step(cfg, model, pts, 0.0, 0.0, True)
+
+    for e in range(warmup):
+        step(e)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for e in range(warmup, warmup + steps):
+        r = step(e)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, r
+
+
 def velocity_inputs(n: int, seed: int = 0):
     """Synthetic inputs with the configuration's shapes: points uniform in
     the unit cube; features (2x - 1 for the coordinates, 12 constant
@@ -412,7 +460,55 @@ def run_workload(args, world, rank, local):
     def dev_inputs(pts, w):
         return torch.tensor(pts, device=dev), torch.tensor(w, device=dev)
 
-    if name == "reference_velocity":
+    if name == "reference_potential":
+        # the reference's own 2D training configuration through its backend
+        # API: GPU updates at each K, and the FP64 oracle's update at K = 32
+        from types import SimpleNamespace
+        from neb_gb300 import hardcoded as H
+        out = {}
+        psteps = max(2, min(args.steps, 10))
+        modes = [int(k) for k in args.modes.split(",")]
+        for Km in modes:
+            ms, r = time_potential(Km, psteps, 2, dev)
+            out[f"K{Km}"] = {"ms_per_update": ms, "updates_per_s": 1e3 / ms, "steps": psteps,
+                             "loss": r["loss"], "orth_error": r["orth_error"]}
+        top = f"K{max(modes)}"
+        cpu = None
+        if not args.no_cpu_baseline:
+            cfg = SimpleNamespace(**dict(REF_POTENTIAL, modes=32))
+            arr = H.initial_arrays(cfg)
+            labels = [f"l{i}" for i in range(cfg.hidden_layers)] + ["output"]
+            Wn = [np.stack([arr[f"m{k:03d}.{lab}.weight"] for k in range(32)]).astype(np.float64)
+                  for lab in labels]
+            bn = [np.stack([arr[f"m{k:03d}.{lab}.bias"] for k in range(32)]).astype(np.float64)
+                  for lab in labels]
+            pts = H.fluid_points(cfg, cfg.points_per_step, 0.0, 0.0, cfg.seed).astype(np.float64)
+            t0 = time.perf_counter()
+            O.potential_peel_step(Wn, bn, O.features_periodic(pts, cfg.frequencies)[:3],
+                                  (2 * math.pi) ** 2 / len(pts),
+                                  O.mode_omegas(cfg.hidden_layers + 1, 8.0, 30.0),
+                                  lr=cfg.learning_rate, clip=cfg.grad_clip)
+            t_cpu = time.perf_counter() - t0
+            cpu = {"value": 1.0 / t_cpu, "unit": "updates/s", "cores": cpu_threads(),
+                   "kind": "port", "sample": "1 training update at K=32 of the FP64 NumPy "
+                   "restatement (potential_peel_step)"}
+        lo, hi = PUBLISHED_POTENTIAL_S_PER_UPDATE
+        line.update({
+            "metric": "Potential (streamfunction Rayleigh peel) training updates/s through the "
+                      "periodic backend API, the reference's per-mode SIREN (24 -> 4x32 sine, "
+                      "omega 8/30), 4096 points per update",
+            "value": out[top]["updates_per_s"], "unit": "updates/s",
+            "ms_per_update": out[top]["ms_per_update"], "dtype": "f32", "modes": out,
+            "e2e_note": "each update samples its points on the host, uploads them and reads "
+                        "the diagnostic table back, as the reference's trainer does",
+            "published_reference_s_per_update_k1024": [lo, hi],
+            "speedup_vs_published_k1024": [lo / (out["K1024"]["ms_per_update"] / 1e3),
+                                           hi / (out["K1024"]["ms_per_update"] / 1e3)]
+            if "K1024" in out else None,
+            "cpu_baseline": cpu,
+            "data": "synthetic: the reference trainer's epoch-0 initialisation and its "
+                    "uniform point sampler"})
+    elif name == "reference_velocity":
         # the reference's own architecture and objective: GPU steps at K = 32
         # and K = 1024, and the FP64 oracle's step at K = 32 on the host
         out = {}

@@ -375,6 +375,17 @@ class HardcodedModel:
 
 
 # ------------------------------------------------------------------ peel step
+TAPE_BUDGET = 1 << 30  # bytes of activation tape one block of modes may hold
+
+
+def _block(core: ModeModel, n: int) -> int:
+    """Modes per block of the peel step: as many as keep the block's tape
+    within TAPE_BUDGET (the reference's mode_forward_batch bounds its own
+    memory; the results do not depend on the blocking)."""
+    per_mode = max(1, N.load().neb_modes_tape_bytes(ctypes.byref(core.net), 1, n))
+    return max(1, min(core.K, TAPE_BUDGET // per_mode))
+
+
 def _streamfunction_peel_step(cfg, model: HardcodedModel, points, training: bool) -> dict:
     """The streamfunction (potential) Rayleigh peel step of the periodic
     backend (hardcoded_backend.py:3383-3771) in Gram form on the device."""
@@ -402,10 +413,16 @@ def _streamfunction_peel_step(cfg, model: HardcodedModel, points, training: bool
     feats = model.features(cfg, points, 1)
     V = torch.empty((n, K), dtype=core.dtype, device=core.device)
     G = torch.empty((2 * n, K), dtype=core.dtype, device=core.device)
-    block = max(1, int(getattr(cfg, "mode_forward_batch", 1)))
-    for a in range(0, K, block):
-        b = min(K, a + block)
-        out, _ = core.forward_packed(feats, None, a, b)
+    block = _block(core, n)
+    blocks = [(a, min(K, a + block)) for a in range(0, K, block)]
+    # one block holds every mode: keep its tape for the reverse pass instead
+    # of recomputing it (the reference recomputes each block, HB:3614-3629)
+    keep = training and len(blocks) == 1
+    tapes = {}
+    for a, b in blocks:
+        out, tape = core.forward_packed(feats, None, a, b, cache=keep)
+        if keep:
+            tapes[a] = tape
         N.call("neb_potential_fields", prec, out.data_ptr(), a, b, n, K, V.data_ptr(),
                G.data_ptr(), s)
     # the additive streamfunction constant is a gauge: project it out
@@ -423,10 +440,8 @@ def _streamfunction_peel_step(cfg, model: HardcodedModel, points, training: bool
         N.call("neb_column_center", prec, n, K, dV.data_ptr(), s)
         gW = [torch.empty_like(w) for w in core.W]
         gb = [torch.empty_like(x) for x in core.b]
-        bblock = max(1, int(getattr(cfg, "mode_backward_batch", block)))
-        for a in range(0, K, bblock):
-            b = min(K, a + bblock)
-            _, tape = core.forward_packed(feats, None, a, b, cache=True)
+        for a, b in blocks:
+            tape = tapes.pop(a, None) or core.forward_packed(feats, None, a, b, cache=True)[1]
             adj = torch.empty((b - a, n, 3, 1), dtype=core.dtype, device=core.device)
             N.call("neb_potential_lift", prec, dV.data_ptr(), dG.data_ptr(), a, b, n, K,
                    adj.data_ptr(), s)
@@ -492,3 +507,69 @@ def peel_step(cfg, model: HardcodedModel, points, beta: float = 0.0, alpha: floa
     if objective in {"pure_vorticity_rayleigh", "velocity_rayleigh"}:
         raise NotImplementedError(f"basis_objective={objective!r} is not built on this path")
     raise ValueError(f"unsupported basis_objective={objective!r}")
+
+
+# ----------------------------------------------------- initialisation, points
+def initial_arrays(cfg) -> dict:
+    """Epoch-0 checkpoint arrays of the reference's trainer preparation
+    (experiments/2d/_backend/flow/cases/vortex_merger/neural_training/
+    prepare_gauge_canonical.py:51-86): one PCG64 generator seeded cfg.seed
+    drawn mode after mode, layer after layer, weight then bias, uniform in
+    +-bound (canonical SIREN: 1 / fan_in on the first layer, sqrt(6 / fan_in)
+    / omega_hidden after and on the output layer, bias bound 1 / sqrt(fan_in);
+    otherwise gain / sqrt(fan_in)), float32; zero Adam moments, step 0."""
+    import math
+    rng = np.random.default_rng(int(cfg.seed))
+    encoding = str(getattr(cfg, "input_encoding", ""))
+    fan0 = int(getattr(cfg, "input_features", 2 if encoding == "raw_xy" else 0))
+    siren = bool(getattr(cfg, "canonical_siren", False))
+    g_first = float(getattr(cfg, "initial_first_layer_gain", 1.0))
+    g_hidden = float(getattr(cfg, "initial_hidden_layer_gain", 1.0))
+    g_out = float(getattr(cfg, "initial_output_layer_gain", 1.0))
+    arrays = {}
+    for mode in range(int(cfg.modes)):
+        prefix = f"m{mode:03d}"
+        names = []
+        fan_in = fan0
+        for layer in range(int(cfg.hidden_layers)):
+            if siren:
+                bound = 1.0 / fan_in if layer == 0 else \
+                    math.sqrt(6.0 / fan_in) / float(cfg.siren_hidden_omega0)
+                bias_bound = 1.0 / math.sqrt(fan_in)
+            else:
+                bound = (g_first if layer == 0 else g_hidden) / math.sqrt(fan_in)
+                bias_bound = bound
+            w, b = f"{prefix}.l{layer}.weight", f"{prefix}.l{layer}.bias"
+            arrays[w] = rng.uniform(-bound, bound, (int(cfg.hidden), fan_in)).astype(np.float32)
+            arrays[b] = rng.uniform(-bias_bound, bias_bound, int(cfg.hidden)).astype(np.float32)
+            names += [w, b]
+            fan_in = int(cfg.hidden)
+        bound = math.sqrt(6.0 / fan_in) / float(cfg.siren_hidden_omega0) if siren else \
+            g_out / math.sqrt(fan_in)
+        bias_bound = 1.0 / math.sqrt(fan_in)
+        w, b = f"{prefix}.output.weight", f"{prefix}.output.bias"
+        arrays[w] = rng.uniform(-bound, bound, (1, fan_in)).astype(np.float32)
+        arrays[b] = rng.uniform(-bias_bound, bias_bound, 1).astype(np.float32)
+        names += [w, b]
+        for index, name in enumerate(names):
+            stem = f"{prefix}.adam.p{index:02d}"
+            arrays[f"{stem}.exp_avg"] = np.zeros_like(arrays[name])
+            arrays[f"{stem}.exp_avg_sq"] = np.zeros_like(arrays[name])
+            arrays[f"{stem}.step"] = np.asarray(0, dtype=np.int64)
+    return arrays
+
+
+def fluid_points(cfg, count: int, beta: float, alpha: float, seed: int) -> np.ndarray:
+    """Quadrature points of one step in the periodic or free box
+    (hardcoded_backend.py:2425-2447, sampling_mode uniform_random; the box
+    has no body, so every candidate is accepted): PCG64 seeded ``seed``,
+    max(2 count, 128) x-draws, then as many y-draws, the first ``count``
+    pairs, float32."""
+    if str(getattr(cfg, "sampling_mode", "")) != "uniform_random":
+        raise NotImplementedError("sampling_mode uniform_random is supported")
+    _trial_space(cfg)
+    rng = np.random.default_rng(seed)
+    draws = max(2 * count, 128)
+    x = rng.uniform(cfg.xmin, cfg.xmax, draws)
+    y = rng.uniform(cfg.ymin, cfg.ymax, draws)
+    return np.column_stack((x, y))[:count].astype(np.float32, copy=False)

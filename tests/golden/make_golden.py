@@ -298,6 +298,41 @@ def main():
     for key, value in hmodel.arrays().items():
         g["hb_out." + key] = np.asarray(value)
 
+    # --- the trainer's epoch-0 arrays and fixed validation points
+    # (prepare_gauge_canonical.py main, run on a three-mode configuration)
+    import json
+    import tempfile
+    os.environ["NEB_2D_VENDOR_ROOT"] = str(reference_root() / "experiments/2d/_backend")
+    prep = load(reference_root() / "experiments/2d/_backend/flow/cases/vortex_merger/"
+                "neural_training/prepare_gauge_canonical.py", "prepare_gauge_canonical")
+    pcfg = dict(seed=3, modes=3, hidden=8, hidden_layers=2, frequencies=2, input_features=8,
+                xmin=0.0, xmax=2 * math.pi, ymin=0.0, ymax=2 * math.pi,
+                geometry_mode="periodic_box", envelope_mode="periodic_identity",
+                input_encoding="periodic_sincos_xy", canonical_siren=True,
+                siren_first_omega0=8.0, siren_hidden_omega0=30.0,
+                basis_objective="potential_rayleigh", spatial_derivative_order=1,
+                sampling_mode="uniform_random", mlp_compute_dtype="float32",
+                mlp_accumulation_dtype="float32", jet_dtype="float32",
+                parameter_backward_dtype="float32", quadrature_dtype="float32",
+                ritz_dtype="float32", master_weight_dtype="float32", optimizer_dtype="float32",
+                validation_points=37, validation_beta_samples=1, validation_alpha_samples=1,
+                alpha_min_deg=0.0, alpha_max_deg=0.0, probe_beta=0.0, probe_alpha_deg=0.0,
+                learning_rate=1e-3)
+    with tempfile.TemporaryDirectory() as tmp:
+        conf = Path(tmp) / "config.json"
+        conf.write_text(json.dumps(pcfg))
+        saved = sys.argv
+        sys.argv = ["prepare", "--config", str(conf), "--output-dir", str(Path(tmp) / "run")]
+        try:
+            prep.main()
+        finally:
+            sys.argv = saved
+        with np.load(Path(tmp) / "run/initial_epoch0000.npz") as z:
+            for key in z.files:
+                g["init." + key] = np.asarray(z[key])
+        with np.load(Path(tmp) / "run/fixed_validation_iid_uniform_v1.npz") as z:
+            g["init_validation_points"] = np.asarray(z["validation_points"][0], np.float64)
+
     g = {key: np.asarray(v, dtype=np.float64) if np.asarray(v).dtype.kind == "f" else np.asarray(v)
          for key, v in g.items()}
     np.savez_compressed(OUT, **g)

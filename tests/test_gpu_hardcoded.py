@@ -282,3 +282,42 @@ def test_active_mask_and_physical_gate():
     v1, g1 = _fields(model, cfg, G["hb_points"])
     v2, g2 = _fields(again, cfg, G["hb_points"])
     assert np.array_equal(v1, v2) and np.array_equal(g1, g2)
+
+
+@pytest.mark.parametrize("precision,rtol", [("fp32", 5e-4), ("fp64", 1e-8)])
+def test_reference_configuration_update_matches_oracle(precision, rtol):
+    """One update of the reference's Potential configuration (24 -> 4 x 32
+    sine, omega 8/30, the trainer's epoch-0 arrays and point sampler) at
+    K = 8 and 512 points against the oracle's restatement."""
+    _needs_gpu()
+    from neb_gb300 import hardcoded as H
+    cfg = _cfg(modes=8, hidden=32, hidden_layers=4, frequencies=6, input_features=24,
+               learning_rate=2e-4, sampling_mode="uniform_random", seed=0)
+    arrays = H.initial_arrays(cfg)
+    model = H.HardcodedModel(cfg, arrays, precision=precision)
+    pts = H.fluid_points(cfg, 512, 0.0, 0.0, 0)
+    res = H.peel_step(cfg, model, pts, 0.0, 0.0, True)
+    labels = ["l0", "l1", "l2", "l3", "output"]
+    W = [np.stack([arrays[f"m{k:03d}.{lab}.weight"] for k in range(8)]).astype(np.float64)
+         for lab in labels]
+    b = [np.stack([arrays[f"m{k:03d}.{lab}.bias"] for k in range(8)]).astype(np.float64)
+         for lab in labels]
+    ref = O.potential_peel_step(W, b, O.features_periodic(pts.astype(np.float64), 6)[:3],
+                                np.float32((2 * math.pi) ** 2) / np.float32(512),
+                                O.mode_omegas(5, 8.0, 30.0), lr=2e-4, clip=5.0)
+    assert res["causal_order"] == list(ref["order"])
+    np.testing.assert_allclose(res["mode_energies"], ref["losses"], rtol=rtol)
+    after = model.arrays()
+    got = np.concatenate([after[f"m{k:03d}.{lab}.weight"].astype(np.float64).ravel()
+                          for j, lab in enumerate(labels) for k in range(8)])
+    want = np.concatenate([ref["state"][0][j][k].ravel()
+                           for j, lab in enumerate(labels) for k in range(8)])
+    if precision == "fp64":
+        np.testing.assert_allclose(got, want, rtol=1e-8, atol=1e-11)
+    else:
+        # Adam's first step is lr g / (|g| + eps): an entry whose gradient is
+        # at the FP32 rounding level of the largest may move anywhere in
+        # +-lr, so bound every entry by lr and nearly all tightly
+        err = np.abs(got - want)
+        assert err.max() <= 2 * cfg.learning_rate
+        assert np.mean(err > 2e-6 + rtol * np.abs(want)) <= 1e-3

@@ -109,3 +109,24 @@ def test_fixed_order_peel_oracle():
     np.testing.assert_allclose(np.diag(T.T @ S @ T), r["losses"], rtol=1e-10)
     s = O.coefficient_peel(M, S)
     assert list(s["order"]) != list(range(6))
+
+
+def test_hardcoded_initial_arrays_and_points_match_reference():
+    """initial_arrays and fluid_points against the reference trainer's own
+    epoch-0 checkpoint and fixed validation points, bit for bit."""
+    from neb_gb300 import hardcoded as H
+    G = np.load(__file__.rsplit("/", 1)[0] + "/golden/reference_vectors.npz")
+    cfg = SimpleNamespace(seed=3, modes=3, hidden=8, hidden_layers=2, frequencies=2,
+                          input_features=8, xmin=0.0, xmax=2 * math.pi, ymin=0.0,
+                          ymax=2 * math.pi, geometry_mode="periodic_box",
+                          envelope_mode="periodic_identity", input_encoding="periodic_sincos_xy",
+                          canonical_siren=True, siren_first_omega0=8.0, siren_hidden_omega0=30.0,
+                          sampling_mode="uniform_random")
+    arrays = H.initial_arrays(cfg)
+    ref = {k[5:]: G[k] for k in G.files if k.startswith("init.")}
+    assert set(arrays) == set(ref)
+    for key, value in ref.items():
+        assert np.array_equal(np.asarray(arrays[key], np.float64), value), key
+    pts = H.fluid_points(cfg, 37, 0.0, 0.0, cfg.seed + 900000)
+    assert pts.dtype == np.float32
+    assert np.array_equal(pts.astype(np.float64), G["init_validation_points"])
