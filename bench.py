@@ -370,7 +370,7 @@ def time_potential(K: int, steps: int, warmup: int, dev):
         r = step(e)
     e1.record()
     torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / steps, r
+    return e0.elapsed_time(e1) / steps, r, step
 
 
 def velocity_inputs(n: int, seed: int = 0):
@@ -469,9 +469,12 @@ def run_workload(args, world, rank, local):
         psteps = max(2, min(args.steps, 10))
         modes = [int(k) for k in args.modes.split(",")]
         for Km in modes:
-            ms, r = time_potential(Km, psteps, 2, dev)
+            ms, r, step = time_potential(Km, psteps, 2, dev)
             out[f"K{Km}"] = {"ms_per_update": ms, "updates_per_s": 1e3 / ms, "steps": psteps,
                              "loss": r["loss"], "orth_error": r["orth_error"]}
+            if Km == max(modes):
+                out[f"K{Km}"]["kernel_ms_per_update"] = _kernel_table(
+                    N, lambda i: step(1000 + i), 2)
         top = f"K{max(modes)}"
         cpu = None
         if not args.no_cpu_baseline:

@@ -395,8 +395,9 @@ int neb_column_gram(int precision, int64_t rows, int K, const void* A, double sc
                     neb_stream_t stream);
 
 /* out = scale A C for A [rows][K] (FP32 or FP64) and C [K][K] FP64, both
- * row-major, computed in FP64; out in A's type.  The field adjoints
- * U Cu / n, D Cd / n of VC:94-95. */
+ * row-major; out in A's type.  FP64: one DGEMM.  FP32: scale C as a sum of
+ * two floats and two FP32 GEMMs with FP32 accumulation.  The field adjoints
+ * U Cu / n, D Cd / n of VC:94-95 and w V Cu, w G Cd of HB:3513-3534. */
 size_t neb_column_apply_workspace_bytes(int64_t rows, int K);
 int neb_column_apply(int precision, int64_t rows, int K, const void* A, const double* C,
                      double scale, void* out, void* workspace, size_t workspace_bytes,

@@ -114,12 +114,18 @@ __device__ __forceinline__ void envelope_mul_reverse(const T* e, const T* a, T* 
   b[0] = xb;
 }
 
-constexpr int kTilePts = 8;  // points per block (two per warp)
 constexpr int kTileK = 32;   // reduction chunk staged in shared memory
-// output columns per thread (one per lane and step of 32): four in FP32,
-// two in FP64, so a block covers 128 or 64 columns
+// output columns per thread: four in FP32, two in FP64.  A block of 128
+// threads covers TC columns with TC / cols_per_thread column threads; the
+// other factor of 128 are row threads of two points each.  Wide tiles (128
+// FP32 / 64 FP64 columns, one row thread per warp, 8 points) serve layers
+// wider than 32; narrow tiles (32 columns; 32 FP32 / 16 FP64 points) keep
+// every lane busy on the 32-wide layers of the periodic networks.
 template <typename T> constexpr int cols_per_thread() { return sizeof(T) == 4 ? 4 : 2; }
 template <typename T> constexpr int tile_cols() { return 32 * cols_per_thread<T>(); }
+constexpr int kNarrowTile = 32;
+template <typename T, int TC> constexpr int col_threads() { return TC / cols_per_thread<T>(); }
+template <typename T, int TC> constexpr int tile_pts() { return 2 * (128 / col_threads<T, TC>()); }
 
 enum { EPI_OUTPUT = 0, EPI_HIDDEN = 1, EPI_REVERSE = 2 };
 
@@ -146,16 +152,16 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 // Shared memory of one pipeline stage of mode_gemm: B tile [kTileK][TC + 1]
-// then A tile [8 C][kTileK]; two stages.
-template <typename T, int C> constexpr int mode_stage_elems() {
-  return kTileK * (tile_cols<T>() + 1) + kTilePts * C * kTileK;
+// then A tile [points x C][kTileK + 1]; two stages.
+template <typename T, int C, int TC> constexpr int mode_stage_elems() {
+  return kTileK * (TC + 1) + tile_pts<T, TC>() * C * (kTileK + 1);
 }
-template <typename T, int C> constexpr int mode_gemm_smem() {
-  return 2 * mode_stage_elems<T, C>() * (int)sizeof(T);
+template <typename T, int C, int TC> constexpr int mode_gemm_smem() {
+  return 2 * mode_stage_elems<T, C, TC>() * (int)sizeof(T);
 }
 
-// Per-mode jet GEMM.  blockIdx.x = tile of 8 points, blockIdx.y = tile of
-// tile_cols<T>() columns, blockIdx.z = mode b of the block; every pointer is
+// Per-mode jet GEMM.  blockIdx.x = tile of tile_pts points, blockIdx.y =
+// tile of TC columns, blockIdx.z = mode b of the block; every pointer is
 // already offset to the block's first mode and advanced by its *_mode stride.
 //   EPI_OUTPUT : out = env * (A W^T + b on the value channel), W [N][Kd]
 //   EPI_HIDDEN : pre = omega (A W^T + b), out = sine_jet(pre),   W [N][Kd]
@@ -164,27 +170,28 @@ template <typename T, int C> constexpr int mode_gemm_smem() {
 // A thread holds 2 points x C channels x cols_per_thread columns: each
 // shared-memory value it reads feeds cols_per_thread (A) or 2 C (B) FMAs.
 // The next reduction chunk is copied into the other shared-memory stage by
-// cp.async while the current one is consumed.
-template <typename T, int DIM, int ORD, int EPI>
+// cp.async while the current one is consumed.  The A rows are padded to
+// kTileK + 1 so the row threads of one warp read distinct banks.
+template <typename T, int DIM, int ORD, int EPI, int TC>
 __global__ void __launch_bounds__(128)
 mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int64_t w_mode,
           const T* __restrict__ bias, int64_t b_mode, const T* __restrict__ env,
           const T* __restrict__ pre_in, T* __restrict__ pre_out, T* __restrict__ out,
           int64_t o_mode, int n, int Kd, int N, T omega) {
   constexpr int C = Jet<DIM, ORD>::C;
-  constexpr int CPT = cols_per_thread<T>(), TC = tile_cols<T>();
-  constexpr int STAGE = mode_stage_elems<T, C>();
+  constexpr int CPT = cols_per_thread<T>(), CT = col_threads<T, TC>(), PTS = tile_pts<T, TC>();
+  constexpr int STAGE = mode_stage_elems<T, C, TC>(), LDA = kTileK + 1;
   extern __shared__ __align__(16) unsigned char mode_smem[];
   T* smem = reinterpret_cast<T*>(mode_smem);
-  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const int tid = threadIdx.x, tx = tid % CT, ty = tid / CT;
   const int mb = blockIdx.z;
-  const int col0 = blockIdx.y * TC, p0 = blockIdx.x * kTilePts;
+  const int col0 = blockIdx.y * TC, p0 = blockIdx.x * PTS;
   A += mb * a_mode;
   W += mb * w_mode;
   // issue the copies of reduction chunk j0 into stage st
   auto stage_copy = [&](int j0, int st) {
     T* Bs = smem + st * STAGE;                 // [kTileK][TC + 1]
-    T* As = Bs + kTileK * (TC + 1);            // [8 C][kTileK]
+    T* As = Bs + kTileK * (TC + 1);            // [PTS C][kTileK + 1]
     for (int e = tid; e < kTileK * TC; e += 128) {
       int jj, col;
       if constexpr (EPI == EPI_REVERSE) {
@@ -199,11 +206,11 @@ mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int6
       const T* src = ok ? (EPI == EPI_REVERSE ? W + (int64_t)j * N + o : W + (int64_t)o * Kd + j) : W;
       cp_async_elem(&Bs[jj * (TC + 1) + col], src, ok);
     }
-    for (int e = tid; e < kTilePts * C * kTileK; e += 128) {
+    for (int e = tid; e < PTS * C * kTileK; e += 128) {
       const int jj = e % kTileK, rc = e / kTileK;
       const int p = p0 + rc / C, c = rc % C, j = j0 + jj;
       const bool ok = p < n && j < Kd;
-      cp_async_elem(&As[rc * kTileK + jj], ok ? A + ((int64_t)p * C + c) * Kd + j : A, ok);
+      cp_async_elem(&As[rc * LDA + jj], ok ? A + ((int64_t)p * C + c) * Kd + j : A, ok);
     }
     cp_async_commit();
   };
@@ -230,12 +237,12 @@ mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int6
     for (int jj = 0; jj < kTileK; ++jj) {
       T bv[CPT];
 #pragma unroll
-      for (int u = 0; u < CPT; ++u) bv[u] = Bs[jj * (TC + 1) + tx + 32 * u];
+      for (int u = 0; u < CPT; ++u) bv[u] = Bs[jj * (TC + 1) + tx + CT * u];
 #pragma unroll
       for (int q = 0; q < 2; ++q)
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-          const T av = As[((ty * 2 + q) * C + c) * kTileK + jj];
+          const T av = As[((ty * 2 + q) * C + c) * LDA + jj];
 #pragma unroll
           for (int u = 0; u < CPT; ++u) acc[q][c][u] += av * bv[u];
         }
@@ -245,7 +252,7 @@ mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int6
   out += mb * o_mode;
 #pragma unroll
   for (int u = 0; u < CPT; ++u) {
-    const int o = col0 + tx + 32 * u;
+    const int o = col0 + tx + CT * u;
     if (o >= N) continue;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
@@ -347,23 +354,26 @@ mode_output_narrow(const T* __restrict__ A, int64_t a_mode, const T* __restrict_
 }
 
 // part[s][b][o][i] = sum over rows r in split s of Abar[b][r][o] X[b][r][i],
-// rows r = (point, channel).  grid = (tiles of 64 x 64, B, splits), 256
-// threads as 16 x 16, 4 x 4 outputs each; rows staged 32 at a time into
-// double-buffered shared memory by cp.async.
-constexpr int kWgTile = 64, kWgRows = 32, kWgLd = kWgTile + 4;
-template <typename T> constexpr int mode_wgrad_smem() {
-  return 2 * 2 * kWgRows * kWgLd * (int)sizeof(T);
+// rows r = (point, channel).  grid = (tiles of WT x WT, B, splits), threads
+// (WT / 4)^2 (256 for 64-wide tiles, 64 for the 32-wide layers), 4 x 4
+// outputs each; rows staged 32 at a time into double-buffered shared memory
+// by cp.async.
+constexpr int kWgRows = 32;
+template <int WT> constexpr int wg_threads() { return (WT / 4) * (WT / 4); }
+template <typename T, int WT> constexpr int mode_wgrad_smem() {
+  return 2 * 2 * kWgRows * (WT + 4) * (int)sizeof(T);
 }
-template <typename T>
-__global__ void __launch_bounds__(256)
+template <typename T, int WT>
+__global__ void __launch_bounds__(wg_threads<WT>())
 mode_wgrad(const T* __restrict__ Abar, const T* __restrict__ X, int64_t x_mode, int64_t rows,
            int N, int Kin, int64_t rows_per_split, T* __restrict__ part) {
+  constexpr int kWgTile = WT, kWgLd = WT + 4, NT = wg_threads<WT>(), TW = WT / 4;
   extern __shared__ __align__(16) unsigned char wg_smem[];
   T* smem = reinterpret_cast<T*>(wg_smem);  // [stage][A, X][kWgRows][kWgLd]
   const int tiles_i = (Kin + kWgTile - 1) / kWgTile;
   const int o0 = (blockIdx.x / tiles_i) * kWgTile, i0 = (blockIdx.x % tiles_i) * kWgTile;
   const int mb = blockIdx.y, s = blockIdx.z;
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int tid = threadIdx.x, tx = tid % TW, ty = tid / TW;
   Abar += (int64_t)mb * rows * N;
   X += mb * x_mode;
   const int64_t r0 = (int64_t)s * rows_per_split;
@@ -371,7 +381,7 @@ mode_wgrad(const T* __restrict__ Abar, const T* __restrict__ X, int64_t x_mode, 
   auto stage_copy = [&](int64_t rb, int st) {
     T* As = smem + st * 2 * kWgRows * kWgLd;
     T* Xs = As + kWgRows * kWgLd;
-    for (int e = tid; e < kWgRows * kWgTile; e += 256) {
+    for (int e = tid; e < kWgRows * kWgTile; e += NT) {
       const int rr = e / kWgTile, cc = e % kWgTile;
       const int64_t r = rb + rr;
       const bool ra = r < r1 && o0 + cc < N, rx = r < r1 && i0 + cc < Kin;
@@ -434,19 +444,38 @@ __global__ void mode_wgrad_reduce(const T* __restrict__ part, int splits, int64_
   }
 }
 
-// gb[b][o] (+)= sum_p Abar[b][p][0][o]; one warp per (b, o), lanes over points.
+// gb[b][o] (+)= sum_p Abar[b][p][0][o].  One block of 16 warps per mode b:
+// warp w sums points w, w + 16, ..., its lanes reading 32 consecutive
+// columns of a point's value row; the partial sums are added in a fixed
+// order.
+constexpr int kBiasWarps = 16;
 template <typename T, int C>
-__global__ void mode_bias(const T* __restrict__ Abar, int n, int N, int B, int accumulate,
-                          T* __restrict__ gb) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (w >= B * N) return;
-  const int mb = w / N, o = w % N;
-  const T* a = Abar + (int64_t)mb * n * C * N + o;
-  T s = T(0);
-  for (int p = lane; p < n; p += 32) s += a[(int64_t)p * C * N];
+__global__ void __launch_bounds__(32 * kBiasWarps)
+mode_bias(const T* __restrict__ Abar, int n, int N, int accumulate, T* __restrict__ gb) {
+  __shared__ T red[kBiasWarps][32];
+  const int mb = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const T* a = Abar + (int64_t)mb * n * C * N;
+  for (int o0 = 0; o0 < N; o0 += 32) {
+    const int o = o0 + lane;
+    T acc[4] = {T(0), T(0), T(0), T(0)};  // four independent chains hide the load latency
+    if (o < N) {
+      int p = w;
+      for (; p + 3 * kBiasWarps < n; p += 4 * kBiasWarps)
 #pragma unroll
-  for (int sh = 16; sh > 0; sh >>= 1) s += __shfl_xor_sync(0xffffffffu, s, sh);
-  if (lane == 0) gb[w] = accumulate ? gb[w] + s : s;
+        for (int k = 0; k < 4; ++k) acc[k] += a[(int64_t)(p + k * kBiasWarps) * C * N + o];
+      for (; p < n; p += kBiasWarps) acc[0] += a[(int64_t)p * C * N + o];
+    }
+    red[w][lane] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+    __syncthreads();
+    if (w == 0 && o < N) {
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < kBiasWarps; ++k) s += red[k][lane];
+      T* g = gb + (int64_t)mb * N + o;
+      *g = accumulate ? *g + s : s;
+    }
+    __syncthreads();
+  }
 }
 
 // adjoint of the raw output: b = envelope_mul_reverse(env, a), [B][n][C][N]
@@ -742,6 +771,28 @@ ModeWs mode_ws(const neb_modes* m, int B, int64_t n) {
   return w;
 }
 
+template <typename T, int DIM, int ORD, int EPI, int TC>
+int run_mode_gemm(int dev, const T* A, int64_t a_mode, const T* W, int64_t w_mode,
+                  const T* bias, int64_t b_mode, const T* env, const T* pre_in, T* pre_out,
+                  T* out, int64_t o_mode, int B, int n, int Kd, int N, double omega,
+                  cudaStream_t s) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  static bool configured[kMaxDevices] = {};
+  constexpr int smem = mode_gemm_smem<T, C, TC>();
+  if (!configured[dev]) {
+    NEB_CUDA_CHECK(cudaFuncSetAttribute(mode_gemm<T, DIM, ORD, EPI, TC>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured[dev] = true;
+  }
+  NEB_REQUIRE(ceil_div(N, TC) <= 65535, "mode GEMM: width %d too large", N);
+  dim3 grid((unsigned)ceil_div(n, tile_pts<T, TC>()), (unsigned)ceil_div(N, TC), (unsigned)B);
+  mode_gemm<T, DIM, ORD, EPI, TC><<<grid, 128, smem, s>>>(A, a_mode, W, w_mode, bias, b_mode,
+                                                          env, pre_in, pre_out, out, o_mode, n,
+                                                          Kd, N, (T)omega);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
 template <typename T, int DIM, int ORD, int EPI>
 int launch_mode_gemm(const T* A, int64_t a_mode, const T* W, int64_t w_mode, const T* bias,
                      int64_t b_mode, const T* env, const T* pre_in, T* pre_out, T* out,
@@ -767,20 +818,13 @@ int launch_mode_gemm(const T* A, int64_t a_mode, const T* W, int64_t w_mode, con
     NEB_LAUNCH_CHECK();
     return NEB_OK;
   }
-  static bool configured[kMaxDevices] = {};
-  constexpr int smem = mode_gemm_smem<T, C>();
-  if (!configured[dev]) {
-    NEB_CUDA_CHECK(cudaFuncSetAttribute(mode_gemm<T, DIM, ORD, EPI>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    configured[dev] = true;
-  }
-  NEB_REQUIRE(ceil_div(N, tile_cols<T>()) <= 65535, "mode GEMM: width %d too large", N);
-  dim3 grid((unsigned)ceil_div(n, kTilePts), (unsigned)ceil_div(N, tile_cols<T>()), (unsigned)B);
-  mode_gemm<T, DIM, ORD, EPI><<<grid, 128, smem, s>>>(A, a_mode, W, w_mode, bias, b_mode, env,
-                                                      pre_in, pre_out, out, o_mode, n, Kd, N,
-                                                      (T)omega);
-  NEB_LAUNCH_CHECK();
-  return NEB_OK;
+  if (N <= kNarrowTile)
+    return run_mode_gemm<T, DIM, ORD, EPI, kNarrowTile>(dev, A, a_mode, W, w_mode, bias, b_mode,
+                                                        env, pre_in, pre_out, out, o_mode, B, n,
+                                                        Kd, N, omega, s);
+  return run_mode_gemm<T, DIM, ORD, EPI, tile_cols<T>()>(dev, A, a_mode, W, w_mode, bias, b_mode,
+                                                         env, pre_in, pre_out, out, o_mode, B, n,
+                                                         Kd, N, omega, s);
 }
 
 template <typename T, int DIM, int ORD>
@@ -816,6 +860,23 @@ int modes_forward_t(const neb_modes* m, int start, int B, const void* const* Wv,
   return NEB_OK;
 }
 
+template <typename T, int WT>
+int run_mode_wgrad(int dev, dim3 grid, const T* Abar, const T* X, int64_t x_mode, int64_t rows,
+                   int N, int Kin, int64_t per, T* part, cudaStream_t s) {
+  static bool configured[kMaxDevices] = {};
+  if (!configured[dev]) {
+    NEB_CUDA_CHECK(cudaFuncSetAttribute(mode_wgrad<T, WT>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        mode_wgrad_smem<T, WT>()));
+    configured[dev] = true;
+  }
+  mode_wgrad<T, WT><<<grid, wg_threads<WT>(), mode_wgrad_smem<T, WT>(), s>>>(Abar, X, x_mode,
+                                                                             rows, N, Kin, per,
+                                                                             part);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
 template <typename T, int DIM, int ORD>
 int modes_backward_t(const neb_modes* m, int start, int B, const void* const* Wv, const T* feats,
                      const T* env, int64_t n, const char* tape, const T* adjoint,
@@ -843,26 +904,24 @@ int modes_backward_t(const neb_modes* m, int start, int B, const void* const* Wv
     const int64_t x_mode = j == 0 ? 0 : (int64_t)n * C * in;
     const int64_t rows = n * C;
     // weight gradient, split over row ranges so that B x tiles x splits
-    // covers the SMs about twice
-    const int tiles = (int)(ceil_div(o, kWgTile) * ceil_div(in, kWgTile));
+    // covers the SMs about twice (in 256-thread equivalents)
+    const bool narrow = o <= 32 && in <= 32;
+    const int wt = narrow ? 32 : 64;
+    const int tiles = (int)(ceil_div(o, wt) * ceil_div(in, wt));
+    const int64_t target = narrow ? 8 * sms : 2 * sms;
     int splits = (int)std::max<int64_t>(1, std::min<int64_t>(kMaxWgradSplits,
-                                                             ceil_div(2 * sms, (int64_t)tiles * B)));
+                                                             ceil_div(target, (int64_t)tiles * B)));
     splits = (int)std::min<int64_t>(splits, ceil_div(rows, kWgRows));
     const int64_t per = ceil_div(ceil_div(rows, splits), kWgRows) * kWgRows;
     splits = (int)ceil_div(rows, per);
     {
       KernelScope ks("mode_weight_grad", s, 2.0 * B * rows * (double)o * in,
                      (double)B * rows * (o + in) * sizeof(T));
-      static bool configured[kMaxDevices] = {};
-      if (!configured[dev]) {
-        NEB_CUDA_CHECK(cudaFuncSetAttribute(mode_wgrad<T>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            mode_wgrad_smem<T>()));
-        configured[dev] = true;
-      }
-      mode_wgrad<T><<<dim3(tiles, B, splits), 256, mode_wgrad_smem<T>(), s>>>(
-          buf[cur], X, x_mode, rows, o, in, per, part);
-      NEB_LAUNCH_CHECK();
+      int st = narrow ? run_mode_wgrad<T, 32>(dev, dim3(tiles, B, splits), buf[cur], X, x_mode,
+                                                rows, o, in, per, part, s)
+                      : run_mode_wgrad<T, 64>(dev, dim3(tiles, B, splits), buf[cur], X, x_mode,
+                                                rows, o, in, per, part, s);
+      if (st) return st;
     }
     {
       const int64_t per_split = (int64_t)B * o * in;
@@ -873,8 +932,8 @@ int modes_backward_t(const neb_modes* m, int start, int B, const void* const* Wv
     }
     {
       KernelScope ks("mode_bias_grad", s, 0, (double)B * n * o * sizeof(T));
-      mode_bias<T, C><<<(int)ceil_div((int64_t)B * o * 32, 256), 256, 0, s>>>(
-          buf[cur], (int)n, o, B, accumulate, (T*)gb[j]);
+      mode_bias<T, C><<<B, 32 * kBiasWarps, 0, s>>>(buf[cur], (int)n, o, accumulate,
+                                                    (T*)gb[j]);
       NEB_LAUNCH_CHECK();
     }
     if (j == 0) break;

@@ -277,7 +277,7 @@ extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, dou
   double* err = ortho_error ? ortho_error : err_tmp;
   const int64_t kk_n = (int64_t)K * K;
   cublasHandle_t h = g_peel.blas;
-  const double one = 1.0, zero = 0.0;
+  const double one = 1.0;
   NEB_CUDA_CHECK(cudaMemsetAsync(info, 0, sizeof(int), s));
   {
     KernelScope ks("peel_order", s, 0, 8.0 * K * K);
@@ -306,11 +306,16 @@ extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, dou
              "cublasDtrsm (L^-T)");
     scale_rows<<<grid_for(kk_n), 256, 0, s>>>(T, scale, K);
     NEB_LAUNCH_CHECK();
-    // second pass: H2 = T^T ms T = L2 L2^T, T <- T L2^-T
-    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, ms, K, T, K, &zero, W1, K),
-             "cublasDgemm (ms T)");
-    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, K, K, K, &one, T, K, W1, K, &zero, L2, K),
-             "cublasDgemm (T^T ms T)");
+    // second pass: H2 = T^T ms T = L2 L2^T, T <- T L2^-T.  T is upper
+    // triangular (a scaled inverse transpose of a lower Cholesky factor, and
+    // after the second pass a product of two upper triangles), so every
+    // product with it is a triangular multiply (half a GEMM's work)
+    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, ms, K, W1, K),
+             "cublasDtrmm (ms T)");
+    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, W1, K, L2, K),
+             "cublasDtrmm (T^T ms T)");
     symmetrize<<<grid_for(kk_n), 256, 0, s>>>(L2, K);
     NEB_LAUNCH_CHECK();
     if (cusolverDnDpotrf(g_peel.solver, CUBLAS_FILL_MODE_LOWER, K, L2, K, work, lwork, dinfo) !=
@@ -325,20 +330,26 @@ extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, dou
              "cublasDtrsm (T L2^-T)");
   }
   {
-    KernelScope ks("peel_objective", s, 8.0 * K * (double)K * K, 0);
-    // O = T^T ms T (orthogonality), F = T^T ss T
-    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, ms, K, T, K, &zero, W1, K),
-             "cublasDgemm (ms T)");
-    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, K, K, K, &one, T, K, W1, K, &zero, L, K),
-             "cublasDgemm (T^T ms T)");
-    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, ss, K, T, K, &zero, W1, K),
-             "cublasDgemm (ss T)");
-    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, K, K, K, &one, T, K, W1, K, &zero, F, K),
-             "cublasDgemm (T^T ss T)");
+    KernelScope ks("peel_objective", s, 5.0 * K * (double)K * K, 0);
+    // O = T^T ms T (orthogonality), F = T^T ss T, TF = T triu(F, 1): all
+    // triangular multiplies with the upper triangular T
+    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, ms, K, W1, K),
+             "cublasDtrmm (ms T)");
+    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, W1, K, L, K),
+             "cublasDtrmm (T^T ms T)");
+    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, ss, K, W1, K),
+             "cublasDtrmm (ss T)");
+    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, W1, K, F, K),
+             "cublasDtrmm (T^T ss T)");
     peel_gate<<<1, 1024, 0, s>>>(T, ms, L, F, K, mass_floor, losses, norm, rel, err, info);
     NEB_LAUNCH_CHECK();
-    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, K, K, &one, T, K, F, K, &zero, TF, K),
-             "cublasDgemm (T triu(F))");
+    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
+                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, F, K, TF, K),
+             "cublasDtrmm (T triu(F))");
     peel_adjoints<<<grid_for(kk_n), 256, 0, s>>>(T, TF, losses, norm, order, K, Cu, Cd, T_out);
     NEB_LAUNCH_CHECK();
   }
@@ -347,11 +358,26 @@ extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, dou
 
 extern "C" size_t neb_column_apply_workspace_bytes(int64_t rows, int K) {
   if (rows <= 0 || K <= 0) return 0;
-  return 2 * a256((size_t)rows * K * sizeof(double));
+  return 2 * a256((size_t)K * K * sizeof(float));
 }
 
-// out = scale * A C, A [rows][K] (FP32 or FP64, row-major), C [K][K] FP64
-// row-major, computed in FP64 (cuBLAS DGEMM), out in A's type.
+// scale * C (FP64) as an unevaluated sum of two floats: hi = fl(x), lo = fl(x - hi).
+__global__ void split_scaled(const double* __restrict__ C, double scale, int64_t n,
+                             float* __restrict__ hi, float* __restrict__ lo) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = scale * C[i];
+    const float h = (float)x;
+    hi[i] = h;
+    lo[i] = (float)(x - (double)h);
+  }
+}
+
+// out = scale * A C, A [rows][K] (row-major), C [K][K] FP64 row-major, out
+// in A's type.  FP64: one cuBLAS DGEMM.  FP32: A is exact in FP32 and
+// scale * C enters as hi + lo (48 bits), two FP32 SGEMMs (out = A hi, then
+// out += A lo) -- the FP32 accumulation is the only rounding beyond the
+// output's own, and FP64 DGEMM runs at ~1/60 of the FP32 rate on this GPU.
 extern "C" int neb_column_apply(int precision, int64_t rows, int K, const void* A,
                                 const double* Cm, double scale, void* out, void* workspace,
                                 size_t workspace_bytes, neb_stream_t stream) {
@@ -362,10 +388,9 @@ extern "C" int neb_column_apply(int precision, int64_t rows, int K, const void* 
   cudaStream_t s = (cudaStream_t)stream;
   int st = peel_handles(s);
   if (st) return st;
-  const int64_t total = rows * K;
   cublasHandle_t h = g_peel.blas;
-  const double zero = 0.0;
   if (precision == NEB_PREC_FP64) {
+    const double zero = 0.0;
     KernelScope ks("cublas_dgemm", s, 2.0 * rows * (double)K * K, 0);
     // row-major out = A C  <=>  column-major out^T = C^T A^T
     NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, (int)rows, K, &scale, Cm, K,
@@ -377,23 +402,27 @@ extern "C" int neb_column_apply(int precision, int64_t rows, int K, const void* 
     set_error("neb_column_apply: workspace too small");
     return NEB_ERR_WORKSPACE;
   }
-  double* A64 = (double*)workspace;
-  double* O64 = (double*)((char*)workspace + a256((size_t)rows * K * sizeof(double)));
+  const int64_t kk = (int64_t)K * K;
+  float* hi = (float*)workspace;
+  float* lo = (float*)((char*)workspace + a256((size_t)kk * sizeof(float)));
   {
-    KernelScope ks("convert", s, 0, 12.0 * total);
-    convert<float, double><<<grid_for(total), 256, 0, s>>>((const float*)A, A64, total, 1.0);
+    KernelScope ks("split_scaled", s, 0, 16.0 * kk);
+    split_scaled<<<grid_for(kk), 256, 0, s>>>(Cm, scale, kk, hi, lo);
     NEB_LAUNCH_CHECK();
   }
   {
-    KernelScope ks("cublas_dgemm", s, 2.0 * rows * (double)K * K, 0);
-    NEB_BLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, (int)rows, K, &scale, Cm, K, A64, K,
-                         &zero, O64, K),
-             "cublasDgemm (columns)");
-  }
-  {
-    KernelScope ks("convert", s, 0, 12.0 * total);
-    convert<double, float><<<grid_for(total), 256, 0, s>>>(O64, (float*)out, total, 1.0);
-    NEB_LAUNCH_CHECK();
+    KernelScope ks("cublas_sgemm", s, 4.0 * rows * (double)K * K, 0);
+    cublasSetMathMode(h, CUBLAS_PEDANTIC_MATH);  // plain FP32 products, no TF32
+    const float one = 1.f, zero = 0.f;
+    const cublasStatus_t r1 = cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, (int)rows, K, &one,
+                                          hi, K, (const float*)A, K, &zero, (float*)out, K);
+    const cublasStatus_t r2 = cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, K, (int)rows, K, &one,
+                                          lo, K, (const float*)A, K, &one, (float*)out, K);
+    cublasSetMathMode(h, CUBLAS_DEFAULT_MATH);
+    if (r1 != CUBLAS_STATUS_SUCCESS || r2 != CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasSgemm (columns) failed");
+      return NEB_ERR_CUDA;
+    }
   }
   return NEB_OK;
 }

@@ -375,7 +375,7 @@ class HardcodedModel:
 
 
 # ------------------------------------------------------------------ peel step
-TAPE_BUDGET = 1 << 30  # bytes of activation tape one block of modes may hold
+TAPE_BUDGET = 16 << 30  # bytes of activation tape one block of modes may hold
 
 
 def _block(core: ModeModel, n: int) -> int:

@@ -339,7 +339,8 @@ def column_gram(A: torch.Tensor, scale: float, compensated: bool = True) -> torc
 
 
 def column_apply(A: torch.Tensor, C: torch.Tensor, scale: float) -> torch.Tensor:
-    """scale A C computed in FP64 (A [rows, K], C [K, K] FP64), in A's type."""
+    """scale A C (A [rows, K], C [K, K] FP64) in A's type: FP64 GEMM for
+    FP64 A; for FP32 A, scale C split into two floats and FP32 GEMMs."""
     rows, K = A.shape
     lib = N.load()
     out = torch.empty_like(A)
