@@ -365,6 +365,66 @@ int neb_potential_lift(int precision, const void* dV, const void* dG, int start,
                        int64_t n_points, int n_modes, void* adjoint, neb_stream_t stream);
 int neb_column_center(int precision, int64_t rows, int K, void* A, neb_stream_t stream);
 
+/* ---- Periodic evaluation of a trained basis (no counterpart entry points in
+ * the reference; they replace its CuPy code at the lines cited). ----
+ *
+ * Fourier feature jets of order 1, 2 or 3 (3, 6 or 10 channels: value,
+ * d/dx, d/dy, xx, xy, yy, xxx, xxy, xyy, yyy) of points already shifted to
+ * the box origin, [n][C][4 n_freq]: sin and cos of 2 pi h s / L for s = x,
+ * then y, h = 1..n_freq (HB:418-438 encoding_jet1, HB:791-809 for Jet3;
+ * the reference's pi h (s_n + 1)). */
+int neb_periodic_features(int precision, int order, int n_freq, double length_x,
+                          double length_y, const double* points, int64_t n_points,
+                          void* features, neb_stream_t stream);
+
+/* Stream-function fields of modes [start, stop) from their output jets
+ * [stop-start][n][C][1] (order 2 or 3): UV [n][2][n_modes] (u = psi_y,
+ * v = -psi_x), Om [n][n_modes] (omega = -lap psi) and, with order 3 and diag
+ * not NULL, diag [n][3][n_modes] (psi, -lap u, -lap v) -- the six channels of
+ * evaluate_large_comparison.py:29-35. */
+int neb_stream_fields(int precision, int order, const void* out, int start, int stop,
+                      int64_t n_points, int n_modes, void* UV, void* Om, void* diag,
+                      neb_stream_t stream);
+
+/* In place: norm_k = sqrt(M_kk), M_ij /= norm_i norm_j, S_ij /= norm_i
+ * norm_j -- the unit-velocity normalisation of every mode before the Ritz
+ * stage (ROLL:173-176), applied to the Grams instead of the fields. */
+int neb_normalize_pencil(int K, double* M, double* S, double* norm, neb_stream_t stream);
+
+/* R [K][K] = D^-1 T with T[:, i] = V[i] (rows of V: M-orthonormal
+ * eigenvectors, as neb_spectral writes them) and D = diag(norm): the map
+ * from Ritz coefficients to coefficients of the raw fields (ROLL:187-192). */
+int neb_ritz_transform(int K, const double* V, const double* norm, double* R,
+                       neb_stream_t stream);
+
+/* ETDRK4 weights coef [6][K] = (e, e2, q, f1, f2, f3) for the linear part
+ * -nu lam and step h, phi functions by the 32-point contour mean (ROLL:56-64). */
+int neb_etdrk4_coefficients(int K, const double* lam, double nu, double h, double* coef,
+                            neb_stream_t stream);
+
+/* Matrix-free Galerkin right-hand side in the Ritz basis (ROLL:37-41):
+ * out = R^T [U^T (w omega v) - V^T (w omega u)] with (u, v, omega) =
+ * (UV[:,0], UV[:,1], Om) R x, FP64 result; FP32 fields are summed with
+ * compensated FP32 arithmetic.  neb_etdrk4_step advances c (FP64 [K]) by one
+ * ETDRK4 step with the weights of neb_etdrk4_coefficients (ROLL:65-72);
+ * neb_rollout_project gives the Ritz coefficients of a velocity field,
+ * c = R^T w (U^T u0 + V^T v0) (ROLL:197); neb_rollout_fields writes
+ * fields [3][n] = (u, v, omega) of the coefficients c.  No host
+ * synchronisation; the step graph-captures. */
+size_t neb_rollout_workspace_bytes(int64_t n_points, int K);
+int neb_rollout_rhs(int precision, int64_t n_points, int K, const void* UV, const void* Om,
+                    const double* R, double weight, const double* x, double* out,
+                    void* workspace, size_t workspace_bytes, neb_stream_t stream);
+int neb_etdrk4_step(int precision, int64_t n_points, int K, const void* UV, const void* Om,
+                    const double* R, double weight, const double* coef, double* c,
+                    void* workspace, size_t workspace_bytes, neb_stream_t stream);
+int neb_rollout_project(int precision, int64_t n_points, int K, const void* UV, const double* R,
+                        const double* u0, const double* v0, double weight, double* c,
+                        void* workspace, size_t workspace_bytes, neb_stream_t stream);
+int neb_rollout_fields(int precision, int64_t n_points, int K, const void* UV, const void* Om,
+                       const double* R, const double* c, double* fields, void* workspace,
+                       size_t workspace_bytes, neb_stream_t stream);
+
 /* Per-mode Adam (NCC:156-171 Model.adam; HB:2184-2277 adam_step_jet1_device):
  * the clip norm of mode k runs over mode k's slice of every tensor (tensors
  * stacked [n_modes][...], sizes[i] elements in total); beta1 0.9, beta2

@@ -122,6 +122,20 @@ _SIGNATURES = {
     "neb_potential_fields": (c_int, [c_int, _P, c_int, c_int, c_int64, c_int, _P, _P, _P]),
     "neb_potential_lift": (c_int, [c_int, _P, _P, c_int, c_int, c_int64, c_int, _P, _P]),
     "neb_column_center": (c_int, [c_int, c_int64, c_int, _P, _P]),
+    "neb_periodic_features": (c_int, [c_int, c_int, c_int, c_double, c_double, _P, c_int64, _P,
+                                      _P]),
+    "neb_stream_fields": (c_int, [c_int, c_int, _P, c_int, c_int, c_int64, c_int, _P, _P, _P, _P]),
+    "neb_normalize_pencil": (c_int, [c_int, _P, _P, _P, _P]),
+    "neb_ritz_transform": (c_int, [c_int, _P, _P, _P, _P]),
+    "neb_etdrk4_coefficients": (c_int, [c_int, _P, c_double, c_double, _P, _P]),
+    "neb_rollout_workspace_bytes": (c_size_t, [c_int64, c_int]),
+    "neb_rollout_rhs": (c_int, [c_int, c_int64, c_int, _P, _P, _P, c_double, _P, _P, _P,
+                                c_size_t, _P]),
+    "neb_etdrk4_step": (c_int, [c_int, c_int64, c_int, _P, _P, _P, c_double, _P, _P, _P,
+                                c_size_t, _P]),
+    "neb_rollout_project": (c_int, [c_int, c_int64, c_int, _P, _P, _P, _P, c_double, _P, _P,
+                                    c_size_t, _P]),
+    "neb_rollout_fields": (c_int, [c_int, c_int64, c_int, _P, _P, _P, _P, _P, _P, c_size_t, _P]),
     "neb_modes_adam_workspace_bytes": (c_size_t, [c_int]),
     "neb_modes_adam": (c_int, [c_int, c_int, c_int, _PP, _PP, _PP, _PP, POINTER(c_int64), _P,
                                c_int, _P, _P, c_double, c_double, _P, _P, _P, c_size_t, _P]),

@@ -21,7 +21,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libneb_gb300.so"
-SOURCES = ["abi.cu", "spectral.cu", "spectral_mixed.cu", "tc_path.cu", "modes.cu", "peel.cu"]
+SOURCES = ["abi.cu", "spectral.cu", "spectral_mixed.cu", "tc_path.cu", "modes.cu", "peel.cu",
+           "rollout.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

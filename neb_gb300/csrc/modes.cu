@@ -40,12 +40,20 @@ __host__ __device__ constexpr int pair_j(int dim, int k) {
   return dim == 2 ? (k == 0 ? 0 : 1) : (k < 3 ? k : (k == 3 ? 1 : 2));
 }
 
+// Channels of a jet: value, gradient, compact Hessian (order >= 2) and, for
+// order 3 in 2D, the third derivatives (xxx, xxy, xyy, yyy) -- the layout of
+// the reference's Jet3 (hardcoded_backend.py:58-152).  Order 3 is a forward
+// (evaluation) jet only.
 template <int DIM, int ORD> struct Jet {
-  static constexpr int NH = ORD == 2 ? DIM * (DIM + 1) / 2 : 0;
-  static constexpr int C = 1 + DIM + NH;
+  static_assert(ORD >= 1 && ORD <= 3 && (ORD < 3 || DIM == 2), "jet order");
+  static constexpr int NH = ORD >= 2 ? DIM * (DIM + 1) / 2 : 0;
+  static constexpr int NT = ORD == 3 ? 4 : 0;
+  static constexpr int C = 1 + DIM + NH + NT;
 };
 
-// y = sin z, grad y = cos z grad z, H y = cos z H z - sin z grad z grad z^T
+// y = sin z, grad y = cos z grad z, H y = cos z H z - sin z grad z grad z^T,
+// and in 2D to third order
+//   y_ijk = cos z z_ijk - sin z (z_ij z_k + z_ik z_j + z_jk z_i) - cos z z_i z_j z_k.
 template <int DIM, int ORD, typename T>
 __device__ __forceinline__ void sine_jet(const T* z, T* y) {
   T s, c;
@@ -56,6 +64,13 @@ __device__ __forceinline__ void sine_jet(const T* z, T* y) {
 #pragma unroll
   for (int k = 0; k < Jet<DIM, ORD>::NH; ++k)
     y[1 + DIM + k] = c * z[1 + DIM + k] - s * z[1 + pair_i(DIM, k)] * z[1 + pair_j(DIM, k)];
+  if constexpr (ORD == 3) {
+    const T zx = z[1], zy = z[2], hxx = z[3], hxy = z[4], hyy = z[5];
+    y[6] = c * z[6] - s * (3 * hxx * zx) - c * zx * zx * zx;
+    y[7] = c * z[7] - s * (hxx * zy + 2 * hxy * zx) - c * zx * zx * zy;
+    y[8] = c * z[8] - s * (hyy * zx + 2 * hxy * zy) - c * zx * zy * zy;
+    y[9] = c * z[9] - s * (3 * hyy * zy) - c * zy * zy * zy;
+  }
 }
 
 // Transpose of sine_jet at z: adjoint a of y -> adjoint b of z.
@@ -264,7 +279,7 @@ mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int6
       const int64_t base = (int64_t)p * C * N + o;
       if constexpr (EPI == EPI_OUTPUT) {
         z[0] += bias[mb * b_mode + o];
-        if (env) {
+        if (ORD < 3 && env) {  // third-order jets take the identity envelope
           T e[C];
 #pragma unroll
           for (int c = 0; c < C; ++c) e[c] = env[(int64_t)p * C + c];
@@ -344,10 +359,15 @@ mode_output_narrow(const T* __restrict__ A, int64_t a_mode, const T* __restrict_
   const int p = p0 + pl;
   if (u >= N || p >= n) return;
   T e[C], y[C];
-#pragma unroll
-  for (int c = 0; c < C; ++c) e[c] = env ? env[(int64_t)p * C + c] : (c == 0 ? T(1) : T(0));
   acc[0] += bias[mb * b_mode + u];
-  envelope_mul<DIM, ORD>(e, acc, y);
+  if constexpr (ORD == 3) {  // third-order jets take the identity envelope
+#pragma unroll
+    for (int c = 0; c < C; ++c) y[c] = acc[c];
+  } else {
+#pragma unroll
+    for (int c = 0; c < C; ++c) e[c] = env ? env[(int64_t)p * C + c] : (c == 0 ? T(1) : T(0));
+    envelope_mul<DIM, ORD>(e, acc, y);
+  }
   T* o = out + mb * o_mode + (int64_t)p * C * N;
 #pragma unroll
   for (int c = 0; c < C; ++c) o[(int64_t)c * N + u] = y[c];
@@ -706,13 +726,14 @@ __global__ void mode_adam_update(ModeAdamTable mt, const double* __restrict__ pa
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
 int mode_channels(const neb_modes* m) {
-  return 1 + m->dim + (m->order == 2 ? m->dim * (m->dim + 1) / 2 : 0);
+  return 1 + m->dim + (m->order >= 2 ? m->dim * (m->dim + 1) / 2 : 0) + (m->order == 3 ? 4 : 0);
 }
 
 int check_modes(const neb_modes* m) {
   NEB_REQUIRE(m != nullptr, "null neb_modes");
   NEB_REQUIRE(m->dim == 2 || m->dim == 3, "neb_modes.dim must be 2 or 3");
-  NEB_REQUIRE(m->order == 1 || m->order == 2, "neb_modes.order must be 1 or 2");
+  NEB_REQUIRE(m->order == 1 || m->order == 2 || (m->order == 3 && m->dim == 2),
+              "neb_modes.order must be 1 or 2 (or 3 in 2D)");
   NEB_REQUIRE(m->n_layers >= 1 && m->n_layers <= NEB_MAX_HIDDEN + 1,
               "neb_modes.n_layers must be in [1, %d]", NEB_MAX_HIDDEN + 1);
   for (int l = 0; l <= m->n_layers; ++l)
@@ -1011,6 +1032,14 @@ extern "C" int neb_modes_forward(const neb_modes* m, int start, int stop, const 
     set_error("neb_modes_forward: tape smaller than neb_modes_tape_bytes");
     return NEB_ERR_WORKSPACE;
   }
+  if (m->order == 3) {
+    NEB_REQUIRE(!envelope, "neb_modes_forward: third-order jets take the identity envelope");
+    return m->precision == NEB_PREC_FP64
+               ? modes_forward_d<double, 2, 3>(m, start, B, W, b, features, envelope, n_points,
+                                               tape, out, (cudaStream_t)stream)
+               : modes_forward_d<float, 2, 3>(m, start, B, W, b, features, envelope, n_points,
+                                              tape, out, (cudaStream_t)stream);
+  }
   return NEB_MODES_DISPATCH(m, modes_forward_d, m, start, B, W, b, features, envelope, n_points,
                             tape, out, (cudaStream_t)stream);
 }
@@ -1035,6 +1064,7 @@ extern "C" int neb_modes_backward(const neb_modes* m, int start, int stop, const
     set_error("neb_modes_backward: workspace smaller than neb_modes_workspace_bytes");
     return NEB_ERR_WORKSPACE;
   }
+  NEB_REQUIRE(m->order <= 2, "neb_modes_backward: third-order jets are forward only");
   return NEB_MODES_DISPATCH(m, modes_backward_d, m, start, B, W, features, envelope, n_points,
                             tape, adjoint, gW, gb, accumulate, workspace, (cudaStream_t)stream);
 }

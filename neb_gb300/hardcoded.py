@@ -182,17 +182,23 @@ class HardcodedModel:
             steps.append(s.pop())
         self.steps = torch.tensor(steps, dtype=torch.int32, device=core.device)
         self.modes = [HardcodedMode(self, k) for k in range(K)]
-        n1 = core.net
-        self._nets = {1: n1, 2: ModeNet(2, 2, n1.n_layers, n1.widths, K, n1.precision,
-                                        n1.omega_first, n1.omega_hidden)}
+        self._nets = {1: core.net}
+
+    def _net(self, order: int):
+        """The stacked network's shape with jets of ``order`` (1, 2 or 3)."""
+        if order not in self._nets:
+            n1 = self._nets[1]
+            self._nets[order] = ModeNet(2, order, n1.n_layers, n1.widths, self.core.K,
+                                        n1.precision, n1.omega_first, n1.omega_hidden)
+        return self._nets[order]
 
     @contextmanager
     def _order(self, order: int):
-        """The stacked network with jets of ``order`` (1 or 2) for the
+        """The stacked network with jets of ``order`` (1, 2 or 3) for the
         duration of one call."""
         core = self.core
         saved = core.net, core.order
-        core.net, core.order = self._nets[order], order
+        core.net, core.order = self._net(order), order
         try:
             yield core
         finally:
@@ -200,16 +206,19 @@ class HardcodedModel:
 
     # ------------------------------------------------------------ features
     def features(self, cfg, points, order: int = 1) -> torch.Tensor:
-        """Input feature jets [n, C, F] (C = 3 for order 1, 6 for order 2 with
-        xx, xy, yy) of points [n, 2]: sin / cos of pi h (s_n + 1) for the
-        coordinate s_n normalised to [-1, 1], h = 1..cfg.frequencies, x then
-        y (hardcoded_backend.py:418-438, :566-600), or the raw coordinates."""
+        """Input feature jets [n, C, F] (C = 3, 6, 10 for order 1, 2, 3:
+        value, x, y[, xx, xy, yy[, xxx, xxy, xyy, yyy]]) of points [n, 2]:
+        sin / cos of pi h (s_n + 1) for the coordinate s_n normalised to
+        [-1, 1], h = 1..cfg.frequencies, x then y (hardcoded_backend.py:
+        418-438 and the Jet2 / Jet3 encodings), or the raw coordinates."""
         core = self.core
         pts = torch.as_tensor(points, device=core.device).to(torch.float64).contiguous()
         if pts.ndim != 2 or pts.shape[1] != 2:
             raise ValueError("points must be [n, 2]")
+        if order not in (1, 2, 3):
+            raise ValueError("jet order 1, 2 or 3")
         n = pts.shape[0]
-        C = 3 if order == 1 else 6
+        C = (3, 6, 10)[order - 1]
         if _trial_space(cfg) == FREE:
             f = torch.zeros((n, C, 2), dtype=core.dtype, device=core.device)
             f[:, 0] = pts.to(core.dtype)
@@ -220,26 +229,13 @@ class HardcodedModel:
         if core.widths[0] != 4 * Fq:
             raise ValueError(f"first layer takes {core.widths[0]} inputs, the encoding "
                              f"{4 * Fq}")
-        lx, ly = float(cfg.xmax - cfg.xmin), float(cfg.ymax - cfg.ymin)
         origin = torch.tensor([cfg.xmin, cfg.ymin], dtype=torch.float64, device=core.device)
-        shifted = pts - origin
-        if ly != lx:
-            shifted[:, 1] *= lx / ly  # one period for both axes; derivatives rescaled below
-        net = N.NebNet.make(2, [4 * Fq, 1, 1], core.precision)
-        lap4 = torch.empty((n, 4, 4 * Fq), dtype=core.dtype, device=core.device)
-        prm = (ctypes.c_double * 1)(lx)
-        N.call("neb_features", ctypes.byref(net), N.FEAT["periodic"], Fq, prm, 1,
-               shifted.contiguous().data_ptr(), n, lap4.data_ptr(), _stream())
-        if ly != lx:
-            lap4[:, 2, 2 * Fq:] *= lx / ly
-            lap4[:, 3, 2 * Fq:] *= (lx / ly) ** 2
-        if order == 1:
-            return lap4[:, :3].contiguous()
-        f = torch.zeros((n, 6, 4 * Fq), dtype=core.dtype, device=core.device)
-        f[:, :3] = lap4[:, :3]
-        f[:, 3, :2 * Fq] = lap4[:, 3, :2 * Fq]   # x-features: the Laplacian is hxx
-        f[:, 5, 2 * Fq:] = lap4[:, 3, 2 * Fq:]   # y-features: the Laplacian is hyy
-        return f
+        shifted = (pts - origin).contiguous()
+        out = torch.empty((n, C, 4 * Fq), dtype=core.dtype, device=core.device)
+        N.call("neb_periodic_features", N.PREC[core.precision], order, Fq,
+               float(cfg.xmax - cfg.xmin), float(cfg.ymax - cfg.ymin), shifted.data_ptr(), n,
+               out.data_ptr(), _stream())
+        return out
 
     # ------------------------------------------------------------- forward
     def _forward_block(self, feats, start, stop, cache, order):
@@ -269,6 +265,36 @@ class HardcodedModel:
                             cache: bool = False):
         """(mode, Jet(value, grad, hess [n, 1, 3] = xx, xy, yy), cache)."""
         yield from self._stream_fields(cfg, points, cache, 2)
+
+    def forward_stream(self, cfg, points, beta: float = 0.0, alpha: float = 0.0,
+                       cache: bool = False, mode_indices=None):
+        """(mode, Jet(value, grad, hess, third [n, 1, 4] = xxx, xxy, xyy,
+        yyy), None) for every mode: the reference's third-order evaluation
+        stream (hardcoded_backend.py:1882-1986), in network order (a given
+        mode_indices must be a permutation of all modes and sets the order).
+        Evaluation only: no reverse pass of third-order jets."""
+        if cache:
+            raise NotImplementedError("third-order jets are evaluation only (cache=False)")
+        K = self.core.K
+        order = list(range(K)) if mode_indices is None else [int(i) for i in mode_indices]
+        if sorted(order) != list(range(K)):
+            raise ValueError("mode_indices must be a permutation of all modes")
+        feats = self.features(cfg, points, 3)
+        block = max(1, int(getattr(cfg, "mode_forward_batch", 1)))
+        cached = {}
+        for start in range(0, K, block):
+            stop = min(K, start + block)
+            for k in order[start:stop]:
+                if k not in cached:
+                    cached.clear()
+                    a = (k // block) * block
+                    out, _ = self._forward_block(feats, a, min(K, a + block), False, 3)
+                    for j in range(a, min(K, a + block)):
+                        cached[j] = out[j - a]
+                o = cached[k]  # [n, 10, 1]
+                yield self.modes[k], Jet(o[:, 0], o[:, 1:3].permute(0, 2, 1),
+                                         hess=o[:, 3:6].permute(0, 2, 1),
+                                         third=o[:, 6:10].permute(0, 2, 1)), None
 
     # ------------------------------------------------------------- reverse
     def _backward_block(self, modes, caches, field_adjoints, order):

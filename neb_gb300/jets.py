@@ -21,6 +21,7 @@ class Jet:
     grad: torch.Tensor
     lap: torch.Tensor | None = None
     hess: torch.Tensor | None = None
+    third: torch.Tensor | None = None  # 2D third derivatives (xxx, xxy, xyy, yyy)
 
     @property
     def dim(self) -> int:

@@ -579,20 +579,28 @@ def jet_pairs(dim):
 
 
 def jet_channels_of(dim, order):
-    return 1 + dim + (len(jet_pairs(dim)) if order == 2 else 0)
+    return 1 + dim + (len(jet_pairs(dim)) if order >= 2 else 0) + (4 if order == 3 else 0)
 
 
 def sine_jet_forward(Z, dim, order):
     """y = sin z, grad y = cos z grad z, H y = cos z H z - sin z grad z grad z^T
-    (velocity_trace_jet2.py:31-34; hardcoded_backend.py sine_forward_jet1)."""
+    (velocity_trace_jet2.py:31-34; hardcoded_backend.py sine_forward_jet1);
+    order 3 (2D): third derivatives (xxx, xxy, xyy, yyy), the chain rule of
+    the reference's Jet3 unary (hardcoded_backend.py:58-152)."""
     s, c = np.sin(Z[0]), np.cos(Z[0])
     Y = np.empty_like(Z)
     Y[0] = s
     for a in range(dim):
         Y[1 + a] = c * Z[1 + a]
-    if order == 2:
+    if order >= 2:
         for k, (i, j) in enumerate(jet_pairs(dim)):
             Y[1 + dim + k] = c * Z[1 + dim + k] - s * Z[1 + i] * Z[1 + j]
+    if order == 3:
+        zx, zy, hxx, hxy, hyy = Z[1], Z[2], Z[3], Z[4], Z[5]
+        Y[6] = c * Z[6] - s * 3 * hxx * zx - c * zx ** 3
+        Y[7] = c * Z[7] - s * (hxx * zy + 2 * hxy * zx) - c * zx * zx * zy
+        Y[8] = c * Z[8] - s * (hyy * zx + 2 * hxy * zy) - c * zx * zy * zy
+        Y[9] = c * Z[9] - s * 3 * hyy * zy - c * zy ** 3
     return Y
 
 
@@ -623,11 +631,27 @@ def envelope_product(E, X, dim, order):
     Y[0] = E[0] * X[0]
     for a in range(dim):
         Y[1 + a] = E[0] * X[1 + a] + E[1 + a] * X[0]
-    if order == 2:
+    if order >= 2:
         for k, (i, j) in enumerate(jet_pairs(dim)):
             q = 1 + dim + k
             Y[q] = E[0] * X[q] + E[q] * X[0] + E[1 + i] * X[1 + j] + E[1 + j] * X[1 + i]
+    if order == 3:
+        # d_ijk (e x) = sum over the subsets S of {i, j, k} of d_S e d_(rest) x
+        for q, idx in zip(range(6, 10), ((0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1))):
+            acc = 0.0
+            for mask in range(8):
+                left = tuple(idx[t] for t in range(3) if mask >> t & 1)
+                right = tuple(idx[t] for t in range(3) if not mask >> t & 1)
+                acc = acc + E[_jet3_slot(left)] * X[_jet3_slot(right)]
+            Y[q] = acc
     return Y
+
+
+def _jet3_slot(multi):
+    """Channel of the 2D derivative d_multi in a third-order jet."""
+    m = tuple(sorted(multi))
+    return {(): 0, (0,): 1, (1,): 2, (0, 0): 3, (0, 1): 4, (1, 1): 5, (0, 0, 0): 6,
+            (0, 0, 1): 7, (0, 1, 1): 8, (1, 1, 1): 9}[m]
 
 
 def envelope_product_backward(E, A, dim, order):
@@ -866,3 +890,106 @@ def potential_peel_step(W, b, X0, weight, omegas, lr=None, clip=8.0, moments=Non
         mW, vW, mb, vb = moments
         obj["state"], obj["norms"] = mode_adam(W, b, mW, vW, mb, vb, gW, gb, epoch, lr, clip)
     return obj
+
+
+# --------------------------------------------------------------------------
+# periodic evaluation: Jet3 fields, Ritz basis, ETDRK4 Galerkin rollout
+# --------------------------------------------------------------------------
+def features_periodic_jet(points, frequencies, order, length=2 * math.pi):
+    """Fourier feature jets of order 1, 2 or 3, [C, n, 4F] with channels
+    (value, x, y[, xx, xy, yy[, xxx, xxy, xyy, yyy]]) (hardcoded_backend.py:
+    418-438 and its Jet3 encoding): sin, cos of 2 pi h s / L, s = x then y."""
+    points = np.asarray(points, dtype=np.float64)
+    n = len(points)
+    C = jet_channels_of(2, order)
+    out = np.zeros((C, n, 4 * frequencies))
+    col = 0
+    for axis in range(2):
+        s = points[:, axis]
+        for h in range(1, frequencies + 1):
+            k = 2.0 * math.pi * h / length
+            for fn, d1 in ((np.sin(k * s), k * np.cos(k * s)), (np.cos(k * s), -k * np.sin(k * s))):
+                out[0, :, col] = fn
+                out[1 + axis, :, col] = d1
+                if order >= 2:
+                    out[3 if axis == 0 else 5, :, col] = -k * k * fn
+                if order == 3:
+                    out[6 if axis == 0 else 9, :, col] = -k * k * d1
+                col += 1
+    return out
+
+
+def stream_fields(out):
+    """The six channels of evaluate_large_comparison.py:29-35 from a mode's
+    third-order output jet [10, n, 1]: psi, u = psi_y, v = -psi_x,
+    omega = -lap psi, -lap u, -lap v."""
+    o = out[:, :, 0]
+    return np.stack([o[0], o[2], -o[1], -(o[3] + o[5]), -(o[7] + o[9]), o[6] + o[8]])
+
+
+def ritz_basis(gu, gv, gw, weight, rank_rtol=1e-12):
+    """Normalisation and Ritz stage of paper_rollout.py:171-192: columns
+    scaled to unit velocity norm, M = w (gu^T gu + gv^T gv), S = w gw^T gw,
+    the full-rank gate on eig(M) (rank = #(e > rtol e_max)), eigh(S, M).
+    Returns (vals, R, norm) with R = D^-1 T mapping Ritz coefficients to
+    coefficients of the raw fields."""
+    norm = np.sqrt(weight * np.sum(gu * gu + gv * gv, axis=0))
+    if not np.all(norm > 0):
+        raise ArithmeticError("a mode with zero velocity")
+    U, V, W = gu / norm, gv / norm, gw / norm
+    mass = weight * (U.T @ U + V.T @ V)
+    stiff = weight * (W.T @ W)
+    mh, sh = (mass + mass.T) / 2, (stiff + stiff.T) / 2
+    ev = np.linalg.eigvalsh(mh)
+    rank = int(np.sum(ev > ev[-1] * rank_rtol))
+    if rank != len(mh):
+        raise ArithmeticError("Full-K rank gate")
+    vals, T = sla.eigh(sh, mh)
+    return vals, T / norm[:, None], norm
+
+
+def etdrk4_weights(lam, nu, h):
+    """(e, e2, q, f1, f2, f3) of paper_rollout.py:56-64."""
+    linear = -nu * lam
+    e = np.exp(h * linear)
+    e2 = np.exp(0.5 * h * linear)
+    roots = np.exp(1j * np.pi * (np.arange(1, 33) - 0.5) / 32)
+    lr = h * linear[:, None] + roots
+    q = h * np.real(np.mean((np.exp(lr / 2) - 1) / lr, axis=-1))
+    f1 = h * np.real(np.mean((-4 - lr + np.exp(lr) * (4 - 3 * lr + lr * lr)) / lr ** 3, axis=-1))
+    f2 = h * np.real(np.mean((2 + lr + np.exp(lr) * (-2 + lr)) / lr ** 3, axis=-1))
+    f3 = h * np.real(np.mean((-4 - 3 * lr - lr * lr + np.exp(lr) * (4 - lr)) / lr ** 3, axis=-1))
+    return e, e2, q, f1, f2, f3
+
+
+def galerkin_rhs(gu, gv, gw, weight, a):
+    """rhs(a) = gu^T (w omega v) - gv^T (w omega u), (u, v, omega) = g a
+    (paper_rollout.py:37-41)."""
+    u, v, w = gu @ a, gv @ a, gw @ a
+    return gu.T @ (weight * w * v) - gv.T @ (weight * w * u)
+
+
+def etdrk4_rollout(gu, gv, gw, lam, nu, c0, times, dt, weight):
+    """The autonomous ETDRK4 rollout of paper_rollout.py:31-79 in the (Ritz)
+    basis gu, gv, gw: for every target time, ceil((t - t_prev) / dt) equal
+    steps; returns the coefficient states [frames, K]."""
+    c = np.asarray(c0, dtype=np.float64).copy()
+    current = 0.0
+    states = []
+    for target in times:
+        steps = max(0, int(np.ceil((target - current) / dt - 1e-10)))
+        if steps:
+            h = (target - current) / steps
+            e, e2, q, f1, f2, f3 = etdrk4_weights(lam, nu, h)
+            rhs = lambda x: galerkin_rhs(gu, gv, gw, weight, x)  # noqa: E731
+            for _ in range(steps):
+                nv = rhs(c)
+                a = e2 * c + q * nv
+                na = rhs(a)
+                b = e2 * c + q * na
+                nb = rhs(b)
+                z = e2 * a + q * (2 * nb - nv)
+                c = e * c + f1 * nv + 2 * f2 * (na + nb) + f3 * rhs(z)
+        current = target
+        states.append(c.copy())
+    return np.array(states)

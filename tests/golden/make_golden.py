@@ -26,8 +26,14 @@ Reference functions exercised (paths relative to the reference project):
 * experiments/periodic/paper_rollout.py:178-187 recipe (Grams, then
   ``scipy.linalg.eigh(S, M)``);
 * hardcoded_backend.py ``HardcodedModel`` (:1705) ``forward_stream_jet1``
-  (:1716), ``arrays`` (:1987) and ``peel_step`` (:3774) with the
-  streamfunction Rayleigh peel (:3383) on a four-mode periodic network.
+  (:1716), ``forward_stream`` (third-order jets, :1882), ``arrays`` (:1987)
+  and ``peel_step`` (:3774) with the streamfunction Rayleigh peel (:3383) on
+  a four-mode periodic network;
+* experiments/2d/_backend/flow/cases/vortex_merger/neural_training/
+  prepare_gauge_canonical.py ``main`` (the trainer's epoch-0 arrays and its
+  fixed validation points);
+* experiments/periodic/paper_rollout.py ``rollout`` (:31), the autonomous
+  ETDRK4 Galerkin rollout, on a six-mode basis of the 128^2 grid.
 
 Usage:  NEB_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 """
@@ -87,6 +93,25 @@ def install_shim():
     sys.modules["cupyx.scipy"] = cupyx_scipy
     sys.modules["cupyx.scipy.linalg"] = cupyx_linalg
     return cp
+
+
+ROLLOUT_WAVES = ((1, 0), (0, 1), (1, 1), (2, 1))
+
+
+def rollout_basis(coef, n):
+    """Smooth periodic (u, v, omega) fields of len(coef) modes on the n x n
+    grid, [3, n^2, K]: field f of mode k is sum over the wave vectors (m1, m2)
+    of coef[k, t, f, 0] cos(m1 x + m2 y + coef[k, t, f, 1]) (the same
+    construction as tests/test_rollout_host.py)."""
+    axis = np.arange(n) * 2 * math.pi / n
+    xg, yg = np.meshgrid(axis, axis)
+    basis = np.zeros((3, n * n, len(coef)))
+    for k in range(len(coef)):
+        for t, (m1, m2) in enumerate(ROLLOUT_WAVES):
+            for f in range(3):
+                amp, phase = coef[k, t, f]
+                basis[f, :, k] += (amp * np.cos(m1 * xg + m2 * yg + phase)).ravel()
+    return basis
 
 
 def load(path, name):
@@ -288,6 +313,10 @@ def main():
     g.update(hb_points=hpts,
              hb_value=np.stack([np.asarray(f.value[:, 0]) for _, f, _ in fields]),
              hb_grad=np.stack([np.asarray(f.grad[:, 0]) for _, f, _ in fields]))
+    # third-order jets of the same networks (forward_stream, HB:1882-1986)
+    fields3 = list(hmodel.forward_stream(hcfg, hpts, 0.0, 0.0, False))
+    for name in ("value", "grad", "hess", "third"):
+        g["hb3_" + name] = np.stack([np.asarray(getattr(f, name)[:, 0]) for _, f, _ in fields3])
     for key, value in harr.items():
         g["hb_in." + key] = np.asarray(value)
     res = HB.peel_step(hcfg, hmodel, hpts, 0.0, 0.0, True)
@@ -332,6 +361,34 @@ def main():
                 g["init." + key] = np.asarray(z[key])
         with np.load(Path(tmp) / "run/fixed_validation_iid_uniform_v1.npz") as z:
             g["init_validation_points"] = np.asarray(z["validation_points"][0], np.float64)
+
+    # --- the autonomous ETDRK4 Galerkin rollout (paper_rollout.py rollout) on
+    # a random six-mode basis of the 128^2 grid
+    roll = load(reference_root() / "experiments/periodic/paper_rollout.py", "paper_rollout")
+    nr, kr = 128, 6
+    coef = rng.normal(size=(kr, len(ROLLOUT_WAVES), 3, 2))
+    basis = rollout_basis(coef, nr)  # [3, n^2, K]
+    u0 = (basis[0, :, 0] - 0.7 * basis[0, :, 1] + 0.4 * basis[0, :, 3]).reshape(nr, nr)
+    v0 = (basis[1, :, 0] - 0.7 * basis[1, :, 1] + 0.4 * basis[1, :, 3]).reshape(nr, nr)
+    # the normalisation and Ritz stage of paper_rollout.py:171-192, then the
+    # rollout in the rotated basis
+    weight = (2 * math.pi / nr) ** 2
+    gu, gv, gw = basis
+    norm = np.sqrt(weight * np.sum(gu * gu + gv * gv, axis=0))
+    gu, gv, gw = gu / norm, gv / norm, gw / norm
+    mass = weight * (gu.T @ gu + gv.T @ gv)
+    stiff = weight * (gw.T @ gw)
+    vals, transform = sla.eigh((stiff + stiff.T) / 2, (mass + mass.T) / 2)
+    rtimes = np.linspace(0.0, 0.3, 7)
+    gt = dict(time=rtimes, velocity_u=u0[None], velocity_v=v0[None], nu=0.05)
+    with tempfile.TemporaryDirectory() as tmp:
+        fields_r, states_r, skew_r, _, _ = roll.rollout(gu @ transform, gv @ transform,
+                                                        gw @ transform, vals, gt, 0.02,
+                                                        Path(tmp), "golden")
+    g.update(roll_coef=coef, roll_vals=vals,
+             roll_times=rtimes, roll_nu=np.asarray(0.05), roll_dt=np.asarray(0.02),
+             roll_states=states_r, roll_u_frames=fields_r[0].reshape(len(rtimes), -1)[:, :64],
+             roll_skew=np.asarray(skew_r))
 
     g = {key: np.asarray(v, dtype=np.float64) if np.asarray(v).dtype.kind == "f" else np.asarray(v)
          for key, v in g.items()}
