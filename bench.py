@@ -75,7 +75,8 @@ def parse():
                     help="mode counts of the reference_velocity workload")
     ap.add_argument("--workload", default="periodic_train",
                     choices=["periodic_train", "periodic_small", "periodic_eval", "multihole",
-                             "metaball3d", "reference_velocity", "reference_potential"],
+                             "metaball3d", "reference_velocity", "reference_potential",
+                             "periodic_rollout"],
                     help="periodic_train is the headline line; the others print one line "
                          "each for the remaining configurations (timing and FP64-oracle "
                          "errors), not the headline metric")
@@ -373,6 +374,31 @@ def time_potential(K: int, steps: int, warmup: int, dev):
     return e0.elapsed_time(e1) / steps, r, step
 
 
+# The reference's frozen-basis evaluation of the periodic Potential basis at
+# K = 1024 (experiments/periodic/paper_rollout.py, evaluate_large_comparison
+# fields): Jet3 sampling on the 256^2 grid and the Gram + Ritz stage, published
+# as 142-150 s and 1.61-1.73 s (data/paper/periodic_merger.json:1280-1281 and
+# the five other records; hardware not stated).  The rollout integrates the
+# vortex merger to T = 18 pi at dt = 0.005 (paper_rollout.py main).
+PUBLISHED_SAMPLING_S = (142.0, 150.0)
+PUBLISHED_RITZ_S = (1.61, 1.73)
+
+
+def vortex_pair(points: np.ndarray, separation: float = 1.35, core: float = 0.3):
+    """Velocity of two co-rotating Gaussian vortices a separation apart about
+    the box centre (a synthetic stand-in for the merger's initial DNS field):
+    psi = sum_j exp(-|x - x_j|^2 / (2 core^2)), (u, v) = (psi_y, -psi_x)."""
+    c = np.array([math.pi, math.pi])
+    u = np.zeros(len(points))
+    v = np.zeros(len(points))
+    for sgn in (-1.0, 1.0):
+        d = points - (c + sgn * np.array([separation / 2, 0.0]))
+        g = np.exp(-(d ** 2).sum(1) / (2 * core * core))
+        u += -d[:, 1] / core ** 2 * g
+        v += d[:, 0] / core ** 2 * g
+    return u, v
+
+
 def velocity_inputs(n: int, seed: int = 0):
     """Synthetic inputs with the configuration's shapes: points uniform in
     the unit cube; features (2x - 1 for the coordinates, 12 constant
@@ -460,7 +486,66 @@ def run_workload(args, world, rank, local):
     def dev_inputs(pts, w):
         return torch.tensor(pts, device=dev), torch.tensor(w, device=dev)
 
-    if name == "reference_potential":
+    if name == "periodic_rollout":
+        # frozen-basis evaluation of the reference's periodic Potential
+        # network at K = 1024: Jet3 sampling on the grid, Ritz, ETDRK4
+        from types import SimpleNamespace
+        from neb_gb300 import hardcoded as H
+        from neb_gb300.rollout import Rollout, grid_points, ritz, sample_basis
+        grid = 256
+        cfg = SimpleNamespace(**REF_POTENTIAL)
+        model = H.HardcodedModel(cfg, H.initial_arrays(cfg), device=dev)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        # warm-up: kernel attributes, the allocator, the cuSOLVER / cuBLAS handles
+        try:
+            ritz(sample_basis(model, cfg, 64))
+        except ArithmeticError:
+            pass
+        torch.cuda.synchronize()
+        ev[0].record()
+        gb = sample_basis(model, cfg, grid, diagnostics=True)
+        ev[1].record()
+        rb = ritz(gb)
+        ev[2].record()
+        roll = Rollout(gb, rb, 1e-3)
+        pts = grid_points(grid, cfg)
+        u0, v0 = vortex_pair(pts)
+        c0 = roll.project(u0, v0)
+        roll.c.copy_(c0)
+        roll._set_step(0.005)
+        roll.advance(2)  # graph capture and warm-up
+        torch.cuda.synchronize()
+        nsteps = max(20, args.steps * 10)
+        ev[3].record()
+        roll.advance(nsteps)
+        ev[4].record()
+        torch.cuda.synchronize()
+        skew = roll.energy_skew()
+        kern_ritz = _kernel_table(N, lambda i: ritz(gb), 1)
+        kern_step = _kernel_table(N, lambda i: roll.rhs(roll.c), 3)
+        t_sample = ev[0].elapsed_time(ev[1]) / 1e3
+        t_ritz = ev[1].elapsed_time(ev[2]) / 1e3
+        ms_step = ev[3].elapsed_time(ev[4]) / nsteps
+        steps_total = int(math.ceil(18 * math.pi / 0.005))
+        line.update({
+            "metric": "frozen-basis evaluation of the reference's periodic Potential basis "
+                      "(K=1024 per-mode SIRENs 24 -> 4x32 sine): Jet3 sampling and Gram + Ritz "
+                      "on the 256^2 grid, ETDRK4 Galerkin steps",
+            "value": 1e3 / ms_step, "unit": "ETDRK4 steps/s", "dtype": "f32 fields, f64 "
+            "coefficients", "sampling_s": t_sample, "published_sampling_s": PUBLISHED_SAMPLING_S,
+            "ritz_s": t_ritz, "published_ritz_s": PUBLISHED_RITZ_S,
+            "speedup_sampling_vs_published": [PUBLISHED_SAMPLING_S[0] / t_sample,
+                                              PUBLISHED_SAMPLING_S[1] / t_sample],
+            "speedup_ritz_vs_published": [PUBLISHED_RITZ_S[0] / t_ritz,
+                                          PUBLISHED_RITZ_S[1] / t_ritz],
+            "ms_per_etdrk4_step": ms_step, "steps_timed": nsteps,
+            "trajectory_T18pi_dt0005_s": ms_step * steps_total / 1e3,
+            "energy_skew": skew, "ritz_lambda_min_max": [float(rb.lam[0]), float(rb.lam[-1])],
+            "ritz_kernel_ms": kern_ritz, "rhs_kernel_ms": kern_step,
+            "points": grid * grid, "modes": model.core.K,
+            "data": "synthetic: the reference trainer's epoch-0 initialisation (no trained "
+                    "checkpoint is available), a Gaussian vortex pair as the initial velocity"})
+    elif name == "reference_potential":
         # the reference's own 2D training configuration through its backend
         # API: GPU updates at each K, and the FP64 oracle's update at K = 32
         from types import SimpleNamespace

@@ -391,9 +391,10 @@ int neb_stream_fields(int precision, int order, const void* out, int start, int 
  * stage (ROLL:173-176), applied to the Grams instead of the fields. */
 int neb_normalize_pencil(int K, double* M, double* S, double* norm, neb_stream_t stream);
 
-/* R [K][K] = D^-1 T with T[:, i] = V[i] (rows of V: M-orthonormal
- * eigenvectors, as neb_spectral writes them) and D = diag(norm): the map
- * from Ritz coefficients to coefficients of the raw fields (ROLL:187-192). */
+/* R [2][K][K]: R = D^-1 T with T[:, i] = V[i] (rows of V: M-orthonormal
+ * eigenvectors, as neb_spectral writes them) and D = diag(norm), the map
+ * from Ritz coefficients to coefficients of the raw fields (ROLL:187-192),
+ * followed by its transpose.  The rollout entry points take this pair. */
 int neb_ritz_transform(int K, const double* V, const double* norm, double* R,
                        neb_stream_t stream);
 

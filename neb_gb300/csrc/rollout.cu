@@ -97,7 +97,9 @@ __global__ void pencil_scale(int K, double* __restrict__ M, double* __restrict__
     S[e] /= d;
   }
 }
-// R[k][i] = V[i][k] / norm[k]: rows of V are M-orthonormal eigenvectors.
+// R[k][i] = V[i][k] / norm[k] (rows of V are M-orthonormal eigenvectors),
+// and its transpose Rt[i][k] = R[k][i] right after it, so that both R x and
+// R^T y are row-wise (coalesced) products.
 __global__ void ritz_transform(int K, const double* __restrict__ V,
                                const double* __restrict__ norm, double* __restrict__ R) {
   const int64_t total = (int64_t)K * K;
@@ -105,6 +107,7 @@ __global__ void ritz_transform(int K, const double* __restrict__ V,
        e += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(e / K), i = (int)(e % K);
     R[e] = V[(int64_t)i * K + k] / norm[k];
+    R[total + e] = V[e] / norm[i];  // Rt[k][i] = R[i][k] = V[k][i] / norm[i]
   }
 }
 
@@ -238,7 +241,27 @@ __global__ void rollout_pass1(int64_t n, int K, const T* __restrict__ UV,
     const T* rw = Om + p * K;
     if constexpr (sizeof(T) == 4) {
       Acc2 au{0.f, 0.f}, av{0.f, 0.f}, aw{0.f, 0.f};
-      for (int k = lane; k < K; k += 32) {
+      int k0 = 0;
+      const bool vec = (K & 3) == 0 &&
+                       ((reinterpret_cast<uintptr_t>(UV) | reinterpret_cast<uintptr_t>(Om)) & 15) == 0;
+      if (vec) {  // 16-byte loads: every row starts on a 16-byte boundary
+        const float4* u4 = reinterpret_cast<const float4*>(ru);
+        const float4* v4 = reinterpret_cast<const float4*>(rv);
+        const float4* w4 = reinterpret_cast<const float4*>(rw);
+        const float4* h4 = reinterpret_cast<const float4*>(bh);
+        const float4* l4 = reinterpret_cast<const float4*>(bl);
+        for (int j = lane; j < (K >> 2); j += 32) {
+          const float4 uu = u4[j], vv = v4[j], ww = w4[j], hh = h4[j], ll = l4[j];
+          add_prod(au, uu.x, hh.x, ll.x); add_prod(au, uu.y, hh.y, ll.y);
+          add_prod(au, uu.z, hh.z, ll.z); add_prod(au, uu.w, hh.w, ll.w);
+          add_prod(av, vv.x, hh.x, ll.x); add_prod(av, vv.y, hh.y, ll.y);
+          add_prod(av, vv.z, hh.z, ll.z); add_prod(av, vv.w, hh.w, ll.w);
+          add_prod(aw, ww.x, hh.x, ll.x); add_prod(aw, ww.y, hh.y, ll.y);
+          add_prod(aw, ww.z, hh.z, ll.z); add_prod(aw, ww.w, hh.w, ll.w);
+        }
+        k0 = K;
+      }
+      for (int k = k0 + lane; k < K; k += 32) {
         const float h = bh[k], l = bl[k];
         add_prod(au, ru[k], h, l);
         add_prod(av, rv[k], h, l);
@@ -329,13 +352,22 @@ rollout_pass2(int64_t n, int K, const T* __restrict__ UV, const double* __restri
   partial[(int64_t)blockIdx.y * K + k] = out;
 }
 
-// y[k] = sum over chunks of partial[chunk][k] (fixed order).
-__global__ void reduce_partials(int K, int chunks, const double* __restrict__ partial,
-                                double* __restrict__ y) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int c = 0; c < chunks; ++c) s += partial[(int64_t)c * K + k];
-    y[k] = s;
+// y[k] = sum over chunks of partial[chunk][k] (fixed order): a block per 32
+// columns, warp w summing chunks w, w + 16, ..., then the 16 warp sums.
+constexpr int kReduceWarps = 16;
+__global__ void __launch_bounds__(32 * kReduceWarps)
+reduce_partials(int K, int chunks, const double* __restrict__ partial, double* __restrict__ y) {
+  __shared__ double red[kReduceWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, k = blockIdx.x * 32 + lane;
+  double s = 0.0;
+  if (k < K)
+    for (int c = w; c < chunks; c += kReduceWarps) s += partial[(int64_t)c * K + k];
+  red[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && k < K) {
+    double t = 0.0;
+    for (int j = 0; j < kReduceWarps; ++j) t += red[j][lane];
+    y[k] = t;
   }
 }
 
@@ -350,9 +382,15 @@ struct Stage {
 __global__ void rollout_finish(int kind, int K, const double* __restrict__ R,
                                const double* __restrict__ y, const double* __restrict__ coef,
                                Stage st) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
+  const double* Rt = R + (int64_t)K * K;
+  const int lane = threadIdx.x & 31;
+  for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < K;
+       k += (gridDim.x * blockDim.x) >> 5) {
     double r = 0.0;
-    for (int i = 0; i < K; ++i) r += R[(int64_t)i * K + k] * y[i];
+    for (int i = lane; i < K; i += 32) r += Rt[(int64_t)k * K + i] * y[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (lane != 0) continue;
     if (kind < 0) {
       st.out[k] = r;
       continue;
@@ -401,6 +439,7 @@ RollWs roll_ws(int64_t n, int K) {
 template <typename T>
 int launch_pass1(int64_t n, int K, const void* UV, const void* Om, char* ws, const RollWs& w,
                  double weight, int mode, double* qout, cudaStream_t s) {
+  KernelScope ks("rollout_pass1", s, 6.0 * n * K, 3.0 * n * K * sizeof(T));
   const int blocks = (int)std::min<int64_t>(ceil_div(n * 32, 256), 65535);
   rollout_pass1<T><<<blocks, 256, 0, s>>>(
       n, K, (const T*)UV, (const T*)Om, (const double*)(ws + w.b64), (const float*)(ws + w.bh),
@@ -412,14 +451,37 @@ int launch_pass1(int64_t n, int K, const void* UV, const void* Om, char* ws, con
 
 template <typename T>
 int launch_pass2(int64_t n, int K, const void* UV, char* ws, const RollWs& w, cudaStream_t s) {
-  dim3 grid((unsigned)ceil_div(K, kColsPerBlock), (unsigned)w.chunks);
-  rollout_pass2<T><<<grid, kColsPerBlock, 0, s>>>(n, K, (const T*)UV, (const double*)(ws + w.q),
-                                                   (const float*)(ws + w.qh),
-                                                   (const float*)(ws + w.ql),
-                                                   (double*)(ws + w.partial));
+  {
+    KernelScope ks("rollout_pass2", s, 4.0 * n * K, 2.0 * n * K * sizeof(T));
+    dim3 grid((unsigned)ceil_div(K, kColsPerBlock), (unsigned)w.chunks);
+    rollout_pass2<T><<<grid, kColsPerBlock, 0, s>>>(n, K, (const T*)UV,
+                                                     (const double*)(ws + w.q),
+                                                     (const float*)(ws + w.qh),
+                                                     (const float*)(ws + w.ql),
+                                                     (double*)(ws + w.partial));
+    NEB_LAUNCH_CHECK();
+  }
+  KernelScope ks("reduce_partials", s, 0, 8.0 * w.chunks * K);
+  reduce_partials<<<(unsigned)ceil_div(K, 32), 32 * kReduceWarps, 0, s>>>(
+      K, w.chunks, (const double*)(ws + w.partial), (double*)(ws + w.y));
   NEB_LAUNCH_CHECK();
-  reduce_partials<<<grid_for(K), 256, 0, s>>>(K, w.chunks, (const double*)(ws + w.partial),
-                                              (double*)(ws + w.y));
+  return NEB_OK;
+}
+
+int launch_gemv(int K, const double* R, const double* x, char* ws, const RollWs& w,
+                cudaStream_t s) {
+  KernelScope ks("ritz_gemv", s, 2.0 * K * K, 8.0 * K * K);
+  gemv_rows<<<grid_for((int64_t)K * 32), 256, 0, s>>>(K, R, x, (double*)(ws + w.b64),
+                                                     (float*)(ws + w.bh), (float*)(ws + w.bl));
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
+int launch_finish(int kind, int K, const double* R, const double* coef, const Stage& st,
+                  char* ws, const RollWs& w, cudaStream_t s) {
+  KernelScope ks("ritz_finish", s, 2.0 * K * K, 8.0 * K * K);
+  rollout_finish<<<grid_for((int64_t)K * 32), 256, 0, s>>>(kind, K, R, (const double*)(ws + w.y),
+                                                          coef, st);
   NEB_LAUNCH_CHECK();
   return NEB_OK;
 }
@@ -429,15 +491,10 @@ template <typename T>
 int rhs_stage(int64_t n, int K, const void* UV, const void* Om, const double* R, double weight,
               const double* x, int kind, const double* coef, const Stage& st, char* ws,
               const RollWs& w, cudaStream_t s) {
-  gemv_rows<<<grid_for((int64_t)K * 32), 256, 0, s>>>(K, R, x, (double*)(ws + w.b64),
-                                                     (float*)(ws + w.bh), (float*)(ws + w.bl));
-  NEB_LAUNCH_CHECK();
+  if (int e = launch_gemv(K, R, x, ws, w, s)) return e;
   if (int e = launch_pass1<T>(n, K, UV, Om, ws, w, weight, 0, (double*)(ws + w.q), s)) return e;
   if (int e = launch_pass2<T>(n, K, UV, ws, w, s)) return e;
-  rollout_finish<<<grid_for(K, 128), 128, 0, s>>>(kind, K, R, (const double*)(ws + w.y), coef,
-                                                  st);
-  NEB_LAUNCH_CHECK();
-  return NEB_OK;
+  return launch_finish(kind, K, R, coef, st, ws, w, s);
 }
 
 Stage stage_of(char* ws, const RollWs& w, double* c, double* out) {
@@ -571,8 +628,6 @@ extern "C" int neb_rollout_rhs(int precision, int64_t n_points, int K, const voi
   const RollWs w = roll_ws(n_points, K);
   char* ws = (char*)workspace;
   const Stage st = stage_of(ws, w, nullptr, out);
-  const size_t es = precision == NEB_PREC_FP64 ? 8 : 4;
-  KernelScope ks("rollout_rhs", s, 10.0 * n_points * K, 5.0 * n_points * K * es, 5);
   return precision == NEB_PREC_FP64
              ? rhs_stage<double>(n_points, K, UV, Om, R, weight, x, -1, nullptr, st, ws, w, s)
              : rhs_stage<float>(n_points, K, UV, Om, R, weight, x, -1, nullptr, st, ws, w, s);
@@ -589,8 +644,6 @@ extern "C" int neb_etdrk4_step(int precision, int64_t n_points, int K, const voi
   char* ws = (char*)workspace;
   const Stage st = stage_of(ws, w, c, nullptr);
   const double* inputs[4] = {c, st.a, st.b, st.z};
-  const size_t es = precision == NEB_PREC_FP64 ? 8 : 4;
-  KernelScope ks("etdrk4_step", s, 40.0 * n_points * K, 20.0 * n_points * K * es, 20);
   for (int kind = 0; kind < 4; ++kind) {
     const int e = precision == NEB_PREC_FP64
                       ? rhs_stage<double>(n_points, K, UV, Om, R, weight, inputs[kind], kind,
@@ -611,24 +664,21 @@ extern "C" int neb_rollout_project(int precision, int64_t n_points, int K, const
   cudaStream_t s = (cudaStream_t)stream;
   const RollWs w = roll_ws(n_points, K);
   char* ws = (char*)workspace;
-  KernelScope ks("rollout_project", s, 4.0 * n_points * K, 2.0 * n_points * K *
-                                                            (precision == NEB_PREC_FP64 ? 8 : 4), 4);
   // q1 = w u0, q2 = -w v0, so that pass 2 forms w (U^T u0 + V^T v0)
   double* q = (double*)(ws + w.q);
   float* qh = (float*)(ws + w.qh);
   float* ql = (float*)(ws + w.ql);
   NEB_CUDA_CHECK(cudaMemcpyAsync(q, u0, n_points * 8, cudaMemcpyDeviceToDevice, s));
   NEB_CUDA_CHECK(cudaMemcpyAsync(q + n_points, v0, n_points * 8, cudaMemcpyDeviceToDevice, s));
-  scale_split<<<grid_for(2 * n_points), 256, 0, s>>>(2 * n_points, n_points, weight, q, qh, ql);
-  NEB_LAUNCH_CHECK();
+  {
+    KernelScope ks("scale_split", s, 0, 32.0 * n_points);
+    scale_split<<<grid_for(2 * n_points), 256, 0, s>>>(2 * n_points, n_points, weight, q, qh, ql);
+    NEB_LAUNCH_CHECK();
+  }
   const int e = precision == NEB_PREC_FP64 ? launch_pass2<double>(n_points, K, UV, ws, w, s)
                                            : launch_pass2<float>(n_points, K, UV, ws, w, s);
   if (e) return e;
-  const Stage st = stage_of(ws, w, nullptr, c);
-  rollout_finish<<<grid_for(K, 128), 128, 0, s>>>(-1, K, R, (const double*)(ws + w.y), nullptr,
-                                                  st);
-  NEB_LAUNCH_CHECK();
-  return NEB_OK;
+  return launch_finish(-1, K, R, nullptr, stage_of(ws, w, nullptr, c), ws, w, s);
 }
 
 extern "C" int neb_rollout_fields(int precision, int64_t n_points, int K, const void* UV,
@@ -640,11 +690,7 @@ extern "C" int neb_rollout_fields(int precision, int64_t n_points, int K, const 
   cudaStream_t s = (cudaStream_t)stream;
   const RollWs w = roll_ws(n_points, K);
   char* ws = (char*)workspace;
-  KernelScope ks("rollout_fields", s, 6.0 * n_points * K,
-                 3.0 * n_points * K * (precision == NEB_PREC_FP64 ? 8 : 4), 2);
-  gemv_rows<<<grid_for((int64_t)K * 32), 256, 0, s>>>(K, R, c, (double*)(ws + w.b64),
-                                                     (float*)(ws + w.bh), (float*)(ws + w.bl));
-  NEB_LAUNCH_CHECK();
+  if (int e = launch_gemv(K, R, c, ws, w, s)) return e;
   return precision == NEB_PREC_FP64
              ? launch_pass1<double>(n_points, K, UV, Om, ws, w, 1.0, 1, fields, s)
              : launch_pass1<float>(n_points, K, UV, Om, ws, w, 1.0, 1, fields, s);

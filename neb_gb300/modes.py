@@ -62,7 +62,9 @@ def siren_init(c, K: int, seed: int, inputs: int, outputs: int):
 
 
 def jet_channels(dim: int, order: int) -> int:
-    return 1 + dim + (dim * (dim + 1) // 2 if order == 2 else 0)
+    """Channels of a jet: value, gradient, compact Hessian (order >= 2) and
+    the four third derivatives of a 2D third-order jet."""
+    return 1 + dim + (dim * (dim + 1) // 2 if order >= 2 else 0) + (4 if order == 3 else 0)
 
 
 def _field(j, name):
@@ -188,6 +190,9 @@ class ModeModel:
         packed inputs, and the tape (kept when ``cache``)."""
         n = feats.shape[0]
         B = stop - start
+        C = jet_channels(self.net.dim, self.net.order)
+        if C != self.channels or feats.shape[1] != C:
+            raise ValueError(f"jets of {C} channels expected, features carry {feats.shape[1]}")
         lib = N.load()
         tb = lib.neb_modes_tape_bytes(ctypes.byref(self.net), B, n)
         tape = torch.empty(max(tb, 256), dtype=torch.uint8, device=self.device) if cache else \

@@ -106,6 +106,7 @@ class RitzBasis:
     R: torch.Tensor
     norm: torch.Tensor
     rank: int
+    pair: torch.Tensor  # [2][K][K]: R and R^T, what the rollout kernels take
 
 
 def ritz(basis: GridBasis, rank_rtol: float = 1e-12) -> RitzBasis:
@@ -134,9 +135,9 @@ def ritz(basis: GridBasis, rank_rtol: float = 1e-12) -> RitzBasis:
         raise ArithmeticError(f"Full-K rank gate: the mass matrix resolves {rank.value}/{K}")
     if int(info.item()) != 0:
         raise ArithmeticError(f"Ritz stage failed (status {int(info.item())})")
-    R = torch.empty((K, K), **f64)
-    N.call("neb_ritz_transform", K, V.data_ptr(), norm.data_ptr(), R.data_ptr(), _stream())
-    return RitzBasis(lam, R, norm, rank.value)
+    RR = torch.empty((2, K, K), **f64)  # R and its transpose
+    N.call("neb_ritz_transform", K, V.data_ptr(), norm.data_ptr(), RR.data_ptr(), _stream())
+    return RitzBasis(lam, RR[0], norm, rank.value, RR)
 
 
 class Rollout:
@@ -162,7 +163,7 @@ class Rollout:
     def _args(self):
         b = self.basis
         return (self.prec, self.n, self.K, b.UV.data_ptr(), b.Om.data_ptr(),
-                self.ritz.R.data_ptr(), b.weight)
+                self.ritz.pair.data_ptr(), b.weight)
 
     def rhs(self, x: torch.Tensor) -> torch.Tensor:
         """The Galerkin right-hand side of Ritz coefficients x (FP64)."""
@@ -181,7 +182,7 @@ class Rollout:
         out = torch.empty(self.K, dtype=torch.float64, device=dev)
         b = self.basis
         N.call("neb_rollout_project", self.prec, self.n, self.K, b.UV.data_ptr(),
-               self.ritz.R.data_ptr(), u.data_ptr(), v.data_ptr(), b.weight, out.data_ptr(),
+               self.ritz.pair.data_ptr(), u.data_ptr(), v.data_ptr(), b.weight, out.data_ptr(),
                self.ws.data_ptr(), self.ws.numel(), _stream())
         return out
 

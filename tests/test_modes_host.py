@@ -26,6 +26,7 @@ def test_siren_init_matches_reference_model():
 
 def test_jet_channel_counts():
     assert [jet_channels(d, o) for d in (2, 3) for o in (1, 2)] == [3, 6, 4, 10]
+    assert jet_channels(2, 3) == 10
 
 
 def _velocity_case(seed=3, K=3, n=9):
