@@ -135,10 +135,10 @@ int neb_envelope_product(const neb_net* net, const void* envelope, int64_t n_poi
  * h_lap^T (FP64, [H][H]); per-CTA partial sums, FP64 cross-CTA reduction.
  * With psi = W_out h + b: M = W_out A_M W_out^T, S = W_out A_S W_out^T, i.e.
  * the Grams of ROLL:178-179 and VC:40-46.  qw: [n] quadrature weights,
- * master type. */
+ * master type.  accumulate != 0 adds to A_M, A_S (point-chunked Grams). */
 int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n_points,
-                    const void* tape, double* A_M, double* A_S, void* workspace,
-                    size_t workspace_bytes, neb_stream_t stream);
+                    const void* tape, double* A_M, double* A_S, int accumulate,
+                    void* workspace, size_t workspace_bytes, neb_stream_t stream);
 
 /* neb_hidden_gram for FP32 / FP64 networks without a workspace argument: no
  * counterpart in the reference (its CuPy code always has a memory pool).
@@ -226,12 +226,13 @@ int neb_pencil_pullback(int K, int H, const double* W_out, const double* A_M,
 /* Reverse pass from the hidden-Gram adjoints (2D scalar potential):
  * h_bar_x,y = 2 w h_x,y G_Mh, h_bar_lap = 2 w h_lap G_Sh, then through every
  * hidden layer (tanh-jet transpose, data and weight gradients).  gW, gb:
- * host arrays of n_hidden device pointers, overwritten.  Replaces
+ * host arrays of n_hidden device pointers, overwritten (accumulate == 0) or
+ * added to (point-chunked reverse passes).  Replaces
  * HB:2034-2138 backward_gradients_block_jet1/2 with HB:1115-1173 and
  * VTJ2:77-82 backward, VC:88-103. */
 int neb_backward_hidden(const neb_net* net, const void* const* W, const double* G_Mh,
                         const double* G_Sh, const void* qw, int64_t n_points,
-                        const void* tape, void* const* gW, void* const* gb,
+                        const void* tape, void* const* gW, void* const* gb, int accumulate,
                         void* workspace, size_t workspace_bytes, neb_stream_t stream);
 
 /* Reverse pass from adjoint output jets psibar ([n][C][stop - start]) of

@@ -72,7 +72,7 @@ _SIGNATURES = {
     "neb_output": (c_int, [POINTER(NebNet), c_void_p, c_void_p, c_int, c_int, c_int64, c_void_p,
                            c_void_p, c_void_p]),
     "neb_hidden_gram": (c_int, [POINTER(NebNet), c_void_p, c_int64, c_void_p, c_void_p, c_void_p,
-                                c_void_p, c_size_t, c_void_p]),
+                                c_int, c_void_p, c_size_t, c_void_p]),
     "neb_hidden_gram_static": (c_int, [POINTER(NebNet), c_void_p, c_int64, c_void_p, c_void_p,
                                        c_void_p, c_void_p]),
     "neb_fields_gram": (c_int, [POINTER(NebNet), c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
@@ -95,7 +95,7 @@ _SIGNATURES = {
                                     c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "neb_backward_hidden": (c_int, [POINTER(NebNet), POINTER(c_void_p), c_void_p, c_void_p,
                                     c_void_p, c_int64, c_void_p, POINTER(c_void_p),
-                                    POINTER(c_void_p), c_void_p, c_size_t, c_void_p]),
+                                    POINTER(c_void_p), c_int, c_void_p, c_size_t, c_void_p]),
     "neb_backward_output": (c_int, [POINTER(NebNet), POINTER(c_void_p), c_int, c_int, c_void_p,
                                     c_int64, c_void_p, POINTER(c_void_p), POINTER(c_void_p), c_int,
                                     c_void_p, c_size_t, c_void_p]),

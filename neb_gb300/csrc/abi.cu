@@ -318,7 +318,8 @@ int backward_layers(const neb_net* net, const void* const* W, int top, T* zb, T*
 template <typename T, int C>
 int backward_hidden_simt(const neb_net* net, const void* const* W, const double* GMh,
                          const double* GSh, const void* qw, int64_t n, const void* tape,
-                         void* const* gW, void* const* gb, void* ws, cudaStream_t s) {
+                         void* const* gW, void* const* gb, void* ws, cudaStream_t s,
+                         int accumulate) {
   const int L = net->n_hidden, H = net->widths[L];
   TapeLayout tl = tape_layout(net, n);
   WsLayout wl = ws_layout(net, n);
@@ -346,7 +347,7 @@ int backward_hidden_simt(const neb_net* net, const void* const* W, const double*
   int st = launch_bwd<T, C, 1>(HL, gM, gS, (const T*)qw, T(2), ZL, zb0, n, H, H, s);
   if (st) return st;
   return backward_layers<T, C>(net, W, L, zb0, zb1, tp, tl, gW, gb, (double*)(w + wl.part),
-                               (double*)(w + wl.partb), n, s);
+                               (double*)(w + wl.partb), n, s, accumulate);
 }
 
 template <typename T, int C>
@@ -382,7 +383,7 @@ int backward_output_simt(const neb_net* net, const void* const* W, int start, in
 
 template <typename T, int C>
 int hidden_gram_simt(const neb_net* net, const void* qw, int64_t n, const void* tape, double* AM,
-                     double* AS, void* ws, cudaStream_t s) {
+                     double* AS, void* ws, cudaStream_t s, int accumulate = 0) {
   const int L = net->n_hidden, H = net->widths[L];
   TapeLayout tl = tape_layout(net, n);
   WsLayout wl = ws_layout(net, n);
@@ -392,10 +393,10 @@ int hidden_gram_simt(const neb_net* net, const void* qw, int64_t n, const void* 
   simt::ChanSet lap{1, {3}};
   const bool comp = net->gram == NEB_GRAM_COMPENSATED;
   int st = launch_rowsum<T, C, double>(HL, H, HL, H, (const T*)qw, grad, n, H, H, true, 1.0, part,
-                                       AM, s, 0, comp);
+                                       AM, s, accumulate, comp);
   if (st) return st;
   return launch_rowsum<T, C, double>(HL, H, HL, H, (const T*)qw, lap, n, H, H, true, 1.0, part, AS,
-                                     s, 0, comp);
+                                     s, accumulate, comp);
 }
 
 // ------------------------------------------------------ direct route
@@ -690,7 +691,7 @@ extern "C" int neb_envelope_product(const neb_net* net, const void* envelope, in
 }
 
 extern "C" int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n, const void* tape,
-                               double* AM, double* AS, void* ws, size_t ws_bytes,
+                               double* AM, double* AS, int accumulate, void* ws, size_t ws_bytes,
                                neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
@@ -705,16 +706,17 @@ extern "C" int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n, co
     TapeLayout tl = tape_layout(net, n);
     WsLayout wl = ws_layout(net, n);
     return tc_hidden_gram(net, (const float*)qw, n, (const char*)tape + tl.x_off[net->n_hidden],
-                          AM, AS, (char*)ws + wl.tc, s);
+                          AM, AS, accumulate, (char*)ws + wl.tc, s);
   }
-  if (net->precision == NEB_PREC_FP64) return hidden_gram_simt<double, 4>(net, qw, n, tape, AM, AS, ws, s);
-  return hidden_gram_simt<float, 4>(net, qw, n, tape, AM, AS, ws, s);
+  if (net->precision == NEB_PREC_FP64)
+    return hidden_gram_simt<double, 4>(net, qw, n, tape, AM, AS, ws, s, accumulate);
+  return hidden_gram_simt<float, 4>(net, qw, n, tape, AM, AS, ws, s, accumulate);
 }
 
 extern "C" int neb_backward_hidden(const neb_net* net, const void* const* W, const double* GMh,
                                    const double* GSh, const void* qw, int64_t n, const void* tape,
-                                   void* const* gW, void* const* gb, void* ws, size_t ws_bytes,
-                                   neb_stream_t stream) {
+                                   void* const* gW, void* const* gb, int accumulate, void* ws,
+                                   size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
   NEB_REQUIRE(net->dim == 2, "neb_backward_hidden: 2D scalar potential only");
@@ -735,11 +737,13 @@ extern "C" int neb_backward_hidden(const neb_net* net, const void* const* W, con
       tt.z[l] = (char*)tape + tl.z_off[l];
     }
     return tc_backward_hidden(net, GMh, GSh, (const float*)qw, n, tt, (float* const*)gW,
-                              (float* const*)gb, (char*)ws + wl.tc, s);
+                              (float* const*)gb, accumulate, (char*)ws + wl.tc, s);
   }
   if (net->precision == NEB_PREC_FP64)
-    return backward_hidden_simt<double, 4>(net, W, GMh, GSh, qw, n, tape, gW, gb, ws, s);
-  return backward_hidden_simt<float, 4>(net, W, GMh, GSh, qw, n, tape, gW, gb, ws, s);
+    return backward_hidden_simt<double, 4>(net, W, GMh, GSh, qw, n, tape, gW, gb, ws, s,
+                                           accumulate);
+  return backward_hidden_simt<float, 4>(net, W, GMh, GSh, qw, n, tape, gW, gb, ws, s,
+                                        accumulate);
 }
 
 extern "C" int neb_backward_output(const neb_net* net, const void* const* W, int start, int stop,

@@ -681,7 +681,8 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }
 
 __global__ void reduce_parts(const float* __restrict__ part, int splits, int M, int ldp, int ncols,
-                             int ldo, int sym, float* __restrict__ outf, double* __restrict__ outd) {
+                             int ldo, int sym, int accumulate, float* __restrict__ outf,
+                             double* __restrict__ outd) {
   const size_t total = (size_t)M * ncols;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -696,8 +697,14 @@ __global__ void reduce_parts(const float* __restrict__ part, int splits, int M, 
       hi *= 0.5f;
       lo *= 0.5f;
     }
-    if (outf) outf[(size_t)m * ldo + j] = hi + lo;
-    if (outd) outd[(size_t)m * ldo + j] = (double)hi + (double)lo;
+    if (outf) {
+      float* o = outf + (size_t)m * ldo + j;
+      *o = accumulate ? *o + (hi + lo) : hi + lo;
+    }
+    if (outd) {
+      double* o = outd + (size_t)m * ldo + j;
+      *o = accumulate ? *o + ((double)hi + (double)lo) : (double)hi + (double)lo;
+    }
   }
 }
 
@@ -707,7 +714,8 @@ __global__ void reduce_parts(const float* __restrict__ part, int splits, int M, 
 // loads, FP32 sums of 8-point groups accumulated in FP64), combined in
 // shared memory.
 __global__ void __launch_bounds__(256) bias_rows_tc(const __nv_bfloat16* __restrict__ zb,
-                                                   int n_pad, int N, float* __restrict__ out) {
+                                                   int n_pad, int N, int accumulate,
+                                                   float* __restrict__ out) {
   __shared__ double part[8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int o = blockIdx.x * 2 + (warp >> 2), quarter = warp & 3;
@@ -736,7 +744,8 @@ __global__ void __launch_bounds__(256) bias_rows_tc(const __nv_bfloat16* __restr
     const int oo = blockIdx.x * 2 + threadIdx.x;
     if (oo < N) {
       const double* q = part + threadIdx.x * 4;
-      out[oo] = (float)((q[0] + q[1]) + (q[2] + q[3]));
+      const float v = (float)((q[0] + q[1]) + (q[2] + q[3]));
+      out[oo] = accumulate ? out[oo] + v : v;
     }
   }
 }
@@ -872,11 +881,12 @@ int launch_rowsum(const void* a_base, int aC, int a_ch0, const void* b_base, int
 }
 
 int reduce(const float* part, int splits, int M, int ldp, int ncols, int ldo, bool sym,
-           float* outf, double* outd, cudaStream_t s) {
+           float* outf, double* outd, cudaStream_t s, int accumulate = 0) {
   KernelScope ks("reduce_chunks", s, 0, (double)splits * M * ncols * 4);
   size_t total = (size_t)M * ncols;
   int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
-  reduce_parts<<<blocks, 256, 0, s>>>(part, splits, M, ldp, ncols, ldo, sym ? 1 : 0, outf, outd);
+  reduce_parts<<<blocks, 256, 0, s>>>(part, splits, M, ldp, ncols, ldo, sym ? 1 : 0, accumulate,
+                                      outf, outd);
   NEB_LAUNCH_CHECK();
   return NEB_OK;
 }
@@ -957,7 +967,7 @@ int tc_forward(const neb_net* net, const float* const* W, const float* const* b,
 }
 
 int tc_hidden_gram(const neb_net* net, const float* qw, int64_t n, const void* hl, double* AM,
-                   double* AS, char* ws, cudaStream_t s) {
+                   double* AS, int accumulate, char* ws, cudaStream_t s) {
   int st = check_dims(net);
   if (st) return st;
   Dims d = dims_of(net, n);
@@ -980,16 +990,17 @@ int tc_hidden_gram(const neb_net* net, const float* qw, int64_t n, const void* h
   if ((st = launch_rowsum(wht, 3, 0, XT, C, 1, 2, H, H, d.n_pad, (float*)part, status, s,
                           "tc_gram", 2.0 * 2 * n * (double)H * H, &splits, true)))
     return st;
-  if ((st = reduce((float*)part, splits, H, H, H, H, true, nullptr, AM, s))) return st;
+  if ((st = reduce((float*)part, splits, H, H, H, H, true, nullptr, AM, s, accumulate)))
+    return st;
   if ((st = launch_rowsum(wht, 3, 2, XT, C, 3, 1, H, H, d.n_pad, (float*)part, status, s,
                           "tc_gram", 2.0 * n * (double)H * H, &splits, true)))
     return st;
-  return reduce((float*)part, splits, H, H, H, H, true, nullptr, AS, s);
+  return reduce((float*)part, splits, H, H, H, H, true, nullptr, AS, s, accumulate);
 }
 
 int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh, const float* qw,
-                       int64_t n, const TcTape& tape, float* const* gW, float* const* gb, char* ws,
-                       cudaStream_t s) {
+                       int64_t n, const TcTape& tape, float* const* gW, float* const* gb,
+                       int accumulate, char* ws, cudaStream_t s) {
   int st = check_dims(net);
   if (st) return st;
   Dims d = dims_of(net, n);
@@ -1057,12 +1068,13 @@ int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh,
                             status, s2, "tc_weight_grad", 2.0 * C * n * (double)out * in,
                             &splits)))
       return st;
-    if ((st = reduce((float*)part, splits, out, inp, in, in, false, gW[l - 1], nullptr, s2)))
+    if ((st = reduce((float*)part, splits, out, inp, in, in, false, gW[l - 1], nullptr, s2,
+                     accumulate)))
       return st;
     {
       KernelScope ks("bias_grad", s2, 0, (double)d.n_pad * out * 4);
       bias_rows_tc<<<(out + 1) / 2, 256, 0, s2>>>((const __nv_bfloat16*)zb[cur], (int)d.n_pad,
-                                                  out, gb[l - 1]);
+                                                  out, accumulate, gb[l - 1]);
       NEB_LAUNCH_CHECK();
     }
     NEB_CUDA_CHECK(cudaEventRecord(ev_w[dev][l & 1], s2));  // side work of layer l issued

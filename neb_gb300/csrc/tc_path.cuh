@@ -22,9 +22,9 @@ int tc_forward(const neb_net* net, const float* const* W, const float* const* b,
 int tc_output(const neb_net* net, const float* Wout, const float* bout, int start, int stop,
               int64_t n, const void* tape, void* psi, cudaStream_t s);
 int tc_hidden_gram(const neb_net* net, const float* qw, int64_t n, const void* hl, double* AM,
-                   double* AS, char* ws, cudaStream_t s);
+                   double* AS, int accumulate, char* ws, cudaStream_t s);
 int tc_backward_hidden(const neb_net* net, const double* GMh, const double* GSh, const float* qw,
-                       int64_t n, const TcTape& tape, float* const* gW, float* const* gb, char* ws,
-                       cudaStream_t s);
+                       int64_t n, const TcTape& tape, float* const* gW, float* const* gb,
+                       int accumulate, char* ws, cudaStream_t s);
 
 }  // namespace neb

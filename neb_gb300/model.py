@@ -307,6 +307,7 @@ class SpectralResult:
     S: torch.Tensor | None = None
     A_M: torch.Tensor | None = None
     A_S: torch.Tensor | None = None
+    chunks: int = 1               # point chunks (the reverse pass recomputes all but the last)
 
 
 class SpectralState:
@@ -450,12 +451,22 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
     st = getattr(model, "_spectral", None) or SpectralState(model)
     model._spectral = st
     s = _stream()
-    tape = model.run_forward(feats)
     H, K = cfg.hidden, cfg.widths[-1]
+    # point chunks: one chunk while the activation tape of all n points fits
+    # the budget; otherwise the Grams accumulate chunk by chunk and the
+    # reverse pass recomputes each chunk's activations (the last chunk's are
+    # still resident and are used first)
+    chunk = int(chunk_points) if chunk_points else _factored_chunk(model, n)
+    if chunk <= 0:
+        raise ValueError("chunk_points must be positive")
+    bounds = [(a, min(n, a + chunk)) for a in range(0, n, chunk)]
     AM, AS = _f64((H, H), dev), _f64((H, H), dev)
-    ws = model._ws(n)
-    N.call("neb_hidden_gram", ctypes.byref(model.net), qw.data_ptr(), n, tape.buffer.data_ptr(),
-           AM.data_ptr(), AS.data_ptr(), ws.data_ptr(), ws.numel(), s)
+    for i, (a, b) in enumerate(bounds):
+        tape = model.run_forward(feats[a:b] if len(bounds) > 1 else feats)
+        ws = model._ws(b - a)
+        N.call("neb_hidden_gram", ctypes.byref(model.net), qw[a:b].data_ptr(), b - a,
+               tape.buffer.data_ptr(), AM.data_ptr(), AS.data_ptr(), int(i > 0), ws.data_ptr(),
+               ws.numel(), s)
     Wout = model.W[-1].to(torch.float64).contiguous()
     pws = st.buf.get("pencil", lib.neb_pencil_workspace_bytes(K, H))
     M = S = None
@@ -488,9 +499,15 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
                    pws.data_ptr(), pws.numel(), s)
             gW[L].copy_(gWo)
         gb[L].zero_()
-        N.call("neb_backward_hidden", ctypes.byref(model.net), N.ptr_array(model.W),
-               GMh.data_ptr(), GSh.data_ptr(), qw.data_ptr(), n, tape.buffer.data_ptr(),
-               N.ptr_array(gW[:L]), N.ptr_array(gb[:L]), ws.data_ptr(), ws.numel(), s)
+        for i, (a, b) in enumerate(reversed(bounds)):
+            if i > 0:  # recompute this chunk's activations
+                tape = model.run_forward(feats[a:b])
+            ws = model._ws(b - a)
+            N.call("neb_backward_hidden", ctypes.byref(model.net), N.ptr_array(model.W),
+                   GMh.data_ptr(), GSh.data_ptr(), qw[a:b].data_ptr(), b - a,
+                   tape.buffer.data_ptr(), N.ptr_array(gW[:L]), N.ptr_array(gb[:L]), int(i > 0),
+                   ws.data_ptr(), ws.numel(), s)
+        res.chunks = len(bounds)
         res.grads = (gW, gb)
     if check:
         model.check_device_status(n)
@@ -499,6 +516,18 @@ def spectral_step(model: Model, points=None, weights=None, training: bool = True
 
 
 DEFAULT_CHUNK_POINTS = 1 << 17
+# activation tape one chunk of the factored route may hold (bytes)
+FACTORED_TAPE_BUDGET = 32 << 30
+
+
+def _factored_chunk(model: Model, n: int) -> int:
+    """Points per chunk of the factored route: all n while their tape fits
+    FACTORED_TAPE_BUDGET, else the largest multiple of 128 that does."""
+    lib = N.load()
+    per = lib.neb_tape_bytes(ctypes.byref(model.net), n)
+    if per <= FACTORED_TAPE_BUDGET:
+        return n
+    return max(128, int(n * FACTORED_TAPE_BUDGET / per) // 128 * 128)
 
 
 def _spectral_step_direct(model: Model, points, weights, training, objective, return_grams,

@@ -195,3 +195,25 @@ def test_metaball3d_subsample(precision):
     eig, grad, rank = _pencil_case(model, O.features_raw3d(ps), ps, ws, 3, False)
     assert rank >= 11
     assert eig <= EIG_TOL and grad <= GRAD_TOL, (eig, grad, rank)
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "fp32"])
+def test_factored_route_point_chunks_recompute(precision):
+    """The factored route over point chunks (Grams accumulated chunk by
+    chunk, the reverse pass recomputing every chunk's activations but the
+    last) equals the one-chunk step, and stays within the oracle targets."""
+    _needs_gpu()
+    cfg = CONFIGS["periodic_train"]
+    pts, w = CF.sample(cfg)
+    model = Model(cfg, precision=precision, seed=1)
+    whole = spectral_step(model, pts, w, training=True)
+    parts = spectral_step(model, pts, w, training=True, chunk_points=4096 + 128)
+    assert whole.chunks == 1 and parts.chunks == 4
+    lam1, lam2 = whole.eigenvalues.cpu().numpy(), parts.eigenvalues.cpu().numpy()
+    assert float(np.max(np.abs(lam1 - lam2) / np.abs(lam1))) <= 1e-5
+    ref = O.objective_and_grad_factored(_params64(model), O.features_periodic(pts, cfg.n_freq), w,
+                                        cfg.objective)
+    g_whole = _grad_rel(whole.grads, ref.grads)
+    g_parts = _grad_rel(parts.grads, ref.grads)
+    assert _eig_rel(parts, ref) <= EIG_TOL and g_parts <= GRAD_TOL, g_parts
+    assert abs(g_parts - g_whole) <= 0.2 * g_whole + 1e-6, (g_whole, g_parts)

@@ -41,7 +41,8 @@ def _grams(model, n, static):
     else:
         ws = model._ws(n)
         N.call("neb_hidden_gram", ctypes.byref(model.net), qw.data_ptr(), n,
-               tape.buffer.data_ptr(), AM.data_ptr(), AS.data_ptr(), ws.data_ptr(), ws.numel(), s)
+               tape.buffer.data_ptr(), AM.data_ptr(), AS.data_ptr(), 0, ws.data_ptr(), ws.numel(),
+               s)
     torch.cuda.synchronize()
     return AM.cpu(), AS.cpu()
 
