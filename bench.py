@@ -72,7 +72,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--modes", default="32,1024",
-                    help="mode counts of the reference_velocity workload")
+                    help="mode counts of the reference_velocity / reference_potential workloads "
+                         "(the largest also sets the periodic_rollout basis)")
+    ap.add_argument("--grid", type=int, default=256,
+                    help="grid side of the periodic_rollout workload")
     ap.add_argument("--workload", default="periodic_train",
                     choices=["periodic_train", "periodic_small", "periodic_eval", "multihole",
                              "metaball3d", "reference_velocity", "reference_potential",
@@ -492,8 +495,9 @@ def run_workload(args, world, rank, local):
         from types import SimpleNamespace
         from neb_gb300 import hardcoded as H
         from neb_gb300.rollout import Rollout, grid_points, ritz, sample_basis
-        grid = 256
-        cfg = SimpleNamespace(**REF_POTENTIAL)
+        grid = int(args.grid)
+        cfg = SimpleNamespace(**dict(REF_POTENTIAL,
+                                     modes=max(int(k) for k in args.modes.split(","))))
         model = H.HardcodedModel(cfg, H.initial_arrays(cfg), device=dev)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
         # warm-up: kernel attributes, the allocator, the cuSOLVER / cuBLAS handles
@@ -505,6 +509,7 @@ def run_workload(args, world, rank, local):
         ev[0].record()
         gb = sample_basis(model, cfg, grid, diagnostics=True)
         ev[1].record()
+        model.core._bufs.clear()  # the sampling tape is not needed any more
         rb = ritz(gb)
         ev[2].record()
         roll = Rollout(gb, rb, 1e-3)
