@@ -510,6 +510,7 @@ def run_workload(args, world, rank, local):
         gb = sample_basis(model, cfg, grid, diagnostics=True)
         ev[1].record()
         model.core._bufs.clear()  # the sampling tape is not needed any more
+        torch.cuda.empty_cache()
         rb = ritz(gb)
         ev[2].record()
         roll = Rollout(gb, rb, 1e-3)
