@@ -25,7 +25,8 @@ int grid_for(int64_t n, int block = 256) {
   return (int)std::min<int64_t>(std::max<int64_t>(ceil_div(n, block), 1), 8192);
 }
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
-constexpr int kChunkPts = 256;   // points per block of the transposed pass
+constexpr int kChunkPts = 256;   // most points per block of the transposed pass
+constexpr int kMinChunkPts = 32; // fewest (small grids: more blocks in flight)
 constexpr int kColsPerBlock = 256;
 
 // ------------------------------------------------------------ feature jets
@@ -313,14 +314,14 @@ __global__ void rollout_pass1(int64_t n, int K, const T* __restrict__ UV,
 // UV[p][0][k] q1[p] - UV[p][1][k] q2[p].  grid (K / 256, chunks).
 template <typename T>
 __global__ void __launch_bounds__(kColsPerBlock)
-rollout_pass2(int64_t n, int K, const T* __restrict__ UV, const double* __restrict__ q,
+rollout_pass2(int64_t n, int K, int chunk, const T* __restrict__ UV, const double* __restrict__ q,
               const float* __restrict__ qh, const float* __restrict__ ql,
               double* __restrict__ partial) {
   __shared__ double s64[2][kChunkPts];
   __shared__ float sh[2][kChunkPts], sl[2][kChunkPts];
   const int k = blockIdx.x * kColsPerBlock + threadIdx.x;
-  const int64_t p0 = (int64_t)blockIdx.y * kChunkPts;
-  const int np = (int)std::min<int64_t>(kChunkPts, n - p0);
+  const int64_t p0 = (int64_t)blockIdx.y * chunk;
+  const int np = (int)std::min<int64_t>(chunk, n - p0);
   for (int i = threadIdx.x; i < np; i += blockDim.x) {
     if constexpr (sizeof(T) == 4) {
       sh[0][i] = qh[p0 + i];
@@ -415,11 +416,23 @@ __global__ void rollout_finish(int kind, int K, const double* __restrict__ R,
 // ------------------------------------------------------------ workspace
 struct RollWs {
   size_t b64, bh, bl, q, qh, ql, partial, y, vec, vec_stride, total;
-  int chunks;
+  int chunks, chunk;
 };
+// Points per block of the transposed pass: kChunkPts, fewer when the grid
+// would otherwise hold less than about four blocks per SM.
+int pass2_chunk(int64_t n, int K) {
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t cols = ceil_div(K, kColsPerBlock);
+  int64_t c = n * cols / (4 * (int64_t)std::max(sms, 1));
+  c = std::max<int64_t>(kMinChunkPts, std::min<int64_t>(kChunkPts, c));
+  return (int)(c / kMinChunkPts * kMinChunkPts);
+}
 RollWs roll_ws(int64_t n, int K) {
   RollWs w{};
-  w.chunks = (int)ceil_div(n, kChunkPts);
+  w.chunk = pass2_chunk(n, K);
+  w.chunks = (int)ceil_div(n, w.chunk);
   size_t o = 0;
   w.b64 = o; o += a256((size_t)K * 8);
   w.bh = o; o += a256((size_t)K * 4);
@@ -427,7 +440,7 @@ RollWs roll_ws(int64_t n, int K) {
   w.q = o; o += a256((size_t)3 * n * 8);
   w.qh = o; o += a256((size_t)2 * n * 4);
   w.ql = o; o += a256((size_t)2 * n * 4);
-  w.partial = o; o += a256((size_t)w.chunks * K * 8);
+  w.partial = o; o += a256((size_t)ceil_div(n, kMinChunkPts) * K * 8);
   w.y = o; o += a256((size_t)K * 8);
   w.vec = o;  // the stage vectors a, b, z, nv, na, nb
   w.vec_stride = a256((size_t)K * 8);
@@ -454,7 +467,7 @@ int launch_pass2(int64_t n, int K, const void* UV, char* ws, const RollWs& w, cu
   {
     KernelScope ks("rollout_pass2", s, 4.0 * n * K, 2.0 * n * K * sizeof(T));
     dim3 grid((unsigned)ceil_div(K, kColsPerBlock), (unsigned)w.chunks);
-    rollout_pass2<T><<<grid, kColsPerBlock, 0, s>>>(n, K, (const T*)UV,
+    rollout_pass2<T><<<grid, kColsPerBlock, 0, s>>>(n, K, w.chunk, (const T*)UV,
                                                      (const double*)(ws + w.q),
                                                      (const float*)(ws + w.qh),
                                                      (const float*)(ws + w.ql),
