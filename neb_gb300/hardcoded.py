@@ -377,6 +377,16 @@ class HardcodedModel:
         return norms, committed
 
     # ----------------------------------------------------------- checkpoint
+    def save(self, path) -> None:
+        """``arrays()`` to an .npz, written to a temporary file and then moved
+        into place (the reference's save_npz)."""
+        from pathlib import Path
+        path = Path(path)
+        tmp = path.with_suffix(path.suffix + ".tmp")
+        with tmp.open("wb") as stream:
+            np.savez(stream, **self.arrays())
+        tmp.replace(path)
+
     def arrays(self) -> dict:
         """Checkpoint arrays under the reference's key schema, one device to
         host copy per stacked tensor."""

@@ -9,8 +9,12 @@
   velocity objective, the ``step`` of experiments/metaball/train.py:208-214
   (objective and gradient, then Adam at the scheduled rate), with the
   peel's status word gating the update on the device.
+* ``potential_train_step``: one epoch of the reference's periodic trainer
+  (train_gauge_canonical.py:825-880): the epoch's points from
+  ``fluid_points`` seeded cfg.seed + 1009 epoch, the learning rate of the
+  schedule, one ``peel_step`` of the periodic backend.
 * ``train``: the epoch loop (sample, step, optional validation, atomic
-  checkpoint every ``checkpoint_every`` epochs) for either model family.
+  checkpoint every ``checkpoint_every`` epochs) for every model family.
 """
 from __future__ import annotations
 
@@ -41,6 +45,17 @@ def velocity_train_step(model, data, lr: float, clip: float = 8.0, block: int = 
     if check and not bool(committed.item()):
         raise FloatingPointError("Invalid parameter gradients; no optimizer update")
     return res
+
+
+def potential_train_step(cfg, model, epoch: int, lr: float) -> dict:
+    """One epoch of the periodic trainer on a HardcodedModel: cfg.learning_rate
+    is set to lr (the schedule's value), points = fluid_points(cfg,
+    cfg.points_per_step, 0, 0, cfg.seed + 1009 epoch), then peel_step with
+    training.  Returns the peel step's diagnostics."""
+    from .hardcoded import fluid_points, peel_step
+    cfg.learning_rate = float(lr)
+    points = fluid_points(cfg, int(cfg.points_per_step), 0.0, 0.0, int(cfg.seed) + epoch * 1009)
+    return peel_step(cfg, model, points, 0.0, 0.0, True)
 
 
 def train(model, step: Callable[[object, int, float], dict], epochs: int, base_lr: float,

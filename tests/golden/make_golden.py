@@ -327,6 +327,46 @@ def main():
     for key, value in hmodel.arrays().items():
         g["hb_out." + key] = np.asarray(value)
 
+    # the same networks with fixed-order sorting, and a three-mode network on
+    # the free box (raw_xy inputs, free_identity envelope): one training step
+    hcfg_fixed = HB.cfg_namespace(dict(vars(hcfg), causal_sorting="fixed_order"))
+    fmodel = HB.HardcodedModel(hcfg_fixed, {k[6:]: v for k, v in g.items()
+                                            if k.startswith("hb_in.")})
+    res = HB.peel_step(hcfg_fixed, fmodel, hpts, 0.0, 0.0, True)
+    g.update(hbf_loss=np.asarray(res["loss"]), hbf_energies=np.asarray(res["mode_energies"]),
+             hbf_order=np.asarray(res["causal_order"]))
+    for key, value in fmodel.arrays().items():
+        g["hbf_out." + key] = np.asarray(value)
+    free = HB.cfg_namespace(dict(
+        modes=3, hidden=8, hidden_layers=2, xmin=-1.0, xmax=2.0, ymin=0.0, ymax=1.5,
+        geometry_mode="free_box", envelope_mode="free_identity", input_encoding="raw_xy",
+        canonical_siren=True, siren_first_omega0=3.0, siren_hidden_omega0=2.0,
+        basis_objective="potential_rayleigh", causal_sorting="geometry_rayleigh",
+        reorthogonalization_passes=2, mass_floor=1e-14, learning_rate=1e-3, grad_clip=5.0,
+        spatial_derivative_order=1, mode_forward_batch=3, mode_backward_batch=3,
+        mlp_compute_dtype="float32", master_weight_dtype="float32"))
+    farr = {}
+    for mode in range(3):
+        for layer, (inside, outside) in enumerate(((2, 8), (8, 8), (8, 1))):
+            label = f"l{layer}" if layer < 2 else "output"
+            for offset, (kind, shape) in enumerate((("weight", (outside, inside)),
+                                                    ("bias", (outside,)))):
+                farr[f"m{mode:03d}.{label}.{kind}"] = rng.normal(0, .5, size=shape)
+                stem = f"m{mode:03d}.adam.p{2 * layer + offset:02d}"
+                farr[stem + ".exp_avg"] = np.zeros(shape)
+                farr[stem + ".exp_avg_sq"] = np.zeros(shape)
+                farr[stem + ".step"] = np.asarray(0, "i8")
+    fpts = np.column_stack((rng.uniform(-1.0, 2.0, 40), rng.uniform(0.0, 1.5, 40)))
+    fm = HB.HardcodedModel(free, farr)
+    res = HB.peel_step(free, fm, fpts, 0.0, 0.0, True)
+    g.update(hbfree_points=fpts, hbfree_loss=np.asarray(res["loss"]),
+             hbfree_energies=np.asarray(res["mode_energies"]),
+             hbfree_order=np.asarray(res["causal_order"]))
+    for key, value in farr.items():
+        g["hbfree_in." + key] = np.asarray(value)
+    for key, value in fm.arrays().items():
+        g["hbfree_out." + key] = np.asarray(value)
+
     # --- the trainer's epoch-0 arrays and fixed validation points
     # (prepare_gauge_canonical.py main, run on a three-mode configuration)
     import json

@@ -321,3 +321,61 @@ def test_reference_configuration_update_matches_oracle(precision, rtol):
         err = np.abs(got - want)
         assert err.max() <= 2 * cfg.learning_rate
         assert np.mean(err > 2e-6 + rtol * np.abs(want)) <= 1e-3
+
+
+def test_potential_training_loop(tmp_path):
+    """Three epochs of the periodic trainer through training.train: the
+    cosine rate, the epoch's seeded points, the peel step, an atomic
+    checkpoint that reloads into the same model; epoch 1 equals one peel
+    step at the schedule's first rate."""
+    _needs_gpu()
+    from neb_gb300 import hardcoded as H
+    from neb_gb300.training import cosine_learning_rate, potential_train_step, train
+    cfg = _cfg(modes=4, learning_rate=0.0, sampling_mode="uniform_random", seed=2,
+               points_per_step=96, epochs=3, base_learning_rate=2e-3, min_learning_rate=1e-4)
+    arrays = H.initial_arrays(SimpleNamespace(**dict(vars(cfg), input_features=12)))
+    model = H.HardcodedModel(cfg, arrays)
+    ckpt = tmp_path / "state.npz"
+    hist = train(model, lambda m, e, lr: potential_train_step(cfg, m, e, lr), cfg.epochs,
+                 cfg.base_learning_rate, cfg.min_learning_rate, checkpoint=ckpt)
+    assert [h["epoch"] for h in hist] == [1, 2, 3]
+    assert hist[0]["learning_rate"] == cosine_learning_rate(2e-3, 1e-4, 1, 3) == 2e-3
+    assert hist[-1]["learning_rate"] == 1e-4
+    assert model.steps.cpu().tolist() == [3, 3, 3, 3]
+    with np.load(ckpt) as z:
+        again = H.HardcodedModel(cfg, {k: z[k] for k in z.files})
+    after = model.arrays()
+    for k, v in again.arrays().items():
+        assert np.array_equal(v, after[k]), k
+    # epoch 1 alone, from the same start, equals the loop's first epoch
+    one = H.HardcodedModel(cfg, arrays)
+    r1 = potential_train_step(cfg, one, 1, 2e-3)
+    assert abs(r1["loss"] - hist[0]["loss"]) <= 1e-12 * abs(r1["loss"])
+
+
+@pytest.mark.parametrize("precision,rtol,atol", [("fp32", 2e-4, 2e-5), ("fp64", 1e-6, 1e-9)])
+@pytest.mark.parametrize("case", ["fixed_order", "free_box"])
+def test_peel_step_variants_match_reference(case, precision, rtol, atol):
+    """The reference's peel step with fixed-order sorting, and on the free
+    box (raw_xy inputs, free_identity envelope): energies, order and every
+    weight after its device Adam."""
+    _needs_gpu()
+    from neb_gb300.hardcoded import peel_step
+    if case == "fixed_order":
+        cfg = _cfg(causal_sorting="fixed_order")
+        arrays, pts, tag = _golden_arrays("hb_in"), G["hb_points"], "hbf"
+    else:
+        cfg = _cfg(modes=3, hidden=8, frequencies=0, xmin=-1.0, xmax=2.0, ymin=0.0, ymax=1.5,
+                   geometry_mode="free_box", envelope_mode="free_identity",
+                   input_encoding="raw_xy", siren_first_omega0=3.0, siren_hidden_omega0=2.0,
+                   mode_forward_batch=3, mode_backward_batch=3)
+        arrays, pts, tag = _golden_arrays("hbfree_in"), G["hbfree_points"], "hbfree"
+    model = _model(cfg, arrays, precision)
+    res = peel_step(cfg, model, pts, 0.0, 0.0, True)
+    assert res["causal_order"] == G[tag + "_order"].tolist()
+    np.testing.assert_allclose(res["mode_energies"], G[tag + "_energies"], rtol=rtol)
+    after = model.arrays()
+    ref = _golden_arrays(tag + "_out")
+    for key, value in ref.items():
+        if key.endswith(".weight"):
+            np.testing.assert_allclose(after[key], value, rtol=rtol, atol=atol, err_msg=key)

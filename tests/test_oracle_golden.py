@@ -319,3 +319,33 @@ def test_potential_peel_step_matches_reference_peel_step():
     for j in range(3):
         np.testing.assert_allclose(r["state"][0][j], W2[j], rtol=1e-9, atol=1e-12)
         np.testing.assert_allclose(r["state"][1][j], b2[j], rtol=1e-9, atol=1e-12)
+
+
+def test_fixed_order_and_free_box_peel_steps_match_reference():
+    """The reference's peel step with fixed-order sorting (the same four
+    periodic networks) and on the free box (raw_xy inputs, three networks):
+    losses, energies, order and the parameters after its device Adam."""
+    W, b = _hb_arrays("hb_in")
+    X0 = O.features_periodic(G["hb_points"], 3)[:3]
+    r = O.potential_peel_step(W, b, X0, (2 * math.pi) ** 2 / 48, O.mode_omegas(3, 8.0, 30.0),
+                              lr=1e-3, clip=5.0, sort=False)
+    np.testing.assert_array_equal(r["order"], G["hbf_order"])
+    np.testing.assert_allclose(r["losses"], G["hbf_energies"], rtol=1e-6)
+    W2, b2 = _hb_arrays("hbf_out")
+    for j in range(3):
+        np.testing.assert_allclose(r["state"][0][j], W2[j], rtol=1e-9, atol=1e-12)
+    labels = ("l0", "l1", "output")
+    Wf = [np.stack([G[f"hbfree_in.m{k:03d}.{lab}.weight"] for k in range(3)]) for lab in labels]
+    bf = [np.stack([G[f"hbfree_in.m{k:03d}.{lab}.bias"] for k in range(3)]) for lab in labels]
+    pts = G["hbfree_points"]
+    X = np.zeros((3, len(pts), 2))
+    X[0] = pts
+    X[1, :, 0] = 1.0
+    X[2, :, 1] = 1.0
+    r = O.potential_peel_step(Wf, bf, X, 3.0 * 1.5 / len(pts), O.mode_omegas(3, 3.0, 2.0),
+                              lr=1e-3, clip=5.0)
+    np.testing.assert_array_equal(r["order"], G["hbfree_order"])
+    np.testing.assert_allclose(r["losses"], G["hbfree_energies"], rtol=1e-6)
+    for j, lab in enumerate(labels):
+        ref = np.stack([G[f"hbfree_out.m{k:03d}.{lab}.weight"] for k in range(3)])
+        np.testing.assert_allclose(r["state"][0][j], ref, rtol=1e-9, atol=1e-12)
