@@ -22,6 +22,7 @@ import math
 from pathlib import Path
 from typing import Callable
 
+import numpy as np
 import torch
 
 
@@ -73,7 +74,12 @@ def train(model, step: Callable[[object, int, float], dict], epochs: int, base_l
         lr = cosine_learning_rate(base_lr, min_lr, epoch, epochs)
         res = step(model, epoch, lr)
         losses = res.get("losses", res.get("loss"))
-        loss = float(torch.as_tensor(losses).double().mean()) if losses is not None else None
+        if losses is None:
+            loss = None
+        elif isinstance(losses, torch.Tensor):
+            loss = float(losses.double().mean())
+        else:  # host values (a float or a list) keep their FP64 value
+            loss = float(np.mean(np.asarray(losses, dtype=np.float64)))
         record = {"epoch": epoch, "learning_rate": lr, "loss": loss}
         if validate is not None and validate_every and epoch % validate_every == 0:
             record["validation"] = validate(model, epoch)

@@ -45,3 +45,16 @@ def test_epoch_loop_schedules_validates_and_checkpoints(tmp_path):
     assert [h["loss"] for h in hist] == [2.5, 3.5, 4.5, 5.5, 6.5]
     assert [h.get("validation") for h in hist] == [None, {"epoch": 3}, None, None, {"epoch": 6}]
     assert len(model.saved) == 3  # epochs 2, 4, 6
+
+
+def test_train_keeps_host_losses_in_fp64():
+    """A step that returns its loss as a host float is recorded exactly (no
+    round trip through a float32 tensor)."""
+    from neb_gb300.training import train
+
+    class M:
+        def save(self, path):
+            pass
+
+    hist = train(M(), lambda m, e, lr: {"loss": 11.814643144231551}, 1, 1e-3, 1e-4)
+    assert hist[0]["loss"] == 11.814643144231551
