@@ -76,10 +76,12 @@ def parse():
                          "(the largest also sets the periodic_rollout basis)")
     ap.add_argument("--grid", type=int, default=256,
                     help="grid side of the periodic_rollout workload")
+    ap.add_argument("--points", type=int, default=0,
+                    help="first points of the metaball_eval workload (0: all 1,599,754)")
     ap.add_argument("--workload", default="periodic_train",
                     choices=["periodic_train", "periodic_small", "periodic_eval", "multihole",
                              "metaball3d", "reference_velocity", "reference_potential",
-                             "periodic_rollout"],
+                             "periodic_rollout", "metaball_eval"],
                     help="periodic_train is the headline line; the others print one line "
                          "each for the remaining configurations (timing and FP64-oracle "
                          "errors), not the headline metric")
@@ -410,9 +412,16 @@ def velocity_inputs(n: int, seed: int = 0):
     first [10, n, F] arrays."""
     rng = np.random.default_rng(seed)
     x = rng.random((n, 3))
+    return velocity_features(x, rng.uniform(-1, 1, 12))
+
+
+def velocity_features(x: np.ndarray, codes: np.ndarray):
+    """Feature and envelope jets of points x [n, 3] in the unit cube with
+    the 12 geometry codes (see velocity_inputs)."""
+    n = len(x)
     X0 = np.zeros((10, n, 15))
     X0[0, :, :3] = 2 * x - 1
-    X0[0, :, 3:] = rng.uniform(-1, 1, 12)[None]
+    X0[0, :, 3:] = codes[None]
     for a in range(3):
         X0[1 + a, :, a] = 2.0
     f = 4 * x * (1 - x)
@@ -489,7 +498,62 @@ def run_workload(args, world, rank, local):
     def dev_inputs(pts, w):
         return torch.tensor(pts, device=dev), torch.tensor(w, device=dev)
 
-    if name == "periodic_rollout":
+    if name == "metaball_eval":
+        # the reference's 3D basis evaluation (experiments/metaball/evaluate.py,
+        # Velocity): u = curl of every mode's vector potential, with the
+        # second-order forward of velocity/core.py fields, at all points of
+        # the metaball region; published 488 s (K = 512) and 748 s (K = 1024)
+        # including the streamed FP64 output (data/paper_results/
+        # primary_basis_runtime.csv:8-9, hardware not stated)
+        from types import SimpleNamespace
+        from neb_gb300 import ModeModel
+        from neb_gb300.modes import velocity_fields
+        Km = max(int(k) for k in args.modes.split(","))
+        c = SimpleNamespace(**{k: REF_VELOCITY[k] for k in ("hidden", "hidden_layers",
+                                                           "siren_first_omega0",
+                                                           "siren_hidden_omega0")})
+        model = ModeModel(c, K=Km, seed=0, inputs=15, outputs=3, dim=3, order=2, device=dev)
+        pts, _ = CF.sample(CONFIGS["metaball3d"])
+        if args.points:
+            pts = pts[:int(args.points)]
+        n = len(pts)
+        codes = np.random.default_rng(1).uniform(-1, 1, 12)
+        chunk, block = 65536, 32
+        host_u = torch.empty((3 * min(chunk, n), Km), dtype=torch.float32, pin_memory=True)
+        warm = velocity_features(pts[:1024], codes)
+        velocity_fields(model, SimpleNamespace(
+            features=torch.tensor(np.moveaxis(warm[0], 0, 1), dtype=torch.float32, device=dev),
+            envelope=torch.tensor(np.moveaxis(warm[1], 0, 1), dtype=torch.float32, device=dev)),
+            block=block)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for a in range(0, n, chunk):
+            X0, E = velocity_features(pts[a:a + chunk], codes)
+            data = SimpleNamespace(
+                features=torch.tensor(np.moveaxis(X0, 0, 1), dtype=torch.float32, device=dev),
+                envelope=torch.tensor(np.moveaxis(E, 0, 1), dtype=torch.float32, device=dev))
+            U, _ = velocity_fields(model, data, block=block)
+            host_u[:U.shape[0]].copy_(U, non_blocking=True)  # the streamed output
+        e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        flops = 2.0 * n * 10 * Km * sum(a * b for a, b in zip(model.widths[:-1], model.widths[1:]))
+        pub = {512: 488.2863621, 1024: 747.6812867}.get(Km)
+        line.update({
+            "metric": "3D basis evaluation: velocity (curl of every mode's vector potential) "
+                      "of the reference's per-mode SIREN (5x128 sine, omega 40/36, second-order "
+                      "jets) at every point of the metaball region",
+            "value": wall, "unit": "s", "higher_is_better": False, "modes": Km, "points": n,
+            "device_s": e0.elapsed_time(e1) / 1e3, "forward_tflops": flops / wall / 1e12,
+            "dtype": "f32", "output": "U [3 n, K] FP32 streamed to pinned host memory per "
+                                      "65,536-point chunk",
+            "published_reference_s": pub,
+            "speedup_vs_published": pub / wall if pub else None,
+            "data": "synthetic: the metaball configuration's 1,599,754 seeded points, 12 "
+                    "constant geometry codes, a bubble envelope; reference initialisation"})
+    elif name == "periodic_rollout":
         # frozen-basis evaluation of the reference's periodic Potential
         # network at K = 1024: Jet3 sampling on the grid, Ritz, ETDRK4
         from types import SimpleNamespace

@@ -366,6 +366,18 @@ int neb_potential_lift(int precision, const void* dV, const void* dG, int start,
                        int64_t n_points, int n_modes, void* adjoint, neb_stream_t stream);
 int neb_column_center(int precision, int64_t rows, int K, void* A, neb_stream_t stream);
 
+/* Evaluation-only forward of modes [start, stop): the same output jets as
+ * neb_modes_forward, with no tape (the hidden layers' outputs alternate
+ * between two buffers of the scratch and no pre-activation is kept), so a
+ * block needs neb_modes_eval_scratch_bytes instead of the tape.  For
+ * basis evaluation at many points (experiments/metaball/evaluate.py:100-105
+ * with velocity/core.py:71-77 fields). */
+size_t neb_modes_eval_scratch_bytes(const neb_modes* m, int n_block, int64_t n_points);
+int neb_modes_forward_eval(const neb_modes* m, int start, int stop, const void* const* W,
+                           const void* const* b, const void* features, const void* envelope,
+                           int64_t n_points, void* scratch, size_t scratch_bytes, void* out,
+                           neb_stream_t stream);
+
 /* ---- Periodic evaluation of a trained basis (no counterpart entry points in
  * the reference; they replace its CuPy code at the lines cited). ----
  *

@@ -115,6 +115,9 @@ _SIGNATURES = {
     "neb_modes_workspace_bytes": (c_size_t, [POINTER(ModeNet), c_int, c_int64]),
     "neb_modes_forward": (c_int, [POINTER(ModeNet), c_int, c_int, _PP, _PP, _P, _P, c_int64, _P,
                                   c_size_t, _P, _P]),
+    "neb_modes_eval_scratch_bytes": (c_size_t, [POINTER(ModeNet), c_int, c_int64]),
+    "neb_modes_forward_eval": (c_int, [POINTER(ModeNet), c_int, c_int, _PP, _PP, _P, _P, c_int64,
+                                       _P, c_size_t, _P, _P]),
     "neb_modes_backward": (c_int, [POINTER(ModeNet), c_int, c_int, _PP, _P, _P, c_int64, _P, _P,
                                    _PP, _PP, c_int, _P, c_size_t, _P]),
     "neb_velocity_fields": (c_int, [c_int, _P, c_int, c_int, c_int64, c_int, _P, _P, _P]),

@@ -293,7 +293,7 @@ mode_gemm(const T* __restrict__ A, int64_t a_mode, const T* __restrict__ W, int6
 #pragma unroll
         for (int c = 0; c < C; ++c) {
           z[c] *= omega;
-          pre_out[mb * o_mode + base + (int64_t)c * N] = z[c];
+          if (pre_out) pre_out[mb * o_mode + base + (int64_t)c * N] = z[c];
         }
         sine_jet<DIM, ORD>(z, y);
       } else {
@@ -851,9 +851,11 @@ int launch_mode_gemm(const T* A, int64_t a_mode, const T* W, int64_t w_mode, con
 template <typename T, int DIM, int ORD>
 int modes_forward_t(const neb_modes* m, int start, int B, const void* const* Wv,
                     const void* const* bv, const T* feats, const T* env, int64_t n, char* tape,
-                    T* out, cudaStream_t s) {
+                    T* out, cudaStream_t s, bool eval = false) {
   constexpr int C = Jet<DIM, ORD>::C;
   ModeTape tl = mode_tape(m, B, n);
+  // evaluation: no pre-activations, the layer outputs in two alternating buffers
+  const size_t ping = a256((size_t)B * n * C * max_width(m) * sizeof(T));
   const T* x = feats;
   int64_t x_mode = 0;
   for (int j = 0; j < m->n_layers; ++j) {
@@ -863,8 +865,8 @@ int modes_forward_t(const neb_modes* m, int start, int B, const void* const* Wv,
     const int64_t o_mode = (int64_t)n * C * o;
     int st;
     if (j + 1 < m->n_layers) {
-      T* pre = (T*)(tape + tl.pre[j]);
-      T* y = (T*)(tape + tl.x[j + 1]);
+      T* pre = eval ? nullptr : (T*)(tape + tl.pre[j]);
+      T* y = eval ? (T*)(tape + (j & 1) * ping) : (T*)(tape + tl.x[j + 1]);
       const double om = j == 0 ? m->omega_first : m->omega_hidden;
       st = launch_mode_gemm<T, DIM, ORD, EPI_HIDDEN>(x, x_mode, W, (int64_t)o * in, b, o, nullptr,
                                                      nullptr, pre, y, o_mode, B, (int)n, in, o, om,
@@ -985,9 +987,13 @@ int modes_backward_t(const neb_modes* m, int start, int B, const void* const* Wv
 template <typename T, int DIM, int ORD>
 int modes_forward_d(const neb_modes* m, int start, int B, const void* const* W,
                     const void* const* b, const void* feats, const void* env, int64_t n,
-                    void* tape, void* out, cudaStream_t s) {
+                    void* tape, void* out, cudaStream_t s, bool eval = false) {
   return modes_forward_t<T, DIM, ORD>(m, start, B, W, b, (const T*)feats, (const T*)env, n,
-                                      (char*)tape, (T*)out, s);
+                                      (char*)tape, (T*)out, s, eval);
+}
+
+size_t eval_scratch_bytes(const neb_modes* m, int B, int64_t n) {
+  return 2 * a256((size_t)B * n * mode_channels(m) * max_width(m) * esize(m));
 }
 
 template <typename T, int DIM, int ORD>
@@ -1042,6 +1048,44 @@ extern "C" int neb_modes_forward(const neb_modes* m, int start, int stop, const 
   }
   return NEB_MODES_DISPATCH(m, modes_forward_d, m, start, B, W, b, features, envelope, n_points,
                             tape, out, (cudaStream_t)stream);
+}
+
+extern "C" size_t neb_modes_eval_scratch_bytes(const neb_modes* m, int n_block,
+                                               int64_t n_points) {
+  if (check_modes(m) || n_block <= 0 || n_points <= 0) return 0;
+  return eval_scratch_bytes(m, n_block, n_points);
+}
+
+extern "C" int neb_modes_forward_eval(const neb_modes* m, int start, int stop,
+                                      const void* const* W, const void* const* b,
+                                      const void* features, const void* envelope,
+                                      int64_t n_points, void* scratch, size_t scratch_bytes,
+                                      void* out, neb_stream_t stream) {
+  int st = check_modes(m);
+  if (st) return st;
+  NEB_REQUIRE(0 <= start && start < stop && stop <= m->n_modes,
+              "neb_modes_forward_eval: modes [%d, %d) outside [0, %d)", start, stop, m->n_modes);
+  NEB_REQUIRE(n_points > 0 && n_points <= (1 << 30) && W && b && features && out,
+              "neb_modes_forward_eval: bad arguments");
+  for (int j = 0; j < m->n_layers; ++j)
+    NEB_REQUIRE(W[j] && b[j], "neb_modes_forward_eval: null parameters of layer %d", j);
+  const int B = stop - start;
+  NEB_REQUIRE(B <= 65535, "neb_modes_forward_eval: at most 65535 modes per call");
+  if (!scratch || scratch_bytes < eval_scratch_bytes(m, B, n_points)) {
+    set_error("neb_modes_forward_eval: scratch smaller than neb_modes_eval_scratch_bytes");
+    return NEB_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (m->order == 3) {
+    NEB_REQUIRE(!envelope, "neb_modes_forward_eval: third-order jets take the identity envelope");
+    return m->precision == NEB_PREC_FP64
+               ? modes_forward_d<double, 2, 3>(m, start, B, W, b, features, envelope, n_points,
+                                               scratch, out, s, true)
+               : modes_forward_d<float, 2, 3>(m, start, B, W, b, features, envelope, n_points,
+                                              scratch, out, s, true);
+  }
+  return NEB_MODES_DISPATCH(m, modes_forward_d, m, start, B, W, b, features, envelope, n_points,
+                            scratch, out, s, true);
 }
 
 extern "C" int neb_modes_backward(const neb_modes* m, int start, int stop, const void* const* W,

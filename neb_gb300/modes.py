@@ -204,6 +204,21 @@ class ModeModel:
                tape.data_ptr(), tape.numel(), out.data_ptr(), _stream())
         return out, (ModeTape(tape, start, stop, feats, env) if cache else None)
 
+    def forward_eval(self, feats: torch.Tensor, env, start: int, stop: int) -> torch.Tensor:
+        """Output jets [stop-start, n, C, outputs] of modes [start, stop)
+        without a tape (evaluation only: two alternating activation buffers)."""
+        n = feats.shape[0]
+        B = stop - start
+        lib = N.load()
+        scratch = self._buf("eval", lib.neb_modes_eval_scratch_bytes(ctypes.byref(self.net), B, n))
+        out = torch.empty((B, n, self.channels, self.widths[-1]), dtype=self.dtype,
+                          device=self.device)
+        N.call("neb_modes_forward_eval", ctypes.byref(self.net), start, stop,
+               N.ptr_array(self.W), N.ptr_array(self.b), feats.data_ptr(),
+               0 if env is None else env.data_ptr(), n, scratch.data_ptr(), scratch.numel(),
+               out.data_ptr(), _stream())
+        return out
+
     def forward(self, data, start: int, stop: int, cache: bool = False):
         """(output jet of modes [start, stop) times the envelope, tape)."""
         feats, env = self._inputs(data)
@@ -355,6 +370,25 @@ def column_apply(A: torch.Tensor, C: torch.Tensor, scale: float) -> torch.Tensor
            A.data_ptr(), C.to(torch.float64).contiguous().data_ptr(), scale, out.data_ptr(),
            ws.data_ptr(), ws.numel(), _stream())
     return out
+
+
+def velocity_fields(model: ModeModel, data, block: int = 32, gradient: bool = True):
+    """Velocity U [3n, K] (rows p*3 + a) and, with ``gradient``, its
+    gradient D [9n, K] of every mode at the data's points: the evaluation
+    of velocity/core.py:71-77 (fields), with the evaluation-only forward."""
+    if model.dim != 3 or model.order != 2 or model.widths[-1] != 3:
+        raise ValueError("velocity fields need a 3D second-order model with 3 outputs per mode")
+    feats, env = model._inputs(data)
+    n, K = feats.shape[0], model.K
+    U = torch.empty((3 * n, K), dtype=model.dtype, device=model.device)
+    D = torch.empty((9 * n, K), dtype=model.dtype, device=model.device)
+    prec = N.PREC[model.precision]
+    for a in range(0, K, block):
+        b = min(K, a + block)
+        out = model.forward_eval(feats, env, a, b)
+        N.call("neb_velocity_fields", prec, out.data_ptr(), a, b, n, K, U.data_ptr(),
+               D.data_ptr(), _stream())
+    return (U, D) if gradient else U
 
 
 def velocity_step(model: ModeModel, data, training: bool = True, block: int = 32,

@@ -214,3 +214,47 @@ def test_velocity_step_matches_oracle(precision, tol):
         num += float((d * d).sum())
         den += float((r * r).sum())
     assert (num / den) ** 0.5 <= tol, (num / den) ** 0.5
+
+
+@pytest.mark.parametrize("dim,order", [(2, 1), (2, 2), (3, 1), (3, 2)])
+def test_evaluation_forward_equals_taped_forward(dim, order):
+    """The tape-free evaluation forward gives the same output jets, bit for
+    bit, as the taped forward (same kernels, outputs kept in two alternating
+    buffers)."""
+    _needs_gpu()
+    cfg = SimpleNamespace(hidden=40, hidden_layers=3, siren_first_omega0=2.0,
+                          siren_hidden_omega0=1.5)
+    model = ModeModel(cfg, K=6, seed=3, inputs=5, outputs=3, dim=dim, order=order)
+    C = model.channels
+    rng = np.random.default_rng(2)
+    feats = torch.tensor(rng.normal(size=(300, C, 5)) * 0.5, dtype=torch.float32,
+                         device="cuda").contiguous()
+    env = torch.tensor(rng.normal(size=(300, C, 1)) * 0.3 + (np.arange(C) == 0)[None, :, None],
+                       dtype=torch.float32, device="cuda").contiguous()
+    a, _ = model.forward_packed(feats, env, 1, 5)
+    b = model.forward_eval(feats, env, 1, 5)
+    assert torch.equal(a, b)
+
+
+def test_velocity_fields_evaluation_matches_oracle():
+    """U and D of every mode (the reference's basis evaluation fields) from
+    the evaluation forward, against the oracle."""
+    _needs_gpu()
+    from neb_gb300.modes import velocity_fields
+    K, n = 5, 120
+    cfg = SimpleNamespace(hidden=24, hidden_layers=2, siren_first_omega0=2.0,
+                          siren_hidden_omega0=1.5)
+    model = ModeModel(cfg, K=K, seed=2, inputs=5, outputs=3, dim=3, order=2, precision="fp64")
+    rng = np.random.default_rng(11)
+    X0 = rng.normal(size=(10, n, 5)) * 0.6
+    E = np.concatenate([rng.uniform(.5, 1, (1, n, 1)), rng.normal(size=(9, n, 1)) * 0.2])
+    data = SimpleNamespace(features=_packed(X0, model), envelope=_packed(E, model))
+    U, D = velocity_fields(model, data, block=2)
+    Wn = [w.double().cpu().numpy() for w in model.W]
+    bn = [x.double().cpu().numpy() for x in model.b]
+    om = O.mode_omegas(3, 2.0, 1.5)
+    for k in range(K):
+        _, _, out = O.mode_forward([w[k] for w in Wn], [x[k] for x in bn], X0, E, 3, 2, om)
+        u, d = O.velocity_fields(out)
+        np.testing.assert_allclose(U[:, k].cpu().numpy(), u.reshape(-1), rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(D[:, k].cpu().numpy(), d.reshape(-1), rtol=1e-10, atol=1e-12)
