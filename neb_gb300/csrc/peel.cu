@@ -206,6 +206,101 @@ __global__ void peel_adjoints(const double* __restrict__ T, const double* __rest
   }
 }
 
+// ------------------------------------------------ double-float K x K products
+// C = op(A) op(B) for column-major K x K FP64 matrices, computed with pairs of
+// floats: every operand is split on the way into shared memory as hi + lo
+// (48 significant bits), a product a b = ah bh + (ah bl + al bh) keeps ah bh
+// exactly (FMA) and the sum is carried as s + c with the TwoSum error of
+// every addition (relative error ~ 2^-48 sqrt(K)).  FP64 runs at ~1 TFLOP/s
+// on this GPU, FP32 some sixty times faster, so these products take the
+// place of FP64 triangular multiplies.  op(X) is X^T when its flag is set.
+// tri: 0 full; 1 op(A) upper (zero for k < i); 2 op(A) lower (zero for
+// k > i); 3 op(B) upper (zero for k > j): the zero blocks are skipped and the
+// zero entries masked.  Operands must lie within the float exponent range.
+constexpr int kDfTile = 64, kDfK = 16, kDfLd = kDfTile + 4;
+
+__device__ __forceinline__ void df_mac(float& s, float& c, float ah, float al, float bh,
+                                       float bl) {
+  const float p = ah * bh;
+  const float e = fmaf(ah, bh, -p);
+  const float t = fmaf(ah, bl, al * bh);
+  const float ss = s + p;
+  const float bb = ss - s;
+  const float err = (s - (ss - bb)) + (p - bb);
+  s = ss;
+  c += err + e + t;
+}
+
+__global__ void __launch_bounds__(256)
+df_gemm(int K, const double* __restrict__ A, int ta, const double* __restrict__ B, int tb, int tri,
+        double* __restrict__ C) {
+  __shared__ __align__(16) float Ah[kDfK][kDfLd], Al[kDfK][kDfLd], Bh[kDfK][kDfLd],
+      Bl[kDfK][kDfLd];
+  const int i0 = blockIdx.x * kDfTile, j0 = blockIdx.y * kDfTile;
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  int kb = 0, ke = K;
+  if (tri == 1) kb = i0 / kDfK * kDfK;
+  if (tri == 2) ke = min(K, i0 + kDfTile);
+  if (tri == 3) ke = min(K, j0 + kDfTile);
+  float s[4][4], c[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) s[u][v] = c[u][v] = 0.f;
+  for (int k0 = kb; k0 < ke; k0 += kDfK) {
+    for (int e = tid; e < kDfK * kDfTile; e += 256) {
+      // A tile element (r, kk): consecutive threads along the contiguous index
+      const int r = ta ? e / kDfK : e % kDfTile, kk = ta ? e % kDfK : e / kDfTile;
+      const int i = i0 + r, k = k0 + kk;
+      double x = 0.0;
+      if (i < K && k < K && !(tri == 1 && k < i) && !(tri == 2 && k > i))
+        x = ta ? A[(int64_t)i * K + k] : A[i + (int64_t)k * K];
+      const float h = (float)x;
+      Ah[kk][r] = h;
+      Al[kk][r] = (float)(x - (double)h);
+      // B tile element (kk, q)
+      const int q = tb ? e % kDfTile : e / kDfK, kb2 = tb ? e / kDfTile : e % kDfK;
+      const int j = j0 + q, kq = k0 + kb2;
+      double y = 0.0;
+      if (j < K && kq < K && !(tri == 3 && kq > j))
+        y = tb ? B[j + (int64_t)kq * K] : B[kq + (int64_t)j * K];
+      const float g = (float)y;
+      Bh[kb2][q] = g;
+      Bl[kb2][q] = (float)(y - (double)g);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < kDfK; ++kk) {
+      const float4 ah = *reinterpret_cast<const float4*>(&Ah[kk][ty * 4]);
+      const float4 al = *reinterpret_cast<const float4*>(&Al[kk][ty * 4]);
+      const float4 bh = *reinterpret_cast<const float4*>(&Bh[kk][tx * 4]);
+      const float4 bl = *reinterpret_cast<const float4*>(&Bl[kk][tx * 4]);
+      const float a_h[4] = {ah.x, ah.y, ah.z, ah.w}, a_l[4] = {al.x, al.y, al.z, al.w};
+      const float b_h[4] = {bh.x, bh.y, bh.z, bh.w}, b_l[4] = {bl.x, bl.y, bl.z, bl.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) df_mac(s[u][v], c[u][v], a_h[u], a_l[u], b_h[v], b_l[v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = i0 + ty * 4 + u, j = j0 + tx * 4 + v;
+      if (i < K && j < K) C[i + (int64_t)j * K] = (double)s[u][v] + (double)c[u][v];
+    }
+}
+
+int launch_df_gemm(int K, const double* A, int ta, const double* B, int tb, int tri, double* C,
+                   cudaStream_t s) {
+  dim3 grid((unsigned)ceil_div(K, kDfTile), (unsigned)ceil_div(K, kDfTile));
+  df_gemm<<<grid, 256, 0, s>>>(K, A, ta, B, tb, tri, C);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
 __global__ void potrf_gate(const int* __restrict__ dev_info, int* __restrict__ info) {
   if (*dev_info != 0 && *info == 0) *info = 1;
 }
@@ -310,12 +405,8 @@ extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, dou
     // triangular (a scaled inverse transpose of a lower Cholesky factor, and
     // after the second pass a product of two upper triangles), so every
     // product with it is a triangular multiply (half a GEMM's work)
-    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, ms, K, W1, K),
-             "cublasDtrmm (ms T)");
-    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T,
-                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, W1, K, L2, K),
-             "cublasDtrmm (T^T ms T)");
+    if ((st = launch_df_gemm(K, ms, 0, T, 0, 3, W1, s))) return st;   // ms T
+    if ((st = launch_df_gemm(K, T, 1, W1, 0, 2, L2, s))) return st;   // T^T (ms T)
     symmetrize<<<grid_for(kk_n), 256, 0, s>>>(L2, K);
     NEB_LAUNCH_CHECK();
     if (cusolverDnDpotrf(g_peel.solver, CUBLAS_FILL_MODE_LOWER, K, L2, K, work, lwork, dinfo) !=
@@ -333,23 +424,13 @@ extern "C" int neb_coefficient_peel(int K, const double* M, const double* S, dou
     KernelScope ks("peel_objective", s, 5.0 * K * (double)K * K, 0);
     // O = T^T ms T (orthogonality), F = T^T ss T, TF = T triu(F, 1): all
     // triangular multiplies with the upper triangular T
-    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, ms, K, W1, K),
-             "cublasDtrmm (ms T)");
-    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T,
-                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, W1, K, L, K),
-             "cublasDtrmm (T^T ms T)");
-    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, ss, K, W1, K),
-             "cublasDtrmm (ss T)");
-    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T,
-                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, W1, K, F, K),
-             "cublasDtrmm (T^T ss T)");
+    if ((st = launch_df_gemm(K, ms, 0, T, 0, 3, W1, s))) return st;   // ms T
+    if ((st = launch_df_gemm(K, T, 1, W1, 0, 2, L, s))) return st;    // O = T^T ms T
+    if ((st = launch_df_gemm(K, ss, 0, T, 0, 3, W1, s))) return st;   // ss T
+    if ((st = launch_df_gemm(K, T, 1, W1, 0, 2, F, s))) return st;    // F = T^T ss T
     peel_gate<<<1, 1024, 0, s>>>(T, ms, L, F, K, mass_floor, losses, norm, rel, err, info);
     NEB_LAUNCH_CHECK();
-    NEB_BLAS(cublasDtrmm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                         CUBLAS_DIAG_NON_UNIT, K, K, &one, T, K, F, K, TF, K),
-             "cublasDtrmm (T triu(F))");
+    if ((st = launch_df_gemm(K, T, 0, F, 0, 1, TF, s))) return st;    // T triu(F, 1)
     peel_adjoints<<<grid_for(kk_n), 256, 0, s>>>(T, TF, losses, norm, order, K, Cu, Cd, T_out);
     NEB_LAUNCH_CHECK();
   }
