@@ -811,14 +811,18 @@ def run_workload(args, world, rank, local):
         pts, w = CF.sample(cfg)
         dp, dw = dev_inputs(pts, w)
         n = len(w)
-        model = Model(cfg, precision="fp32", seed=0, device=dev)
+        forms = {}
+        for prec in ("tf32", "bf16x9", "fp32"):
+            model = Model(cfg, precision=prec, seed=0, device=dev)
 
-        def step(i):
-            r = spectral_step(model, dp, dw, training=True, check=False)
-            model.adam_async(*r.grads, lr=cfg.lr, clip=cfg.clip)
-            return r
+            def step(i, model=model):
+                r = spectral_step(model, dp, dw, training=True, check=False)
+                model.adam_async(*r.grads, lr=cfg.lr, clip=cfg.clip)
+                return r
 
-        ms = _timed(step, W, K)
+            t = _timed(step, W, K)
+            forms[prec] = {"ms_per_step": t, "steps_per_s": 1e3 / t}
+        ms = forms["fp32"]["ms_per_step"]
         kern = _kernel_table(N, step, 1)
         r_full = spectral_step(Model(cfg, precision="fp32", seed=0, device=dev), dp, dw,
                                training=False)
@@ -827,7 +831,7 @@ def run_workload(args, world, rank, local):
         ps, ws_ = pts[sub], w[sub] * (n / len(sub))
         X0 = O.features_raw3d(ps)
         acc = {}
-        for prec in ("fp32", "fp64"):
+        for prec in ("tf32", "bf16x9", "fp32", "fp64"):
             m0 = Model(cfg, precision=prec, seed=0, device=dev)
             rt = m0.rank_rtol
             ref = O.objective_and_grad(_params64(m0), X0, ws_, 3, cfg.objective, rank_rtol=rt)
@@ -837,10 +841,14 @@ def run_workload(args, world, rank, local):
         line.update({
             "metric": "objective+grad steps/s, 3D curl basis K=512, 1,599,754 points",
             "value": 1e3 / ms, "unit": "steps/s", "ms_per_step": ms, "dtype": "f32",
+            "forms": forms, "tf32_vs_fp32": ms / forms["tf32"]["ms_per_step"],
+            "bf16x9_vs_fp32": ms / forms["bf16x9"]["ms_per_step"],
             "points": n, "chunk_points": 1 << 17, "rank_at_init": int(r_full.rank),
             "kernels_ms_per_step": kern, "accuracy_subsample_8192": acc,
             "gram": gram_rate(_gram_ms(kern), (3 * n, 3 * n), cfg.K),
-            "note": "FP32 SIMT kernels with point-chunked recompute and compensated Grams; at "
+            "note": "fp32: SIMT kernels; tf32 / bf16x9: the same with the layer GEMMs on the "
+                    "tensor cores (cuBLAS, TF32 inputs or the BF16x9 emulation of FP32 "
+                    "products); point-chunked recompute and compensated Grams; at "
                     "Glorot init the curl fields are nearly dependent, so M is numerically "
                     "singular and the pencil is solved on range(M) in FP64 at the form's rank "
                     "tolerance"})

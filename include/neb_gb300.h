@@ -47,7 +47,13 @@ enum {
   NEB_ERR_TIMEOUT = -8       /* a bounded device-side wait gave up                  */
 };
 
-enum { NEB_PREC_FP32 = 0, NEB_PREC_FP64 = 1, NEB_PREC_BF16X3 = 2 };
+enum { NEB_PREC_FP32 = 0, NEB_PREC_FP64 = 1, NEB_PREC_BF16X3 = 2, NEB_PREC_TF32 = 3,
+       NEB_PREC_BF16X9 = 4 };
+/* NEB_PREC_TF32 / NEB_PREC_BF16X9: FP32 storage, masters and jet epilogues as
+ * NEB_PREC_FP32, with the layer GEMMs (forward, data and weight gradients)
+ * on the tensor cores through cuBLAS -- TF32 inputs with FP32 accumulation
+ * (one pass), or the BF16x9 emulation of FP32 products; the Grams keep the
+ * FP32 (optionally compensated) sums. */
 /* Accumulation of the FP32 Grams (FP64 always sums in FP64; split-BF16 sums
  * in tensor memory, drained every 64 points): PLAIN sums the products in
  * FP32; COMPENSATED forms every product exactly (FMA) and keeps each chunk

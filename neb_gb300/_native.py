@@ -21,7 +21,7 @@ NEB_ERR_SOLVER = -6
 NEB_ERR_UNSUPPORTED = -7
 NEB_ERR_TIMEOUT = -8
 
-PREC = {"fp32": 0, "fp64": 1, "bf16x3": 2}
+PREC = {"fp32": 0, "fp64": 1, "bf16x3": 2, "tf32": 3, "bf16x9": 4}
 FEAT = {"periodic": 0, "multihole": 1, "raw3d": 2}
 MAX_HIDDEN = 8
 

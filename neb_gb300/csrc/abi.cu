@@ -1,6 +1,9 @@
 // extern "C" entry points of the jet MLP, the Grams and the reverse pass.
 // Precision dispatch: NEB_PREC_FP32 / NEB_PREC_FP64 run the SIMT kernels;
-// NEB_PREC_BF16X3 runs the tcgen05 kernels of tc_path.cu.
+// NEB_PREC_BF16X3 runs the tcgen05 kernels of tc_path.cu; NEB_PREC_TF32 /
+// NEB_PREC_BF16X9 run the FP32 SIMT path with its layer GEMMs on the tensor
+// cores through cuBLAS (plain GEMMs; the jet epilogues stay ours).
+#include <cublas_v2.h>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -70,6 +73,110 @@ namespace {
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// ------------------------------------------------ tensor-core layer GEMMs
+// The compute type of the calling entry point's precision (0: the SIMT
+// kernels), set for the duration of one ABI call by GemmScope.
+thread_local int tl_gemm_compute = 0;
+struct GemmScope {
+  int saved;
+  explicit GemmScope(const neb_net* net) : saved(tl_gemm_compute) {
+    tl_gemm_compute = net->precision == NEB_PREC_TF32     ? (int)CUBLAS_COMPUTE_32F_FAST_TF32
+                      : net->precision == NEB_PREC_BF16X9 ? (int)CUBLAS_COMPUTE_32F_EMULATED_16BFX9
+                                                          : 0;
+  }
+  ~GemmScope() { tl_gemm_compute = saved; }
+};
+cublasHandle_t g_layer_blas[kMaxDevices] = {};
+std::mutex g_layer_blas_mutex;
+
+int layer_blas(cudaStream_t s, cublasHandle_t* h) {
+  int dev = 0;
+  NEB_CUDA_CHECK(cudaGetDevice(&dev));
+  NEB_REQUIRE(dev >= 0 && dev < kMaxDevices, "device index %d", dev);
+  {
+    std::lock_guard<std::mutex> lock(g_layer_blas_mutex);
+    if (!g_layer_blas[dev] && cublasCreate(&g_layer_blas[dev]) != CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasCreate failed");
+      return NEB_ERR_CUDA;
+    }
+  }
+  *h = g_layer_blas[dev];
+  if (cublasSetStream(*h, s) != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasSetStream failed");
+    return NEB_ERR_CUDA;
+  }
+  return NEB_OK;
+}
+
+// Row-major C [rows][ldc] = alpha op(A) op(B) + beta C through cublasGemmEx
+// in FP32 storage with the scope's tensor-core compute type, expressed in
+// cuBLAS's column-major terms by the caller.
+int tc_sgemm(cudaStream_t s, cublasOperation_t ta, cublasOperation_t tb, int m, int64_t n,
+             int64_t k, float alpha, const float* A, int lda, const float* B, int ldb, float beta,
+             float* C, int ldc, const char* name) {
+  NEB_REQUIRE(n <= INT32_MAX && k <= INT32_MAX, "%s: %lld x %lld too large for one GEMM", name,
+              (long long)n, (long long)k);
+  cublasHandle_t h;
+  if (int st = layer_blas(s, &h)) return st;
+  KernelScope ks(name, s, 2.0 * m * (double)n * k, 4.0 * ((double)m * k + (double)n * k + (double)m * n));
+  const cublasStatus_t r =
+      cublasGemmEx(h, ta, tb, m, (int)n, (int)k, &alpha, A, CUDA_R_32F, lda, B, CUDA_R_32F, ldb,
+                   &beta, C, CUDA_R_32F, ldc, (cublasComputeType_t)tl_gemm_compute,
+                   CUBLAS_GEMM_DEFAULT);
+  if (r != CUBLAS_STATUS_SUCCESS) {
+    set_error("%s: cublasGemmEx failed (status %d)", name, (int)r);
+    return NEB_ERR_CUDA;
+  }
+  return NEB_OK;
+}
+
+// Bias on the value channel and the tanh jet of a pre-activation Z already
+// formed by a GEMM: Z [n*C][ldo] (updated in place), Y [n*C][ldo].
+template <int C>
+__global__ void jet_act_epilogue(float* __restrict__ Z, const float* __restrict__ bias,
+                                 float* __restrict__ Y, int64_t n, int N, int ldo) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * N;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = e / N;
+    const int o = (int)(e % N);
+    float z[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) z[c] = Z[(p * C + c) * ldo + o];
+    if (bias) {
+      z[0] += bias[o];
+      Z[p * C * ldo + o] = z[0];
+    }
+    if (Y) {
+      jet_act_forward<C>(z);
+#pragma unroll
+      for (int c = 0; c < C; ++c) Y[(p * C + c) * ldo + o] = z[c];
+    }
+  }
+}
+
+// The tanh-jet transpose with the pre-activation Zprev, in place on
+// Out [n*C][N].
+template <int C>
+__global__ void jet_act_transpose(const float* __restrict__ Zprev, float* __restrict__ Out,
+                                  int64_t n, int N) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * N;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = e / N;
+    const int i = (int)(e % N);
+    float z[C], yb[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      z[c] = Zprev[(p * C + c) * N + i];
+      yb[c] = Out[(p * C + c) * N + i];
+    }
+    jet_act_backward<C>(z, yb);
+#pragma unroll
+    for (int c = 0; c < C; ++c) Out[(p * C + c) * N + i] = yb[c];
+  }
+}
+
+int ew_grid(int64_t n) { return (int)std::min<int64_t>(std::max<int64_t>(ceil_div(n, 256), 1), 65535); }
+
 int net_channels(const neb_net* net) { return net->dim == 2 ? 4 : 10; }
 
 int check_net(const neb_net* net) {
@@ -81,7 +188,8 @@ int check_net(const neb_net* net) {
     NEB_REQUIRE(net->widths[l] > 0 && net->widths[l] <= 65536, "neb_net.widths[%d] = %d invalid", l,
                 net->widths[l]);
   NEB_REQUIRE(net->precision == NEB_PREC_FP32 || net->precision == NEB_PREC_FP64 ||
-                  net->precision == NEB_PREC_BF16X3,
+                  net->precision == NEB_PREC_BF16X3 || net->precision == NEB_PREC_TF32 ||
+                  net->precision == NEB_PREC_BF16X9,
               "unknown precision %d", net->precision);
   NEB_REQUIRE(net->gram == NEB_GRAM_PLAIN || net->gram == NEB_GRAM_COMPENSATED,
               "unknown Gram accumulation %d", net->gram);
@@ -179,6 +287,20 @@ WsLayout ws_layout(const neb_net* net, int64_t n) {
 template <typename T, int C>
 int launch_fwd(const T* X, const T* W, const T* b, T* Z, T* Y, int64_t n, int K, int N, int ldo,
                cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (tl_gemm_compute) {
+      // row-major Z [n C][ldo] = X [n C][K] W^T: column-major Z^T = W^T(K x N)^T X^T
+      int st = tc_sgemm(s, CUBLAS_OP_T, CUBLAS_OP_N, N, n * C, K, 1.f, W, K, X, K, 0.f, Z, ldo,
+                        Y ? "tc_layer_fwd" : "tc_output_fwd");
+      if (st) return st;
+      if (b || Y) {
+        KernelScope ks("jet_act_epilogue", s, 0, (double)n * C * N * (Y ? 12 : 8));
+        jet_act_epilogue<C><<<ew_grid(n * N), 256, 0, s>>>(Z, b, Y, n, N, ldo);
+        NEB_LAUNCH_CHECK();
+      }
+      return NEB_OK;
+    }
+  }
   using Tl = simt::Tile<C>;
   dim3 grid((unsigned)ceil_div(N, simt::kBN), (unsigned)ceil_div(n * C, Tl::BM));
   KernelScope ks(Y ? "simt_jet_layer_fwd" : "simt_jet_output_fwd", s, 2.0 * n * C * K * N,
@@ -194,6 +316,20 @@ int launch_fwd(const T* X, const T* W, const T* b, T* Z, T* Y, int64_t n, int K,
 template <typename T, int C, int MAP>
 int launch_bwd(const T* A, const T* B0, const T* B1, const T* rowscale, T scale, const T* Zprev,
                T* Out, int64_t n, int K, int N, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4 && MAP == 0) {
+    if (tl_gemm_compute && !rowscale) {
+      // row-major Out [n C][N] = scale A [n C][K] B0 [K][N]
+      int st = tc_sgemm(s, CUBLAS_OP_N, CUBLAS_OP_N, N, n * C, K, (float)scale, B0, N, A, K, 0.f,
+                        Out, N, "tc_layer_bwd_data");
+      if (st) return st;
+      if (Zprev) {
+        KernelScope ks("jet_act_transpose", s, 0, (double)n * C * N * 12);
+        jet_act_transpose<C><<<ew_grid(n * N), 256, 0, s>>>(Zprev, Out, n, N);
+        NEB_LAUNCH_CHECK();
+      }
+      return NEB_OK;
+    }
+  }
   using Tl = simt::Tile<C>;
   dim3 grid((unsigned)ceil_div(N, simt::kBN), (unsigned)ceil_div(n * C, Tl::BM));
   KernelScope ks(MAP ? "simt_gram_adjoint_bwd" : "simt_jet_layer_bwd_data", s,
@@ -214,6 +350,13 @@ template <typename T, int C, typename OutT>
 int launch_rowsum(const T* P, int ldp, const T* Q, int ldq, const T* w, simt::ChanSet chans,
                   int64_t n, int M, int N, bool sym, double scale, double* part, OutT* out,
                   cudaStream_t s, int accumulate = 0, bool comp = false) {
+  if constexpr (sizeof(T) == 4 && sizeof(OutT) == 4) {
+    if (tl_gemm_compute && !sym && !w && chans.n == C) {
+      // every channel row of every point: row-major out [M][N] = scale sum_r P[r][M]^T Q[r][N]
+      return tc_sgemm(s, CUBLAS_OP_N, CUBLAS_OP_T, N, M, n * C, (float)scale, Q, ldq, P, ldp,
+                      accumulate ? 1.f : 0.f, (float*)out, N, "tc_weight_grad");
+    }
+  }
   const int64_t cp = chunk_points(n);
   const int chunks = (int)ceil_div(n, cp);
   const int mt = (int)ceil_div(M, 128), nt = (int)ceil_div(N, simt::kBN);
@@ -615,6 +758,7 @@ extern "C" int neb_forward(const neb_net* net, const void* const* W, const void*
                            neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
+  GemmScope gemm(net);
   NEB_REQUIRE(n > 0 && W && b && feats && tape, "neb_forward: bad arguments");
   for (int l = 0; l < net->n_hidden; ++l) NEB_REQUIRE(W[l] && b[l], "neb_forward: null W/b[%d]", l);
   cudaStream_t s = (cudaStream_t)stream;
@@ -651,6 +795,7 @@ extern "C" int neb_output(const neb_net* net, const void* Wout, const void* bout
                           int stop, int64_t n, const void* tape, void* psi, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
+  GemmScope gemm(net);
   const int K = net->widths[net->n_hidden + 1];
   NEB_REQUIRE(n > 0 && Wout && tape && psi && 0 <= start && start < stop && stop <= K,
               "neb_output: bad arguments");
@@ -695,6 +840,7 @@ extern "C" int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n, co
                                neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
+  GemmScope gemm(net);
   NEB_REQUIRE(net->dim == 2, "neb_hidden_gram: 2D scalar potential only");
   NEB_REQUIRE(n > 0 && qw && tape && AM && AS, "neb_hidden_gram: bad arguments");
   if (ws_bytes < ws_layout(net, n).total || !ws) {
@@ -719,6 +865,7 @@ extern "C" int neb_backward_hidden(const neb_net* net, const void* const* W, con
                                    size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
+  GemmScope gemm(net);
   NEB_REQUIRE(net->dim == 2, "neb_backward_hidden: 2D scalar potential only");
   NEB_REQUIRE(n > 0 && W && GMh && GSh && qw && tape && gW && gb, "neb_backward_hidden: bad arguments");
   for (int l = 0; l < net->n_hidden; ++l)
@@ -752,6 +899,7 @@ extern "C" int neb_backward_output(const neb_net* net, const void* const* W, int
                                    size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
+  GemmScope gemm(net);
   const int K = net->widths[net->n_hidden + 1];
   NEB_REQUIRE(n > 0 && W && psibar && tape && gW && gb && 0 <= start && start < stop && stop <= K,
               "neb_backward_output: bad arguments");
@@ -772,6 +920,7 @@ extern "C" int neb_fields_gram(const neb_net* net, const void* Wout, const void*
                                size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
+  GemmScope gemm(net);
   NEB_REQUIRE(n > 0 && Wout && qw && tape && M && S, "neb_fields_gram: bad arguments");
   NEB_REQUIRE(net->precision != NEB_PREC_BF16X3,
               "neb_fields_gram: the direct route runs in NEB_PREC_FP32 or NEB_PREC_FP64");
@@ -789,6 +938,7 @@ extern "C" int neb_backward_fields(const neb_net* net, const void* const* W, con
                                    size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
+  GemmScope gemm(net);
   NEB_REQUIRE(n > 0 && W && GM && GS && qw && tape && gW && gb,
               "neb_backward_fields: bad arguments");
   for (int l = 0; l <= net->n_hidden; ++l)

@@ -106,7 +106,7 @@ class Model:
         self.vb = [torch.zeros_like(b) for b in self.b]
         # Gram accumulation of the FP32 form (FP64 sums in FP64, split-BF16
         # in tensor memory)
-        self.gram = gram or (cfg.gram if precision == "fp32" else "plain")
+        self.gram = gram or (cfg.gram if precision in ("fp32", "tf32", "bf16x9") else "plain")
         self.net = N.NebNet.make(cfg.dim, cfg.widths, precision, self.gram)
         # the reference-API forward/backward evaluate output-layer jets, which
         # the tensor-core path does not store: they run the FP32 kernels
@@ -373,7 +373,9 @@ def _solve(model: Model, m: int, PM, PS, kind: str):
 # adjoints) 1e-5; split-BF16 (16-bit activations, FP32 accumulation in
 # tensor memory) 1e-4.  The FP64 oracle solves the same pencil at the same
 # tolerance, and the ranks agree.
-RANK_RTOL = {"fp64": 1e-10, "fp32": 1e-5, "bf16x3": 1e-4}
+# tf32: one pass of 10-bit TF32 inputs in the layer GEMMs; bf16x9: the
+# BF16x9 emulation of FP32 products (FP32-class accuracy)
+RANK_RTOL = {"fp64": 1e-10, "fp32": 1e-5, "bf16x3": 1e-4, "tf32": 1e-4, "bf16x9": 1e-5}
 
 
 def _solve_range(model: Model, m: int, PM, PS, kind: str, rank_rtol: float = 1e-10):

@@ -31,6 +31,14 @@ pytestmark = pytest.mark.gpu
 
 EIG_TOL = 1e-4
 GRAD_TOL = 1e-3
+# one pass of TF32 inputs (10-bit mantissa) in the layer GEMMs does not meet
+# the targets: measured eig 3.5e-4 / 7.8e-4, grad 1.0e-3 / 4.1e-3 on
+# multihole / the metaball subsample; it is checked at this looser bar
+TF32_TOL = (2e-3, 1e-2)
+
+
+def _tols(precision):
+    return TF32_TOL if precision == "tf32" else (EIG_TOL, GRAD_TOL)
 
 
 def _needs_gpu():
@@ -169,7 +177,7 @@ def _pencil_case(model, X0, pts, w, dim, factored):
     return _eig_rel(res, ref), _grad_rel(res.grads, ref.grads), res.rank
 
 
-@pytest.mark.parametrize("precision", ["bf16x3", "fp32", "fp64"])
+@pytest.mark.parametrize("precision", ["bf16x3", "fp32", "fp64", "tf32", "bf16x9"])
 def test_multihole_200k(precision):
     _needs_gpu()
     cfg = CONFIGS["multihole"]
@@ -178,11 +186,12 @@ def test_multihole_200k(precision):
     assert model.rank_rtol == RANK_RTOL[precision]
     X0 = O.features_multihole(pts, np.asarray(cfg.centres))
     eig, grad, rank = _pencil_case(model, X0, pts, w, 2, True)
-    assert rank >= 19
-    assert eig <= EIG_TOL and grad <= GRAD_TOL, (eig, grad, rank)
+    assert rank >= (10 if precision == "tf32" else 19)
+    eig_tol, grad_tol = _tols(precision)
+    assert eig <= eig_tol and grad <= grad_tol, (eig, grad, rank)
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("precision", ["fp32", "fp64", "tf32", "bf16x9"])
 def test_metaball3d_subsample(precision):
     """8,192 seeded points of the 1,599,754 (weights rescaled to the full
     volume): the direct route with curl and curl-curl fields."""
@@ -193,8 +202,9 @@ def test_metaball3d_subsample(precision):
     ps, ws = pts[sub], w[sub] * (len(w) / 8192)
     model = Model(cfg, precision=precision, seed=0)
     eig, grad, rank = _pencil_case(model, O.features_raw3d(ps), ps, ws, 3, False)
-    assert rank >= 11
-    assert eig <= EIG_TOL and grad <= GRAD_TOL, (eig, grad, rank)
+    assert rank >= (5 if precision == "tf32" else 11)
+    eig_tol, grad_tol = _tols(precision)
+    assert eig <= eig_tol and grad <= grad_tol, (eig, grad, rank)
 
 
 @pytest.mark.parametrize("precision", ["bf16x3", "fp32"])
