@@ -76,6 +76,10 @@ def parse():
                          "(the largest also sets the periodic_rollout basis)")
     ap.add_argument("--grid", type=int, default=256,
                     help="grid side of the periodic_rollout workload")
+    ap.add_argument("--mode-precision", default="fp32", choices=["fp32", "bf16x9", "tf32"],
+                    help="per-mode network form of reference_velocity / metaball_eval: FP32 "
+                         "SIMT, or the per-mode GEMMs on the tensor cores (BF16x9 emulation "
+                         "of FP32 products, TF32)")
     ap.add_argument("--points", type=int, default=0,
                     help="first points of the metaball_eval workload (0: all 1,599,754)")
     ap.add_argument("--workload", default="periodic_train",
@@ -439,7 +443,8 @@ def velocity_features(x: np.ndarray, codes: np.ndarray):
     return X0, E
 
 
-def time_velocity(K: int, steps: int, warmup: int, dev, block: int = 256):
+def time_velocity(K: int, steps: int, warmup: int, dev, block: int = 256,
+                  precision: str = "fp32"):
     """ms per training step (velocity objective + gradient + Adam) of the
     reference's velocity configuration at K modes, CUDA events."""
     import torch
@@ -449,7 +454,8 @@ def time_velocity(K: int, steps: int, warmup: int, dev, block: int = 256):
     c = SimpleNamespace(**{k: REF_VELOCITY[k] for k in ("hidden", "hidden_layers",
                                                        "siren_first_omega0",
                                                        "siren_hidden_omega0")})
-    model = ModeModel(c, K=K, seed=0, inputs=15, outputs=3, dim=3, order=2, device=dev)
+    model = ModeModel(c, K=K, seed=0, inputs=15, outputs=3, dim=3, order=2, device=dev,
+                      precision=precision)
     X0, E = velocity_inputs(REF_VELOCITY["points"])
     feats = torch.tensor(np.moveaxis(X0, 0, 1), dtype=torch.float32, device=dev).contiguous()
     env = torch.tensor(np.moveaxis(E, 0, 1), dtype=torch.float32, device=dev).contiguous()
@@ -512,7 +518,8 @@ def run_workload(args, world, rank, local):
         c = SimpleNamespace(**{k: REF_VELOCITY[k] for k in ("hidden", "hidden_layers",
                                                            "siren_first_omega0",
                                                            "siren_hidden_omega0")})
-        model = ModeModel(c, K=Km, seed=0, inputs=15, outputs=3, dim=3, order=2, device=dev)
+        model = ModeModel(c, K=Km, seed=0, inputs=15, outputs=3, dim=3, order=2, device=dev,
+                          precision=args.mode_precision)
         pts, _ = CF.sample(CONFIGS["metaball3d"])
         if args.points:
             pts = pts[:int(args.points)]
@@ -547,6 +554,7 @@ def run_workload(args, world, rank, local):
                       "jets) at every point of the metaball region",
             "value": wall, "unit": "s", "higher_is_better": False, "modes": Km, "points": n,
             "device_s": e0.elapsed_time(e1) / 1e3, "forward_tflops": flops / wall / 1e12,
+            "mode_precision": args.mode_precision,
             "dtype": "f32", "output": "U [3 n, K] FP32 streamed to pinned host memory per "
                                       "65,536-point chunk",
             "published_reference_s": pub,
@@ -673,7 +681,7 @@ def run_workload(args, world, rank, local):
         vsteps = max(1, min(args.steps, 5))
         modes = [int(k) for k in args.modes.split(",")]
         for K in modes:
-            ms, info = time_velocity(K, vsteps, 1, dev)
+            ms, info = time_velocity(K, vsteps, 1, dev, precision=args.mode_precision)
             out[f"K{K}"] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms, "steps": vsteps,
                             "peel_info": info}
         top = f"K{max(modes)}"
@@ -699,6 +707,7 @@ def run_workload(args, world, rank, local):
                       "(5x128 sine, omega 40/36), 6144 points, causal peel",
             "value": out[top]["steps_per_s"], "unit": "steps/s",
             "ms_per_step": out[top]["ms_per_step"], "dtype": "f32", "modes": out,
+            "mode_precision": args.mode_precision,
             "published_reference_s_per_update_k1024": REF_VELOCITY["published_s_per_update_k1024"],
             "speedup_vs_published_k1024": (REF_VELOCITY["published_s_per_update_k1024"]
                                            / (out["K1024"]["ms_per_step"] / 1e3))

@@ -13,9 +13,15 @@
 #include "simt_kernels.cuh"
 #include "elementwise.cuh"
 #include "tc_path.cuh"
+#include "tc_blas.cuh"
 #include "fields.cuh"
 
 namespace neb {
+
+int& gemm_compute() {
+  thread_local int compute = 0;
+  return compute;
+}
 
 thread_local std::string g_last_error;
 
@@ -74,18 +80,6 @@ namespace {
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // ------------------------------------------------ tensor-core layer GEMMs
-// The compute type of the calling entry point's precision (0: the SIMT
-// kernels), set for the duration of one ABI call by GemmScope.
-thread_local int tl_gemm_compute = 0;
-struct GemmScope {
-  int saved;
-  explicit GemmScope(const neb_net* net) : saved(tl_gemm_compute) {
-    tl_gemm_compute = net->precision == NEB_PREC_TF32     ? (int)CUBLAS_COMPUTE_32F_FAST_TF32
-                      : net->precision == NEB_PREC_BF16X9 ? (int)CUBLAS_COMPUTE_32F_EMULATED_16BFX9
-                                                          : 0;
-  }
-  ~GemmScope() { tl_gemm_compute = saved; }
-};
 cublasHandle_t g_layer_blas[kMaxDevices] = {};
 std::mutex g_layer_blas_mutex;
 
@@ -114,20 +108,8 @@ int layer_blas(cudaStream_t s, cublasHandle_t* h) {
 int tc_sgemm(cudaStream_t s, cublasOperation_t ta, cublasOperation_t tb, int m, int64_t n,
              int64_t k, float alpha, const float* A, int lda, const float* B, int ldb, float beta,
              float* C, int ldc, const char* name) {
-  NEB_REQUIRE(n <= INT32_MAX && k <= INT32_MAX, "%s: %lld x %lld too large for one GEMM", name,
-              (long long)n, (long long)k);
-  cublasHandle_t h;
-  if (int st = layer_blas(s, &h)) return st;
-  KernelScope ks(name, s, 2.0 * m * (double)n * k, 4.0 * ((double)m * k + (double)n * k + (double)m * n));
-  const cublasStatus_t r =
-      cublasGemmEx(h, ta, tb, m, (int)n, (int)k, &alpha, A, CUDA_R_32F, lda, B, CUDA_R_32F, ldb,
-                   &beta, C, CUDA_R_32F, ldc, (cublasComputeType_t)tl_gemm_compute,
-                   CUBLAS_GEMM_DEFAULT);
-  if (r != CUBLAS_STATUS_SUCCESS) {
-    set_error("%s: cublasGemmEx failed (status %d)", name, (int)r);
-    return NEB_ERR_CUDA;
-  }
-  return NEB_OK;
+  return tc_sgemm_batched(s, ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1,
+                          name);
 }
 
 // Bias on the value channel and the tanh jet of a pre-activation Z already
@@ -288,7 +270,7 @@ template <typename T, int C>
 int launch_fwd(const T* X, const T* W, const T* b, T* Z, T* Y, int64_t n, int K, int N, int ldo,
                cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
-    if (tl_gemm_compute) {
+    if (gemm_compute()) {
       // row-major Z [n C][ldo] = X [n C][K] W^T: column-major Z^T = W^T(K x N)^T X^T
       int st = tc_sgemm(s, CUBLAS_OP_T, CUBLAS_OP_N, N, n * C, K, 1.f, W, K, X, K, 0.f, Z, ldo,
                         Y ? "tc_layer_fwd" : "tc_output_fwd");
@@ -317,7 +299,7 @@ template <typename T, int C, int MAP>
 int launch_bwd(const T* A, const T* B0, const T* B1, const T* rowscale, T scale, const T* Zprev,
                T* Out, int64_t n, int K, int N, cudaStream_t s) {
   if constexpr (sizeof(T) == 4 && MAP == 0) {
-    if (tl_gemm_compute && !rowscale) {
+    if (gemm_compute() && !rowscale) {
       // row-major Out [n C][N] = scale A [n C][K] B0 [K][N]
       int st = tc_sgemm(s, CUBLAS_OP_N, CUBLAS_OP_N, N, n * C, K, (float)scale, B0, N, A, K, 0.f,
                         Out, N, "tc_layer_bwd_data");
@@ -351,7 +333,7 @@ int launch_rowsum(const T* P, int ldp, const T* Q, int ldq, const T* w, simt::Ch
                   int64_t n, int M, int N, bool sym, double scale, double* part, OutT* out,
                   cudaStream_t s, int accumulate = 0, bool comp = false) {
   if constexpr (sizeof(T) == 4 && sizeof(OutT) == 4) {
-    if (tl_gemm_compute && !sym && !w && chans.n == C) {
+    if (gemm_compute() && !sym && !w && chans.n == C) {
       // every channel row of every point: row-major out [M][N] = scale sum_r P[r][M]^T Q[r][N]
       return tc_sgemm(s, CUBLAS_OP_N, CUBLAS_OP_T, N, M, n * C, (float)scale, Q, ldq, P, ldp,
                       accumulate ? 1.f : 0.f, (float*)out, N, "tc_weight_grad");
@@ -627,6 +609,32 @@ int backward_fields_simt(const neb_net* net, const void* const* W, const double*
 }
 
 }  // namespace
+
+int tc_sgemm_batched(cudaStream_t s, cublasOperation_t ta, cublasOperation_t tb, int m,
+                     int64_t n, int64_t k, float alpha, const float* A, int lda, int64_t sa,
+                     const float* B, int ldb, int64_t sb, float beta, float* C, int ldc,
+                     int64_t sc, int batch, const char* name) {
+  NEB_REQUIRE(n <= INT32_MAX && k <= INT32_MAX, "%s: %lld x %lld too large for one GEMM", name,
+              (long long)n, (long long)k);
+  cublasHandle_t h;
+  if (int st = layer_blas(s, &h)) return st;
+  KernelScope ks(name, s, 2.0 * batch * m * (double)n * k,
+                 4.0 * batch * ((double)m * k + (double)n * k + (double)m * n));
+  const cublasComputeType_t ct = (cublasComputeType_t)gemm_compute();
+  const cublasStatus_t r =
+      batch == 1 ? cublasGemmEx(h, ta, tb, m, (int)n, (int)k, &alpha, A, CUDA_R_32F, lda, B,
+                                CUDA_R_32F, ldb, &beta, C, CUDA_R_32F, ldc, ct,
+                                CUBLAS_GEMM_DEFAULT)
+                 : cublasGemmStridedBatchedEx(h, ta, tb, m, (int)n, (int)k, &alpha, A, CUDA_R_32F,
+                                              lda, sa, B, CUDA_R_32F, ldb, sb, &beta, C,
+                                              CUDA_R_32F, ldc, sc, batch, ct, CUBLAS_GEMM_DEFAULT);
+  if (r != CUBLAS_STATUS_SUCCESS) {
+    set_error("%s: cuBLAS GEMM failed (status %d)", name, (int)r);
+    return NEB_ERR_CUDA;
+  }
+  return NEB_OK;
+}
+
 }  // namespace neb
 
 using namespace neb;
@@ -758,7 +766,7 @@ extern "C" int neb_forward(const neb_net* net, const void* const* W, const void*
                            neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
-  GemmScope gemm(net);
+  GemmScope gemm(net->precision);
   NEB_REQUIRE(n > 0 && W && b && feats && tape, "neb_forward: bad arguments");
   for (int l = 0; l < net->n_hidden; ++l) NEB_REQUIRE(W[l] && b[l], "neb_forward: null W/b[%d]", l);
   cudaStream_t s = (cudaStream_t)stream;
@@ -795,7 +803,7 @@ extern "C" int neb_output(const neb_net* net, const void* Wout, const void* bout
                           int stop, int64_t n, const void* tape, void* psi, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
-  GemmScope gemm(net);
+  GemmScope gemm(net->precision);
   const int K = net->widths[net->n_hidden + 1];
   NEB_REQUIRE(n > 0 && Wout && tape && psi && 0 <= start && start < stop && stop <= K,
               "neb_output: bad arguments");
@@ -840,7 +848,7 @@ extern "C" int neb_hidden_gram(const neb_net* net, const void* qw, int64_t n, co
                                neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
-  GemmScope gemm(net);
+  GemmScope gemm(net->precision);
   NEB_REQUIRE(net->dim == 2, "neb_hidden_gram: 2D scalar potential only");
   NEB_REQUIRE(n > 0 && qw && tape && AM && AS, "neb_hidden_gram: bad arguments");
   if (ws_bytes < ws_layout(net, n).total || !ws) {
@@ -865,7 +873,7 @@ extern "C" int neb_backward_hidden(const neb_net* net, const void* const* W, con
                                    size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
-  GemmScope gemm(net);
+  GemmScope gemm(net->precision);
   NEB_REQUIRE(net->dim == 2, "neb_backward_hidden: 2D scalar potential only");
   NEB_REQUIRE(n > 0 && W && GMh && GSh && qw && tape && gW && gb, "neb_backward_hidden: bad arguments");
   for (int l = 0; l < net->n_hidden; ++l)
@@ -899,7 +907,7 @@ extern "C" int neb_backward_output(const neb_net* net, const void* const* W, int
                                    size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
-  GemmScope gemm(net);
+  GemmScope gemm(net->precision);
   const int K = net->widths[net->n_hidden + 1];
   NEB_REQUIRE(n > 0 && W && psibar && tape && gW && gb && 0 <= start && start < stop && stop <= K,
               "neb_backward_output: bad arguments");
@@ -920,7 +928,7 @@ extern "C" int neb_fields_gram(const neb_net* net, const void* Wout, const void*
                                size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
-  GemmScope gemm(net);
+  GemmScope gemm(net->precision);
   NEB_REQUIRE(n > 0 && Wout && qw && tape && M && S, "neb_fields_gram: bad arguments");
   NEB_REQUIRE(net->precision != NEB_PREC_BF16X3,
               "neb_fields_gram: the direct route runs in NEB_PREC_FP32 or NEB_PREC_FP64");
@@ -938,7 +946,7 @@ extern "C" int neb_backward_fields(const neb_net* net, const void* const* W, con
                                    size_t ws_bytes, neb_stream_t stream) {
   int st = check_net(net);
   if (st) return st;
-  GemmScope gemm(net);
+  GemmScope gemm(net->precision);
   NEB_REQUIRE(n > 0 && W && GM && GS && qw && tape && gW && gb,
               "neb_backward_fields: bad arguments");
   for (int l = 0; l <= net->n_hidden; ++l)

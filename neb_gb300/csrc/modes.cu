@@ -28,6 +28,7 @@
 #include <math_constants.h>
 #include "neb_common.cuh"
 #include "elementwise.cuh"
+#include "tc_blas.cuh"
 
 namespace neb {
 namespace {
@@ -738,8 +739,9 @@ int check_modes(const neb_modes* m) {
               "neb_modes.n_layers must be in [1, %d]", NEB_MAX_HIDDEN + 1);
   for (int l = 0; l <= m->n_layers; ++l)
     NEB_REQUIRE(m->widths[l] > 0 && m->widths[l] <= 65536, "neb_modes.widths[%d] invalid", l);
-  NEB_REQUIRE(m->precision == NEB_PREC_FP32 || m->precision == NEB_PREC_FP64,
-              "neb_modes: FP32 or FP64 parameters");
+  NEB_REQUIRE(m->precision == NEB_PREC_FP32 || m->precision == NEB_PREC_FP64 ||
+                  m->precision == NEB_PREC_TF32 || m->precision == NEB_PREC_BF16X9,
+              "neb_modes: FP32 (also with TF32 / BF16x9 tensor-core GEMMs) or FP64 parameters");
   NEB_REQUIRE(m->n_modes > 0, "neb_modes.n_modes must be positive");
   return NEB_OK;
 }
@@ -792,6 +794,88 @@ ModeWs mode_ws(const neb_modes* m, int B, int64_t n) {
   return w;
 }
 
+// Epilogue of a per-mode GEMM whose product Z is already in place (the
+// tensor-core forms): EPI_HIDDEN: z = omega (Z + b on the value channel) ->
+// pre (when kept), out = sine_jet(z); EPI_OUTPUT: out = env * (Z + b);
+// EPI_REVERSE: out = omega sine_jet^T(pre_in, Z).  Z lives in pre (hidden
+// layers with a tape) or in out; each thread owns one (mode, point, column).
+template <int DIM, int ORD, int EPI>
+__global__ void mode_epilogue(const float* __restrict__ Zsrc, const float* __restrict__ bias,
+                              int64_t b_mode, const float* __restrict__ env,
+                              const float* __restrict__ pre_in, float* __restrict__ pre_out,
+                              float* __restrict__ out, int64_t o_mode, int B, int n, int N,
+                              float omega) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  const int64_t total = (int64_t)B * n * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int o = (int)(e % N);
+    const int64_t bp = e / N;
+    const int p = (int)(bp % n), mb = (int)(bp / n);
+    const int64_t base = mb * o_mode + (int64_t)p * C * N + o;
+    float z[C], y[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) z[c] = Zsrc[base + (int64_t)c * N];
+    if constexpr (EPI == EPI_HIDDEN) {
+      z[0] += bias[mb * b_mode + o];
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        z[c] *= omega;
+        if (pre_out) pre_out[base + (int64_t)c * N] = z[c];
+      }
+      sine_jet<DIM, ORD>(z, y);
+    } else if constexpr (EPI == EPI_OUTPUT) {
+      z[0] += bias[mb * b_mode + o];
+      if (ORD < 3 && env) {
+        float ev[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) ev[c] = env[(int64_t)p * C + c];
+        envelope_mul<DIM, ORD>(ev, z, y);
+      } else {
+#pragma unroll
+        for (int c = 0; c < C; ++c) y[c] = z[c];
+      }
+    } else {
+      float pz[C];
+#pragma unroll
+      for (int c = 0; c < C; ++c) pz[c] = pre_in[base + (int64_t)c * N];
+      sine_jet_reverse<DIM, ORD>(pz, z, y);
+#pragma unroll
+      for (int c = 0; c < C; ++c) y[c] *= omega;
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) out[base + (int64_t)c * N] = y[c];
+  }
+}
+
+// The per-mode GEMM of the tensor-core forms: one strided-batched cuBLAS
+// GEMM over the block's modes (the shared features have stride 0), then the
+// epilogue.  Rows are (point, channel) pairs: [n C][Kd] per mode.
+template <int DIM, int ORD, int EPI>
+int tc_mode_gemm(const float* A, int64_t a_mode, const float* W, int64_t w_mode,
+                 const float* bias, int64_t b_mode, const float* env, const float* pre_in,
+                 float* pre_out, float* out, int64_t o_mode, int B, int n, int Kd, int N,
+                 double omega, cudaStream_t s, const char* name) {
+  constexpr int C = Jet<DIM, ORD>::C;
+  const int64_t R = (int64_t)n * C;
+  float* Z = (EPI == EPI_HIDDEN && pre_out) ? pre_out : out;
+  int st;
+  if constexpr (EPI == EPI_REVERSE)  // [R][N] = A [R][Kd] W [Kd][N]
+    st = tc_sgemm_batched(s, CUBLAS_OP_N, CUBLAS_OP_N, N, R, Kd, 1.f, W, N, w_mode, A, Kd,
+                          a_mode, 0.f, Z, N, o_mode, B, name);
+  else  // [R][N] = A [R][Kd] W^T, W [N][Kd]
+    st = tc_sgemm_batched(s, CUBLAS_OP_T, CUBLAS_OP_N, N, R, Kd, 1.f, W, Kd, w_mode, A, Kd,
+                          a_mode, 0.f, Z, N, o_mode, B, name);
+  if (st) return st;
+  const int64_t total = (int64_t)B * n * N;
+  KernelScope ks("mode_epilogue", s, 0, (double)total * C * 4 * (EPI == EPI_REVERSE ? 3 : 2));
+  mode_epilogue<DIM, ORD, EPI><<<(int)std::min<int64_t>(ceil_div(total, 256), 65535), 256, 0, s>>>(
+      Z, bias, b_mode, env, pre_in, EPI == EPI_HIDDEN ? pre_out : nullptr, out, o_mode, B, n, N,
+      (float)omega);
+  NEB_LAUNCH_CHECK();
+  return NEB_OK;
+}
+
 template <typename T, int DIM, int ORD, int EPI, int TC>
 int run_mode_gemm(int dev, const T* A, int64_t a_mode, const T* W, int64_t w_mode,
                   const T* bias, int64_t b_mode, const T* env, const T* pre_in, T* pre_out,
@@ -824,6 +908,11 @@ int launch_mode_gemm(const T* A, int64_t a_mode, const T* W, int64_t w_mode, con
                  (double)B * n * C * (Kd + N * (EPI == EPI_OUTPUT ? 1 : 2)) * sizeof(T));
   int dev = 0, sms = 0;
   if (int st = device_sms(&dev, &sms)) return st;
+  if constexpr (sizeof(T) == 4) {
+    if (gemm_compute() && !(EPI == EPI_OUTPUT && N <= kNarrowCols))
+      return tc_mode_gemm<DIM, ORD, EPI>(A, a_mode, W, w_mode, bias, b_mode, env, pre_in, pre_out,
+                                         out, o_mode, B, n, Kd, N, omega, s, name);
+  }
   if (EPI == EPI_OUTPUT && N <= kNarrowCols) {
     const int smem = narrow_smem<T, C>(N, Kd);
     NEB_REQUIRE(smem <= 200 * 1024, "mode output layer: %d inputs too many", Kd);
@@ -937,21 +1026,34 @@ int modes_backward_t(const neb_modes* m, int start, int B, const void* const* Wv
     splits = (int)std::min<int64_t>(splits, ceil_div(rows, kWgRows));
     const int64_t per = ceil_div(ceil_div(rows, splits), kWgRows) * kWgRows;
     splits = (int)ceil_div(rows, per);
-    {
-      KernelScope ks("mode_weight_grad", s, 2.0 * B * rows * (double)o * in,
-                     (double)B * rows * (o + in) * sizeof(T));
-      int st = narrow ? run_mode_wgrad<T, 32>(dev, dim3(tiles, B, splits), buf[cur], X, x_mode,
-                                                rows, o, in, per, part, s)
-                      : run_mode_wgrad<T, 64>(dev, dim3(tiles, B, splits), buf[cur], X, x_mode,
-                                                rows, o, in, per, part, s);
-      if (st) return st;
+    bool wg_done = false;
+    if constexpr (sizeof(T) == 4) {
+      if (gemm_compute()) {
+        // gW[b] [o][in] = sum_r Abar_b[r][o] X_b[r][in]: column-major gW^T = X^T Abar
+        int st = tc_sgemm_batched(s, CUBLAS_OP_N, CUBLAS_OP_T, in, o, rows, 1.f, X, in, x_mode,
+                                  buf[cur], o, rows * o, accumulate ? 1.f : 0.f, (float*)gW[j],
+                                  in, (int64_t)o * in, B, "tc_mode_weight_grad");
+        if (st) return st;
+        wg_done = true;
+      }
     }
-    {
-      const int64_t per_split = (int64_t)B * o * in;
-      KernelScope ks("mode_weight_grad_reduce", s, 0, (double)splits * per_split * sizeof(T));
-      mode_wgrad_reduce<T><<<(int)std::min<int64_t>(ceil_div(per_split, 256), 4096), 256, 0, s>>>(
-          part, splits, per_split, accumulate, (T*)gW[j]);
-      NEB_LAUNCH_CHECK();
+    if (!wg_done) {
+      {
+        KernelScope ks("mode_weight_grad", s, 2.0 * B * rows * (double)o * in,
+                       (double)B * rows * (o + in) * sizeof(T));
+        int st = narrow ? run_mode_wgrad<T, 32>(dev, dim3(tiles, B, splits), buf[cur], X, x_mode,
+                                                  rows, o, in, per, part, s)
+                        : run_mode_wgrad<T, 64>(dev, dim3(tiles, B, splits), buf[cur], X, x_mode,
+                                                  rows, o, in, per, part, s);
+        if (st) return st;
+      }
+      {
+        const int64_t per_split = (int64_t)B * o * in;
+        KernelScope ks("mode_weight_grad_reduce", s, 0, (double)splits * per_split * sizeof(T));
+        mode_wgrad_reduce<T><<<(int)std::min<int64_t>(ceil_div(per_split, 256), 4096), 256, 0,
+                               s>>>(part, splits, per_split, accumulate, (T*)gW[j]);
+        NEB_LAUNCH_CHECK();
+      }
     }
     {
       KernelScope ks("mode_bias_grad", s, 0, (double)B * n * o * sizeof(T));
@@ -1026,6 +1128,7 @@ extern "C" int neb_modes_forward(const neb_modes* m, int start, int stop, const 
                                  size_t tape_bytes, void* out, neb_stream_t stream) {
   int st = check_modes(m);
   if (st) return st;
+  GemmScope gemm(m->precision);
   NEB_REQUIRE(0 <= start && start < stop && stop <= m->n_modes,
               "neb_modes_forward: modes [%d, %d) outside [0, %d)", start, stop, m->n_modes);
   NEB_REQUIRE(n_points > 0 && n_points <= (1 << 30) && W && b && features && out,
@@ -1063,6 +1166,7 @@ extern "C" int neb_modes_forward_eval(const neb_modes* m, int start, int stop,
                                       void* out, neb_stream_t stream) {
   int st = check_modes(m);
   if (st) return st;
+  GemmScope gemm(m->precision);
   NEB_REQUIRE(0 <= start && start < stop && stop <= m->n_modes,
               "neb_modes_forward_eval: modes [%d, %d) outside [0, %d)", start, stop, m->n_modes);
   NEB_REQUIRE(n_points > 0 && n_points <= (1 << 30) && W && b && features && out,
@@ -1095,6 +1199,7 @@ extern "C" int neb_modes_backward(const neb_modes* m, int start, int stop, const
                                   size_t workspace_bytes, neb_stream_t stream) {
   int st = check_modes(m);
   if (st) return st;
+  GemmScope gemm(m->precision);
   NEB_REQUIRE(0 <= start && start < stop && stop <= m->n_modes,
               "neb_modes_backward: modes [%d, %d) outside [0, %d)", start, stop, m->n_modes);
   NEB_REQUIRE(n_points > 0 && n_points <= (1 << 30) && W && features && adjoint && gW && gb,

@@ -232,7 +232,7 @@ class HardcodedModel:
         origin = torch.tensor([cfg.xmin, cfg.ymin], dtype=torch.float64, device=core.device)
         shifted = (pts - origin).contiguous()
         out = torch.empty((n, C, 4 * Fq), dtype=core.dtype, device=core.device)
-        N.call("neb_periodic_features", N.PREC[core.precision], order, Fq,
+        N.call("neb_periodic_features", core.storage_prec, order, Fq,
                float(cfg.xmax - cfg.xmin), float(cfg.ymax - cfg.ymin), shifted.data_ptr(), n,
                out.data_ptr(), _stream())
         return out
@@ -444,7 +444,7 @@ def _streamfunction_peel_step(cfg, model: HardcodedModel, points, training: bool
         raise ValueError("configuration/model mode count mismatch")
     weight = float(np.float32((cfg.xmax - cfg.xmin) * (cfg.ymax - cfg.ymin)) / np.float32(n))
     mass_floor = float(cfg.mass_floor)
-    prec = N.PREC[core.precision]
+    prec = core.storage_prec
     s = _stream()
     feats = model.features(cfg, points, 1)
     V = torch.empty((n, K), dtype=core.dtype, device=core.device)

@@ -125,8 +125,9 @@ class ModeModel:
     def __init__(self, c, K: int = 32, seed: int = 0, inputs: int = 15, outputs: int = 3,
                  dim: int = 3, order: int = 1, precision: str = "fp32",
                  device: str | torch.device = "cuda"):
-        if precision not in ("fp32", "fp64"):
-            raise ValueError("precision must be 'fp32' or 'fp64'")
+        if precision not in ("fp32", "fp64", "tf32", "bf16x9"):
+            raise ValueError("precision must be 'fp32', 'fp64', 'tf32' or 'bf16x9' (FP32 "
+                             "parameters with the per-mode GEMMs on the tensor cores)")
         if dim not in (2, 3) or order not in (1, 2):
             raise ValueError("dim must be 2 or 3 and order 1 or 2")
         self.c, self.K, self.dim, self.order = c, K, dim, order
@@ -160,6 +161,11 @@ class ModeModel:
     @epoch.setter
     def epoch(self, value: int) -> None:
         self._steps.fill_(int(value))
+
+    @property
+    def storage_prec(self) -> int:
+        """Precision code of the stored arrays (FP32 for the tensor-core forms)."""
+        return N.PREC["fp64" if self.dtype == torch.float64 else "fp32"]
 
     @property
     def channels(self) -> int:
@@ -382,7 +388,7 @@ def velocity_fields(model: ModeModel, data, block: int = 32, gradient: bool = Tr
     n, K = feats.shape[0], model.K
     U = torch.empty((3 * n, K), dtype=model.dtype, device=model.device)
     D = torch.empty((9 * n, K), dtype=model.dtype, device=model.device)
-    prec = N.PREC[model.precision]
+    prec = model.storage_prec
     for a in range(0, K, block):
         b = min(K, a + block)
         out = model.forward_eval(feats, env, a, b)
@@ -406,7 +412,7 @@ def velocity_step(model: ModeModel, data, training: bool = True, block: int = 32
     dt = model.dtype
     U = torch.empty((3 * n, K), dtype=dt, device=model.device)
     D = torch.empty((9 * n, K), dtype=dt, device=model.device)
-    prec = N.PREC[model.precision]
+    prec = model.storage_prec
     blocks = [(a, min(K, a + block)) for a in range(0, K, block)]
     for a, b in blocks:
         out, _ = model.forward_packed(feats, env, a, b)

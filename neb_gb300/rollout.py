@@ -88,14 +88,14 @@ def sample_basis(model: HardcodedModel, cfg, grid: int, diagnostics: bool = Fals
     lib = N.load()
     per_mode = max(1, lib.neb_modes_tape_bytes(ctypes.byref(net3), 1, n))
     block = max(1, min(K, TAPE_BUDGET // per_mode))
-    prec = N.PREC[core.precision]
+    prec = core.storage_prec
     with model._order(3):
         for a in range(0, K, block):
             b = min(K, a + block)
             out, _ = core.forward_packed(feats, None, a, b)
             N.call("neb_stream_fields", prec, 3, out.data_ptr(), a, b, n, K, UV.data_ptr(),
                    Om.data_ptr(), 0 if diag is None else diag.data_ptr(), _stream())
-    return GridBasis(UV, Om, diag, float(weight), core.precision)
+    return GridBasis(UV, Om, diag, float(weight), "fp64" if dt == torch.float64 else "fp32")
 
 
 @dataclass
@@ -154,7 +154,7 @@ class Rollout:
                               dtype=torch.uint8, device=dev)
         self.c = torch.zeros(self.K, dtype=torch.float64, device=dev)
         self.coef = torch.zeros((6, self.K), dtype=torch.float64, device=dev)
-        self.prec = N.PREC[basis.precision]
+        self.prec = N.PREC["fp64" if basis.Om.dtype == torch.float64 else "fp32"]
         self.h = None
         self.use_graph = use_graph
         self._graph = None

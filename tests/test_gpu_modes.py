@@ -103,7 +103,8 @@ def _packed(arr, model):  # oracle [C, n, F] -> device [n, C, F]
     return torch.tensor(np.moveaxis(arr, 0, 1), dtype=model.dtype, device="cuda").contiguous()
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-4)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-4), ("bf16x9", 1e-4),
+                                           ("tf32", 3e-3)])
 @pytest.mark.parametrize("dim,order", [(2, 1), (2, 2), (3, 1), (3, 2)])
 def test_mode_jets_forward_reverse_match_oracle(dim, order, precision, tol):
     _needs_gpu()
@@ -190,7 +191,7 @@ def test_coefficient_peel_matches_oracle():
 
 
 # ----------------------------------------------------- 3D velocity objective
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("fp32", 2e-3)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("fp32", 2e-3), ("bf16x9", 2e-3)])
 def test_velocity_step_matches_oracle(precision, tol):
     _needs_gpu()
     K, n = 12, 400
