@@ -354,7 +354,7 @@ REF_POTENTIAL = dict(modes=1024, hidden=32, hidden_layers=4, frequencies=6, inpu
 PUBLISHED_POTENTIAL_S_PER_UPDATE = (6228.0 / 2000, 6599.0 / 2000)
 
 
-def time_potential(K: int, steps: int, warmup: int, dev):
+def time_potential(K: int, steps: int, warmup: int, dev, precision: str = "fp32"):
     """ms per training update of the reference's Potential configuration at
     K modes through the periodic backend's API (hardcoded.peel_step): each
     update samples its points on the host (fluid_points, seed + 1009 epoch,
@@ -364,7 +364,7 @@ def time_potential(K: int, steps: int, warmup: int, dev):
     from types import SimpleNamespace
     from neb_gb300 import hardcoded as H
     cfg = SimpleNamespace(**dict(REF_POTENTIAL, modes=K))
-    model = H.HardcodedModel(cfg, H.initial_arrays(cfg), device=dev)
+    model = H.HardcodedModel(cfg, H.initial_arrays(cfg), precision=precision, device=dev)
     n = cfg.points_per_step
 
     def step(epoch):
@@ -632,7 +632,7 @@ def run_workload(args, world, rank, local):
         psteps = max(2, min(args.steps, 10))
         modes = [int(k) for k in args.modes.split(",")]
         for Km in modes:
-            ms, r, step = time_potential(Km, psteps, 2, dev)
+            ms, r, step = time_potential(Km, psteps, 2, dev, precision=args.mode_precision)
             out[f"K{Km}"] = {"ms_per_update": ms, "updates_per_s": 1e3 / ms, "steps": psteps,
                              "loss": r["loss"], "orth_error": r["orth_error"]}
             if Km == max(modes):
@@ -665,6 +665,7 @@ def run_workload(args, world, rank, local):
                       "omega 8/30), 4096 points per update",
             "value": out[top]["updates_per_s"], "unit": "updates/s",
             "ms_per_update": out[top]["ms_per_update"], "dtype": "f32", "modes": out,
+            "mode_precision": args.mode_precision,
             "e2e_note": "each update samples its points on the host, uploads them and reads "
                         "the diagnostic table back, as the reference's trainer does",
             "published_reference_s_per_update_k1024": [lo, hi],
