@@ -462,8 +462,9 @@ __global__ void split_scaled(const double* __restrict__ C, double scale, int64_t
 extern "C" int neb_column_apply(int precision, int64_t rows, int K, const void* A,
                                 const double* Cm, double scale, void* out, void* workspace,
                                 size_t workspace_bytes, neb_stream_t stream) {
-  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64,
-              "neb_column_apply: FP32 or FP64");
+  NEB_REQUIRE(precision == NEB_PREC_FP32 || precision == NEB_PREC_FP64 ||
+                  precision == NEB_PREC_TF32 || precision == NEB_PREC_BF16X9,
+              "neb_column_apply: FP32 (also TF32 / BF16x9 products) or FP64");
   NEB_REQUIRE(rows > 0 && rows <= (int64_t)1 << 31 && K > 0 && A && Cm && out,
               "neb_column_apply: bad arguments");
   cudaStream_t s = (cudaStream_t)stream;
@@ -490,6 +491,24 @@ extern "C" int neb_column_apply(int precision, int64_t rows, int K, const void* 
     KernelScope ks("split_scaled", s, 0, 16.0 * kk);
     split_scaled<<<grid_for(kk), 256, 0, s>>>(Cm, scale, kk, hi, lo);
     NEB_LAUNCH_CHECK();
+  }
+  if (precision != NEB_PREC_FP32) {
+    // the tensor-core forms: the two products through cuBLAS with their compute type
+    KernelScope ks("cublas_gemm_tc", s, 4.0 * rows * (double)K * K, 0);
+    const cublasComputeType_t ct = precision == NEB_PREC_TF32 ? CUBLAS_COMPUTE_32F_FAST_TF32
+                                                              : CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+    const float one = 1.f, zero = 0.f;
+    const cublasStatus_t r1 =
+        cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, K, (int)rows, K, &one, hi, CUDA_R_32F, K, A,
+                     CUDA_R_32F, K, &zero, out, CUDA_R_32F, K, ct, CUBLAS_GEMM_DEFAULT);
+    const cublasStatus_t r2 =
+        cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, K, (int)rows, K, &one, lo, CUDA_R_32F, K, A,
+                     CUDA_R_32F, K, &one, out, CUDA_R_32F, K, ct, CUBLAS_GEMM_DEFAULT);
+    if (r1 != CUBLAS_STATUS_SUCCESS || r2 != CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasGemmEx (columns) failed");
+      return NEB_ERR_CUDA;
+    }
+    return NEB_OK;
   }
   {
     KernelScope ks("cublas_sgemm", s, 4.0 * rows * (double)K * K, 0);

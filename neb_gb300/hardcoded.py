@@ -471,8 +471,8 @@ def _streamfunction_peel_step(cfg, model: HardcodedModel, points, training: bool
     norms = torch.full((K,), float("nan"), **f64)
     committed = torch.zeros((), dtype=torch.int32, device=core.device)
     if training:
-        dV = column_apply(V, peel.Cu, weight)
-        dG = column_apply(G, peel.Cd, weight)
+        dV = column_apply(V, peel.Cu, weight, core.precision)
+        dG = column_apply(G, peel.Cd, weight, core.precision)
         N.call("neb_column_center", prec, n, K, dV.data_ptr(), s)
         gW = [torch.empty_like(w) for w in core.W]
         gb = [torch.empty_like(x) for x in core.b]

@@ -364,15 +364,19 @@ def column_gram(A: torch.Tensor, scale: float, compensated: bool = True) -> torc
     return G
 
 
-def column_apply(A: torch.Tensor, C: torch.Tensor, scale: float) -> torch.Tensor:
+def column_apply(A: torch.Tensor, C: torch.Tensor, scale: float,
+                 form: str | None = None) -> torch.Tensor:
     """scale A C (A [rows, K], C [K, K] FP64) in A's type: FP64 GEMM for
-    FP64 A; for FP32 A, scale C split into two floats and FP32 GEMMs."""
+    FP64 A; for FP32 A, scale C split into two floats and FP32 GEMMs (on the
+    tensor cores for ``form`` "tf32" / "bf16x9")."""
     rows, K = A.shape
     lib = N.load()
     out = torch.empty_like(A)
     ws = torch.empty(max(lib.neb_column_apply_workspace_bytes(rows, K), 256), dtype=torch.uint8,
                      device=A.device)
-    N.call("neb_column_apply", N.PREC["fp64" if A.dtype == torch.float64 else "fp32"], rows, K,
+    code = N.PREC["fp64" if A.dtype == torch.float64 else
+                  (form if form in ("tf32", "bf16x9") else "fp32")]
+    N.call("neb_column_apply", code, rows, K,
            A.data_ptr(), C.to(torch.float64).contiguous().data_ptr(), scale, out.data_ptr(),
            ws.data_ptr(), ws.numel(), _stream())
     return out
@@ -425,8 +429,8 @@ def velocity_step(model: ModeModel, data, training: bool = True, block: int = 32
                relative_mass=peel.relative_mass, gram_max=peel.gram_max, info=peel.info,
                M=M, S=S)
     if training:
-        gu = column_apply(U, peel.Cu, 1.0 / n)
-        gd = column_apply(D, peel.Cd, 1.0 / n)
+        gu = column_apply(U, peel.Cu, 1.0 / n, model.precision)
+        gd = column_apply(D, peel.Cd, 1.0 / n, model.precision)
         gW = [torch.empty_like(w) for w in model.W]
         gb = [torch.empty_like(x) for x in model.b]
         for a, b in blocks:
