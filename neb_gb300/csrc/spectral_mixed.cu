@@ -39,10 +39,9 @@
 //                                          eigenvalues refined to FP64 Rayleigh quotients
 //   side: wy_factor / wy_apply on I        Q^T (FP32), 32 reflectors per block in
 //                                          compact WY form, during the two above
-//   SGEMM                                  X = Z^T Q^T (rows x_k = Q z_k)
-//   df_solve_rl, SGEMMs                    V rows = (L^-T x_k)^T, G_S, G_M
+//   gemm_tn                                X = Z^T Q^T (rows x_k = Q z_k)
+//   df_solve_rl, gemm_tn                   V rows = (L^-T x_k)^T; G_S and G_M in one pass
 #include <cooperative_groups.h>
-#include <cublas_v2.h>
 #include "elementwise.cuh"
 
 namespace cg = cooperative_groups;
@@ -63,6 +62,9 @@ __device__ __forceinline__ uint32_t sh_u32(const void* p) {
 }
 __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sh_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sh_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sh_u32(dst)), "l"(src)
@@ -360,20 +362,28 @@ constexpr int kSolveCols = 4;  // eigenvectors per block of the back-transformat
 //   per right-hand side, the 32 factor entries loaded before the barrier).
 // Each row keeps its accumulators in registers from the load of B to the
 // store of Y; the only sequential chain is the 16 blocks (at m = 512), with
-// one barrier each.  B(r, c) = b_trans ? B[c][r] : B[r][c] (FP64 or FP32);
+// one barrier each.  The inverse diagonal blocks are staged in shared memory
+// (rows padded to 33 pairs: a warp reading one row per lane is free of bank
+// conflicts) while B loads, so the block's warp reads D_b without a trip to
+// L2 on the chain.  B(r, c) = b_trans ? B[c][r] : B[r][c] (FP64 or FP32);
 // Y(r, c) goes to out[r][c] or, with out_trans, out[c][r].
 constexpr int kRLCols = 4;
+constexpr int kDPad = kCB + 1;
+size_t solve_smem(int m) { return (size_t)(m / kCB) * kCB * kDPad * sizeof(df); }
 __global__ void __launch_bounds__(kMaxM) df_solve_rl(const df* __restrict__ F,
                                                      const df* __restrict__ D, int m, int upper,
                                                      const void* __restrict__ B, int b_f32,
                                                      int b_trans, void* __restrict__ out,
                                                      int out_f32, int out_trans) {
+  extern __shared__ df dsh[];            // [nb][kCB][kDPad] inverse diagonal blocks
   __shared__ df stage[kCB][kRLCols];     // accumulators of the block being finished
   __shared__ df ys[2][kCB][kRLCols];     // y of the finished block, by parity
   const int i = threadIdx.x, lane = i & 31, wb = i >> 5;  // row, its block
   const int c0 = blockIdx.x * kRLCols;
   const int nb = m / kCB;
   const bool has = i < m;
+  for (int t = i; t < nb * kCB * kCB; t += blockDim.x)
+    cp_async8(dsh + (size_t)(t / kCB) * kDPad + t % kCB, D + t);
   df acc[kRLCols];
 #pragma unroll
   for (int c = 0; c < kRLCols; ++c) {
@@ -383,12 +393,14 @@ __global__ void __launch_bounds__(kMaxM) df_solve_rl(const df* __restrict__ F,
       acc[c] = df_from(b_f32 ? (double)((const float*)B)[bi] : ((const double*)B)[bi]);
     }
   }
+  cp_async_wait_all();
+  __syncthreads();
   for (int bb = 0; bb < nb; ++bb) {
     const int b = upper ? nb - 1 - bb : bb, par = bb & 1;
     const int r0 = b * kCB;
     const bool pending = has && (upper ? wb < b : wb > b);
     if (wb == b) {
-      const df* dp = D + ((size_t)b * kCB + lane) * kCB;  // row lane of D_b
+      const df* dp = dsh + ((size_t)b * kCB + lane) * kDPad;  // row lane of D_b
 #pragma unroll
       for (int c = 0; c < kRLCols; ++c) stage[lane][c] = acc[c];
       __syncwarp();
@@ -1228,15 +1240,95 @@ __global__ void __launch_bounds__(256) wy_apply(const float* __restrict__ Vh,
   }
 }
 
-// Scale rows of E by f_k = c_k (G_S) or c_k lam_k (G_M) into Es.
-__global__ void scale_rows(const float* __restrict__ E, const double* __restrict__ c,
-                           const double* __restrict__ lam, int m, float* __restrict__ Es) {
-  const size_t n = (size_t)m * m;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    int k = (int)(i / m);
-    Es[i] = E[i] * (float)(c[k] * (lam ? lam[k] : 1.0));
+// C1 = s1 A^T diag(w1) B and, with TWO, C2 = s2 A^T diag(w2) B, for A, B
+// [m][m] FP32 row-major: C[i][j] = sum_k A[k][i] w_k B[k][j], w1_k = f_k (1
+// without f), w2_k = f_k g_k.  The back-transformation X = Z^T Q^T and the
+// objective adjoints G_S = E^T diag(c) E, G_M = -E^T diag(c lam) E have this
+// form.  32 x 32 output tiles, 256 threads with 2 x 2 outputs each, FP32
+// products and sums; k in chunks of 32 staged in shared memory, the next
+// chunk loaded into registers while the current one is multiplied.  sym
+// (A = B): only the tiles with bj <= bi, every entry computed once and
+// mirrored, so the outputs are exactly symmetric.
+constexpr int kGT = 32;
+template <typename TOut, bool TWO>
+__global__ void __launch_bounds__(256) gemm_tn(const float* __restrict__ A,
+                                               const float* __restrict__ B,
+                                               const double* __restrict__ f,
+                                               const double* __restrict__ g, int m, int sym,
+                                               TOut* __restrict__ C1, float s1,
+                                               TOut* __restrict__ C2, float s2) {
+  __shared__ __align__(16) float as[kGT][kGT];
+  __shared__ __align__(16) float bs1[kGT][kGT];
+  __shared__ __align__(16) float bs2[TWO ? kGT : 1][kGT];
+  const int nt = m / kGT;
+  int t = blockIdx.x, bi = 0, bj;
+  if (sym) {
+    while (t > bi) {
+      t -= bi + 1;
+      ++bi;
+    }
+    bj = t;
+  } else {
+    bi = t / nt;
+    bj = t % nt;
   }
+  const int i0 = bi * kGT, j0 = bj * kGT;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int lc = tid & 31, lr = tid >> 5;  // staged elements: rows lr + 8 q, column lc
+  float ra[4], rb1[4], rb2[4];
+  auto fetch = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + lr + 8 * q;
+      ra[q] = A[(size_t)k * m + i0 + lc];
+      const float bv = B[(size_t)k * m + j0 + lc];
+      const double w = f ? f[k] : 1.0;
+      rb1[q] = bv * (float)w;
+      if constexpr (TWO) rb2[q] = bv * (float)(w * g[k]);
+    }
+  };
+  float acc1[2][2] = {}, acc2[2][2] = {};
+  fetch(0);
+  for (int k0 = 0; k0 < m; k0 += kGT) {
+    __syncthreads();  // every read of the previous chunk is done
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      as[lr + 8 * q][lc] = ra[q];
+      bs1[lr + 8 * q][lc] = rb1[q];
+      if constexpr (TWO) bs2[lr + 8 * q][lc] = rb2[q];
+    }
+    __syncthreads();
+    if (k0 + kGT < m) fetch(k0 + kGT);
+#pragma unroll 8
+    for (int kk = 0; kk < kGT; ++kk) {
+      const float2 a = *reinterpret_cast<const float2*>(&as[kk][2 * ty]);
+      const float2 b = *reinterpret_cast<const float2*>(&bs1[kk][2 * tx]);
+      acc1[0][0] = fmaf(a.x, b.x, acc1[0][0]);
+      acc1[0][1] = fmaf(a.x, b.y, acc1[0][1]);
+      acc1[1][0] = fmaf(a.y, b.x, acc1[1][0]);
+      acc1[1][1] = fmaf(a.y, b.y, acc1[1][1]);
+      if constexpr (TWO) {
+        const float2 d = *reinterpret_cast<const float2*>(&bs2[kk][2 * tx]);
+        acc2[0][0] = fmaf(a.x, d.x, acc2[0][0]);
+        acc2[0][1] = fmaf(a.x, d.y, acc2[0][1]);
+        acc2[1][0] = fmaf(a.y, d.x, acc2[1][0]);
+        acc2[1][1] = fmaf(a.y, d.y, acc2[1][1]);
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 2; ++cc) {
+      const int i = i0 + 2 * ty + r, j = j0 + 2 * tx + cc;
+      if (sym && j > i) continue;  // diagonal tiles: the lower triangle, mirrored
+      C1[(size_t)i * m + j] = (TOut)(s1 * acc1[r][cc]);
+      if (sym && i != j) C1[(size_t)j * m + i] = (TOut)(s1 * acc1[r][cc]);
+      if constexpr (TWO) {
+        C2[(size_t)i * m + j] = (TOut)(s2 * acc2[r][cc]);
+        if (sym && i != j) C2[(size_t)j * m + i] = (TOut)(s2 * acc2[r][cc]);
+      }
+    }
 }
 
 __global__ void fill_identity(float* __restrict__ I, int m) {
@@ -1302,31 +1394,6 @@ MixedWs mixed_ws(int m) {
   return w;
 }
 
-// Row-major single-precision C[m][n] = alpha op(A) op(B) + beta C via cuBLAS.
-int sgemm_rm(cublasHandle_t h, bool ta, bool tb, int m, int n, int k, float alpha,
-             const float* A, int lda, const float* B, int ldb, float beta, float* C, int ldc) {
-  cublasStatus_t st = cublasSgemm(h, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N,
-                                  n, m, k, &alpha, B, ldb, A, lda, &beta, C, ldc);
-  if (st != CUBLAS_STATUS_SUCCESS) {
-    set_error("cublasSgemm failed (%d)", (int)st);
-    return NEB_ERR_CUDA;
-  }
-  return NEB_OK;
-}
-
-thread_local cublasHandle_t g_blas32 = nullptr;
-
-int blas32(cudaStream_t s, cublasHandle_t* out) {
-  if (!g_blas32 && cublasCreate(&g_blas32) != CUBLAS_STATUS_SUCCESS) {
-    set_error("cublasCreate failed");
-    return NEB_ERR_CUDA;
-  }
-  cublasSetStream(g_blas32, s);
-  cublasSetMathMode(g_blas32, CUBLAS_DEFAULT_MATH);  // true FP32, no TF32
-  *out = g_blas32;
-  return NEB_OK;
-}
-
 }  // namespace
 }  // namespace neb
 
@@ -1372,6 +1439,17 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
   const size_t mm = (size_t)m * m;
   const int nb = m / kCB;
 
+  {
+    int dev = 0, sms = 0;
+    int st0;
+    if ((st0 = device_sms(&dev, &sms))) return st0;
+    static bool solve_configured[kMaxDevices] = {};
+    if (!solve_configured[dev]) {
+      NEB_CUDA_CHECK(cudaFuncSetAttribute(df_solve_rl, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)solve_smem(kMaxM)));
+      solve_configured[dev] = true;
+    }
+  }
   NEB_CUDA_CHECK(cudaMemsetAsync(info, 0, sizeof(int), s));
   {
     KernelScope ks("spec_cholesky_df", s, (double)m * m * m / 3.0, 16.0 * mm, nb + 1);
@@ -1402,15 +1480,13 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     }
     {
       KernelScope k2("df_solve_rl", s, 0, 0, 0);
-      df_solve_rl<<<m / kRLCols, kMaxM, 0, s>>>(LTd, DL, m, 0, S, 0, 0, Y, 0, 0);
+      df_solve_rl<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(LTd, DL, m, 0, S, 0, 0, Y, 0, 0);
       NEB_LAUNCH_CHECK();
     }
     KernelScope k3("df_solve_rl", s, 0, 0, 0);
-    df_solve_rl<<<m / kRLCols, kMaxM, 0, s>>>(LTd, DL, m, 0, Y, 0, 1, C, 1, 0);
+    df_solve_rl<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(LTd, DL, m, 0, Y, 0, 1, C, 1, 0);
     NEB_LAUNCH_CHECK();
   }
-  cublasHandle_t h;
-  if ((st = blas32(s, &h))) return st;
   {
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1511,29 +1587,26 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     NEB_CUDA_CHECK(cudaStreamWaitEvent(s, ev_join[dev], 0));
     join.armed = false;
     KernelScope ks("spec_backtransform_fp32", s, 2.0 * m * mm, 12.0 * mm, 1);
-    if ((st = sgemm_rm(h, true, false, m, m, m, 1.f, Z, m, G, m, 0.f, X, m))) return st;
+    const int nt = m / kGT;
+    gemm_tn<float, false><<<nt * nt, 256, 0, s>>>(Z, G, nullptr, nullptr, m, 0, X, 1.f,
+                                                   (float*)nullptr, 0.f);
+    NEB_LAUNCH_CHECK();
   }
   {
-    KernelScope ks("spec_adjoints_fp32", s, 6.0 * m * mm, 24.0 * mm, 9);
+    KernelScope ks("spec_adjoints_fp32", s, 6.0 * m * mm, 24.0 * mm, 4);
     // rows of V: e_k = (L^-T x_k)^T, a backward solve with L^T on the columns of X^T
     {
       KernelScope k1("df_solve_rl", s, 0, 0, 0);
-      df_solve_rl<<<m / kRLCols, kMaxM, 0, s>>>(Ld, DU, m, 1, X, 1, 1, E, 1, 1);
+      df_solve_rl<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(Ld, DU, m, 1, X, 1, 1, E, 1, 1);
       NEB_LAUNCH_CHECK();
     }
     int blocks = (int)std::min<size_t>((mm + 255) / 256, 2048);
     f32_to_f64<<<blocks, 256, 0, s>>>(E, V, mm, 1.0);
     NEB_LAUNCH_CHECK();
-    // G_S = E^T diag(c) E ; G_M = -E^T diag(c lam) E
-    scale_rows<<<blocks, 256, 0, s>>>(E, c, nullptr, m, Es);
-    NEB_LAUNCH_CHECK();
-    if ((st = sgemm_rm(h, true, false, m, m, m, 1.f, E, m, Es, m, 0.f, G, m))) return st;
-    f32_to_f64<<<blocks, 256, 0, s>>>(G, G_S, mm, 1.0);
-    NEB_LAUNCH_CHECK();
-    scale_rows<<<blocks, 256, 0, s>>>(E, c, lam, m, Es);
-    NEB_LAUNCH_CHECK();
-    if ((st = sgemm_rm(h, true, false, m, m, m, 1.f, E, m, Es, m, 0.f, G, m))) return st;
-    f32_to_f64<<<blocks, 256, 0, s>>>(G, G_M, mm, -1.0);
+    // G_S = E^T diag(c) E ; G_M = -E^T diag(c lam) E, one pass over E
+    const int nt = m / kGT;
+    gemm_tn<double, true><<<nt * (nt + 1) / 2, 256, 0, s>>>(E, E, c, lam, m, 1, G_S, 1.f, G_M,
+                                                             -1.f);
     NEB_LAUNCH_CHECK();
     mixed_loss<<<1, 256, 0, s>>>(c, lam, m, loss, info);
     NEB_LAUNCH_CHECK();
