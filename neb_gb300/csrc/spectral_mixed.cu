@@ -25,7 +25,7 @@
 //                                          panel launches overlap their
 //                                          predecessor (programmatic dependent
 //                                          launch)
-//   2 x df_solve_rl                        C = L^-1 S L^-T by two right-looking
+//   2 x df_solve                           C = L^-1 S L^-T by two left-looking
 //                                          blocked triangular solves with inverse
 //                                          diagonal blocks, compensated FP32
 //   tridiag_cluster                        FP32 Householder tridiagonalisation in
@@ -40,7 +40,7 @@
 //   side: wy_factor / wy_apply on I        Q^T (FP32), 32 reflectors per block in
 //                                          compact WY form, during the two above
 //   gemm_tn                                X = Z^T Q^T (rows x_k = Q z_k)
-//   df_solve_rl, gemm_tn                   V rows = (L^-T x_k)^T; G_S and G_M in one pass
+//   df_solve, gemm_tn                      V rows = (L^-T x_k)^T; G_S and G_M in one pass
 #include <cooperative_groups.h>
 #include "elementwise.cuh"
 
@@ -350,98 +350,106 @@ __global__ void __launch_bounds__(1024) split_dinv(const df* __restrict__ linv_p
 
 constexpr int kSolveCols = 4;  // eigenvectors per block of the back-transformation
 
-// Right-looking blocked triangular solve, compensated FP32: A Y = B with
+// Left-looking blocked triangular solve, compensated FP32: A Y = B with
 // A = L (upper == 0, forward) or A = L^T (upper == 1, backward), kRLCols
-// right-hand sides per CTA, one thread per row (m <= 512).  F holds the
-// columns of A as rows, F[j][i] = A[i][j] (L^T as float pairs for the
-// forward solve, L for the backward one), so the update reads of a warp are
-// coalesced.  Per 32-row block b, in elimination order:
-//   the warp owning block b forms y_b = D_b acc_b (its accumulators, staged
-//   through shared memory, times the inverse diagonal block);
-//   every row i still pending subtracts A_i,b y_b (32-term Dot2 sums, one
-//   per right-hand side, the 32 factor entries loaded before the barrier).
-// Each row keeps its accumulators in registers from the load of B to the
-// store of Y; the only sequential chain is the 16 blocks (at m = 512), with
-// one barrier each.  The inverse diagonal blocks are staged in shared memory
-// (rows padded to 33 pairs: a warp reading one row per lane is free of bank
-// conflicts) while B loads, so the block's warp reads D_b without a trip to
-// L2 on the chain.  B(r, c) = b_trans ? B[c][r] : B[r][c] (FP64 or FP32);
-// Y(r, c) goes to out[r][c] or, with out_trans, out[c][r].
+// right-hand sides per CTA of 512 threads (m <= 512).  F holds the columns of
+// A as rows, F[j][i] = A[i][j] (L^T as float pairs for the forward solve, L
+// for the backward one), so a warp reading one row of the current block per
+// lane reads 256 contiguous bytes.  Per 32-row block b, in elimination order:
+//   every warp sums A_(r0+lane),j y_j over its share of the finished rows j
+//   (Dot2, one sum per right-hand side), so the block's work is spread over
+//   all sixteen warps instead of falling on the warps of the later blocks;
+//   four warps (one per right-hand side) take B_b minus the sixteen partial
+//   sums and multiply by the inverse diagonal block; y_b joins the finished
+//   rows in shared memory.
+// The factor entries of the next block do not depend on y, so they are
+// loaded while the current block is reduced and solved.  The inverse
+// diagonal blocks (rows padded to 33 pairs: a warp reading one row per lane
+// is free of bank conflicts), B and Y live in shared memory.
+// B(r, c) = b_trans ? B[c][r] : B[r][c] (FP64 or FP32); Y(r, c) goes to
+// out[r][c] or, with out_trans, out[c][r].
 constexpr int kRLCols = 4;
 constexpr int kDPad = kCB + 1;
-size_t solve_smem(int m) { return (size_t)(m / kCB) * kCB * kDPad * sizeof(df); }
-__global__ void __launch_bounds__(kMaxM) df_solve_rl(const df* __restrict__ F,
-                                                     const df* __restrict__ D, int m, int upper,
-                                                     const void* __restrict__ B, int b_f32,
-                                                     int b_trans, void* __restrict__ out,
-                                                     int out_f32, int out_trans) {
-  extern __shared__ df dsh[];            // [nb][kCB][kDPad] inverse diagonal blocks
-  __shared__ df stage[kCB][kRLCols];     // accumulators of the block being finished
-  __shared__ df ys[2][kCB][kRLCols];     // y of the finished block, by parity
-  const int i = threadIdx.x, lane = i & 31, wb = i >> 5;  // row, its block
-  const int c0 = blockIdx.x * kRLCols;
+constexpr int kSolveWarps = kMaxM / 32;                  // 16
+constexpr int kMaxJ = (kMaxM - kCB) / kSolveWarps;       // finished rows per warp, at most
+size_t solve_smem(int m) {
+  return ((size_t)(m / kCB) * kCB * kDPad + 2 * (size_t)m * kRLCols +
+          (size_t)kSolveWarps * kRLCols * kCB) *
+         sizeof(df);
+}
+__global__ void __launch_bounds__(kMaxM) df_solve(const df* __restrict__ F,
+                                                  const df* __restrict__ D, int m, int upper,
+                                                  const void* __restrict__ B, int b_f32,
+                                                  int b_trans, void* __restrict__ out,
+                                                  int out_f32, int out_trans) {
+  extern __shared__ df dsh[];  // [nb][kCB][kDPad] inverse diagonal blocks
+  __shared__ df stage[kRLCols][kCB];
   const int nb = m / kCB;
-  const bool has = i < m;
-  for (int t = i; t < nb * kCB * kCB; t += blockDim.x)
+  df* ysh = dsh + (size_t)nb * kCB * kDPad;      // [kRLCols][m] solution
+  df* bsh = ysh + (size_t)kRLCols * m;           // [kRLCols][m] right-hand sides
+  df* part = bsh + (size_t)kRLCols * m;          // [kSolveWarps][kRLCols][kCB] partial sums
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int c0 = blockIdx.x * kRLCols;
+  for (int t = tid; t < nb * kCB * kCB; t += blockDim.x)
     cp_async8(dsh + (size_t)(t / kCB) * kDPad + t % kCB, D + t);
-  df acc[kRLCols];
-#pragma unroll
-  for (int c = 0; c < kRLCols; ++c) {
-    acc[c] = df{0.f, 0.f};
-    if (has) {
-      const size_t bi = b_trans ? (size_t)(c0 + c) * m + i : (size_t)i * m + c0 + c;
-      acc[c] = df_from(b_f32 ? (double)((const float*)B)[bi] : ((const double*)B)[bi]);
-    }
+  for (int t = tid; t < m * kRLCols; t += blockDim.x) {
+    const int r = b_trans ? t % m : t / kRLCols, c = b_trans ? t / m : t % kRLCols;
+    const size_t bi = b_trans ? (size_t)(c0 + c) * m + r : (size_t)r * m + c0 + c;
+    bsh[(size_t)c * m + r] =
+        df_from(b_f32 ? (double)((const float*)B)[bi] : ((const double*)B)[bi]);
   }
   cp_async_wait_all();
   __syncthreads();
+  df fv[kMaxJ];  // F entries of this warp's finished rows for the current block
   for (int bb = 0; bb < nb; ++bb) {
-    const int b = upper ? nb - 1 - bb : bb, par = bb & 1;
-    const int r0 = b * kCB;
-    const bool pending = has && (upper ? wb < b : wb > b);
-    if (wb == b) {
-      const df* dp = dsh + ((size_t)b * kCB + lane) * kDPad;  // row lane of D_b
+    const int b = upper ? nb - 1 - bb : bb, r0 = b * kCB;
+    const int d0 = upper ? r0 + kCB : 0;       // finished rows [d0, d0 + bb kCB)
+    const int nj = bb * kCB / kSolveWarps;     // of which this warp takes nj
+    dot2 u[kRLCols];
+    // nj is uniform over the CTA: leaving the unrolled loop by a branch issues
+    // only the nj terms (a guard would issue all kMaxJ, predicated off)
 #pragma unroll
-      for (int c = 0; c < kRLCols; ++c) stage[lane][c] = acc[c];
-      __syncwarp();
-      dot2 y[kRLCols];
-#pragma unroll 8
-      for (int j = 0; j < kCB; ++j) {
-        const df d = dp[j];
+    for (int q = 0; q < kMaxJ; ++q) {
+      if (q >= nj) break;
+      const int j = d0 + w + kSolveWarps * q;
 #pragma unroll
-        for (int c = 0; c < kRLCols; ++c) dot2_add(y[c], d, stage[j][c]);
-      }
+      for (int c = 0; c < kRLCols; ++c) dot2_add(u[c], fv[q], ysh[(size_t)c * m + j]);
+    }
+    if (bb + 1 < nb) {  // the next block's entries, in flight during the reduction
+      const int b1 = upper ? nb - 2 - bb : bb + 1, r1 = b1 * kCB;
+      const int e0 = upper ? r1 + kCB : 0, nj1 = (bb + 1) * kCB / kSolveWarps;
 #pragma unroll
-      for (int c = 0; c < kRLCols; ++c) {
-        acc[c] = dot2_df(y[c]);  // this row's solution
-        ys[par][lane][c] = acc[c];
+      for (int q = 0; q < kMaxJ; ++q) {
+        if (q >= nj1) break;
+        fv[q] = F[(size_t)(e0 + w + kSolveWarps * q) * m + r1 + lane];
       }
     }
-    df f[kCB];  // A_i,r0+j, loaded while the block's warp finishes
-    if (pending) {
 #pragma unroll
-      for (int j = 0; j < kCB; ++j) f[j] = F[(size_t)(r0 + j) * m + i];
+    for (int c = 0; c < kRLCols; ++c)
+      part[((size_t)w * kRLCols + c) * kCB + lane] = dot2_df(u[c]);
+    __syncthreads();
+    if (w < kRLCols) {  // warp c: right-hand side c of the block
+      const int c = w, row = r0 + lane;
+      df s = bsh[(size_t)c * m + row];
+#pragma unroll
+      for (int v = 0; v < kSolveWarps; ++v)
+        s = df_add(s, df_neg(part[((size_t)v * kRLCols + c) * kCB + lane]));
+      stage[c][lane] = s;
+      __syncwarp();
+      const df* dp = dsh + ((size_t)b * kCB + lane) * kDPad;  // row lane of D_b
+      dot2 y;
+#pragma unroll 8
+      for (int j = 0; j < kCB; ++j) dot2_add(y, dp[j], stage[c][j]);
+      ysh[(size_t)c * m + row] = dot2_df(y);
     }
     __syncthreads();
-    if (pending) {
-      dot2 u[kRLCols];
-#pragma unroll
-      for (int j = 0; j < kCB; ++j)
-#pragma unroll
-        for (int c = 0; c < kRLCols; ++c) dot2_add(u[c], f[j], ys[par][j][c]);
-#pragma unroll
-      for (int c = 0; c < kRLCols; ++c) acc[c] = df_add(acc[c], df_neg(dot2_df(u[c])));
-    }
-    // ys[par] is rewritten two blocks later, after the next barrier; stage is
-    // rewritten by the next block's warp, whose own reads of it are done
   }
-  if (has) {
-#pragma unroll
-    for (int c = 0; c < kRLCols; ++c) {
-      const size_t oi = out_trans ? (size_t)(c0 + c) * m + i : (size_t)i * m + c0 + c;
-      if (out_f32) ((float*)out)[oi] = acc[c].h + acc[c].l;
-      else ((double*)out)[oi] = df_to(acc[c]);
-    }
+  for (int t = tid; t < m * kRLCols; t += blockDim.x) {
+    const int r = out_trans ? t % m : t / kRLCols, c = out_trans ? t / m : t % kRLCols;
+    const size_t oi = out_trans ? (size_t)(c0 + c) * m + r : (size_t)r * m + c0 + c;
+    const df v = ysh[(size_t)c * m + r];
+    if (out_f32) ((float*)out)[oi] = v.h + v.l;
+    else ((double*)out)[oi] = df_to(v);
   }
 }
 
@@ -1445,7 +1453,7 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     if ((st0 = device_sms(&dev, &sms))) return st0;
     static bool solve_configured[kMaxDevices] = {};
     if (!solve_configured[dev]) {
-      NEB_CUDA_CHECK(cudaFuncSetAttribute(df_solve_rl, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      NEB_CUDA_CHECK(cudaFuncSetAttribute(df_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)solve_smem(kMaxM)));
       solve_configured[dev] = true;
     }
@@ -1479,12 +1487,12 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
       NEB_LAUNCH_CHECK();
     }
     {
-      KernelScope k2("df_solve_rl", s, 0, 0, 0);
-      df_solve_rl<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(LTd, DL, m, 0, S, 0, 0, Y, 0, 0);
+      KernelScope k2("df_solve", s, 0, 0, 0);
+      df_solve<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(LTd, DL, m, 0, S, 0, 0, Y, 0, 0);
       NEB_LAUNCH_CHECK();
     }
-    KernelScope k3("df_solve_rl", s, 0, 0, 0);
-    df_solve_rl<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(LTd, DL, m, 0, Y, 0, 1, C, 1, 0);
+    KernelScope k3("df_solve", s, 0, 0, 0);
+    df_solve<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(LTd, DL, m, 0, Y, 0, 1, C, 1, 0);
     NEB_LAUNCH_CHECK();
   }
   {
@@ -1596,8 +1604,8 @@ extern "C" int neb_spectral_mixed(int m, const double* M, const double* S, const
     KernelScope ks("spec_adjoints_fp32", s, 6.0 * m * mm, 24.0 * mm, 4);
     // rows of V: e_k = (L^-T x_k)^T, a backward solve with L^T on the columns of X^T
     {
-      KernelScope k1("df_solve_rl", s, 0, 0, 0);
-      df_solve_rl<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(Ld, DU, m, 1, X, 1, 1, E, 1, 1);
+      KernelScope k1("df_solve", s, 0, 0, 0);
+      df_solve<<<m / kRLCols, kMaxM, solve_smem(m), s>>>(Ld, DU, m, 1, X, 1, 1, E, 1, 1);
       NEB_LAUNCH_CHECK();
     }
     int blocks = (int)std::min<size_t>((mm + 255) / 256, 2048);

@@ -83,12 +83,23 @@ def test_mixed_spectral_every_supported_size(m):
         pytest.skip("no CUDA device")
     M, S = _pencil(m, 7 * m)
     ref = O.spectral_objective(M, S, "ordering")
-    info, lam, V, GM, GS, loss = _run("neb_spectral_mixed", M, S,
-                                      O.objective_weights("ordering", m))
+    c = O.objective_weights("ordering", m)
+    info, lam, V, GM, GS, loss = _run("neb_spectral_mixed", M, S, c)
     assert info == 0
     np.testing.assert_allclose(lam, ref["lam"], rtol=1e-5)
-    for g, r in ((GM, ref["GM"]), (GS, ref["GS"])):
-        assert np.linalg.norm(g - r) <= 5e-4 * np.linalg.norm(r)
+    # G = sum_k c_k v_k v_k^T turns a rotation of a near-degenerate pair
+    # (k, k+1) of FP32 eigenvectors into an error of (c_k - c_k+1) times the
+    # angle, itself ~ eps_32 lam_max / gap_k: the relative error of an FP32
+    # eigenvector stage is ~ eps_32 kappa, kappa = max_k |c_k - c_k+1| / max|c|
+    # lam_max / gap_k.  Random pencils put a near-degenerate pair among the
+    # low modes at some seeds (kappa 1e3 - 1e4; measured errors up to 15
+    # eps_32 kappa over 42 pencils and three builds of the stage).
+    kappa = lambda w: np.max(np.abs(np.diff(w)) / np.abs(w).max() * ref["lam"].max()
+                             / np.diff(ref["lam"]))
+    eps32 = float(np.finfo(np.float32).eps)
+    for g, r, w in ((GM, ref["GM"], c * ref["lam"]), (GS, ref["GS"], c)):
+        tol = max(5e-4, 15 * eps32 * kappa(w))
+        assert np.linalg.norm(g - r) <= tol * np.linalg.norm(r)
 
 
 def test_mixed_spectral_on_periodic_hidden_pencil():
