@@ -680,31 +680,60 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   hi = s;
 }
 
-__global__ void reduce_parts(const float* __restrict__ part, int splits, int M, int ldp, int ncols,
-                             int ldo, int sym, int accumulate, float* __restrict__ outf,
-                             double* __restrict__ outd) {
-  const size_t total = (size_t)M * ncols;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-       i += (size_t)gridDim.x * blockDim.x) {
-    int m = (int)(i / ncols), j = (int)(i % ncols);
-    float hi = 0.f, lo = 0.f;
-    for (int z = 0; z < splits; ++z) two_sum_acc(hi, lo, part[((size_t)z * M + m) * ldp + j]);
-    if (sym) {
-      float th = 0.f, tl = 0.f;
-      for (int z = 0; z < splits; ++z) two_sum_acc(th, tl, part[((size_t)z * M + j) * ldp + m]);
-      two_sum_acc(hi, lo, th);
-      lo += tl;
-      hi *= 0.5f;
-      lo *= 0.5f;
-    }
-    if (outf) {
-      float* o = outf + (size_t)m * ldo + j;
-      *o = accumulate ? *o + (hi + lo) : hi + lo;
-    }
-    if (outd) {
-      double* o = outd + (size_t)m * ldo + j;
-      *o = accumulate ? *o + ((double)hi + (double)lo) : (double)hi + (double)lo;
-    }
+// Sum of the FP32 chunk-group partials part[z][m][j] over z (in order,
+// TwoSum compensated, four z loads in flight), one output per thread, a
+// 256-thread block on 8 rows x 32 columns (a warp reads 128-byte lines).
+// sym (square): out = (P + P^T) / 2; the mirrored 32 x 8 tile is summed on
+// reads of 32-byte row pieces and exchanged through shared memory.
+__device__ __forceinline__ void sum_splits(const float* __restrict__ p, size_t zs, int splits,
+                                           float& hi, float& lo) {
+  hi = 0.f;
+  lo = 0.f;
+  int z = 0;
+  for (; z + 4 <= splits; z += 4) {
+    const float a0 = p[z * zs], a1 = p[(z + 1) * zs], a2 = p[(z + 2) * zs],
+                a3 = p[(z + 3) * zs];
+    two_sum_acc(hi, lo, a0);
+    two_sum_acc(hi, lo, a1);
+    two_sum_acc(hi, lo, a2);
+    two_sum_acc(hi, lo, a3);
+  }
+  for (; z < splits; ++z) two_sum_acc(hi, lo, p[z * zs]);
+}
+
+__global__ void __launch_bounds__(256) reduce_parts(const float* __restrict__ part, int splits,
+                                                    int M, int ldp, int ncols, int ldo, int sym,
+                                                    int accumulate, float* __restrict__ outf,
+                                                    double* __restrict__ outd) {
+  __shared__ float th[32][9], tl[32][9];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int j0 = blockIdx.x * 32, m0 = blockIdx.y * 8;
+  const size_t zs = (size_t)M * ldp;
+  const int m = m0 + ty, j = j0 + tx;
+  float hi = 0.f, lo = 0.f;
+  if (m < M && j < ncols) sum_splits(part + (size_t)m * ldp + j, zs, splits, hi, lo);
+  if (sym) {
+    // thread t sums the mirror element (j0 + t / 8, m0 + t % 8)
+    const int r = threadIdx.x >> 3, c = threadIdx.x & 7;
+    float a = 0.f, b = 0.f;
+    if (j0 + r < M && m0 + c < ncols)
+      sum_splits(part + (size_t)(j0 + r) * ldp + m0 + c, zs, splits, a, b);
+    th[r][c] = a;
+    tl[r][c] = b;
+    __syncthreads();
+    two_sum_acc(hi, lo, th[tx][ty]);  // element (j, m)
+    lo += tl[tx][ty];
+    hi *= 0.5f;
+    lo *= 0.5f;
+  }
+  if (m >= M || j >= ncols) return;
+  if (outf) {
+    float* o = outf + (size_t)m * ldo + j;
+    *o = accumulate ? *o + (hi + lo) : hi + lo;
+  }
+  if (outd) {
+    double* o = outd + (size_t)m * ldo + j;
+    *o = accumulate ? *o + ((double)hi + (double)lo) : (double)hi + (double)lo;
   }
 }
 
@@ -883,10 +912,10 @@ int launch_rowsum(const void* a_base, int aC, int a_ch0, const void* b_base, int
 int reduce(const float* part, int splits, int M, int ldp, int ncols, int ldo, bool sym,
            float* outf, double* outd, cudaStream_t s, int accumulate = 0) {
   KernelScope ks("reduce_chunks", s, 0, (double)splits * M * ncols * 4);
-  size_t total = (size_t)M * ncols;
-  int blocks = (int)std::min<size_t>((total + 255) / 256, 4096);
-  reduce_parts<<<blocks, 256, 0, s>>>(part, splits, M, ldp, ncols, ldo, sym ? 1 : 0, accumulate,
-                                      outf, outd);
+  NEB_REQUIRE(!sym || M == ncols, "reduce: a symmetric sum needs a square matrix");
+  const dim3 grid((ncols + 31) / 32, (M + 7) / 8);
+  reduce_parts<<<grid, 256, 0, s>>>(part, splits, M, ldp, ncols, ldo, sym ? 1 : 0, accumulate,
+                                    outf, outd);
   NEB_LAUNCH_CHECK();
   return NEB_OK;
 }
