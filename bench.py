@@ -481,7 +481,7 @@ def run_workload(args, world, rank, local):
     """One line per configuration other than the headline: device-timed
     steps, the plain FP32 form where the configuration asks for it, and the
     errors of eigenvalues, Gram entries and gradients against the FP64
-    oracle (the checker) on the same seeded inputs."""
+    oracle on the same seeded inputs."""
     import torch
     sys.path.insert(0, str(ROOT))
     from neb_gb300 import CONFIGS, Model, spectral_step, train_step

@@ -1,7 +1,7 @@
 """FP64 NumPy oracle for the neural-eigenfluid hot path.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker that the CUDA product is
-compared against; the product (``neb_gb300``) never imports, links or calls it.
+TEST INFRASTRUCTURE ONLY.  This module is the reference that the CUDA product
+is compared against; the product (``neb_gb300``) never imports, links or calls it.
 Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
 ``--impl reference`` legs of ``bench.py`` may use it.
 
