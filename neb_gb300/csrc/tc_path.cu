@@ -130,6 +130,49 @@ template <int EPI> struct JetCfg {
 };
 
 
+// Tile schedule of the persistent jet GEMM: whole rounds of 128 x BN tiles
+// dealt round-robin to the CTAs, then, for the forward layer, the R tiles left
+// over as 2R half tiles of BN / 2 outputs, one per CTA, when 2R fits the
+// grid (512 tiles on 152 CTAs: three rounds, then 112 half tiles instead of
+// a fourth round of 56 full ones while 96 CTAs wait).  A half tile loads the
+// same operand stages (the B box from its first output row) and multiplies
+// with N = BN / 2.
+struct TileSched {
+  int n_tiles, full_end, halves;  // halves: 0, or 2R half tiles after full_end
+};
+
+__device__ __forceinline__ TileSched make_sched(int total, int n_tiles, bool split) {
+  TileSched s{n_tiles, total, 0};
+  if (split) {
+    const int G = gridDim.x, full = total / G * G, R = total - full;
+    if (R > 0 && 2 * R <= G) {
+      s.full_end = full;
+      s.halves = 2 * R;
+    }
+  }
+  return s;
+}
+
+// The i-th tile of this CTA (false: none): first output n0, first point p0,
+// half = 1 for a half tile.
+__device__ __forceinline__ bool tile_of(const TileSched& s, int i, int BN, int& n0, int& p0,
+                                        int& half) {
+  const int t = blockIdx.x + i * gridDim.x;
+  if (t < s.full_end) {
+    n0 = (t % s.n_tiles) * BN;
+    p0 = (t / s.n_tiles) * 128;
+    half = 0;
+    return true;
+  }
+  if (s.halves == 0 || (int)blockIdx.x >= s.halves || i != s.full_end / (int)gridDim.x)
+    return false;
+  const int tf = s.full_end + blockIdx.x / 2;
+  n0 = (tf % s.n_tiles) * BN + (blockIdx.x & 1) * (BN / 2);
+  p0 = (tf / s.n_tiles) * 128;
+  half = 1;
+  return true;
+}
+
 // Persistent tcgen05 jet GEMM: tiles of 128 points x BN outputs (all jet
 // channels) are dealt round-robin to the CTAs (one per SM).  The producer
 // keeps loading operand stages across tile boundaries; the accumulators are
@@ -163,6 +206,10 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
   const int KC = g.K / 64;
   const int n_tiles = g.N / BN;
   const int total = n_tiles * (g.n_pad / 128);
+  // the forward layer runs alone on the GPU; the reverse-data GEMM shares it
+  // with the weight-gradient GEMM on a side stream, so its CTAs do not all
+  // start together and a last round of half tiles would not shorten it
+  const TileSched sched = make_sched(total, n_tiles, EPI == 0);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < A_ST; ++i) {
@@ -195,8 +242,9 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     // untouched; the copies already issued are drained before the CTA exits.
     int ai = 0, bi = 0;
     bool ok = true;
-    for (int t = blockIdx.x; ok && t < total; t += gridDim.x) {
-      const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
+    for (int i = 0; ok; ++i) {
+      int n0, p0, half;
+      if (!tile_of(sched, i, BN, n0, p0, half)) break;
       for (int kc = 0; ok && kc < KC; ++kc) {
         const int bs = bi % B_ST;
         if (!tc::mbar_wait(&b_empty[bs], ((bi / B_ST) & 1) ^ 1, g.status)) {
@@ -230,10 +278,14 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     tc::drain_ring(a_full, A_ST, ai, g.status);
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer (stops at the first wait that gives up)
-    constexpr uint32_t idesc = tc::idesc_bf16(128, BN, true);
-    int ai = 0, bi = 0, it = 0;
+    constexpr uint32_t idesc_full = tc::idesc_bf16(128, BN, true);
+    constexpr uint32_t idesc_half = tc::idesc_bf16(128, BN / 2, true);
+    int ai = 0, bi = 0;
     bool ok = true;
-    for (int t = blockIdx.x; ok && t < total; t += gridDim.x, ++it) {
+    for (int it = 0; ok; ++it) {
+      int n0, p0, half;
+      if (!tile_of(sched, it, BN, n0, p0, half)) break;
+      const uint32_t idesc = half ? idesc_half : idesc_full;
       const int buf = it % Cfg::NBUF, use = it / Cfg::NBUF;
       if (!tc::mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status)) break;
       tc::tc_fence_after();
@@ -293,10 +345,10 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
     const int q = warp & 3, slice = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     const size_t plane = (size_t)C * g.n_pad * g.N;  // elements of one hi or lo plane
-    int it = 0;
     bool ok = true;
-    for (int t = blockIdx.x; ok && t < total; t += gridDim.x, ++it) {
-      const int n0 = (t % n_tiles) * BN, p0 = (t / n_tiles) * 128;
+    for (int it = 0; ok; ++it) {
+      int n0, p0, half;
+      if (!tile_of(sched, it, BN, n0, p0, half)) break;
       const int p = p0 + row;
       const int buf = it % Cfg::NBUF, use = it / Cfg::NBUF;
       float w2 = 0.f;
@@ -305,8 +357,11 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
       constexpr int kW = EPI == 0 ? kJetEpiCols : kJetEpiCols / 2;
       constexpr int kSlice = BN / (kJetEpiWarps / 4);  // columns of this warp
       constexpr int kChunks = kSlice / kW;
-      for (int jc = 0; jc < kChunks; ++jc) {
-        const int j0 = slice * kSlice + jc * kW;
+      // a half tile: half the columns per warp, every warp still drains (and
+      // releases) its share of the accumulator buffer
+      const int slice_w = half ? kSlice / 2 : kSlice, nchunks = half ? kChunks / 2 : kChunks;
+      for (int jc = 0; jc < nchunks; ++jc) {
+        const int j0 = slice * slice_w + jc * kW;
         const int col = n0 + j0;
         // global operands first (bias, or the pre-activations of the target
         // layer), so their latency overlaps the accumulator wait and loads
@@ -342,7 +397,7 @@ tc_jet_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUt
 #pragma unroll
           for (int j = 0; j < kW; ++j) acc[ci][j] = __uint_as_float(raw[ci][j]);
         }
-        if (jc == kChunks - 1) {  // this warp's columns of the buffer are drained
+        if (jc == nchunks - 1) {  // this warp's columns of the buffer are drained
           tc::tc_fence_before();
           __syncwarp();
           if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
