@@ -32,7 +32,7 @@ import torch
 
 from . import _native as N
 from .hardcoded import HardcodedModel, TAPE_BUDGET
-from .modes import ModeNet, column_gram
+from .modes import column_gram
 
 
 def _stream() -> int:

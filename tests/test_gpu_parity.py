@@ -12,7 +12,7 @@ import pytest
 import torch
 
 from oracle import neb_oracle as O
-from neb_gb300 import CONFIGS, Jet, Model, SpectralObjective, spectral_step, train_step
+from neb_gb300 import CONFIGS, Model, SpectralObjective, spectral_step, train_step
 from neb_gb300 import configs as CF
 
 pytestmark = pytest.mark.gpu

@@ -3,11 +3,9 @@
 matrix C = L^-1 S L^-T; the pencils here have cond(M) = 1e4 and cond(C) = 40
 like the training pencils.  Tolerances: eigenvalues 1e-5 relative, objective
 adjoints 1e-4 relative (norm)."""
-import ctypes
 
 import numpy as np
 import pytest
-import scipy.linalg as sla
 import torch
 
 from oracle import neb_oracle as O
